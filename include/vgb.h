@@ -1,0 +1,214 @@
+/*
+ * vgb.h - C ABI of the GB300 spectral ray-tracing hot path (vira_gb300).
+ *
+ * This is the drop-in boundary for Vira's CPU path tracer.  The reference is a
+ * header-only C++ template library with two seams on this path:
+ *
+ *   (1) the renderer object   CPUPathTracer::render(Camera&, Scene&), its public
+ *       `options` and `renderPasses` (include/vira/rendering/cpu_path_tracer.hpp:46-58),
+ *       called from Scene::pathtraceRender / renderTotalPower
+ *       (include/implementation/scene.ipp:840-915);
+ *   (2) the acceleration plugin  TLAS::intersect(Ray&) / BLAS::intersect
+ *       (include/vira/rendering/acceleration/tlas.hpp:20-31, blas.hpp:20-37), which
+ *       Embree fills through rtcIntersect1
+ *       (include/implementation/rendering/acceleration/embree_tlas.ipp:128-173).
+ *
+ * Every entry point returns a vgb_status and never throws or aborts.  Buffers are
+ * owned by the caller unless a vgb_*_create function made them.  A context owns one
+ * CUDA stream and is not thread-safe: use one host thread per context.
+ *
+ * Conventions
+ *   - B = number of spectral bands (1..VGB_MAX_BANDS).
+ *   - Images are planar, row-major: plane[b][j][i] at b*W*H + j*W + i, which is the
+ *     reference's linear index i + j*W (include/implementation/images/image.ipp:137)
+ *     with the bands split into planes.
+ *   - Matrices are column-major like glm: m[c*rows + r].
+ *   - Triangle ids are the index of the triangle in the caller's index buffer.
+ */
+#ifndef VGB_H
+#define VGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VGB_API __declspec(dllexport)
+#else
+#define VGB_API __attribute__((visibility("default")))
+#endif
+
+#define VGB_MAX_BANDS 8
+#define VGB_NO_HIT 0xFFFFFFFFu
+
+typedef enum vgb_status {
+    VGB_OK = 0,
+    VGB_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or option (reference: std::runtime_error) */
+    VGB_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+    VGB_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed */
+    VGB_ERR_NOT_READY = 4,        /* no scene uploaded / no BVH built yet */
+    VGB_ERR_DEVICE_LIMIT = 5,     /* a kernel hit its traversal-stack or iteration cap */
+    VGB_ERR_INTERNAL = 6
+} vgb_status;
+
+typedef struct vgb_context vgb_context;
+
+/* ---- camera: FP32 constants derived on the host in FP64 -------------------------
+ * Replaces Camera::pixelToRay (include/implementation/cameras/camera.ipp:1126-1131,
+ * 1143-1163), pixelToDirectionHelper (:1738-1749) and
+ * ReferenceFrame::localDirectionToGlobal (include/implementation/reference_frame.ipp:361-364).
+ * The ray of pixel coordinate (x, y) is
+ *     d_cam = { kinv·(x, y, 1) [row 0],  z_dir * kinv·(x, y, 1) [row 1],  z_dir }
+ *     dir   = normalize(rotation · d_cam),   origin = origin.
+ */
+typedef struct vgb_camera {
+    uint32_t width;            /* resolution x (columns, index i) */
+    uint32_t height;           /* resolution y (rows, index j) */
+    float origin[3];           /* camera position in the scene frame (rebased in FP64, then FP32) */
+    float rotation[9];         /* camera-to-scene rotation, column-major 3x3 */
+    float kinv[6];             /* inverse intrinsic matrix, column-major 3 columns x 2 rows */
+    float z_dir;               /* +1, or -1 for the Blender frame */
+    float power_scale[VGB_MAX_BANDS]; /* optical efficiency[b] * aperture area (received power) */
+} vgb_camera;
+
+/* ---- sphere light (Vira's SphereLight; the Sun is one) --------------------------
+ * include/implementation/lights/sphere_light.ipp:17-153. */
+typedef struct vgb_light {
+    float position[3];         /* centre in the scene frame (FP64 ephemeris, rebased, FP32) */
+    float radius;              /* metres */
+    float radiance[VGB_MAX_BANDS]; /* spectral radiance per band */
+} vgb_light;
+
+/* ---- path tracer options: CPUPathTracerOptions + RenderPasses switches ----------
+ * include/vira/rendering/cpu_path_tracer.hpp:30-43, include/vira/rendering/passes.hpp:72-84. */
+typedef struct vgb_pt_options {
+    uint32_t samples;            /* options.samples (>= 1) */
+    uint32_t bounces;            /* options.bounces */
+    uint32_t show_background;    /* options.show_background (uniform background emission) */
+    uint32_t simulate_lighting;  /* renderPasses.simulate_lighting */
+    uint32_t smooth_shading;     /* Mesh::getSmoothShading */
+    uint32_t deterministic_light;/* 1: RNG-free SphereLight::sample (sphere_light.ipp:31-64) */
+    uint32_t rr_depth;           /* Russian roulette from this bounce on; 0 = off (reference) */
+    uint32_t has_ambient;        /* Scene::hasAmbient */
+    uint64_t seed;               /* counter-based RNG key */
+    uint32_t frame;              /* counter-based RNG key, second word */
+    uint32_t nbands;             /* B */
+    float ambient[VGB_MAX_BANDS];
+    float background[VGB_MAX_BANDS];
+} vgb_pt_options;
+
+/* ---- film: RenderPasses planes (caller-owned; NULL = pass not written) ----------
+ * include/vira/rendering/passes.hpp:51-95, passes.ipp:43-128. */
+typedef struct vgb_film {
+    float* total_radiance;     /* [B][H][W] */
+    float* direct_radiance;    /* [B][H][W] */
+    float* indirect_radiance;  /* [B][H][W] */
+    float* received_power;     /* [B][H][W]; needs pixel_solid_angle */
+    float* albedo;             /* [B][H][W] */
+    float* normal_global;      /* [3][H][W] */
+    float* depth;              /* [H][W]; +inf where nothing was hit */
+    float* alpha;              /* [H][W] */
+    uint32_t* triangle_id;     /* [H][W]; VGB_NO_HIT where nothing was hit */
+    const float* pixel_solid_angle; /* [H][W] input, from vgb_pixel_solid_angle */
+    int32_t on_device;         /* 1: every pointer is device memory; 0: host memory */
+} vgb_film;
+
+/* ---- BVH build options -------------------------------------------------------- */
+typedef struct vgb_bvh_options {
+    uint32_t max_leaf_size;    /* triangles per leaf (1..8); 0 = default */
+    uint32_t builder;          /* 0 = binned SAH (host, threaded), 1 = reserved */
+    uint32_t threads;          /* host threads for the build; 0 = all */
+} vgb_bvh_options;
+
+/* ---- statistics of the last render / trace ------------------------------------ */
+typedef struct vgb_stats {
+    uint64_t rays_closest;     /* closest-hit queries (primary + bounce) */
+    uint64_t rays_shadow;      /* shadow (any-hit) queries */
+    uint64_t nodes_visited;    /* only filled by a counting pass */
+    uint64_t tris_tested;      /* only filled by a counting pass */
+    uint32_t bvh_nodes;        /* wide nodes in the device BVH */
+    uint32_t bvh_node_bytes;   /* bytes per wide node */
+    uint32_t tri_record_bytes; /* bytes per triangle record */
+    uint32_t kernel_launches;  /* kernels launched by the last render */
+    uint32_t device_error;     /* last device error word (0 = none) */
+    float ms_last;             /* device time of the last render (CUDA events) */
+} vgb_stats;
+
+/* ========================= context ============================================= */
+VGB_API vgb_status vgb_context_create(vgb_context** out, int device);
+VGB_API vgb_status vgb_context_destroy(vgb_context* ctx);
+VGB_API const char* vgb_last_error(const vgb_context* ctx);
+VGB_API const char* vgb_version(void);
+/* Make the context use an existing CUDA stream (cudaStream_t passed as void*); NULL = own. */
+VGB_API vgb_status vgb_set_stream(vgb_context* ctx, void* stream);
+VGB_API vgb_status vgb_synchronize(vgb_context* ctx);
+
+/* ========================= host-side geometry ================================== */
+/* Mesh::calculateNormals (include/implementation/geometry/mesh.ipp:199-233): each vertex
+ * normal is the sum, in triangle order, of the unit face normals normalize(cross(p1-p0,
+ * p2-p0)) of its triangles (NaN face normals skipped), then normalised.  Host C++. */
+VGB_API vgb_status vgb_compute_vertex_normals(const float* positions, uint32_t nverts,
+                                              const uint32_t* indices, uint32_t ntris,
+                                              float* normals_out);
+/* DEM::makeVertexBuffer (include/implementation/dems/dem.ipp:165-211) with the non-OGR grid
+ * mapping (include/implementation/dems/dem_projection.ipp:131-141) and imageToIndexBuffer
+ * (include/implementation/images/image_utils.ipp:364-409).  heights: [H][W] row-major.
+ * positions_out: 3*W*H floats; indices_out: up to 6*(W-1)*(H-1); *ntris_out = count. */
+VGB_API vgb_status vgb_dem_triangulate(const float* heights, uint32_t width, uint32_t height,
+                                       double posting_x, double posting_y,
+                                       float* positions_out, uint32_t* indices_out,
+                                       uint32_t* ntris_out);
+/* Camera::initializeIntrinsicMatrix (include/implementation/cameras/camera.ipp:1526-1568),
+ * evaluated in FP32 as the reference's TFloat = float instantiation does.
+ * px/py = +inf selects the image centre. */
+VGB_API vgb_status vgb_camera_intrinsics(float focal_length, float sensor_x, float sensor_y,
+                                         uint32_t width, uint32_t height, float px, float py,
+                                         float kxy, float kyx, float z_dir, float kinv_out[6]);
+
+/* ========================= scene / BVH ========================================= */
+/* Scene::buildTLAS input (include/implementation/scene.ipp:712-812): one flattened triangle
+ * mesh in the scene frame.  vert_albedo: B floats per vertex or NULL (=1);
+ * vert_normal: 3 floats per vertex or NULL (computed); vert_uv: 2 floats per vertex or NULL
+ * (=0); texture: albedo map [tex_h][tex_w][B] or NULL (1x1 of 1.0, material.hpp:72).
+ * Host pointers.  Uploading replaces the scene and invalidates the BVH. */
+VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* positions, uint32_t nverts,
+                                    const uint32_t* indices, uint32_t ntris, uint32_t nbands,
+                                    const float* vert_albedo, const float* vert_normal,
+                                    const float* vert_uv, const float* texture,
+                                    uint32_t tex_w, uint32_t tex_h);
+/* Replaces Mesh::buildBVH -> EmbreeBLAS (include/implementation/geometry/mesh.ipp:396-408,
+ * include/implementation/rendering/acceleration/embree_blas.ipp:14-71). */
+VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts);
+
+/* ========================= rendering =========================================== */
+/* Camera::initializePixelSolidAngle (include/implementation/cameras/camera.ipp:1622-1666):
+ * Girard's theorem on the four corner directions, FP64, one device kernel.
+ * out: [H][W] floats, device memory if out_on_device else host. */
+VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam, float* out,
+                                         int out_on_device);
+/* CPUPathTracer::render (include/implementation/rendering/cpu_path_tracer.ipp:29-161). */
+VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                              uint32_t nlights, const vgb_pt_options* opts, vgb_film* film);
+/* TLAS::intersect(Ray&) seam (include/vira/rendering/acceleration/tlas.hpp:24): a batch of
+ * rays, closest hit (any_hit = 0) or occlusion (any_hit = 1, tmax per ray or +inf).
+ * origins/dirs: 3 floats per ray.  tri_out: VGB_NO_HIT on a miss; t_out: +inf on a miss;
+ * bary_out: 3 floats per ray, Interaction::w order {w(v1), w(v2), w(v0)} (ray.hpp:49,
+ * embree_tlas.ipp:159-161).  tmax, t_out, bary_out may be NULL.
+ * All arrays device memory if on_device else host. */
+VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* origins, const float* dirs,
+                                  const float* tmax, uint32_t nrays, int any_hit,
+                                  uint32_t* tri_out, float* t_out, float* bary_out,
+                                  int on_device);
+/* Statistics of the last render/trace.  If count_pass is set, the next render/trace also runs
+ * a counting pass that fills nodes_visited/tris_tested (algorithmic traffic). */
+VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out);
+VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VGB_H */

@@ -1,0 +1,190 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the oracle (oracle/vgb_oracle.cpp).
+
+The oracle is a CPU restatement of Vira's CPU path tracer used as the parity checker and as
+the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline /
+reference legs may use it.  Parity with the reference itself is unpinned (the reference
+cannot be built here and ships no golden vectors); see the header of vgb_oracle.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from vira_gb300 import capi
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "libvgb_oracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "vgb_oracle.cpp"
+    hdr = HERE.parent / "include" / "vgb.h"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
+        r = subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = C.CDLL(str(LIB))
+    P, U32 = C.c_void_p, C.c_uint32
+    sig = {
+        "oracle_philox": (None, [P, P, P]),
+        "oracle_compute_normals": (C.c_int, [P, U32, P, U32, P]),
+        "oracle_dem_triangulate": (C.c_int, [P, U32, U32, C.c_double, C.c_double, P, P, C.POINTER(U32)]),
+        "oracle_intrinsics": (C.c_int, [C.c_float] * 3 + [U32, U32] + [C.c_float] * 5 + [P]),
+        "oracle_pixel_solid_angle": (C.c_int, [C.POINTER(capi.Camera), P, C.c_int]),
+        "oracle_blackbody_band": (C.c_double, [C.c_double, C.c_float, C.c_float, U32]),
+        "oracle_scene_create": (P, [P, U32, P, U32, U32, P, P, P, P, U32, U32]),
+        "oracle_scene_destroy": (None, [P]),
+        "oracle_scene_bvh_nodes": (U32, [P]),
+        "oracle_trace": (C.c_int, [P, P, P, P, U32, C.c_int, C.c_int, P, P, P, C.c_int, P, P]),
+        "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
+                                    C.POINTER(capi.Film), U32, U32, C.c_int, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def nthreads() -> int:
+    return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
+
+
+def philox(ctr, key):
+    c = np.array(ctr, np.uint32)
+    k = np.array(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    load().oracle_philox(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    return out
+
+
+def compute_normals(pos, idx):
+    p = np.ascontiguousarray(pos, np.float32)
+    i = np.ascontiguousarray(idx, np.uint32)
+    n = np.empty_like(p)
+    assert load().oracle_compute_normals(p.ctypes.data, p.shape[0], i.ctypes.data, i.shape[0], n.ctypes.data) == 0
+    return n
+
+
+def dem_triangulate(heights, posting):
+    h = np.ascontiguousarray(heights, np.float32)
+    H, W = h.shape
+    pos = np.empty((H * W, 3), np.float32)
+    idx = np.empty((2 * (W - 1) * (H - 1), 3), np.uint32)
+    nt = C.c_uint32(0)
+    assert load().oracle_dem_triangulate(h.ctypes.data, W, H, posting, posting, pos.ctypes.data, idx.ctypes.data,
+                                         C.byref(nt)) == 0
+    return pos, idx[: nt.value].copy()
+
+
+def intrinsics(focal, sx, sy, W, H, px=np.inf, py=np.inf, kxy=0.0, kyx=0.0, z_dir=1.0):
+    out = (C.c_float * 6)()
+    load().oracle_intrinsics(focal, sx, sy, W, H, px, py, kxy, kyx, z_dir, out)
+    return np.array(out[:], np.float32)
+
+
+def pixel_solid_angle(cam: capi.Camera):
+    out = np.empty((cam.height, cam.width), np.float32)
+    assert load().oracle_pixel_solid_angle(C.byref(cam), out.ctypes.data, nthreads()) == 0
+    return out
+
+
+def blackbody_band(T, lmin_m, lmax_m, steps=1000):
+    return load().oracle_blackbody_band(T, lmin_m, lmax_m, steps)
+
+
+class OracleScene:
+    """A flattened scene on the CPU with the reference's own BVH (vira_blas.ipp)."""
+
+    def __init__(self, positions, indices, nbands, albedo=None, normals=None, uv=None, texture=None):
+        self.keep = [np.ascontiguousarray(positions, np.float32), np.ascontiguousarray(indices, np.uint32)]
+        p, i = self.keep
+        opt = []
+        for a in (albedo, normals, uv, texture):
+            arr = None if a is None else np.ascontiguousarray(a, np.float32)
+            opt.append(arr)
+            self.keep.append(arr)
+        tex = opt[3]
+        th, tw = (tex.shape[0], tex.shape[1]) if tex is not None else (0, 0)
+        ptrs = [None if a is None else a.ctypes.data for a in opt]
+        self.h = load().oracle_scene_create(p.ctypes.data, p.shape[0], i.ctypes.data, i.shape[0], nbands,
+                                            ptrs[0], ptrs[1], ptrs[2], ptrs[3], tw, th)
+        if not self.h:
+            raise ValueError("oracle_scene_create rejected the scene")
+        self.nbands = nbands
+
+    @staticmethod
+    def from_flat(flat, nbands):
+        return OracleScene(flat["positions"], flat["indices"], nbands, flat["albedo"], flat["normals"], flat["uv"],
+                           flat["texture"])
+
+    def close(self):
+        if self.h:
+            load().oracle_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def trace(self, origins, dirs, any_hit=False, tmax=None, mode=0, threads=None):
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(dirs, np.float32)
+        n = o.shape[0]
+        tri = np.empty(n, np.uint32)
+        t = np.empty(n, np.float32)
+        w = np.empty((n, 3), np.float32)
+        tm = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+        nodes = C.c_uint64(0)
+        tris = C.c_uint64(0)
+        assert load().oracle_trace(self.h, o.ctypes.data, d.ctypes.data, None if tm is None else tm.ctypes.data, n,
+                                   int(any_hit), mode, tri.ctypes.data, t.ctypes.data, w.ctypes.data,
+                                   threads or nthreads(), C.byref(nodes), C.byref(tris)) == 0
+        return tri, t, w
+
+    def render(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, omega=None, rows=None,
+               threads=None):
+        """Renders rows [r0, r1) (all rows by default) into host planes; returns (planes, ray_counts)."""
+        W, H, B = cam.width, cam.height, self.nbands
+        planes = {
+            "total_radiance": np.full((B, H, W), np.nan, np.float32),
+            "direct_radiance": np.full((B, H, W), np.nan, np.float32),
+            "indirect_radiance": np.full((B, H, W), np.nan, np.float32),
+            "albedo": np.full((B, H, W), np.nan, np.float32),
+            "normal_global": np.full((3, H, W), np.nan, np.float32),
+            "depth": np.full((H, W), np.nan, np.float32),
+            "alpha": np.full((H, W), np.nan, np.float32),
+            "triangle_id": np.full((H, W), 0xFFFFFFFF, np.uint32),
+        }
+        f = capi.Film()
+        for k, v in planes.items():
+            setattr(f, k, v.ctypes.data)
+        if omega is not None:
+            planes["received_power"] = np.full((B, H, W), np.nan, np.float32)
+            om = np.ascontiguousarray(omega, np.float32)
+            f.received_power = planes["received_power"].ctypes.data
+            f.pixel_solid_angle = om.ctypes.data
+        f.on_device = 0
+        r0, r1 = rows if rows is not None else (0, H)
+        counts = (C.c_uint64 * 2)()
+        rc = load().oracle_render(self.h, C.byref(cam), C.cast(lights, C.c_void_p) if nlights else None, nlights,
+                                  C.byref(opts), C.byref(f), r0, r1, threads or nthreads(), counts)
+        if rc != 0:
+            raise ValueError("oracle_render rejected its arguments")
+        return planes, (int(counts[0]), int(counts[1]))

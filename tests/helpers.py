@@ -1,0 +1,74 @@
+"""Shared test utilities: primary rays in numpy FP32 (same operation order as the kernels and
+the oracle), GPU renders into host arrays, and comparisons."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from vira_gb300 import capi
+
+F = np.float32
+
+
+def primary_rays(cam: capi.Camera):
+    """Camera::pixelToRay for sample 0 (pixel corner), FP32, glm operation order."""
+    W, H = cam.width, cam.height
+    j, i = np.meshgrid(np.arange(H, dtype=F), np.arange(W, dtype=F), indexing="ij")
+    K = np.array(cam.kinv[:], F)
+    R = np.array(cam.rotation[:], F)
+    hx = (K[0] * i + K[2] * j) + K[4] * F(1)
+    hy = (K[1] * i + K[3] * j) + K[5] * F(1)
+    zd = F(cam.z_dir)
+    dc = [hx, zd * hy, np.full_like(hx, zd)]
+    dw = [(R[r] * dc[0] + R[3 + r] * dc[1]) + R[6 + r] * dc[2] for r in range(3)]
+    n2 = (dw[0] * dw[0] + dw[1] * dw[1]) + dw[2] * dw[2]
+    s = F(1) / np.sqrt(n2)
+    d = np.stack([dw[0] * s, dw[1] * s, dw[2] * s], -1).reshape(-1, 3).astype(F)
+    o = np.broadcast_to(np.array(cam.origin[:], F), d.shape).copy()
+    return o, d
+
+
+def gpu_render_host(scene, cam_id):
+    """Renders through the Python API and returns host numpy planes."""
+    import torch
+
+    rp = scene.pathtracer.render(scene[cam_id], scene)
+    torch.cuda.synchronize()
+    out = {}
+    for k in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo",
+              "normal_global", "depth", "alpha"):
+        v = getattr(rp, k)
+        if v is not None:
+            out[k] = v.cpu().numpy()
+    out["triangle_id"] = rp.triangle_id.cpu().numpy().view(np.uint32)
+    return out
+
+
+def oracle_render(scene, cam_id, omega=None, rows=None):
+    from oracle import oracle
+
+    cam = scene[cam_id].to_c(scene.origin, scene.bands.size)
+    if scene.flat is None:
+        scene.flatten()
+    osc = oracle.OracleScene.from_flat(scene.flat, scene.bands.size)
+    lights, nl = scene.c_lights()
+    planes, counts = osc.render(cam, lights, nl, scene.pathtracer.c_options(scene), omega=omega, rows=rows)
+    osc.close()
+    return planes, counts
+
+
+def rel_err(a, b, floor=1e-30):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    both_nan = np.isnan(a) & np.isnan(b)
+    both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
+    e = np.abs(a - b) / np.maximum(np.abs(b), floor)
+    e[both_nan | both_inf] = 0.0
+    return e
+
+
+def same_bits(a, b) -> bool:
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))

@@ -1,0 +1,142 @@
+"""ctypes view of the C ABI declared in include/vgb.h.
+
+The structs below mirror include/vgb.h field for field; ``load()`` opens the in-tree
+``libvgb.so`` and raises if it is missing, so nothing silently falls back to another path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+MAX_BANDS = 8
+NO_HIT = 0xFFFFFFFF
+
+STATUS = {
+    0: "VGB_OK",
+    1: "VGB_ERR_INVALID_ARGUMENT",
+    2: "VGB_ERR_CUDA",
+    3: "VGB_ERR_OUT_OF_MEMORY",
+    4: "VGB_ERR_NOT_READY",
+    5: "VGB_ERR_DEVICE_LIMIT",
+    6: "VGB_ERR_INTERNAL",
+}
+
+
+class VgbError(RuntimeError):
+    """A vgb_* call returned a status other than VGB_OK."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Camera(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32),
+        ("origin", C.c_float * 3), ("rotation", C.c_float * 9), ("kinv", C.c_float * 6),
+        ("z_dir", C.c_float), ("power_scale", C.c_float * MAX_BANDS),
+    ]
+
+
+class Light(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("radius", C.c_float), ("radiance", C.c_float * MAX_BANDS)]
+
+
+class PtOptions(C.Structure):
+    _fields_ = [
+        ("samples", C.c_uint32), ("bounces", C.c_uint32), ("show_background", C.c_uint32),
+        ("simulate_lighting", C.c_uint32), ("smooth_shading", C.c_uint32),
+        ("deterministic_light", C.c_uint32), ("rr_depth", C.c_uint32), ("has_ambient", C.c_uint32),
+        ("seed", C.c_uint64), ("frame", C.c_uint32), ("nbands", C.c_uint32),
+        ("ambient", C.c_float * MAX_BANDS), ("background", C.c_float * MAX_BANDS),
+    ]
+
+
+class Film(C.Structure):
+    _fields_ = [
+        ("total_radiance", C.c_void_p), ("direct_radiance", C.c_void_p), ("indirect_radiance", C.c_void_p),
+        ("received_power", C.c_void_p), ("albedo", C.c_void_p), ("normal_global", C.c_void_p),
+        ("depth", C.c_void_p), ("alpha", C.c_void_p), ("triangle_id", C.c_void_p),
+        ("pixel_solid_angle", C.c_void_p), ("on_device", C.c_int32),
+    ]
+
+
+class BvhOptions(C.Structure):
+    _fields_ = [("max_leaf_size", C.c_uint32), ("builder", C.c_uint32), ("threads", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64), ("nodes_visited", C.c_uint64),
+        ("tris_tested", C.c_uint64), ("bvh_nodes", C.c_uint32), ("bvh_node_bytes", C.c_uint32),
+        ("tri_record_bytes", C.c_uint32), ("kernel_launches", C.c_uint32), ("device_error", C.c_uint32),
+        ("ms_last", C.c_float),
+    ]
+
+
+# exported symbol -> (restype, argtypes); the symbol list is the one include/vgb.h declares
+_P = C.c_void_p
+_U32 = C.c_uint32
+SIGNATURES = {
+    "vgb_context_create": (C.c_int, [C.POINTER(_P), C.c_int]),
+    "vgb_context_destroy": (C.c_int, [_P]),
+    "vgb_last_error": (C.c_char_p, [_P]),
+    "vgb_version": (C.c_char_p, []),
+    "vgb_set_stream": (C.c_int, [_P, _P]),
+    "vgb_synchronize": (C.c_int, [_P]),
+    "vgb_compute_vertex_normals": (C.c_int, [_P, _U32, _P, _U32, _P]),
+    "vgb_dem_triangulate": (C.c_int, [_P, _U32, _U32, C.c_double, C.c_double, _P, _P, C.POINTER(_U32)]),
+    "vgb_camera_intrinsics": (C.c_int, [C.c_float, C.c_float, C.c_float, _U32, _U32, C.c_float, C.c_float,
+                                        C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]),
+    "vgb_scene_upload": (C.c_int, [_P, _P, _U32, _P, _U32, _U32, _P, _P, _P, _P, _U32, _U32]),
+    "vgb_bvh_build": (C.c_int, [_P, C.POINTER(BvhOptions)]),
+    "vgb_pixel_solid_angle": (C.c_int, [_P, C.POINTER(Camera), _P, C.c_int]),
+    "vgb_render": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
+    "vgb_trace_rays": (C.c_int, [_P, _P, _P, _P, _U32, C.c_int, _P, _P, _P, C.c_int]),
+    "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
+    "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
+}
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "_build" / "libvgb.so"
+
+
+def load(build_if_missing: bool = True):
+    """Open libvgb.so (building it first if it is missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if build_if_missing:
+        from . import build as _build
+        _build.build()
+    if not path.exists():
+        raise RuntimeError(f"libvgb.so not found at {path}: run vira_gb300.build.build()")
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int, ctx=None, what: str = ""):
+    if status != 0:
+        msg = what
+        if ctx:
+            m = load().vgb_last_error(ctx)
+            msg = (what + ": " if what else "") + (m.decode() if m else "")
+        raise VgbError(status, msg)
+
+
+def ptr(a) -> int | None:
+    """Raw pointer of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

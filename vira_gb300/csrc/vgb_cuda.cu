@@ -1,0 +1,1152 @@
+// vgb_cuda.cu -- wavefront path-tracing kernels for sm_103a and the C ABI around them.
+//
+// Stages of one render (CPUPathTracer::render, cpu_path_tracer.ipp:29-161), per sample:
+//   k_extend  (bounce 0: camera rays over all pixels, 8x4-pixel warp tiles; bounce b>0: the
+//              compacted queue of live paths)  closest-hit traversal + processIntersection:
+//              AOVs, shading point, origin offset, NEE shadow-ray enqueue (one queue per light),
+//              cosine bounce sampling, throughput update, live-path enqueue (warp ballot);
+//   k_shadow  (one launch per light)  occlusion traversal of the queued shadow rays, adding
+//              each unoccluded contribution to the path's per-bounce radiance;
+//   k_end_sample  per pixel: folds the last bounce's radiance into the path and the path into
+//              the pixel; on the last sample writes the RenderPasses planes.
+// Path state, queues and accumulators are structure-of-arrays planes indexed by pixel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/vgb.h"
+#include "vgb_device.cuh"
+#include "vgb_internal.h"
+
+using namespace vgbd;
+
+#define VGB_MAX_LIGHTS 8
+
+namespace {
+
+// ------------------------------------------------------------------ device data
+struct DevScene {
+    const float4* nodes;
+    const float4* tris;
+    const uint32_t* idx;   // 3 per triangle, caller order
+    const float4* vpos;    // xyz
+    const float4* vnrm;    // xyz
+    const float2* vuv;
+    const float* valb;     // B per vertex
+    const float* tex;      // [th][tw][B]
+    uint32_t tw, th;
+};
+
+struct DevState {
+    // per-pixel path state
+    float* org;    // [3][P]
+    float* dir;    // [3][P]
+    float* thr;    // [B][P]
+    float* prad;   // [B][P]   radiance of the current sample's path
+    float* brad;   // [B][P]   radiance of the current bounce (ambient + NEE)
+    uint32_t* pend;  // [P]    0: nothing to fold, 1: bounce-0 radiance, 2: later bounce
+    // per-pixel accumulators over samples
+    float* arad;   // [B][P]
+    float* adir;   // [B][P]
+    float* aalb;   // [B][P]
+    float* anrm;   // [3][P]
+    float* adep;   // [P]
+    uint32_t* acnt;   // [P]
+    uint32_t* atri;   // [P]
+    // queues
+    uint32_t* pq[2];  // path queues (slots)
+    float* sq_org[VGB_MAX_LIGHTS];   // [3][P]
+    float* sq_dir[VGB_MAX_LIGHTS];   // [3][P]
+    float* sq_tmax[VGB_MAX_LIGHTS];  // [P]
+    uint32_t* sq_slot[VGB_MAX_LIGHTS];
+    float* sq_con[VGB_MAX_LIGHTS];   // [B][P]
+    uint32_t* counters;  // see C_* below
+    uint64_t* stats;     // [0] nodes, [1] tris, [2] closest rays, [3] shadow rays
+    size_t P;            // plane stride
+};
+
+enum { C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_ERR = 2 + VGB_MAX_LIGHTS, C_COUNT = 3 + VGB_MAX_LIGHTS };
+
+struct FrameParams {
+    vgb_camera cam;
+    vgb_pt_options opt;
+    vgb_light lights[VGB_MAX_LIGHTS];
+    uint32_t nlights;
+    uint32_t nb;
+    uint32_t tiles_x, tiles_y;
+};
+
+struct FilmOut {
+    float *total, *direct, *indirect, *power, *albedo, *normal, *depth, *alpha;
+    uint32_t* tri;
+    const float* omega;
+};
+
+__device__ __forceinline__ void warp_reduce_add(uint64_t* dst, uint32_t v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long*)dst, (unsigned long long)v);
+}
+
+// warp-aggregated queue append; every lane of the warp must call it
+__device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool pred) {
+    const unsigned mask = __ballot_sync(0xffffffffu, pred);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (mask) {
+        const int leader = __ffs(mask) - 1;
+        if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// SphereLight::sample with and without RNG (sphere_light.ipp:31-124)
+__device__ __forceinline__ void light_sample(const vgb_light& L, F3 p, bool det, float rand1, float rand2,
+                                             F3& dir, float& distance, float& pdf) {
+    F3 c{L.position[0], L.position[1], L.position[2]};
+    F3 ptl = c - p;
+    distance = length(ptl);
+    float dinv = 1.0f / distance;
+    float r = L.radius;
+    if (det) {
+        dir = dinv * ptl;
+        if (distance <= r) {
+            if (distance < 1e-3f) dir = F3{1, 0, 0};
+            distance = r;
+            pdf = 1.0f / (4.0f * kPi * r * r);
+            return;
+        }
+        float r2 = r * r;
+        float omega = 2 * kPi * (1.f - sqrtf((distance * distance) - r2) / distance);
+        pdf = 1.f / omega;
+        return;
+    }
+    F3 W = dinv * ptl;
+    F3 N1{1, 0, 0}, N2{0, 1, 0};
+    F3 N = (dot(N1, W) < dot(N2, W)) ? N1 : N2;
+    F3 Vv = normalize(cross(W, N));
+    F3 U = normalize(cross(W, Vv));
+    float phi = 2 * kPi * rand1;
+    float zeta = rand2;
+    float cc = r / distance;
+    float theta = acosf(1 - zeta + zeta * sqrtf(1 - (cc * cc)));
+    float sinT = sinf(theta), sinP = sinf(phi), cosT = cosf(theta), cosP = cosf(phi);
+    float a = cosP * sinT, b = cosT, e = sinP * sinT;
+    dir = F3{(a * U.x + b * W.x) + e * Vv.x, (a * U.y + b * W.y) + e * Vv.y, (a * U.z + b * W.z) + e * Vv.z};
+    float r2 = r * r;
+    float omega = 2 * kPi * (1.f - sqrtf((distance * distance) - r2) / distance);
+    pdf = 1.f / omega;
+}
+
+// SphereLight::getPDF (sphere_light.ipp:127-153)
+__device__ __forceinline__ float light_pdf(const vgb_light& L, F3 p, F3 dir) {
+    F3 c{L.position[0], L.position[1], L.position[2]};
+    F3 tc = c - p;
+    float dc = length(tc);
+    float r = L.radius;
+    if (dc <= r) return 1.0f / (4.0f * kPi * r * r);
+    F3 tcn{tc.x / dc, tc.y / dc, tc.z / dc};
+    float cosmax = sqrtf(1.0f - (r * r) / (dc * dc));
+    float ca = dot(dir, tcn);
+    if (ca < cosmax) return 0.0f;
+    float r2 = r * r, d2 = dc * dc;
+    float omega = 2 * kPi * (1.0f - sqrtf(d2 - r2) / dc);
+    return 1.0f / omega;
+}
+
+__device__ __forceinline__ float power_heuristic(float fpdf, float gpdf) {
+    float f = 1.0f * fpdf, g = 1.0f * gpdf;
+    return (f * f) / (f * f + g * g);
+}
+
+// ConcentricDiskSample + CosineHemisphereSample (sampling.ipp:53-84)
+__device__ __forceinline__ F3 cosine_sample(float rand1, float rand2) {
+    float ux = 2.f * rand1 - 1.f, uy = 2.f * rand2 - 1.f;
+    float dx, dy;
+    if (fabsf(ux) < 1e-6f && fabsf(uy) < 1e-6f) {
+        dx = 0; dy = 0;
+    } else {
+        float theta, r;
+        const float P4 = kPi / 4.0f, P2 = kPi / 2.0f;
+        if (fabsf(ux) > fabsf(uy)) { r = ux; theta = P4 * (uy / ux); }
+        else { r = uy; theta = P2 - P4 * (ux / uy); }
+        dx = r * cosf(theta); dy = r * sinf(theta);
+    }
+    float z = sqrtf(smax(0.f, 1 - dx * dx - dy * dy));
+    return F3{dx, dy, z};
+}
+
+// Image::sampleUVs + interpolatePixel (image.ipp:589-671), one band
+template <int NB>
+__device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float u, float v, float* out) {
+    float rx = (float)s.tw, ry = (float)s.th;
+    float px = fmodf(u * rx, rx), py = fmodf(v * ry, ry);
+    if (px < 0) px += rx;
+    if (py < 0) py += ry;
+    int x0 = (int)floorf(px), y0 = (int)floorf(py);
+    x0 = min(x0, (int)s.tw - 1); y0 = min(y0, (int)s.th - 1);
+    int x1 = min(x0 + 1, (int)s.tw - 1), y1 = min(y0 + 1, (int)s.th - 1);
+    float dx = px - (float)x0, dy = py - (float)y0;
+    const float* p00 = &s.tex[((size_t)y0 * s.tw + x0) * nb];
+    const float* p10 = &s.tex[((size_t)y0 * s.tw + x1) * nb];
+    const float* p01 = &s.tex[((size_t)y1 * s.tw + x0) * nb];
+    const float* p11 = &s.tex[((size_t)y1 * s.tw + x1) * nb];
+    float a = (1.f - dx) * (1.f - dy), b = dx * (1.f - dy), c = (1.f - dx) * dy, e = dx * dy;
+#pragma unroll
+    for (int k = 0; k < NB; ++k)
+        if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
+}
+
+// ------------------------------------------------------------------ k_extend
+template <int NB, bool COUNT>
+__global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
+                                                uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
+    const uint32_t nb = fp.nb;
+    const size_t P = st.P;
+    const uint32_t W = fp.cam.width, H = fp.cam.height;
+    const int lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
+    uint32_t* out_count = &st.counters[(in_q ^ 1u)];
+    uint32_t* out_q = st.pq[in_q ^ 1u];
+    const uint32_t* in_queue = st.pq[in_q];
+    uint32_t err = 0;
+    Counters cnt{0, 0};
+    uint32_t nclosest = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n_items; base += stride) {
+        const uint32_t item = base + lane;
+        bool active = item < n_items;
+        uint32_t slot = 0, pi = 0, pj = 0;
+        F3 ro{0, 0, 0}, rd{0, 0, 1};
+        float thr[NB];
+        float prad[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) { thr[k] = 1.f; prad[k] = 0.f; }
+        if (active) {
+            if (bounce == 0) {
+                const uint32_t tile = item >> 5, ln = item & 31u;
+                const uint32_t tx = tile % fp.tiles_x, ty = tile / fp.tiles_x;
+                pi = tx * 8u + (ln & 7u);
+                pj = ty * 4u + (ln >> 3);
+                active = (pi < W) && (pj < H);
+                slot = pj * W + pi;
+                if (active) {
+                    float X = (float)pi, Y = (float)pj;
+                    if (sample != 0) {
+                        U4 jr = philox(U4{slot, sample, fp.opt.frame, kSlotJitter}, (uint32_t)fp.opt.seed,
+                                       (uint32_t)(fp.opt.seed >> 32));
+                        X = X + u01(jr.x);
+                        Y = Y + u01(jr.y);
+                    }
+                    const float* K = fp.cam.kinv;
+                    float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
+                    float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
+                    F3 dc{hx, fp.cam.z_dir * hy, fp.cam.z_dir};
+                    const float* R = fp.cam.rotation;
+                    F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
+                          (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
+                    rd = normalize(dw);
+                    ro = F3{fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]};
+                    if (sample == 0) {
+#pragma unroll
+                        for (int k = 0; k < NB; ++k)
+                            if (k < (int)nb) { st.arad[k * P + slot] = 0.f; st.adir[k * P + slot] = 0.f; st.aalb[k * P + slot] = 0.f; }
+                        st.anrm[slot] = 0.f; st.anrm[P + slot] = 0.f; st.anrm[2 * P + slot] = 0.f;
+                        st.adep[slot] = 0.f; st.acnt[slot] = 0u; st.atri[slot] = VGB_NO_HIT;
+                    }
+                    st.pend[slot] = 0u;
+                }
+            } else {
+                slot = in_queue[item];
+                ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
+                rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
+                const uint32_t pend = st.pend[slot];
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (k < (int)nb) {
+                        thr[k] = st.thr[k * P + slot];
+                        prad[k] = st.prad[k * P + slot];
+                        if (pend) {
+                            const float br = st.brad[k * P + slot];
+                            prad[k] += br;
+                            if (pend == 1u) st.adir[k * P + slot] += br;
+                        }
+                    }
+                }
+                st.pend[slot] = 0u;
+            }
+        }
+        // ---- closest hit
+        HitOut h;
+        h.t = __int_as_float(0x7f800000); h.id = VGB_NO_HIT; h.U = h.V = h.W = 0.f; h.det = 1.f;
+        WRay wr = make_wray(ro, rd);
+        if (active) {
+            traverse<false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+            nclosest++;
+        }
+        bool hit = active && h.id != VGB_NO_HIT;
+        bool cont = false;
+        bool lit = false;  // hit and simulate_lighting: NEE runs for this lane
+        F3 Pp{0, 0, 0}, N{0, 0, 1};
+        float alb[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) alb[k] = 0.f;
+        U4 r0{0, 0, 0, 0};
+        const uint32_t k0 = (uint32_t)fp.opt.seed, k1 = (uint32_t)(fp.opt.seed >> 32);
+        if (active && !hit) {
+            if (fp.opt.simulate_lighting && fp.opt.show_background) {
+                float x = rd.x, y = rd.y, z = rd.z;
+                float u = atan2f(y, x) / (2 * kPi);
+                float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+                float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+                if (px < 0) px += 1.f;
+                if (py < 0) py += 1.f;
+                float dx = px - 0.f, dy = py - 0.f;
+                float a = (1.f - dx) * (1.f - dy), b = dx * (1.f - dy), c = (1.f - dx) * dy, e = dx * dy;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (k < (int)nb) {
+                        const float bgv = fp.opt.background[k];
+                        float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
+                        prad[k] += thr[k] * (bg * 1.f);
+                    }
+                }
+            }
+        }
+        F3 tg{1, 0, 0}, bt{0, 1, 0};
+        if (hit) {
+            // ---- processIntersection (cpu_path_tracer.ipp:280-469)
+            const uint32_t t = h.id;
+            const float rcp = 1.0f / h.det;
+            float w[3];
+            w[0] = h.V * rcp;
+            w[1] = h.W * rcp;
+            w[2] = 1.0f - w[0] - w[1];
+            const uint32_t i0 = __ldg(&s.idx[3 * t]), i1 = __ldg(&s.idx[3 * t + 1]), i2 = __ldg(&s.idx[3 * t + 2]);
+            const uint32_t vi[3] = {i1, i2, i0};
+            F3 vp[3], vn[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { vp[k] = ld3(__ldg(&s.vpos[vi[k]])); vn[k] = ld3(__ldg(&s.vnrm[vi[k]])); }
+            const float2 uva = __ldg(&s.vuv[vi[0]]), uvb = __ldg(&s.vuv[vi[1]]), uvc = __ldg(&s.vuv[vi[2]]);
+            const float uvx = (w[0] * uva.x + w[1] * uvb.x) + w[2] * uvc.x;
+            const float uvy = (w[0] * uva.y + w[1] * uvb.y) + w[2] * uvc.y;
+            // Triangle::init face normal from the caller's vertex order (v0, v1, v2) = (vp[2], vp[0], vp[1])
+            F3 fnn = normalize(cross(vp[2] - vp[0], vp[1] - vp[2]));
+            F3 fnrm{-fnn.x, -fnn.y, -fnn.z};
+            F3 Nl = fnrm;
+            if (fp.opt.smooth_shading) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
+            N = Nl;
+            F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
+            tg = normalize(cross(arb, N));
+            bt = cross(N, tg);
+            float texv[NB];
+            sample_uvs<NB>(s, nb, uvx, uvy, texv);
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k < (int)nb) {
+                    float va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
+                               w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
+                    alb[k] = va * texv[k];
+                }
+            }
+            Pp = (w[0] * vp[0] + w[1] * vp[1]) + w[2] * vp[2];
+            {
+                F3 q[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) q[k] = Pp - dot(Pp - vp[k], vn[k]) * vn[k];
+                F3 sp = (q[0] * w[0] + q[1] * w[1]) + q[2] * w[2];
+                if (dot(sp - Pp, Nl) > 0) Pp = sp;
+            }
+            if (bounce == 0) {
+                if (st.atri[slot] == VGB_NO_HIT) st.atri[slot] = t;
+#pragma unroll
+                for (int k = 0; k < NB; ++k)
+                    if (k < (int)nb) st.aalb[k * P + slot] += alb[k];
+                st.anrm[slot] += N.x; st.anrm[P + slot] += N.y; st.anrm[2 * P + slot] += N.z;
+                st.adep[slot] += h.t;
+                st.acnt[slot] += 1u;
+            }
+            if (fp.opt.simulate_lighting) {
+                lit = true;
+                Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (k < (int)nb)
+                        st.brad[k * P + slot] = (bounce == 0 && fp.opt.has_ambient) ? 0.f + thr[k] * (fp.opt.ambient[k] * alb[k]) : 0.f;
+                }
+                st.pend[slot] = (bounce == 0) ? 1u : 2u;
+                r0 = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | kSlotMain}, k0, k1);
+            }
+        }
+        // ---- NEE: one shadow ray per light, appended to that light's queue (warp ballot)
+        for (uint32_t l = 0; l < fp.nlights; ++l) {
+            bool pred = false;
+            F3 Ld{0, 0, 1};
+            float dist = 0.f, lpdf = 0.f, nl = 0.f, cos_t = 0.f, wgt = 0.f;
+            if (lit) {
+                float ru1, ru2;
+                if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                else {
+                    U4 rl = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | (1u + l)}, k0, k1);
+                    ru1 = u01(rl.x); ru2 = u01(rl.y);
+                }
+                light_sample(fp.lights[l], Pp, fp.opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                if (lpdf > 0) {
+                    pred = true;
+                    nl = dot(N, Ld);
+                    cos_t = smax(0.0f, dot(Ld, N));
+                    const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                    wgt = power_heuristic(lpdf, mpdf);
+                }
+            }
+            const uint32_t qi = warp_append(&st.counters[C_SQ + l], pred);
+            if (pred) {
+                st.sq_org[l][qi] = Pp.x; st.sq_org[l][P + qi] = Pp.y; st.sq_org[l][2 * P + qi] = Pp.z;
+                st.sq_dir[l][qi] = Ld.x; st.sq_dir[l][P + qi] = Ld.y; st.sq_dir[l][2 * P + qi] = Ld.z;
+                st.sq_tmax[l][qi] = dist;
+                st.sq_slot[l][qi] = slot;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    if (k < (int)nb) {
+                        const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+                        st.sq_con[l][k * P + qi] = thr[k] * bsdf * fp.lights[l].radiance[k] * cos_t * wgt / lpdf;
+                    }
+                }
+            }
+        }
+        // ---- BSDF-sampled continuation
+        if (lit && bounce < fp.opt.bounces) {
+            F3 ls = cosine_sample(u01(r0.z), u01(r0.w));
+            const float mpdf = ls.z * kInvPi;
+            F3 nd{(tg.x * ls.x + bt.x * ls.y) + N.x * ls.z, (tg.y * ls.x + bt.y * ls.y) + N.y * ls.z,
+                  (tg.z * ls.x + bt.z * ls.y) + N.z * ls.z};
+            cont = true;
+            if (mpdf > 0) {
+                const float nl = dot(N, nd);
+                const float cos_t = smax(0.0f, dot(nd, N));
+                float lp = 0;
+                for (uint32_t l = 0; l < fp.nlights; ++l) lp += light_pdf(fp.lights[l], Pp, nd);
+                lp /= (float)fp.nlights;
+                const float wgt = power_heuristic(mpdf, lp);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+                    if (k < (int)nb) thr[k] *= bsdf * cos_t * wgt / mpdf;
+                }
+                ro = Pp; rd = nd;
+                if (fp.opt.rr_depth != 0 && bounce + 1 >= fp.opt.rr_depth) {
+                    float q = 0.f;
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) if (k < (int)nb) q = smax(q, thr[k]);
+                    q = smin(q, 1.0f);
+                    const U4 rr = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | kSlotRR}, k0, k1);
+                    if (u01(rr.x) >= q) {
+                        cont = false;
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) if (k < (int)nb) thr[k] = thr[k] / q;
+                    }
+                }
+            }
+            // mpdf == 0: the reference keeps the incoming ray and throughput
+        }
+        // ---- write path state and append live paths
+        if (active) {
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k < (int)nb) {
+                    st.prad[k * P + slot] = prad[k];
+                    if (cont) st.thr[k * P + slot] = thr[k];
+                }
+            }
+            if (cont) {
+                st.org[slot] = ro.x; st.org[P + slot] = ro.y; st.org[2 * P + slot] = ro.z;
+                st.dir[slot] = rd.x; st.dir[P + slot] = rd.y; st.dir[2 * P + slot] = rd.z;
+            }
+        }
+        const uint32_t pqi = warp_append(out_count, cont);
+        if (cont) out_q[pqi] = slot;
+    }
+    if (err) atomicOr(&st.counters[C_ERR], err);
+    warp_reduce_add(&st.stats[2], nclosest);
+    if (COUNT) {
+        warp_reduce_add(&st.stats[0], cnt.nodes);
+        warp_reduce_add(&st.stats[1], cnt.tris);
+    }
+}
+
+// ------------------------------------------------------------------ k_shadow
+template <int NB, bool COUNT>
+__global__ void __launch_bounds__(256) k_shadow(const DevScene s, DevState st, uint32_t light, uint32_t nb) {
+    const size_t P = st.P;
+    const uint32_t n = st.counters[C_SQ + light];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t err = 0, nsh = 0;
+    Counters cnt{0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        F3 o{st.sq_org[light][i], st.sq_org[light][P + i], st.sq_org[light][2 * P + i]};
+        F3 d{st.sq_dir[light][i], st.sq_dir[light][P + i], st.sq_dir[light][2 * P + i]};
+        const float tmax = st.sq_tmax[light][i];
+        WRay wr = make_wray(o, d);
+        HitOut h;
+        traverse<true, COUNT>(s.nodes, s.tris, wr, tmax, h, err, cnt);
+        nsh++;
+        if (h.id == VGB_NO_HIT) {
+            const uint32_t slot = st.sq_slot[light][i];
+#pragma unroll
+            for (int k = 0; k < NB; ++k)
+                if (k < (int)nb) st.brad[k * P + slot] += st.sq_con[light][k * P + i];
+        }
+    }
+    if (err) atomicOr(&st.counters[C_ERR], err);
+    warp_reduce_add(&st.stats[3], nsh);
+    if (COUNT) {
+        warp_reduce_add(&st.stats[0], cnt.nodes);
+        warp_reduce_add(&st.stats[1], cnt.tris);
+    }
+}
+
+// ------------------------------------------------------------------ k_end_sample
+template <int NB>
+__global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_constant__ FrameParams fp, uint32_t last, FilmOut f) {
+    const size_t P = st.P;
+    const uint32_t nb = fp.nb;
+    const uint32_t npix = fp.cam.width * fp.cam.height;
+    const float sf = (float)fp.opt.samples;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const uint32_t pend = st.pend[p];
+        float tot[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k < (int)nb) {
+                float pr = st.prad[k * P + p];
+                if (pend) {
+                    const float br = st.brad[k * P + p];
+                    pr += br;
+                    if (pend == 1u) st.adir[k * P + p] += br;
+                }
+                tot[k] = st.arad[k * P + p] + pr;
+                st.arad[k * P + p] = tot[k];
+            }
+        }
+        st.pend[p] = 0u;
+        if (!last) continue;
+        // unidirectional (cpu_path_tracer.ipp:229-240) + RenderPasses::updateImages (passes.ipp:82-128)
+        const uint32_t count = st.acnt[p];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k < (int)nb) {
+                const float total = tot[k] / sf;
+                const float direct = st.adir[k * P + p] / sf;
+                if (f.total) f.total[k * P + p] = total;
+                if (f.direct) f.direct[k * P + p] = direct;
+                if (f.indirect) f.indirect[k * P + p] = total - direct;
+                if (f.albedo) f.albedo[k * P + p] = st.aalb[k * P + p] / sf;
+                if (f.power) f.power[k * P + p] = (fp.cam.power_scale[k] * f.omega[p]) * total;
+            }
+        }
+        if (f.normal) {
+            F3 n = normalize(F3{st.anrm[p], st.anrm[P + p], st.anrm[2 * P + p]});
+            f.normal[p] = n.x; f.normal[P + p] = n.y; f.normal[2 * P + p] = n.z;
+        }
+        if (f.depth) f.depth[p] = (count == 0) ? __int_as_float(0x7f800000) : st.adep[p] / (float)count;
+        if (f.alpha) f.alpha[p] = (float)count / sf;
+        if (f.tri) f.tri[p] = st.atri[p];
+    }
+}
+
+// ------------------------------------------------------------------ pixel solid angle (FP64)
+__device__ double3 corner_dir(const vgb_camera& c, double x, double y) {
+    const float* K = c.kinv;
+    double hx = ((double)K[0] * x + (double)K[2] * y) + (double)K[4] * 1.0;
+    double hy = ((double)K[1] * x + (double)K[3] * y) + (double)K[5] * 1.0;
+    double zd = (double)c.z_dir;
+    double vx = hx, vy = zd * hy, vz = zd;
+    double s = 1.0 / sqrt((vx * vx + vy * vy) + vz * vz);
+    return make_double3(vx * s, vy * s, vz * s);
+}
+__device__ double3 dcross(double3 a, double3 b) {
+    return make_double3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+__device__ double ddot(double3 a, double3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ double3 dtangent(double3 p0, double3 p1) {
+    double3 p = make_double3(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z);
+    double3 t = dcross(dcross(p0, p), p0);
+    double s = 1.0 / sqrt(ddot(t, t));
+    return make_double3(t.x * s, t.y * s, t.z * s);
+}
+__device__ double tri_omega(double3 c0, double3 c1, double3 c2) {
+    double a0 = acos(ddot(dtangent(c0, c1), dtangent(c0, c2)));
+    double a1 = acos(ddot(dtangent(c1, c0), dtangent(c1, c2)));
+    double a2 = acos(ddot(dtangent(c2, c0), dtangent(c2, c1)));
+    return ((a0 + a1) + a2) - 3.141592653589793238462;
+}
+__global__ void k_pixel_solid_angle(const vgb_camera cam, float* out) {
+    const uint32_t W = cam.width, H = cam.height;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W * H; p += gridDim.x * blockDim.x) {
+        const uint32_t i = p % W, j = p / W;
+        double3 c0 = corner_dir(cam, i, j), c1 = corner_dir(cam, i + 1, j);
+        double3 c2 = corner_dir(cam, i + 1, j + 1), c3 = corner_dir(cam, i, j + 1);
+        out[p] = (float)(tri_omega(c0, c1, c2) + tri_omega(c0, c2, c3));
+    }
+}
+
+// ------------------------------------------------------------------ batch trace (TLAS::intersect seam)
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(256) k_trace(const DevScene s, const float* org, const float* dir, const float* tmax,
+                                               uint32_t n, uint32_t* tri, float* tout, float* bary,
+                                               uint32_t* counters, uint64_t* stats) {
+    uint32_t err = 0;
+    Counters cnt{0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        F3 o{org[3 * i], org[3 * i + 1], org[3 * i + 2]};
+        F3 d{dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]};
+        WRay wr = make_wray(o, d);
+        HitOut h;
+        h.U = h.V = h.W = 0.f; h.det = 1.f;
+        traverse<ANY, COUNT>(s.nodes, s.tris, wr, tmax ? tmax[i] : __int_as_float(0x7f800000), h, err, cnt);
+        tri[i] = h.id;
+        if (tout) tout[i] = h.t;
+        if (bary) {
+            float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+            if (h.id != VGB_NO_HIT && !ANY) {
+                const float rcp = 1.0f / h.det;
+                w0 = h.V * rcp; w1 = h.W * rcp; w2 = 1.0f - w0 - w1;
+            }
+            bary[3 * i] = w0; bary[3 * i + 1] = w1; bary[3 * i + 2] = w2;
+        }
+    }
+    if (err) atomicOr(&counters[C_ERR], err);
+    if (COUNT) {
+        warp_reduce_add(&stats[0], cnt.nodes);
+        warp_reduce_add(&stats[1], cnt.tris);
+    }
+}
+
+}  // namespace
+
+// ====================================================================== context
+struct vgb_context {
+    int device = 0;
+    int num_sms = 1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // scene
+    uint32_t nverts = 0, ntris = 0, nbands = 0;
+    float4* d_vpos = nullptr;
+    float4* d_vnrm = nullptr;
+    float2* d_vuv = nullptr;
+    float* d_valb = nullptr;
+    uint32_t* d_idx = nullptr;
+    float* d_tex = nullptr;
+    uint32_t tw = 1, th = 1;
+    std::vector<float> h_pos;   // kept for the BVH build
+    std::vector<uint32_t> h_idx;
+    // BVH
+    float4* d_nodes = nullptr;
+    float4* d_tris = nullptr;
+    uint32_t nnodes = 0;
+    bool bvh_ready = false;
+    // render scratch
+    size_t cap_P = 0;
+    uint32_t cap_B = 0, cap_L = 0;
+    std::vector<void*> scratch;
+    DevState st{};
+    uint32_t* d_counters = nullptr;
+    uint64_t* d_stats = nullptr;
+    // staging for host films / host rays
+    std::vector<void*> staging;
+    size_t staging_bytes = 0;
+    void* staging_base = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    vgb_stats stats{};
+    bool count_pass = false;
+};
+
+namespace {
+
+vgb_status fail(vgb_context* c, vgb_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? VGB_ERR_OUT_OF_MEMORY : VGB_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+        }                                                                                         \
+    } while (0)
+
+template <typename T>
+vgb_status dalloc(vgb_context* ctx, T** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc((void**)p, bytes);
+    if (e != cudaSuccess) return fail(ctx, VGB_ERR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return VGB_OK;
+}
+
+void dfree(void* p) { if (p) cudaFree(p); }
+
+void free_scene(vgb_context* ctx) {
+    dfree(ctx->d_vpos); dfree(ctx->d_vnrm); dfree(ctx->d_vuv); dfree(ctx->d_valb); dfree(ctx->d_idx); dfree(ctx->d_tex);
+    ctx->d_vpos = nullptr; ctx->d_vnrm = nullptr; ctx->d_vuv = nullptr; ctx->d_valb = nullptr; ctx->d_idx = nullptr; ctx->d_tex = nullptr;
+}
+void free_bvh(vgb_context* ctx) {
+    dfree(ctx->d_nodes); dfree(ctx->d_tris);
+    ctx->d_nodes = nullptr; ctx->d_tris = nullptr; ctx->bvh_ready = false; ctx->nnodes = 0;
+}
+void free_scratch(vgb_context* ctx) {
+    for (void* p : ctx->scratch) dfree(p);
+    ctx->scratch.clear();
+    ctx->cap_P = 0; ctx->cap_B = 0; ctx->cap_L = 0;
+}
+void free_staging(vgb_context* ctx) {
+    dfree(ctx->staging_base);
+    ctx->staging_base = nullptr;
+    ctx->staging_bytes = 0;
+}
+
+vgb_status ensure_staging(vgb_context* ctx, size_t bytes) {
+    if (bytes <= ctx->staging_bytes) return VGB_OK;
+    free_staging(ctx);
+    vgb_status s = dalloc(ctx, &ctx->staging_base, bytes);
+    if (s != VGB_OK) return s;
+    ctx->staging_bytes = bytes;
+    return VGB_OK;
+}
+
+vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
+    if (P <= ctx->cap_P && B <= ctx->cap_B && L <= ctx->cap_L) return VGB_OK;
+    P = std::max(P, ctx->cap_P);
+    B = std::max(B, ctx->cap_B);
+    L = std::max(L, ctx->cap_L);
+    free_scratch(ctx);
+    DevState& st = ctx->st;
+    auto A = [&](auto** p, size_t n) -> vgb_status {
+        vgb_status s = dalloc(ctx, p, n);
+        if (s == VGB_OK) ctx->scratch.push_back((void*)*p);
+        return s;
+    };
+    vgb_status s = VGB_OK;
+    const size_t f = sizeof(float), u = sizeof(uint32_t);
+#define AL(ptr, n) do { s = A(&(ptr), (n)); if (s != VGB_OK) { free_scratch(ctx); return s; } } while (0)
+    AL(st.org, 3 * P * f); AL(st.dir, 3 * P * f); AL(st.thr, B * P * f); AL(st.prad, B * P * f);
+    AL(st.brad, B * P * f); AL(st.pend, P * u);
+    AL(st.arad, B * P * f); AL(st.adir, B * P * f); AL(st.aalb, B * P * f); AL(st.anrm, 3 * P * f);
+    AL(st.adep, P * f); AL(st.acnt, P * u); AL(st.atri, P * u);
+    AL(st.pq[0], P * u); AL(st.pq[1], P * u);
+    for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
+        if (l < L) {
+            AL(st.sq_org[l], 3 * P * f); AL(st.sq_dir[l], 3 * P * f); AL(st.sq_tmax[l], P * f);
+            AL(st.sq_slot[l], P * u); AL(st.sq_con[l], B * P * f);
+        } else {
+            st.sq_org[l] = st.sq_dir[l] = st.sq_tmax[l] = st.sq_con[l] = nullptr; st.sq_slot[l] = nullptr;
+        }
+    }
+#undef AL
+    st.counters = ctx->d_counters;
+    st.stats = ctx->d_stats;
+    st.P = P;
+    ctx->cap_P = P; ctx->cap_B = B; ctx->cap_L = L;
+    return VGB_OK;
+}
+
+DevScene dev_scene(const vgb_context* ctx) {
+    DevScene s;
+    s.nodes = ctx->d_nodes; s.tris = ctx->d_tris; s.idx = ctx->d_idx; s.vpos = ctx->d_vpos; s.vnrm = ctx->d_vnrm;
+    s.vuv = ctx->d_vuv; s.valb = ctx->d_valb; s.tex = ctx->d_tex; s.tw = ctx->tw; s.th = ctx->th;
+    return s;
+}
+
+int grid_for(const vgb_context* ctx, size_t n, int per_sm = 8) {
+    size_t blocks = (n + 255) / 256;
+    size_t cap = (size_t)ctx->num_sms * per_sm;
+    return (int)std::max<size_t>(1, std::min(blocks, cap));
+}
+
+template <int NB, bool COUNT>
+void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
+    const DevScene s = dev_scene(ctx);
+    DevState st = ctx->st;
+    const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
+    const int g0 = grid_for(ctx, n0);
+    const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
+    for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
+        uint32_t q = 0;
+        for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
+            // reset the output path queue and the shadow queues
+            cudaMemsetAsync(&ctx->d_counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
+            cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
+            k_extend<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            launches++;
+            for (uint32_t l = 0; l < fp.nlights; ++l) {
+                k_shadow<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                launches++;
+            }
+            q ^= 1u;
+        }
+        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        launches++;
+    }
+}
+
+template <bool COUNT>
+void dispatch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
+    if (fp.nb <= 1) launch_render<1, COUNT>(ctx, fp, film, launches);
+    else if (fp.nb <= 4) launch_render<4, COUNT>(ctx, fp, film, launches);
+    else launch_render<8, COUNT>(ctx, fp, film, launches);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+VGB_API const char* vgb_version(void) { return "vira_gb300 0.1 (sm_103a)"; }
+
+VGB_API vgb_status vgb_context_create(vgb_context** out, int device) {
+    if (!out) return VGB_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    vgb_context* ctx = new (std::nothrow) vgb_context();
+    if (!ctx) return VGB_ERR_OUT_OF_MEMORY;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n) {
+        delete ctx;
+        return VGB_ERR_CUDA;
+    }
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return VGB_ERR_CUDA; }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { delete ctx; return VGB_ERR_CUDA; }
+    ctx->own_stream = true;
+    if (cudaMalloc(&ctx->d_counters, sizeof(uint32_t) * C_COUNT) != cudaSuccess ||
+        cudaMalloc(&ctx->d_stats, sizeof(uint64_t) * 8) != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return VGB_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemset(ctx->d_counters, 0, sizeof(uint32_t) * C_COUNT);
+    cudaMemset(ctx->d_stats, 0, sizeof(uint64_t) * 8);
+    cudaEventCreate(&ctx->ev0);
+    cudaEventCreate(&ctx->ev1);
+    *out = ctx;
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_scene(ctx); free_bvh(ctx); free_scratch(ctx); free_staging(ctx);
+    dfree(ctx->d_counters); dfree(ctx->d_stats);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return VGB_OK;
+}
+
+VGB_API const char* vgb_last_error(const vgb_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+VGB_API vgb_status vgb_set_stream(vgb_context* ctx, void* stream) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    if (stream) { ctx->stream = (cudaStream_t)stream; ctx->own_stream = false; }
+    else { CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)); ctx->own_stream = true; }
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_synchronize(vgb_context* ctx) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t nverts, const uint32_t* idx,
+                                    uint32_t ntris, uint32_t nbands, const float* valb, const float* vnrm,
+                                    const float* vuv, const float* tex, uint32_t tw, uint32_t th) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!pos || !idx || nverts == 0 || ntris == 0)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_upload: empty mesh or null buffer");
+    if (nbands == 0 || nbands > VGB_MAX_BANDS)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_upload: nbands must be 1..8");
+    if (tex && (tw == 0 || th == 0)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_upload: empty texture");
+    for (size_t k = 0; k < (size_t)3 * ntris; ++k)
+        if (idx[k] >= nverts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_upload: index out of range");
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    free_scene(ctx);
+    free_bvh(ctx);
+    ctx->nverts = nverts; ctx->ntris = ntris; ctx->nbands = nbands;
+    std::vector<float> nrm;
+    if (!vnrm) {
+        nrm.resize(3 * (size_t)nverts);
+        vgb_status s = vgb_compute_vertex_normals(pos, nverts, idx, ntris, nrm.data());
+        if (s != VGB_OK) return fail(ctx, s, "scene_upload: normals");
+        vnrm = nrm.data();
+    }
+    std::vector<float4> p4(nverts), n4(nverts);
+    for (uint32_t v = 0; v < nverts; ++v) {
+        p4[v] = make_float4(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2], 0.f);
+        n4[v] = make_float4(vnrm[3 * v], vnrm[3 * v + 1], vnrm[3 * v + 2], 0.f);
+    }
+    std::vector<float2> uv2(nverts, make_float2(0.f, 0.f));
+    if (vuv) for (uint32_t v = 0; v < nverts; ++v) uv2[v] = make_float2(vuv[2 * v], vuv[2 * v + 1]);
+    std::vector<float> alb;
+    if (!valb) { alb.assign((size_t)nverts * nbands, 1.f); valb = alb.data(); }
+    std::vector<float> one;
+    if (!tex) { one.assign(nbands, 1.f); tex = one.data(); tw = th = 1; }
+    vgb_status s;
+    if ((s = dalloc(ctx, &ctx->d_vpos, sizeof(float4) * nverts)) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_vnrm, sizeof(float4) * nverts)) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_vuv, sizeof(float2) * nverts)) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_valb, sizeof(float) * nverts * (size_t)nbands)) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_idx, sizeof(uint32_t) * 3 * (size_t)ntris)) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_tex, sizeof(float) * (size_t)tw * th * nbands)) != VGB_OK) return s;
+    CK(cudaMemcpy(ctx->d_vpos, p4.data(), sizeof(float4) * nverts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_vnrm, n4.data(), sizeof(float4) * nverts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_vuv, uv2.data(), sizeof(float2) * nverts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_valb, valb, sizeof(float) * nverts * (size_t)nbands, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_idx, idx, sizeof(uint32_t) * 3 * (size_t)ntris, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tex, tex, sizeof(float) * (size_t)tw * th * nbands, cudaMemcpyHostToDevice));
+    ctx->tw = tw; ctx->th = th;
+    ctx->h_pos.assign(pos, pos + 3 * (size_t)nverts);
+    ctx->h_idx.assign(idx, idx + 3 * (size_t)ntris);
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "bvh_build: no scene uploaded");
+    uint32_t leaf = opts ? opts->max_leaf_size : 0, threads = opts ? opts->threads : 0;
+    if (opts && opts->builder != 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: unknown builder");
+    if (leaf > vgb::kMaxLeaf) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8");
+    vgb::BvhHost bvh;
+    const char* why = "";
+    if (!vgb::build_bvh2(ctx->h_pos.data(), ctx->nverts, ctx->h_idx.data(), ctx->ntris, leaf, threads, bvh, &why))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("bvh_build: ") + why);
+    cudaSetDevice(ctx->device);
+    free_bvh(ctx);
+    vgb_status s;
+    if ((s = dalloc(ctx, &ctx->d_nodes, bvh.nodes.size() * sizeof(float))) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_tris, bvh.tris.size() * sizeof(float))) != VGB_OK) return s;
+    CK(cudaMemcpy(ctx->d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->nnodes = bvh.num_nodes;
+    ctx->bvh_ready = true;
+    ctx->stats.bvh_nodes = bvh.num_nodes;
+    ctx->stats.bvh_node_bytes = 64;
+    ctx->stats.tri_record_bytes = 48;
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam, float* out, int on_device) {
+    if (!ctx || !cam || !out) return VGB_ERR_INVALID_ARGUMENT;
+    if (cam->width == 0 || cam->height == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "pixel_solid_angle: empty image");
+    cudaSetDevice(ctx->device);
+    const size_t n = (size_t)cam->width * cam->height;
+    float* d = out;
+    if (!on_device) {
+        vgb_status s = ensure_staging(ctx, n * sizeof(float));
+        if (s != VGB_OK) return s;
+        d = (float*)ctx->staging_base;
+    }
+    k_pixel_solid_angle<<<grid_for(ctx, n, 16), 256, 0, ctx->stream>>>(*cam, d);
+    CK(cudaGetLastError());
+    if (!on_device) CK(cudaMemcpyAsync(out, d, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    ctx->count_pass = enable != 0;
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out) {
+    if (!ctx || !out) return VGB_ERR_INVALID_ARGUMENT;
+    *out = ctx->stats;
+    return VGB_OK;
+}
+
+static vgb_status check_device_error(vgb_context* ctx) {
+    uint32_t e = 0;
+    CK(cudaMemcpy(&e, &ctx->d_counters[C_ERR], sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    ctx->stats.device_error = e;
+    if (e) {
+        CK(cudaMemset(&ctx->d_counters[C_ERR], 0, sizeof(uint32_t)));
+        return fail(ctx, VGB_ERR_DEVICE_LIMIT,
+                    std::string("device traversal limit hit:") + ((e & kErrStack) ? " stack" : "") +
+                        ((e & kErrIter) ? " iterations" : ""));
+    }
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                              const vgb_pt_options* opts, vgb_film* film) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: null camera/options/film");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render: build the BVH first");
+    if (opts->samples == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: options.samples must be >= 1");
+    if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: nbands differs from the scene");
+    if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: at most 8 lights");
+    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > (1ull << 31))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: bad resolution");
+    if (film->received_power && !film->pixel_solid_angle)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: received_power needs pixel_solid_angle");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)cam->width * cam->height;
+    const uint32_t B = ctx->nbands;
+    vgb_status s = ensure_scratch(ctx, P, B, std::max<uint32_t>(1, nlights));
+    if (s != VGB_OK) return s;
+    FrameParams fp;
+    std::memset(&fp, 0, sizeof(fp));
+    fp.cam = *cam;
+    fp.opt = *opts;
+    for (uint32_t l = 0; l < nlights; ++l) fp.lights[l] = lights[l];
+    fp.nlights = nlights;
+    fp.nb = B;
+    fp.tiles_x = (cam->width + 7) / 8;
+    fp.tiles_y = (cam->height + 3) / 4;
+    // film planes: device pointers as given, or staging buffers for host films
+    FilmOut f{};
+    struct Plane { float** host_f; uint32_t** host_u; size_t n; };
+    float* hf[8] = {film->total_radiance, film->direct_radiance, film->indirect_radiance, film->received_power,
+                    film->albedo, film->normal_global, film->depth, film->alpha};
+    const size_t nplane[8] = {B * P, B * P, B * P, B * P, B * P, 3 * P, P, P};
+    float* df[8];
+    uint32_t* dtri = film->triangle_id;
+    const float* domega = film->pixel_solid_angle;
+    if (film->on_device) {
+        for (int k = 0; k < 8; ++k) df[k] = hf[k];
+    } else {
+        size_t total = 0;
+        for (int k = 0; k < 8; ++k) if (hf[k]) total += nplane[k];
+        total += P + (film->pixel_solid_angle ? P : 0);
+        if ((s = ensure_staging(ctx, total * sizeof(float))) != VGB_OK) return s;
+        float* cur = (float*)ctx->staging_base;
+        for (int k = 0; k < 8; ++k) { df[k] = hf[k] ? cur : nullptr; if (hf[k]) cur += nplane[k]; }
+        dtri = film->triangle_id ? (uint32_t*)cur : nullptr;
+        cur += P;
+        if (film->pixel_solid_angle) {
+            CK(cudaMemcpyAsync(cur, film->pixel_solid_angle, P * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+            domega = cur;
+        }
+    }
+    f.total = df[0]; f.direct = df[1]; f.indirect = df[2]; f.power = df[3]; f.albedo = df[4];
+    f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+    uint32_t launches = 0;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    dispatch_render<false>(ctx, fp, f, launches);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!film->on_device) {
+        for (int k = 0; k < 8; ++k)
+            if (hf[k]) CK(cudaMemcpyAsync(hf[k], df[k], nplane[k] * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (film->triangle_id) CK(cudaMemcpyAsync(film->triangle_id, dtri, P * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    uint64_t hs[8];
+    CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    ctx->stats.rays_closest = hs[2];
+    ctx->stats.rays_shadow = hs[3];
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.ms_last = ms;
+    ctx->stats.nodes_visited = 0;
+    ctx->stats.tris_tested = 0;
+    if ((s = check_device_error(ctx)) != VGB_OK) return s;
+    if (ctx->count_pass) {
+        // counting pass: same kernels with traversal counters, into scratch film planes
+        FilmOut none{};
+        none.omega = domega;
+        none.power = nullptr;
+        CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+        uint32_t l2 = 0;
+        dispatch_render<true>(ctx, fp, none, l2);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+        ctx->stats.nodes_visited = hs[0];
+        ctx->stats.tris_tested = hs[1];
+        if ((s = check_device_error(ctx)) != VGB_OK) return s;
+    }
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const float* dir, const float* tmax,
+                                  uint32_t n, int any_hit, uint32_t* tri, float* tout, float* bary, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!org || !dir || !tri) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "trace_rays: null buffer");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "trace_rays: build the BVH first");
+    if (n == 0) return VGB_OK;
+    cudaSetDevice(ctx->device);
+    const float *dorg = org, *ddir = dir, *dtmax = tmax;
+    uint32_t* dtri = tri;
+    float *dt = tout, *db = bary;
+    vgb_status s;
+    if (!on_device) {
+        size_t need = (size_t)n * (3 + 3 + (tmax ? 1 : 0) + 1 + (tout ? 1 : 0) + (bary ? 3 : 0));
+        if ((s = ensure_staging(ctx, need * 4)) != VGB_OK) return s;
+        float* cur = (float*)ctx->staging_base;
+        float* o2 = cur; cur += 3 * (size_t)n;
+        float* d2 = cur; cur += 3 * (size_t)n;
+        float* m2 = nullptr; if (tmax) { m2 = cur; cur += n; }
+        uint32_t* r2 = (uint32_t*)cur; cur += n;
+        float* t2 = nullptr; if (tout) { t2 = cur; cur += n; }
+        float* b2 = nullptr; if (bary) { b2 = cur; cur += 3 * (size_t)n; }
+        CK(cudaMemcpyAsync(o2, org, 12 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d2, dir, 12 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        if (tmax) CK(cudaMemcpyAsync(m2, tmax, 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        dorg = o2; ddir = d2; dtmax = m2; dtri = r2; dt = t2; db = b2;
+    }
+    const DevScene sc = dev_scene(ctx);
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const int g = grid_for(ctx, n);
+    if (any_hit) {
+        if (ctx->count_pass) k_trace<true, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+        else k_trace<true, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+    } else {
+        if (ctx->count_pass) k_trace<false, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+        else k_trace<false, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+    }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!on_device) {
+        CK(cudaMemcpyAsync(tri, dtri, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (tout) CK(cudaMemcpyAsync(tout, dt, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (bary) CK(cudaMemcpyAsync(bary, db, 12 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    uint64_t hs[8];
+    CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    ctx->stats.ms_last = ms;
+    ctx->stats.kernel_launches = 1;
+    ctx->stats.nodes_visited = hs[0];
+    ctx->stats.tris_tested = hs[1];
+    if (any_hit) { ctx->stats.rays_shadow = n; ctx->stats.rays_closest = 0; }
+    else { ctx->stats.rays_closest = n; ctx->stats.rays_shadow = 0; }
+    return check_device_error(ctx);
+}
+
+}  // extern "C"

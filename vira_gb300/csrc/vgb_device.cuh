@@ -1,0 +1,215 @@
+// vgb_device.cuh -- device helpers of the hot path: counter-based RNG, the reference's FP32
+// expression order, the watertight ray/triangle test and BVH traversal.
+//
+// The translation unit is compiled with --fmad=false: every `a * b + c` below rounds the
+// product and the sum separately, exactly as the oracle (built with -ffp-contract=off) and
+// the reference's glm code do.  Fused multiply-adds appear only where written explicitly.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/vgb.h"
+
+namespace vgbd {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = (float)(1. / 3.141592653589793238462);
+constexpr uint32_t kSlotMain = 0u, kSlotRR = 0xFEu, kSlotJitter = 0xFFu;
+
+// device error word bits
+constexpr uint32_t kErrStack = 1u, kErrIter = 2u;
+
+constexpr int kStackSize = 64;
+constexpr uint32_t kIterCap = 1u << 22;  // traversal steps per ray before giving up
+
+// ------------------------------------------------------------------ Philox-4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011.
+struct U4 { uint32_t x, y, z, w; };
+__device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += W0; k1 += W1; }
+        uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    }
+    return c;
+}
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// std::max / std::min semantics (first argument wins on NaN comparisons)
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+
+struct F3 { float x, y, z; };
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator*(float s, F3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) {
+    return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y};
+}
+__device__ __forceinline__ float length(F3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ F3 normalize(F3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
+__device__ __forceinline__ float pick(F3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+__device__ __forceinline__ F3 ld3(const float4& v) { return F3{v.x, v.y, v.z}; }
+
+// offsetIntersection, float path (include/implementation/rendering/ray.ipp:107-123)
+__device__ __forceinline__ float offset1(float p, float n) {
+    const float origin = 1.f / 32.f, float_scale = 1.f / 65536.f, int_scale = 256.f;
+    int32_t of = (int32_t)(int_scale * n);
+    int32_t pi = __float_as_int(p) + ((p < 0) ? -of : of);
+    return (fabsf(p) < origin) ? p + float_scale * n : __int_as_float(pi);
+}
+
+// ------------------------------------------------------------------ watertight test
+// Woop, Benthin, Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1), 2013.
+struct WRay {
+    F3 o, d;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+    float ix, iy, iz;  // slab reciprocals, |d| clamped away from 0
+};
+
+__device__ __forceinline__ float safe_rcp(float d) {
+    const float tiny = 1e-30f;
+    float a = fabsf(d) < tiny ? copysignf(tiny, d) : d;
+    return 1.0f / a;
+}
+
+__device__ __forceinline__ WRay make_wray(F3 o, F3 d) {
+    WRay r;
+    r.o = o; r.d = d;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    if (pick(d, kz) < 0.0f) { int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    float dz = pick(d, kz);
+    r.Sx = pick(d, kx) / dz;
+    r.Sy = pick(d, ky) / dz;
+    r.Sz = 1.0f / dz;
+    r.ix = safe_rcp(d.x); r.iy = safe_rcp(d.y); r.iz = safe_rcp(d.z);
+    return r;
+}
+
+// Returns false on a miss.  t > 0 required.  U, V, W: unnormalised weights of v0, v1, v2.
+__device__ __forceinline__ bool wt_test(const WRay& r, F3 v0, F3 v1, F3 v2, float& t_out, float& U_out,
+                                        float& V_out, float& W_out, float& det_out) {
+    F3 A = v0 - r.o, B = v1 - r.o, C = v2 - r.o;
+    float Akz = pick(A, r.kz), Bkz = pick(B, r.kz), Ckz = pick(C, r.kz);
+    float Ax = pick(A, r.kx) - r.Sx * Akz;
+    float Ay = pick(A, r.ky) - r.Sy * Akz;
+    float Bx = pick(B, r.kx) - r.Sx * Bkz;
+    float By = pick(B, r.ky) - r.Sy * Bkz;
+    float Cx = pick(C, r.kx) - r.Sx * Ckz;
+    float Cy = pick(C, r.ky) - r.Sy * Ckz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        double CxBy = (double)Cx * (double)By, CyBx = (double)Cy * (double)Bx;
+        U = (float)(CxBy - CyBx);
+        double AxCy = (double)Ax * (double)Cy, AyCx = (double)Ay * (double)Cx;
+        V = (float)(AxCy - AyCx);
+        double BxAy = (double)Bx * (double)Ay, ByAx = (double)By * (double)Ax;
+        W = (float)(BxAy - ByAx);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float T = (U * (r.Sz * Akz) + V * (r.Sz * Bkz)) + W * (r.Sz * Ckz);
+    float t = T * (1.0f / det);
+    if (!(t > 0.0f)) return false;
+    t_out = t; U_out = U; V_out = V; W_out = W; det_out = det;
+    return true;
+}
+
+// ------------------------------------------------------------------ BVH2 traversal
+struct HitOut {
+    float t;
+    uint32_t id;
+    float U, V, W, det;
+};
+
+struct Counters { uint32_t nodes, tris; };
+
+// Closest hit (ANY = false; ties in t go to the smaller id) or occlusion (ANY = true, any
+// hit with t <= tmax).  Box tests are conservative: slab distances (lo - o) * (1/d) carry a
+// relative error below 2*gamma(3) (Ize 2013), and the exit distance is widened by 2^-20.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                         const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+    const float widen = 1.0f + 0x1p-20f;
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0;
+    float best = ANY ? tmax : __int_as_float(0x7f800000);
+    h.t = __int_as_float(0x7f800000);
+    h.id = VGB_NO_HIT;
+    uint32_t iter = 0;
+    const float ox = r.o.x, oy = r.o.y, oz = r.o.z, ix = r.ix, iy = r.iy, iz = r.iz;
+    while (true) {
+        while (node >= 0) {
+            if (++iter > kIterCap) { err |= kErrIter; return; }
+            const float4 n0 = __ldg(&nodes[4 * node + 0]);
+            const float4 n1 = __ldg(&nodes[4 * node + 1]);
+            const float4 n2 = __ldg(&nodes[4 * node + 2]);
+            const float4 n3 = __ldg(&nodes[4 * node + 3]);
+            if (COUNT) cnt.nodes++;
+            float a0 = (n0.x - ox) * ix, a1 = (n0.y - ox) * ix;
+            float b0 = (n0.z - oy) * iy, b1 = (n0.w - oy) * iy;
+            float c0 = (n2.x - oz) * iz, c1 = (n2.y - oz) * iz;
+            float tn0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+            float tf0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), best)) * widen;
+            float d0 = (n1.x - ox) * ix, d1 = (n1.y - ox) * ix;
+            float e0 = (n1.z - oy) * iy, e1 = (n1.w - oy) * iy;
+            float f0 = (n2.z - oz) * iz, f1 = (n2.w - oz) * iz;
+            float tn1 = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1)), fmaxf(fminf(f0, f1), 0.0f));
+            float tf1 = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1)), fminf(fmaxf(f0, f1), best)) * widen;
+            const bool h0 = tn0 <= tf0, h1 = tn1 <= tf1;
+            const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                int nearc = ch0, farc = ch1;
+                if (tn1 < tn0) { nearc = ch1; farc = ch0; }
+                if (sp >= kStackSize) { err |= kErrStack; return; }
+                stack[sp++] = farc;
+                node = nearc;
+            } else if (h0) {
+                node = ch0;
+            } else if (h1) {
+                node = ch1;
+            } else {
+                if (sp == 0) return;
+                node = stack[--sp];
+            }
+        }
+        // leaf
+        const uint32_t x = ~(uint32_t)node;
+        const uint32_t start = x >> 3, cntl = (x & 7u) + 1u;
+        for (uint32_t k = 0; k < cntl; ++k) {
+            const float4 t0 = __ldg(&tris[3 * (start + k) + 0]);
+            const float4 t1 = __ldg(&tris[3 * (start + k) + 1]);
+            const float4 t2 = __ldg(&tris[3 * (start + k) + 2]);
+            if (COUNT) cnt.tris++;
+            float tt, U, V, W, det;
+            if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
+                const uint32_t id = __float_as_uint(t0.w);
+                if (ANY) {
+                    if (tt <= tmax) { h.t = tt; h.id = id; return; }
+                } else if (tt < h.t || (tt == h.t && id < h.id)) {
+                    h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
+                    best = tt;
+                }
+            }
+        }
+        if (sp == 0) return;
+        node = stack[--sp];
+    }
+}
+
+}  // namespace vgbd

@@ -1,0 +1,36 @@
+// vgb_internal.h -- layouts shared by the host builder and the CUDA kernels.
+//
+// Device BVH (binary, "two boxes per node"): one node is four 16-byte words.
+//   w0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   w1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   w2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   w3 = (child0, child1, 0, 0) as int32: >= 0 inner node index, < 0 leaf ~(first << 3 | count-1)
+// A leaf holds 1..8 consecutive triangle records.  The root is node 0; a scene whose root
+// is a leaf gets one inner node whose second child is empty (an inverted box).
+//
+// Triangle record (watertight test input), three 16-byte words in leaf order:
+//   (v0.x, v0.y, v0.z, id as bits), (v1.xyz, 0), (v2.xyz, 0)
+// id is the triangle's index in the caller's index buffer.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace vgb {
+
+constexpr int kLeafShift = 3;
+constexpr uint32_t kMaxLeaf = 8;
+
+struct BvhHost {
+    std::vector<float> nodes;      // 16 floats per node
+    std::vector<float> tris;       // 12 floats per triangle record
+    uint32_t num_nodes = 0;
+    uint32_t max_depth = 0;
+    float root_lo[3] = {0, 0, 0}, root_hi[3] = {0, 0, 0};
+};
+
+// Binned-SAH build over the triangles of (positions, indices).  Deterministic for a given
+// input and leaf size, whatever the thread count.
+bool build_bvh2(const float* positions, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
+                uint32_t max_leaf, uint32_t threads, BvhHost& out, const char** err);
+
+}  // namespace vgb

@@ -1,0 +1,539 @@
+"""Host side of the hot path, mirroring Vira's scene / camera / path-tracer API.
+
+Names follow the reference (``Scene.new_camera``, ``scene[cam].set_resolution``,
+``scene.pathtracer.options.samples``, ``scene.pathtracer.render_passes.simulate_lighting``,
+``scene.pathtrace_render(cam)``), as its Python example uses them
+(examples/virapy_examples/pyvira_orex.py:52-110).  Poses, the sun ephemeris and the rebasing of
+everything into a local scene frame are FP64 on the host; the device sees FP32 in that frame.
+Rendering goes through the C ABI of include/vgb.h (libvgb.so); film planes are torch CUDA
+tensors (PyTorch provides device memory only).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi
+from .spectral import AU_TO_M, SOLAR_RADIUS, SpectralBands, black_body_radiance
+
+PI_F = np.float32(3.14159265358979323846)
+
+
+# ============================================================================ camera
+class Camera:
+    """Pinhole camera: Camera (include/vira/cameras/camera.hpp) without the sensor chain.
+
+    Defaults follow camera.hpp:220-235: focal length 50 mm, sensor 36 x 20.25 mm,
+    resolution 1920 x 1080, f-stop 2.8, optical efficiency 1, principal point at the centre.
+    """
+
+    def __init__(self):
+        self.focal_length = np.float32(50.0 / 1000.0)
+        self.resolution = (1920, 1080)
+        self.sensor_size = (np.float32(36.0 / 1000.0), np.float32(20.25 / 1000.0))
+        self.square_pixel = True
+        self.f_stop = np.float32(2.8)
+        self.aperture_diameter = np.float32(self.focal_length / self.f_stop)
+        self.optical_efficiency = 1.0
+        self.principal_point = (np.float32(np.inf), np.float32(np.inf))
+        self.skew = (np.float32(0.0), np.float32(0.0))
+        self.blender_frame = False
+        self.position = np.zeros(3, np.float64)          # FP64, scene (global) frame
+        self.rotation = np.eye(3, dtype=np.float64)       # FP64, columns = camera axes
+        self._kinv = None
+
+    # --- setters (camera.ipp:235-470)
+    def set_focal_length(self, f: float):
+        if not f > 0:
+            raise ValueError("Focal Length must be positive")
+        self.focal_length = np.float32(f)
+        self.f_stop = np.float32(np.float32(f) / self.aperture_diameter)
+
+    def set_f_stop(self, f_stop: float):
+        if not f_stop > 0:
+            raise ValueError("F-Stop must be positive")
+        self.f_stop = np.float32(f_stop)
+        self.aperture_diameter = np.float32(self.focal_length / self.f_stop)
+
+    def set_resolution(self, x: int, y: int):
+        self.resolution = (int(x), int(y))
+        if self.square_pixel:
+            self.set_sensor_size(float(self.sensor_size[0]))
+
+    def set_sensor_size(self, x: float, y: float | None = None):
+        if y is None:
+            yy = float(self.resolution[1]) * (float(x) / float(self.resolution[0]))
+            self.sensor_size = (np.float32(x), np.float32(yy))
+            self.square_pixel = True
+        else:
+            self.sensor_size = (np.float32(x), np.float32(y))
+            self.square_pixel = False
+
+    def set_field_of_view(self, fov_deg: float):
+        """Focal length giving the horizontal field of view for the current sensor width."""
+        self.set_focal_length(float(self.sensor_size[0]) / 2.0 / math.tan(math.radians(fov_deg) / 2.0))
+
+    def set_optical_efficiency(self, eff):
+        self.optical_efficiency = eff
+
+    def enable_blender_frame(self):
+        self.blender_frame = True
+
+    def set_local_position(self, x, y=None, z=None):
+        self.position = np.array([x, y, z] if y is not None else x, np.float64).reshape(3)
+
+    def set_local_rotation(self, matrix):
+        self.rotation = np.array(matrix, np.float64).reshape(3, 3)
+
+    def look_at(self, target, up=(0.0, 0.0, 1.0)):
+        self.look_in_direction(np.asarray(target, np.float64) - self.position, up)
+
+    def look_in_direction(self, direction, up=(0.0, 0.0, 1.0)):
+        """Camera::lookInDirection (camera.ipp:1455-1500), evaluated in FP64."""
+        up = np.asarray(up, np.float64)
+        up = up / np.linalg.norm(up)
+        d = np.asarray(direction, np.float64)
+        d = d / np.linalg.norm(d)
+        if abs(float(d @ up)) > 0.999:
+            for cand in ((0.0, 1.0, 0.0), (0.0, 0.0, 1.0), (1.0, 0.0, 0.0)):
+                if abs(float(d @ np.array(cand))) < 0.999:
+                    up = np.array(cand)
+                    break
+        if self.blender_frame:
+            y_axis, z_axis = up, -d
+        else:
+            y_axis, z_axis = -up, d
+        x_axis = np.cross(y_axis, z_axis)
+        x_axis /= np.linalg.norm(x_axis)
+        y_axis = np.cross(z_axis, x_axis)
+        y_axis /= np.linalg.norm(y_axis)
+        self.rotation = np.stack([x_axis, y_axis, z_axis / np.linalg.norm(z_axis)], axis=1)
+
+    # --- derived constants
+    @property
+    def z_dir(self) -> np.float32:
+        return np.float32(-1.0 if self.blender_frame else 1.0)
+
+    def kinv(self) -> np.ndarray:
+        """Inverse intrinsic matrix, FP32, through the C ABI (camera.ipp:1526-1568)."""
+        lib = capi.load()
+        out = (C.c_float * 6)()
+        W, H = self.resolution
+        capi.check(lib.vgb_camera_intrinsics(self.focal_length, self.sensor_size[0], self.sensor_size[1], W, H,
+                                             self.principal_point[0], self.principal_point[1], self.skew[0],
+                                             self.skew[1], self.z_dir, out), what="camera_intrinsics")
+        return np.array(out[:], np.float32)
+
+    def aperture_area(self) -> np.float32:
+        """CircularAperture::getArea after Camera::initialize (aperture.ipp:25-31)."""
+        d = np.float32(self.focal_length / self.f_stop)
+        r = np.float32(d / np.float32(2.0))
+        return np.float32(np.float32(PI_F * r) * r)
+
+    def to_c(self, scene_origin: np.ndarray, nbands: int) -> capi.Camera:
+        c = capi.Camera()
+        c.width, c.height = self.resolution
+        o = (self.position - scene_origin).astype(np.float32)    # FP64 rebasing, then FP32
+        for k in range(3):
+            c.origin[k] = float(o[k])
+        R = self.rotation.astype(np.float32)
+        for col in range(3):
+            for row in range(3):
+                c.rotation[3 * col + row] = float(R[row, col])
+        kinv = self.kinv()
+        for k in range(6):
+            c.kinv[k] = float(kinv[k])
+        c.z_dir = float(self.z_dir)
+        eff = np.broadcast_to(np.asarray(self.optical_efficiency, np.float32), (nbands,))
+        area = self.aperture_area()
+        for k in range(nbands):
+            c.power_scale[k] = float(np.float32(eff[k] * area))
+        return c
+
+
+# ============================================================================ assets
+@dataclass
+class Mesh:
+    """Mesh (include/vira/geometry/mesh.hpp): FP32 vertices in the mesh frame."""
+
+    positions: np.ndarray                  # (n, 3) float32
+    indices: np.ndarray                    # (t, 3) uint32
+    albedo: np.ndarray | None = None       # (n, B) float32 per-vertex albedo (Vertex::albedo)
+    uv: np.ndarray | None = None           # (n, 2) float32
+    normals: np.ndarray | None = None      # (n, 3) float32; computed by Mesh::init when absent
+    albedo_map: np.ndarray | None = None   # (h, w, B) float32 material albedo texture
+    smooth_shading: bool = False
+
+    def set_smooth_shading(self, on: bool):
+        self.smooth_shading = bool(on)
+
+    def compute_normals(self) -> np.ndarray:
+        if self.normals is None:
+            lib = capi.load()
+            p = np.ascontiguousarray(self.positions, np.float32)
+            i = np.ascontiguousarray(self.indices, np.uint32)
+            n = np.empty_like(p)
+            capi.check(lib.vgb_compute_vertex_normals(capi.ptr(p), p.shape[0], capi.ptr(i), i.shape[0], capi.ptr(n)),
+                       what="compute_vertex_normals")
+            self.normals = n
+        return self.normals
+
+    @staticmethod
+    def from_dem(heights: np.ndarray, posting: float, albedo=None, nbands: int = 1) -> "Mesh":
+        """DEM::makeMesh with the non-OGR projection (dem.ipp:138-211)."""
+        lib = capi.load()
+        h = np.ascontiguousarray(heights, np.float32)
+        H, W = h.shape
+        pos = np.empty((H * W, 3), np.float32)
+        idx = np.empty((2 * (W - 1) * (H - 1), 3), np.uint32)
+        nt = C.c_uint32(0)
+        capi.check(lib.vgb_dem_triangulate(capi.ptr(h), W, H, float(posting), float(posting), capi.ptr(pos),
+                                           capi.ptr(idx), C.byref(nt)), what="dem_triangulate")
+        alb = None
+        if albedo is not None:
+            a = np.asarray(albedo, np.float32)
+            if a.ndim == 0 or a.size == nbands:
+                alb = np.broadcast_to(a.reshape(1, -1) if a.ndim else a, (H * W, nbands)).astype(np.float32)
+            else:
+                alb = a.reshape(H * W, -1).astype(np.float32)
+        return Mesh(pos, idx[: nt.value].copy(), albedo=alb)
+
+
+@dataclass
+class Instance:
+    mesh: int
+    position: np.ndarray = field(default_factory=lambda: np.zeros(3))   # FP64
+    rotation: np.ndarray = field(default_factory=lambda: np.eye(3))     # FP64
+    scale: float = 1.0
+    visible: bool = True
+
+    def set_local_position(self, x, y=None, z=None):
+        self.position = np.array([x, y, z] if y is not None else x, np.float64).reshape(3)
+
+    def set_local_rotation(self, matrix):
+        self.rotation = np.array(matrix, np.float64).reshape(3, 3)
+
+
+@dataclass
+class SphereLight:
+    """SphereLight (include/implementation/lights/sphere_light.ipp:17-28)."""
+
+    radiance: np.ndarray        # FP32 per band
+    radius: np.float32
+    position: np.ndarray = field(default_factory=lambda: np.zeros(3))   # FP64
+
+    def set_local_position(self, x, y=None, z=None):
+        self.position = np.array([x, y, z] if y is not None else x, np.float64).reshape(3)
+
+
+# ============================================================================ path tracer
+@dataclass
+class PathTracerOptions:
+    """CPUPathTracerOptions (include/vira/rendering/cpu_path_tracer.hpp:30-43) plus the
+    counter-based RNG key and the two additions (deterministic light sampling, Russian roulette)."""
+
+    samples: int = 1
+    bounces: int = 0
+    show_background: bool = False
+    denoise: bool = False
+    seed: int = 0
+    frame: int = 0
+    deterministic_light: bool = False
+    rr_depth: int = 0
+
+
+@dataclass
+class RenderPasses:
+    """RenderPasses (include/vira/rendering/passes.hpp:51-95): planes are torch CUDA tensors
+    [B][H][W] / [3][H][W] / [H][W] after a render."""
+
+    simulate_lighting: bool = False
+    depth: object = None
+    alpha: object = None
+    albedo: object = None
+    normal_global: object = None
+    triangle_id: object = None
+    received_power: object = None
+    total_radiance: object = None
+    direct_radiance: object = None
+    indirect_radiance: object = None
+
+
+class PathTracer:
+    """GPU replacement of CPUPathTracer: same ``render(camera, scene)``, ``options``,
+    ``render_passes`` (cpu_path_tracer.hpp:46-58)."""
+
+    def __init__(self):
+        self.options = PathTracerOptions()
+        self.render_passes = RenderPasses()
+        self.last_stats = None
+
+    def c_options(self, scene: "Scene") -> capi.PtOptions:
+        o = capi.PtOptions()
+        opt = self.options
+        if opt.samples < 1:
+            raise ValueError("options.samples must be >= 1")
+        o.samples, o.bounces = int(opt.samples), int(opt.bounces)
+        o.show_background = int(bool(opt.show_background))
+        o.simulate_lighting = int(bool(self.render_passes.simulate_lighting))
+        o.smooth_shading = int(scene.smooth_shading())
+        o.deterministic_light = int(bool(opt.deterministic_light))
+        o.rr_depth = int(opt.rr_depth)
+        o.seed, o.frame = int(opt.seed), int(opt.frame)
+        o.nbands = scene.bands.size
+        if scene.ambient is not None:
+            o.has_ambient = 1
+            for k in range(scene.bands.size):
+                o.ambient[k] = float(scene.ambient[k])
+        for k in range(scene.bands.size):
+            o.background[k] = float(scene.background[k])
+        return o
+
+    def render(self, camera: Camera, scene: "Scene"):
+        import torch
+
+        scene.build_tlas()
+        ctx = scene.context()
+        lib = capi.load()
+        W, H = camera.resolution
+        B = scene.bands.size
+        dev = torch.device("cuda", scene.device)
+        cam = camera.to_c(scene.origin, B)
+        lights, nl = scene.c_lights()
+        opts = self.c_options(scene)
+        rp = self.render_passes
+        omega = scene.pixel_solid_angle(camera, cam)
+        rp.depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+        rp.alpha = torch.empty((H, W), dtype=torch.float32, device=dev)
+        rp.albedo = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+        rp.normal_global = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+        rp.triangle_id = torch.empty((H, W), dtype=torch.int32, device=dev)
+        if rp.simulate_lighting:
+            rp.total_radiance = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+            rp.direct_radiance = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+            rp.indirect_radiance = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+            rp.received_power = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+        else:
+            rp.total_radiance = rp.direct_radiance = rp.indirect_radiance = rp.received_power = None
+        f = capi.Film()
+        for name in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo",
+                     "normal_global", "depth", "alpha", "triangle_id"):
+            setattr(f, name, capi.ptr(getattr(rp, name)))
+        f.pixel_solid_angle = capi.ptr(omega)
+        f.on_device = 1
+        torch.cuda.current_stream(dev).synchronize()
+        capi.check(lib.vgb_render(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(f)), ctx, "render")
+        st = capi.Stats()
+        lib.vgb_get_stats(ctx, C.byref(st))
+        self.last_stats = st
+        return rp
+
+
+# ============================================================================ scene
+class Scene:
+    """Scene (include/vira/scene.hpp) reduced to what the path tracer reads.
+
+    ``origin`` is the FP64 point of the global frame that becomes the local scene frame's
+    origin on the device (rebasing); instances, lights and cameras are placed in FP64.
+    """
+
+    def __init__(self, bands: SpectralBands, device: int = 0):
+        self.bands = bands
+        self.device = device
+        self.origin = np.zeros(3, np.float64)
+        self.meshes: list[Mesh] = []
+        self.instances: list[Instance] = []
+        self.lights: list[SphereLight] = []
+        self.cameras: list[Camera] = []
+        self.ambient = None
+        self.background = np.zeros(bands.size, np.float32)
+        self.pathtracer = PathTracer()
+        self.bvh_options = capi.BvhOptions(0, 0, 0)
+        self._ctx = None
+        self._dirty = True
+        self._omega_cache = {}
+        self.flat = None
+
+    # --- graph (scene/group.hpp:88-133)
+    def new_camera(self) -> int:
+        self.cameras.append(Camera())
+        return ("camera", len(self.cameras) - 1)
+
+    def add_mesh(self, mesh: Mesh) -> tuple:
+        self.meshes.append(mesh)
+        self._dirty = True
+        return ("mesh", len(self.meshes) - 1)
+
+    def new_instance(self, mesh_id) -> tuple:
+        self.instances.append(Instance(mesh=mesh_id[1]))
+        self._dirty = True
+        return ("instance", len(self.instances) - 1)
+
+    def new_sphere_light(self, spectral_input, radius, is_power: bool = False) -> tuple:
+        s = np.broadcast_to(np.asarray(spectral_input, np.float32), (self.bands.size,)).astype(np.float32)
+        r = np.float32(radius)
+        if is_power:
+            s = (s / np.float32(np.float32(np.float32(np.float32(4) * PI_F) * np.float32(r * r)) * PI_F)).astype(np.float32)
+        self.lights.append(SphereLight(s, r))
+        return ("light", len(self.lights) - 1)
+
+    def new_sun(self, temperature: float = 5800.0, steps: int = 1000) -> tuple:
+        """Group::newSun (scene/group.ipp:585-591): blackbody sphere light of solar radius."""
+        rad = black_body_radiance(self.bands, temperature, steps)
+        return self.new_sphere_light(rad, SOLAR_RADIUS, False)
+
+    def set_sun_direction(self, light_id, azimuth_deg: float, elevation_deg: float, distance: float = AU_TO_M):
+        """Places a light at `distance` in the direction (azimuth, elevation) from the scene origin, FP64."""
+        az, el = math.radians(azimuth_deg), math.radians(elevation_deg)
+        d = np.array([math.cos(el) * math.cos(az), math.cos(el) * math.sin(az), math.sin(el)])
+        self[light_id].position = self.origin + distance * d
+
+    def set_ambient(self, ambient):
+        self.ambient = np.broadcast_to(np.asarray(ambient, np.float32), (self.bands.size,)).astype(np.float32)
+
+    def set_background_emission(self, bg):
+        self.background = np.broadcast_to(np.asarray(bg, np.float32), (self.bands.size,)).astype(np.float32)
+
+    def __getitem__(self, key):
+        kind, i = key
+        return {"camera": self.cameras, "mesh": self.meshes, "instance": self.instances, "light": self.lights}[kind][i]
+
+    def mark_dirty(self):
+        self._dirty = True
+
+    def smooth_shading(self) -> bool:
+        used = {inst.mesh for inst in self.instances if inst.visible}
+        flags = {self.meshes[m].smooth_shading for m in used}
+        if len(flags) > 1:
+            raise ValueError("meshes with mixed smooth-shading flags are not supported in one scene")
+        return flags.pop() if flags else False
+
+    # --- device
+    def context(self):
+        if self._ctx is None:
+            lib = capi.load()
+            h = C.c_void_p()
+            capi.check(lib.vgb_context_create(C.byref(h), self.device), what="context_create (is a GPU present?)")
+            self._ctx = h
+        return self._ctx
+
+    def close(self):
+        if self._ctx is not None:
+            capi.load().vgb_context_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def flatten(self):
+        """Scene::processSceneGraph + buildTLAS input: every visible instance's mesh moved into
+        the local scene frame in FP64 (rotation, scale, translation, minus `origin`), then FP32."""
+        B = self.bands.size
+        pos, idx, alb, uv, nrm = [], [], [], [], []
+        tex = None
+        base = 0
+        tri_offsets = []
+        for ii, inst in enumerate(self.instances):
+            if not inst.visible:
+                continue
+            m = self.meshes[inst.mesh]
+            n = m.compute_normals()
+            p64 = m.positions.astype(np.float64)
+            if not (np.array_equal(inst.rotation, np.eye(3)) and inst.scale == 1.0 and not inst.position.any()
+                    and not self.origin.any()):
+                p64 = (p64 * inst.scale) @ inst.rotation.T + (inst.position - self.origin)
+                n = (n.astype(np.float64) @ inst.rotation.T).astype(np.float32)
+            pos.append(p64.astype(np.float32))
+            nrm.append(n.astype(np.float32))
+            idx.append(m.indices.astype(np.uint32) + np.uint32(base))
+            a = m.albedo if m.albedo is not None else np.ones((m.positions.shape[0], B), np.float32)
+            alb.append(np.broadcast_to(a, (m.positions.shape[0], B)).astype(np.float32))
+            uv.append(m.uv if m.uv is not None else np.zeros((m.positions.shape[0], 2), np.float32))
+            if m.albedo_map is not None:
+                if tex is not None and tex is not m.albedo_map:
+                    raise ValueError("one albedo texture per scene is supported")
+                tex = m.albedo_map
+            tri_offsets.append((ii, base, int(m.indices.shape[0])))
+            base += m.positions.shape[0]
+        if not pos:
+            raise ValueError("scene has no visible instances")
+        self.flat = dict(
+            positions=np.ascontiguousarray(np.concatenate(pos)),
+            indices=np.ascontiguousarray(np.concatenate(idx)),
+            albedo=np.ascontiguousarray(np.concatenate(alb)),
+            uv=np.ascontiguousarray(np.concatenate(uv)),
+            normals=np.ascontiguousarray(np.concatenate(nrm)),
+            texture=None if tex is None else np.ascontiguousarray(tex, np.float32),
+            tri_offsets=tri_offsets,
+        )
+        return self.flat
+
+    def build_tlas(self):
+        """Scene::buildTLAS (scene.ipp:712-812): flatten, upload and build the BVH when dirty."""
+        if not self._dirty:
+            return
+        f = self.flatten()
+        lib = capi.load()
+        ctx = self.context()
+        tex = f["texture"]
+        th, tw = (tex.shape[0], tex.shape[1]) if tex is not None else (0, 0)
+        capi.check(lib.vgb_scene_upload(ctx, capi.ptr(f["positions"]), f["positions"].shape[0], capi.ptr(f["indices"]),
+                                        f["indices"].shape[0], self.bands.size, capi.ptr(f["albedo"]),
+                                        capi.ptr(f["normals"]), capi.ptr(f["uv"]), capi.ptr(tex), tw, th),
+                   ctx, "scene_upload")
+        capi.check(lib.vgb_bvh_build(ctx, C.byref(self.bvh_options)), ctx, "bvh_build")
+        self._dirty = False
+
+    def c_lights(self):
+        arr = (capi.Light * max(1, len(self.lights)))()
+        for k, L in enumerate(self.lights):
+            p = (L.position - self.origin).astype(np.float32)
+            for a in range(3):
+                arr[k].position[a] = float(p[a])
+            arr[k].radius = float(L.radius)
+            for b in range(self.bands.size):
+                arr[k].radiance[b] = float(L.radiance[b])
+        return arr, len(self.lights)
+
+    def pixel_solid_angle(self, camera: Camera, cam_c: capi.Camera):
+        """Camera::initializePixelSolidAngle (camera.ipp:1622-1666) on the device, FP64, cached."""
+        import torch
+
+        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir))
+        om = self._omega_cache.get(key)
+        if om is None:
+            W, H = camera.resolution
+            om = torch.empty((H, W), dtype=torch.float32, device=torch.device("cuda", self.device))
+            torch.cuda.current_stream(om.device).synchronize()
+            ctx = self.context()
+            capi.check(capi.load().vgb_pixel_solid_angle(ctx, C.byref(cam_c), capi.ptr(om), 1), ctx, "pixel_solid_angle")
+            self._omega_cache = {key: om}
+        return om
+
+    # --- renders (scene.ipp:840-915)
+    def pathtrace_render(self, camera_id):
+        """Renders and returns the received-power pass (the sensor chain is not part of this path)."""
+        rp = self.pathtracer.render(self[camera_id], self)
+        return rp.received_power
+
+    def intersect(self, origins: np.ndarray, directions: np.ndarray, any_hit: bool = False, tmax=None):
+        """Scene::intersect / TLAS::intersect (scene.hpp:230) for a batch of rays (host arrays)."""
+        self.build_tlas()
+        lib = capi.load()
+        ctx = self.context()
+        o = np.ascontiguousarray(origins, np.float32)
+        d = np.ascontiguousarray(directions, np.float32)
+        n = o.shape[0]
+        tri = np.empty(n, np.uint32)
+        t = np.empty(n, np.float32)
+        w = np.empty((n, 3), np.float32)
+        tm = None if tmax is None else np.ascontiguousarray(tmax, np.float32)
+        capi.check(lib.vgb_trace_rays(ctx, capi.ptr(o), capi.ptr(d), capi.ptr(tm), n, int(any_hit), capi.ptr(tri),
+                                      capi.ptr(t), capi.ptr(w), 0), ctx, "trace_rays")
+        return tri, t, w
