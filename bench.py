@@ -1,0 +1,474 @@
+#!/usr/bin/env python
+"""Benchmark of the spectral ray-tracing hot path on one GB300 (or N replicas).
+
+Workload (default): the plain path-tracing configuration -- 4097^2 fBm DEM plus a Poisson
+crater field (33.5M triangles), 4096^2 lognormal albedo texture, 8 bands 400-1000 nm, 2048^2
+image, 64 spp, 3 bounces with sun NEE, Russian roulette after bounce 2.  A step is one full
+render of that frame.  Metric: Mrays/s (closest-hit + shadow queries, each one traversal).
+
+  value    device time of K renders, CUDA events on the render stream, inputs resident in HBM
+  e2e      the same renders through vgb_render() with host (pinned) film planes: host<->device
+           copies inside the timed region
+  roofline the dominant kernel family's algorithmic bytes per launch (node and triangle visits
+           from a counting pass of the same BVH and rays, ray I/O, shading gathers) over its
+           average launch time, against MEASURED_PEAKS.json's HBM copy bandwidth
+  cpu_baseline  the oracle (CPU restatement) on the host cores over a bounded band of rows
+
+`--impl reference` times the reference's CPU path tracer as restated by the oracle (the
+reference itself cannot be compiled: Embree, TBB and glm are absent) on all host threads.
+Multi-GPU: replicas only (the path does not need a collective); each rank renders its own frame.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NODE_BYTES = 64
+TRI_BYTES = 48
+RAY_IO_CLOSEST = 32 + 16
+RAY_IO_SHADOW = 32 + 4
+
+
+def shade_bytes(B: int) -> int:
+    """Per shaded hit: 3 indices, 3 x (position 16 + normal 16 + uv 8 + B albedo), 4 texels x B,
+    and the path-state / film read-modify-writes (3 x B floats)."""
+    return 12 + 3 * (40 + 4 * B) + 16 * B + 12 * B
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["path_traced", "plain_direct"], default="path_traced")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrinks posts and pixels (tests only)")
+    ap.add_argument("--spp", type=int, default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-direct", action="store_true", help="skip the extra plain-direct line item")
+    return ap.parse_args()
+
+
+def workload_params(args):
+    if args.workload == "path_traced":
+        posts = int(round((4096 * args.scale))) + 1
+        tex = max(2, int(round(4096 * args.scale)))
+        res = max(8, int(round(2048 * args.scale)))
+        spp = args.spp or 64
+        return dict(kind="path_traced", posts=posts, tex=tex, resolution=res, spp=spp, bounces=3, rr_depth=2)
+    posts = int(round(512 * args.scale)) + 1
+    res = max(8, int(round(1024 * args.scale)))
+    return dict(kind="plain_direct", posts=posts, resolution=res, spp=args.spp or 1, bounces=0)
+
+
+def build_scene(p, device):
+    from vira_gb300 import workloads
+
+    if p["kind"] == "path_traced":
+        scene, cam = workloads.path_traced(posts=p["posts"], tex=p["tex"], resolution=p["resolution"], spp=p["spp"],
+                                           bounces=p["bounces"], rr_depth=p["rr_depth"], device=device)
+    else:
+        scene, cam = workloads.plain_direct(posts=p["posts"], resolution=p["resolution"], device=device)
+        scene.pathtracer.options.samples = p["spp"]
+    return scene, cam
+
+
+def config_name(p):
+    if p["kind"] == "path_traced":
+        return f"path_traced_dem{p['posts']}_tex{p['tex']}_{p['resolution']}px_{p['spp']}spp_{p['bounces']}b_rr{p['rr_depth']}_8band"
+    return f"plain_direct_dem{p['posts']}_{p['resolution']}px_{p['spp']}spp_4band"
+
+
+# ------------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4) if r[k].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------------ CPU legs
+def cpu_sample(scene, cam_id, seconds: float, threads: int):
+    """Times the oracle over bands of rows of the same frame until ~`seconds` of CPU work."""
+    from oracle import oracle
+
+    if scene.flat is None:
+        scene.flatten()
+    t0 = time.perf_counter()
+    osc = oracle.OracleScene.from_flat(scene.flat, scene.bands.size)
+    build_s = time.perf_counter() - t0
+    cam = scene[cam_id].to_c(scene.origin, scene.bands.size)
+    lights, nl = scene.c_lights()
+    opts = scene.pathtracer.c_options(scene)
+    H = cam.height
+    rows, total_rays, total_t, spp_px = 0, 0, 0.0, 0
+    r = max(1, H // 2 - 1)
+    nrows = 1
+    while total_t < seconds and r < H:
+        t = time.perf_counter()
+        _, counts = osc.render(cam, lights, nl, opts, rows=(r, min(H, r + nrows)), threads=threads)
+        dt = time.perf_counter() - t
+        total_t += dt
+        total_rays += counts[0] + counts[1]
+        done = min(H, r + nrows) - r
+        rows += done
+        spp_px += done * cam.width * opts.samples
+        r += done
+        if dt < seconds / 8:
+            nrows = min(H, nrows * 2)
+    osc.close()
+    return {"mrays_s": total_rays / total_t / 1e6, "spp_s": spp_px / total_t, "rows": rows, "seconds": total_t,
+            "rays": total_rays, "oracle_bvh_build_s": build_s}
+
+
+def run_reference(args, p, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle
+
+    scene, cam_id = build_scene(p, device=0)
+    threads = oracle.nthreads()
+    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_sample(scene, cam_id, min(per_step, 2.0), threads)
+    vals, spps, rows = [], [], 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = cpu_sample(scene, cam_id, per_step, threads)
+        vals.append(s["mrays_s"])
+        spps.append(s["spp_s"])
+        rows = s["rows"]
+    elapsed = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    W = scene[cam_id].resolution[0]
+    line = {
+        "metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm + craters)",
+        "impl": "reference",
+        "config": {"workload": config_name(p), "parallelism": "host threads"},
+        "spectral_path_samples_per_s": float(np.mean(spps)),
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"each step: a band of ~{rows} rows x {W} px of the frame at full spp "
+                                   f"(CPU restatement of cpu_path_tracer.ipp, BVH2 of vira_blas.ipp, not Embree)"},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    scene.close()
+
+
+# ------------------------------------------------------------------------ GPU leg
+class Renderer:
+    """Lean render loop over the C ABI with preallocated device planes."""
+
+    def __init__(self, scene, cam_id, torch, stream):
+        from vira_gb300 import capi
+
+        self.capi = capi
+        self.lib = capi.load()
+        self.scene = scene
+        self.torch = torch
+        self.ctx = scene.context()
+        camera = scene[cam_id]
+        self.cam = camera.to_c(scene.origin, scene.bands.size)
+        self.lights, self.nl = scene.c_lights()
+        self.opts = scene.pathtracer.c_options(scene)
+        self.omega = scene.pixel_solid_angle(camera, self.cam)
+        capi.check(self.lib.vgb_set_stream(self.ctx, C.c_void_p(stream.cuda_stream)), self.ctx, "set_stream")
+        W, H, B = self.cam.width, self.cam.height, scene.bands.size
+        dev = self.omega.device
+        self.planes = {
+            "total_radiance": torch.empty((B, H, W), device=dev), "received_power": torch.empty((B, H, W), device=dev),
+            "triangle_id": torch.empty((H, W), dtype=torch.int32, device=dev), "depth": torch.empty((H, W), device=dev),
+        }
+        self.film = capi.Film()
+        for k, v in self.planes.items():
+            setattr(self.film, k, v.data_ptr())
+        self.film.pixel_solid_angle = self.omega.data_ptr()
+        self.film.on_device = 1
+        # host (pinned) planes for the end-to-end leg
+        self.host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in self.planes.items()}
+        self.omega_host = self.omega.cpu().pin_memory()
+        self.hfilm = capi.Film()
+        for k, v in self.host.items():
+            setattr(self.hfilm, k, v.data_ptr())
+        self.hfilm.pixel_solid_angle = self.omega_host.data_ptr()
+        self.hfilm.on_device = 0
+        self.d2h_bytes = sum(v.numel() * v.element_size() for v in self.host.values())
+        self.h2d_bytes = (self.omega_host.numel() * 4 + C.sizeof(self.cam) + C.sizeof(self.opts)
+                          + C.sizeof(capi.Light) * max(1, self.nl))
+
+    def render(self, host=False):
+        f = self.hfilm if host else self.film
+        self.capi.check(self.lib.vgb_render(self.ctx, C.byref(self.cam), self.lights, self.nl, C.byref(self.opts),
+                                            C.byref(f)), self.ctx, "render")
+
+    def stats(self):
+        st = self.capi.Stats()
+        self.lib.vgb_get_stats(self.ctx, C.byref(st))
+        return st
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_ours(args, p, rank, world, local_rank):
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    t0 = time.perf_counter()
+    scene, cam_id = build_scene(p, device=local_rank)
+    scene.pathtracer.options.frame = rank  # replicas render distinct sample streams
+    t1 = time.perf_counter()
+    scene.build_tlas()
+    t2 = time.perf_counter()
+    stream = torch.cuda.Stream(device=dev)
+    r = Renderer(scene, cam_id, torch, stream)
+    lib = r.lib
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    for _ in range(args.warmup):
+        r.render()
+    lib.vgb_set_profiling(r.ctx, 1)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms, rays, paths, st_list = [], 0, 0, []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)  # L2 flush between timed renders, outside the event pair
+            ev0.record(stream)
+        r.render()
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        ms.append(ev0.elapsed_time(ev1))
+        st = r.stats()
+        st_list.append(st)
+        rays += st.rays_closest + st.rays_shadow
+        paths += r.cam.width * r.cam.height * r.opts.samples
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    lib.vgb_set_profiling(r.ctx, 0)
+    total_ms = float(sum(ms))
+    if world > 1:
+        t = torch.tensor([total_ms, float(rays), float(paths)], dtype=torch.float64, device=dev)
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
+        total_ms, rays, paths = float(tmax[0]), float(t[1]), float(t[2])
+    value = rays / (total_ms / 1000.0) / 1e6
+
+    # e2e through the C ABI with host buffers (wall clock around the blocking call)
+    e2e_ms = []
+    e2e_rays = 0
+    for _ in range(max(1, min(args.steps, 3))):
+        t = time.perf_counter()
+        r.render(host=True)
+        e2e_ms.append((time.perf_counter() - t) * 1000.0)
+        st = r.stats()
+        e2e_rays += st.rays_closest + st.rays_shadow
+    e2e_value = e2e_rays / (sum(e2e_ms) / 1000.0) / 1e6 * (world if world > 1 else 1)
+
+    # roofline: counting pass for algorithmic bytes, live per-family times from the timed region
+    lib.vgb_set_count_pass(r.ctx, 1)
+    r.render()
+    lib.vgb_set_count_pass(r.ctx, 0)
+    cst = r.stats()
+    s0 = st_list[-1]
+    fam = {"k_extend": (sum(s.ms_extend for s in st_list), sum(s.launches_extend for s in st_list)),
+           "k_shadow": (sum(s.ms_shadow for s in st_list), sum(s.launches_shadow for s in st_list)),
+           "k_end_sample": (sum(s.ms_film for s in st_list), sum(s.launches_film for s in st_list))}
+    B = scene.bands.size
+    nodes_sh = cst.nodes_visited - cst.nodes_closest
+    tris_sh = cst.tris_tested - cst.tris_closest
+    alg = {
+        "k_extend": cst.nodes_closest * NODE_BYTES + cst.tris_closest * TRI_BYTES + cst.rays_closest * RAY_IO_CLOSEST
+        + cst.hits_closest * shade_bytes(B),
+        "k_shadow": nodes_sh * NODE_BYTES + tris_sh * TRI_BYTES + cst.rays_shadow * (RAY_IO_SHADOW + 4 * B + 8),
+        "k_end_sample": r.cam.width * r.cam.height * r.opts.samples * 4 * (4 * B + 2),
+    }
+    dominant = max(fam, key=lambda k: fam[k][0])
+    dms, dl = fam[dominant]
+    per_launch_bytes = alg[dominant] / max(1, s0.__getattribute__(
+        {"k_extend": "launches_extend", "k_shadow": "launches_shadow", "k_end_sample": "launches_film"}[dominant]))
+    per_launch_ms = dms / max(1, dl)
+    achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic_per_launch.json"
+    if tfile.exists():
+        try:
+            tj = json.loads(tfile.read_text())
+            ent = tj.get(config_name(p), {}).get(dominant)
+            if ent:
+                traffic = float(ent)
+        except Exception:
+            traffic = None
+
+    direct = None
+    if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
+        direct = plain_direct_item(torch, dev)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle
+
+        threads = oracle.nthreads()
+        c = cpu_sample(scene, cam_id, args.cpu_seconds, threads)
+        cpu = {"value": c["mrays_s"], "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"rows {c['rows']} x {r.cam.width} px of the same frame at {r.opts.samples} spp "
+                         f"({c['rays']} rays in {c['seconds']:.1f} s; CPU restatement, BVH2 of vira_blas.ipp, not Embree)"}
+    if rank == 0:
+        launches = int(sum(s.kernel_launches for s in st_list))
+        line = {
+            "metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded fBm DEM + Poisson craters, lognormal albedo); random-free poses",
+            "config": {"workload": config_name(p), "triangles": int(scene.flat["indices"].shape[0]),
+                       "image": [r.cam.width, r.cam.height], "spp": int(r.opts.samples),
+                       "bounces": int(r.opts.bounces), "rr_after_bounce": int(r.opts.rr_depth), "bands": B,
+                       "l2": "flushed between timed renders (256 MB write); scene working set also exceeds L2",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "spectral_path_samples_per_s": paths / (total_ms / 1000.0),
+            "rays_per_step": rays / args.steps / max(1, world),
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(r.h2d_bytes),
+                    "d2h_bytes_per_step": int(r.d2h_bytes)},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                         "kernel_share": {k: v[0] / max(1e-9, sum(x[0] for x in fam.values())) for k, v in fam.items()}},
+            "gpu_launches": launches,
+            "setup_s": {"scene": t1 - t0, "upload_and_bvh": t2 - t1},
+            "clocks": clk,
+        }
+        if direct is not None:
+            line["plain_direct"] = direct
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    scene.close()
+
+
+def plain_direct_item(torch, dev):
+    """The 513^2 / 1024^2 direct-lighting frame: Mrays/s (primary + shadow) on the same GPU."""
+    from vira_gb300 import workloads
+
+    scene, cam_id = workloads.plain_direct(device=dev.index)
+    scene.build_tlas()
+    stream = torch.cuda.Stream(device=dev)
+    r = Renderer(scene, cam_id, torch, stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    for _ in range(5):
+        r.render()
+    ms, rays = [], 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(20):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            ev0.record(stream)
+        r.render()
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        ev1.synchronize()
+        ms.append(ev0.elapsed_time(ev1))
+        st = r.stats()
+        rays += st.rays_closest + st.rays_shadow
+    scene.close()
+    tot = sum(ms)
+    return {"workload": "plain_direct_dem513_1024px_1spp_4band", "mrays_s": rays / (tot / 1000.0) / 1e6,
+            "ms_per_frame": tot / len(ms), "rays_per_frame": rays / len(ms)}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    p = workload_params(args)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        if args.impl == "reference":
+            if rank != 0:
+                return
+        else:
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, p, rank, world)
+        return
+    run_ours(args, p, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -127,14 +127,20 @@ typedef struct vgb_bvh_options {
 typedef struct vgb_stats {
     uint64_t rays_closest;     /* closest-hit queries (primary + bounce) */
     uint64_t rays_shadow;      /* shadow (any-hit) queries */
-    uint64_t nodes_visited;    /* only filled by a counting pass */
-    uint64_t tris_tested;      /* only filled by a counting pass */
-    uint32_t bvh_nodes;        /* wide nodes in the device BVH */
-    uint32_t bvh_node_bytes;   /* bytes per wide node */
+    uint64_t nodes_visited;    /* counting pass only: wide nodes visited, all queries */
+    uint64_t tris_tested;      /* counting pass only: triangle records tested, all queries */
+    uint64_t nodes_closest;    /* counting pass only: nodes visited by closest-hit queries */
+    uint64_t tris_closest;     /* counting pass only: triangles tested by closest-hit queries */
+    uint64_t hits_closest;     /* closest-hit queries that hit (shaded) */
+    uint32_t bvh_nodes;        /* nodes in the device BVH */
+    uint32_t bvh_node_bytes;   /* bytes per node */
     uint32_t tri_record_bytes; /* bytes per triangle record */
     uint32_t kernel_launches;  /* kernels launched by the last render */
     uint32_t device_error;     /* last device error word (0 = none) */
     float ms_last;             /* device time of the last render (CUDA events) */
+    /* profiling mode only (vgb_set_profiling): device time and launches per kernel family */
+    float ms_extend, ms_shadow, ms_film;
+    uint32_t launches_extend, launches_shadow, launches_film;
 } vgb_stats;
 
 /* ========================= context ============================================= */
@@ -206,6 +212,9 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* origins, const 
  * a counting pass that fills nodes_visited/tris_tested (algorithmic traffic). */
 VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out);
 VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
+/* Per-launch CUDA events around every kernel of vgb_render, summed per kernel family into
+ * vgb_stats.ms_extend / ms_shadow / ms_film. */
+VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
 
 #ifdef __cplusplus
 }

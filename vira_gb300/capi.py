@@ -68,9 +68,11 @@ class BvhOptions(C.Structure):
 class Stats(C.Structure):
     _fields_ = [
         ("rays_closest", C.c_uint64), ("rays_shadow", C.c_uint64), ("nodes_visited", C.c_uint64),
-        ("tris_tested", C.c_uint64), ("bvh_nodes", C.c_uint32), ("bvh_node_bytes", C.c_uint32),
+        ("tris_tested", C.c_uint64), ("nodes_closest", C.c_uint64), ("tris_closest", C.c_uint64),
+        ("hits_closest", C.c_uint64), ("bvh_nodes", C.c_uint32), ("bvh_node_bytes", C.c_uint32),
         ("tri_record_bytes", C.c_uint32), ("kernel_launches", C.c_uint32), ("device_error", C.c_uint32),
-        ("ms_last", C.c_float),
+        ("ms_last", C.c_float), ("ms_extend", C.c_float), ("ms_shadow", C.c_float), ("ms_film", C.c_float),
+        ("launches_extend", C.c_uint32), ("launches_shadow", C.c_uint32), ("launches_film", C.c_uint32),
     ]
 
 
@@ -95,6 +97,7 @@ SIGNATURES = {
     "vgb_trace_rays": (C.c_int, [_P, _P, _P, _P, _U32, C.c_int, _P, _P, _P, C.c_int]),
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
+    "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
 }
 
 _LIB = None

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
     const uint32_t* in_queue = st.pq[in_q];
     uint32_t err = 0;
     Counters cnt{0, 0};
-    uint32_t nclosest = 0;
+    uint32_t nclosest = 0, nhits = 0;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n_items; base += stride) {
         const uint32_t item = base + lane;
         bool active = item < n_items;
@@ -290,6 +290,7 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
             nclosest++;
         }
         bool hit = active && h.id != VGB_NO_HIT;
+        nhits += hit ? 1u : 0u;
         bool cont = false;
         bool lit = false;  // hit and simulate_lighting: NEE runs for this lane
         F3 Pp{0, 0, 0}, N{0, 0, 1};
@@ -474,9 +475,12 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
     }
     if (err) atomicOr(&st.counters[C_ERR], err);
     warp_reduce_add(&st.stats[2], nclosest);
+    warp_reduce_add(&st.stats[6], nhits);
     if (COUNT) {
         warp_reduce_add(&st.stats[0], cnt.nodes);
         warp_reduce_add(&st.stats[1], cnt.tris);
+        warp_reduce_add(&st.stats[4], cnt.nodes);
+        warp_reduce_add(&st.stats[5], cnt.tris);
     }
 }
 
@@ -625,6 +629,10 @@ __global__ void __launch_bounds__(256) k_trace(const DevScene s, const float* or
     if (COUNT) {
         warp_reduce_add(&stats[0], cnt.nodes);
         warp_reduce_add(&stats[1], cnt.tris);
+        if (!ANY) {
+            warp_reduce_add(&stats[4], cnt.nodes);
+            warp_reduce_add(&stats[5], cnt.tris);
+        }
     }
 }
 
@@ -667,6 +675,10 @@ struct vgb_context {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     vgb_stats stats{};
     bool count_pass = false;
+    bool profiling = false;
+    std::vector<cudaEvent_t> prof_events;   // pairs around each launch
+    std::vector<int> prof_family;           // 0 extend, 1 shadow, 2 film
+    size_t prof_used = 0;
 };
 
 namespace {
@@ -773,6 +785,30 @@ int grid_for(const vgb_context* ctx, size_t n, int per_sm = 8) {
     return (int)std::max<size_t>(1, std::min(blocks, cap));
 }
 
+struct Prof {
+    vgb_context* ctx;
+    int family;
+    size_t slot;
+    Prof(vgb_context* c, int fam) : ctx(c), family(fam), slot(0) {
+        if (!ctx->profiling) return;
+        if (ctx->prof_used + 2 > ctx->prof_events.size()) {
+            for (int k = 0; k < 64; ++k) {
+                cudaEvent_t e;
+                cudaEventCreate(&e);
+                ctx->prof_events.push_back(e);
+            }
+            ctx->prof_family.resize(ctx->prof_events.size() / 2);
+        }
+        slot = ctx->prof_used;
+        ctx->prof_used += 2;
+        ctx->prof_family[slot / 2] = family;
+        cudaEventRecord(ctx->prof_events[slot], ctx->stream);
+    }
+    ~Prof() {
+        if (ctx->profiling) cudaEventRecord(ctx->prof_events[slot + 1], ctx->stream);
+    }
+};
+
 template <int NB, bool COUNT>
 void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
     const DevScene s = dev_scene(ctx);
@@ -786,15 +822,22 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             // reset the output path queue and the shadow queues
             cudaMemsetAsync(&ctx->d_counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
             cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
-            k_extend<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            {
+                Prof p(ctx, 0);
+                k_extend<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            }
             launches++;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
+                Prof p(ctx, 1);
                 k_shadow<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
         }
-        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        {
+            Prof p(ctx, 2);
+            k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        }
         launches++;
     }
 }
@@ -849,6 +892,7 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_scene(ctx); free_bvh(ctx); free_scratch(ctx); free_staging(ctx);
     dfree(ctx->d_counters); dfree(ctx->d_stats);
+    for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -977,6 +1021,12 @@ VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable) {
     return VGB_OK;
 }
 
+VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    ctx->profiling = enable != 0;
+    return VGB_OK;
+}
+
 VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out) {
     if (!ctx || !out) return VGB_ERR_INVALID_ARGUMENT;
     *out = ctx->stats;
@@ -1052,6 +1102,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     uint32_t launches = 0;
+    ctx->prof_used = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     dispatch_render<false>(ctx, fp, f, launches);
     CK(cudaGetLastError());
@@ -1068,10 +1119,26 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
     ctx->stats.rays_closest = hs[2];
     ctx->stats.rays_shadow = hs[3];
+    ctx->stats.hits_closest = hs[6];
     ctx->stats.kernel_launches = launches;
     ctx->stats.ms_last = ms;
     ctx->stats.nodes_visited = 0;
     ctx->stats.tris_tested = 0;
+    ctx->stats.nodes_closest = 0;
+    ctx->stats.tris_closest = 0;
+    ctx->stats.ms_extend = ctx->stats.ms_shadow = ctx->stats.ms_film = 0.f;
+    ctx->stats.launches_extend = ctx->stats.launches_shadow = ctx->stats.launches_film = 0;
+    if (ctx->profiling) {
+        float* fam_ms[3] = {&ctx->stats.ms_extend, &ctx->stats.ms_shadow, &ctx->stats.ms_film};
+        uint32_t* fam_n[3] = {&ctx->stats.launches_extend, &ctx->stats.launches_shadow, &ctx->stats.launches_film};
+        for (size_t k = 0; k < ctx->prof_used; k += 2) {
+            float e = 0.f;
+            cudaEventElapsedTime(&e, ctx->prof_events[k], ctx->prof_events[k + 1]);
+            const int fam = ctx->prof_family[k / 2];
+            *fam_ms[fam] += e;
+            *fam_n[fam] += 1;
+        }
+    }
     if ((s = check_device_error(ctx)) != VGB_OK) return s;
     if (ctx->count_pass) {
         // counting pass: same kernels with traversal counters, into scratch film planes
@@ -1080,12 +1147,17 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
         none.power = nullptr;
         CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
         uint32_t l2 = 0;
+        const bool prof = ctx->profiling;
+        ctx->profiling = false;
         dispatch_render<true>(ctx, fp, none, l2);
+        ctx->profiling = prof;
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(ctx->stream));
         CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
         ctx->stats.nodes_visited = hs[0];
         ctx->stats.tris_tested = hs[1];
+        ctx->stats.nodes_closest = hs[4];
+        ctx->stats.tris_closest = hs[5];
         if ((s = check_device_error(ctx)) != VGB_OK) return s;
     }
     return VGB_OK;
@@ -1144,6 +1216,8 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
     ctx->stats.kernel_launches = 1;
     ctx->stats.nodes_visited = hs[0];
     ctx->stats.tris_tested = hs[1];
+    ctx->stats.nodes_closest = hs[4];
+    ctx->stats.tris_closest = hs[5];
     if (any_hit) { ctx->stats.rays_shadow = n; ctx->stats.rays_closest = 0; }
     else { ctx->stats.rays_closest = n; ctx->stats.rays_shadow = 0; }
     return check_device_error(ctx);
