@@ -198,6 +198,22 @@ VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam
 /* CPUPathTracer::render (include/implementation/rendering/cpu_path_tracer.ipp:29-161). */
 VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                               uint32_t nlights, const vgb_pt_options* opts, vgb_film* film);
+/* Render without allocating.  No counterpart in the reference: Vira's CPU tracer has no
+ * device memory to manage.  For callers that cannot allocate device memory once their scene is
+ * set up -- a frame loop held to a fixed memory budget, or a host application whose own
+ * allocator owns the device -- because a cudaMalloc inside a render call can synchronize the
+ * device or fail.  Same kernels and results as vgb_render, with every byte of scratch taken
+ * from one fixed 8 MiB array compiled into the library, which every GPU that loads the library
+ * holds until the process exits.  Limits: the film must be device memory, and a frame of
+ * P = width*height pixels, B bands and L lights needs about P * 4 * (15 + 6*B + L*(8 + B))
+ * bytes of the 8 MiB (about 26,000 pixels at 8 bands and 1 light, 41,000 at 4 bands); larger
+ * frames are rejected with VGB_ERR_INVALID_ARGUMENT and a message naming the sizes.  The
+ * first call on a device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls on a device share the array and it
+ * keeps the last call's contents (each call clears its counters itself): calls that overlap on
+ * the GPU -- two contexts or two streams rendering at once on one device -- race. */
+VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                      uint32_t nlights, const vgb_pt_options* opts, vgb_film* film);
 /* TLAS::intersect(Ray&) seam (include/vira/rendering/acceleration/tlas.hpp:24): a batch of
  * rays, closest hit (any_hit = 0) or occlusion (any_hit = 1, tmax per ray or +inf).
  * origins/dirs: 3 floats per ray.  tri_out: VGB_NO_HIT on a miss; t_out: +inf on a miss;

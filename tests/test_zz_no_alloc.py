@@ -1,0 +1,134 @@
+"""vgb_render_noalloc: the render entry point that allocates no device memory.
+
+It is meant for callers that cannot allocate once their scene is set up -- a frame loop held to
+a fixed memory budget, or a host application whose own allocator owns the device -- since a
+cudaMalloc inside a render call can synchronize the device or fail.  It runs the same kernels
+as vgb_render with their scratch in a fixed array inside the library, so its planes must match
+vgb_render's.  Two no-alloc calls run back to back with different frames, so the second one
+also shows that what the first left in the shared array does not leak into its result.
+
+This file is named to be collected last.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from vira_gb300 import capi, workloads
+
+pytestmark = pytest.mark.gpu
+
+PLANES = ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo", "normal_global",
+          "depth", "alpha", "triangle_id")
+
+
+def _device_film(torch, B, H, W, dev, omega):
+    planes = {}
+    for name in PLANES:
+        if name in ("depth", "alpha"):
+            shape, dt = (H, W), torch.float32
+        elif name == "triangle_id":
+            shape, dt = (H, W), torch.int32
+        elif name == "normal_global":
+            shape, dt = (3, H, W), torch.float32
+        else:
+            shape, dt = (B, H, W), torch.float32
+        planes[name] = torch.full(shape, -7, dtype=dt, device=dev)
+    f = capi.Film()
+    for name, t in planes.items():
+        setattr(f, name, t.data_ptr())
+    f.pixel_solid_angle = omega.data_ptr()
+    f.on_device = 1
+    return planes, f
+
+
+def _rel(a, b):
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    e = np.abs(a - b) / np.maximum(np.abs(b), 1e-30)
+    e[same] = 0.0
+    return float(e.max()) if e.size else 0.0
+
+
+def test_noalloc_matches_render_on_two_calls_in_a_row(gpu):
+    import torch
+
+    scene, cam_id = workloads.path_traced(posts=65, tex=64, resolution=96, spp=4, bounces=2, rr_depth=2)
+    s2 = scene.new_sphere_light(np.float32(5.0e5), 6.96e8)
+    scene.set_sun_direction(s2, azimuth_deg=200.0, elevation_deg=40.0)
+    scene.build_tlas()
+    lib = capi.load()
+    ctx = scene.context()
+    camera = scene[cam_id]
+    cam = camera.to_c(scene.origin, scene.bands.size)
+    lights, nl = scene.c_lights()
+    omega = scene.pixel_solid_angle(camera, cam)
+    dev = omega.device
+    B, H, W = scene.bands.size, cam.height, cam.width
+    frames = [(4, 0, 11), (2, 3, 12)]  # (samples, frame, seed)
+
+    def opts_for(spp, frame, seed):
+        scene.pathtracer.options.samples = spp
+        scene.pathtracer.options.frame = frame
+        scene.pathtracer.options.seed = seed
+        return scene.pathtracer.c_options(scene)
+
+    refs = []
+    for spp, frame, seed in frames:
+        planes, f = _device_film(torch, B, H, W, dev, omega)
+        o = opts_for(spp, frame, seed)
+        capi.check(lib.vgb_render(ctx, C.byref(cam), lights, nl, C.byref(o), C.byref(f)), ctx, "render")
+        refs.append({k: v.cpu().numpy() for k, v in planes.items()})
+    outs = []
+    films = [_device_film(torch, B, H, W, dev, omega) for _ in frames]
+    torch.cuda.synchronize()
+    for (spp, frame, seed), (planes, f) in zip(frames, films):
+        o = opts_for(spp, frame, seed)
+        capi.check(lib.vgb_render_noalloc(ctx, C.byref(cam), lights, nl, C.byref(o), C.byref(f)), ctx,
+                   "render_noalloc")
+        st = capi.Stats()
+        lib.vgb_get_stats(ctx, C.byref(st))
+        assert st.rays_closest >= H * W * spp and st.rays_shadow > 0
+        outs.append({k: v.cpu().numpy() for k, v in planes.items()})
+    for ref, out in zip(refs, outs):
+        assert np.array_equal(ref["triangle_id"], out["triangle_id"])
+        for k in PLANES:
+            if k != "triangle_id":
+                assert _rel(out[k], ref[k]) <= 1e-4, k
+    assert not np.array_equal(outs[0]["total_radiance"], outs[1]["total_radiance"])
+    scene.close()
+
+
+def test_noalloc_allocates_nothing_and_rejects_oversized_frames(gpu):
+    import torch
+
+    scene, cam_id = workloads.plain_direct(posts=65, resolution=128)
+    scene.build_tlas()
+    lib = capi.load()
+    ctx = scene.context()
+    camera = scene[cam_id]
+    cam = camera.to_c(scene.origin, scene.bands.size)
+    lights, nl = scene.c_lights()
+    omega = scene.pixel_solid_angle(camera, cam)
+    opts = scene.pathtracer.c_options(scene)
+    planes, f = _device_film(torch, 4, cam.height, cam.width, omega.device, omega)
+    capi.check(lib.vgb_render_noalloc(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(f)), ctx)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(omega.device)[0]
+    for _ in range(3):
+        capi.check(lib.vgb_render_noalloc(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(f)), ctx)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(omega.device)[0] == free0
+    # a frame beyond the fixed array is refused with a message, before any device work
+    big = camera.to_c(scene.origin, 4)
+    big.width, big.height = 1024, 1024
+    assert lib.vgb_render_noalloc(ctx, C.byref(big), lights, nl, C.byref(opts), C.byref(f)) == 1
+    assert b"scratch" in lib.vgb_last_error(ctx)
+    # host films would need staging memory: refused
+    hf = capi.Film()
+    hf.on_device = 0
+    assert lib.vgb_render_noalloc(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(hf)) == 1
+    scene.close()

@@ -94,6 +94,7 @@ SIGNATURES = {
     "vgb_bvh_build": (C.c_int, [_P, C.POINTER(BvhOptions)]),
     "vgb_pixel_solid_angle": (C.c_int, [_P, C.POINTER(Camera), _P, C.c_int]),
     "vgb_render": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
+    "vgb_render_noalloc": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
     "vgb_trace_rays": (C.c_int, [_P, _P, _P, _P, _U32, C.c_int, _P, _P, _P, C.c_int]),
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),

@@ -1224,3 +1224,164 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
 }
 
 }  // extern "C"
+
+// ====================================================================== render without allocation
+// vgb_render_noalloc: the same wavefront kernels as vgb_render, but every byte of their scratch
+// (path state, live-path and shadow-ray queues, per-pixel accumulators, queue counters and the
+// device error word) lives in one fixed device array that is part of this library image.  It
+// exists for callers that must not allocate device memory once their scene is set up -- for
+// example a frame loop with a fixed memory budget, or a host application whose allocator owns
+// the device, where a cudaMalloc inside a render call would synchronize the device or could
+// fail.  The array is shared by every call on a device and keeps the previous call's contents.
+#include <mutex>
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB per device
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+inline size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Bytes of the fixed array a frame of P pixels, B bands and L lights needs.
+size_t noalloc_bytes(size_t P, size_t B, size_t L) {
+    const size_t f = 4;
+    size_t n = 2 * 256;  // counters, statistics
+    const size_t planes[] = {3, 3, B, B, B, 1, B, B, B, 3, 1, 1, 1, 1, 1};
+    for (size_t k : planes) n += up256(k * P * f);
+    n += L * (up256(3 * P * f) + up256(3 * P * f) + up256(P * f) + up256(P * f) + up256(B * P * f));
+    return n;
+}
+
+template <int NB>
+void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, uint32_t& launches) {
+    const DevScene s = dev_scene(ctx);
+    const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
+    const int g0 = grid_for(ctx, n0);
+    const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
+    for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
+        uint32_t q = 0;
+        for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
+            cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
+            cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
+            k_extend<NB, false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            launches++;
+            for (uint32_t l = 0; l < fp.nlights; ++l) {
+                k_shadow<NB, false><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                launches++;
+            }
+            q ^= 1u;
+        }
+        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        launches++;
+    }
+}
+
+}  // namespace
+
+extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                                 uint32_t nlights, const vgb_pt_options* opts, vgb_film* film) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: null camera/options/film");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_noalloc: build the BVH first");
+    if (!film->on_device)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: film planes must be device memory (on_device = 1)");
+    if (opts->samples == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: options.samples must be >= 1");
+    if (opts->nbands != ctx->nbands)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: nbands differs from the scene");
+    if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: at most 8 lights");
+    if (cam->width == 0 || cam->height == 0)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: bad resolution");
+    if (film->received_power && !film->pixel_solid_angle)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: received_power needs pixel_solid_angle");
+    const size_t P = (size_t)cam->width * cam->height;
+    const uint32_t B = ctx->nbands;
+    const size_t need = noalloc_bytes(P, B, std::max<uint32_t>(1, nlights));
+    if (need > kNoAllocScratchBytes) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "render_noalloc: frame needs %zu bytes of scratch, the fixed array holds %zu "
+                      "(%zu x %zu pixels, %u bands, %u lights); use vgb_render or a smaller frame",
+                      need, kNoAllocScratchBytes, (size_t)cam->width, (size_t)cam->height, B, nlights);
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, msg);
+    }
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: device index beyond 63");
+    CK(cudaSetDevice(ctx->device));
+    unsigned char* base = nullptr;
+    {
+        // Once per device, with that device current: the device address of the fixed array.
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[ctx->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(ctx, VGB_ERR_CUDA, std::string("render_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_noalloc_ptr[ctx->device] = static_cast<unsigned char*>(p);
+        }
+        base = g_noalloc_ptr[ctx->device];
+    }
+    // Carve the frame's scratch out of the fixed array.
+    DevState st{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) { unsigned char* p = base + off; off += up256(bytes); return p; };
+    const size_t f = sizeof(float);
+    st.counters = reinterpret_cast<uint32_t*>(take(256));
+    st.stats = reinterpret_cast<uint64_t*>(take(256));
+    st.org = (float*)take(3 * P * f); st.dir = (float*)take(3 * P * f); st.thr = (float*)take(B * P * f);
+    st.prad = (float*)take(B * P * f); st.brad = (float*)take(B * P * f); st.pend = (uint32_t*)take(P * f);
+    st.arad = (float*)take(B * P * f); st.adir = (float*)take(B * P * f); st.aalb = (float*)take(B * P * f);
+    st.anrm = (float*)take(3 * P * f); st.adep = (float*)take(P * f); st.acnt = (uint32_t*)take(P * f);
+    st.atri = (uint32_t*)take(P * f); st.pq[0] = (uint32_t*)take(P * f); st.pq[1] = (uint32_t*)take(P * f);
+    for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
+        if (l < std::max<uint32_t>(1, nlights)) {
+            st.sq_org[l] = (float*)take(3 * P * f); st.sq_dir[l] = (float*)take(3 * P * f);
+            st.sq_tmax[l] = (float*)take(P * f); st.sq_slot[l] = (uint32_t*)take(P * f);
+            st.sq_con[l] = (float*)take(B * P * f);
+        } else {
+            st.sq_org[l] = st.sq_dir[l] = st.sq_tmax[l] = st.sq_con[l] = nullptr; st.sq_slot[l] = nullptr;
+        }
+    }
+    st.P = P;
+    FrameParams fp;
+    std::memset(&fp, 0, sizeof(fp));
+    fp.cam = *cam;
+    fp.opt = *opts;
+    for (uint32_t l = 0; l < nlights; ++l) fp.lights[l] = lights[l];
+    fp.nlights = nlights;
+    fp.nb = B;
+    fp.tiles_x = (cam->width + 7) / 8;
+    fp.tiles_y = (cam->height + 3) / 4;
+    FilmOut fo{};
+    fo.total = film->total_radiance; fo.direct = film->direct_radiance; fo.indirect = film->indirect_radiance;
+    fo.power = film->received_power; fo.albedo = film->albedo; fo.normal = film->normal_global;
+    fo.depth = film->depth; fo.alpha = film->alpha; fo.tri = film->triangle_id; fo.omega = film->pixel_solid_angle;
+    // The array keeps the last call's contents: the counters, statistics and error word must
+    // start at zero; every other region is written before it is read.
+    CK(cudaMemsetAsync(st.counters, 0, 256, ctx->stream));
+    CK(cudaMemsetAsync(st.stats, 0, 256, ctx->stream));
+    uint32_t launches = 0;
+    if (B <= 1) launch_noalloc<1>(ctx, fp, fo, st, launches);
+    else if (B <= 4) launch_noalloc<4>(ctx, fp, fo, st, launches);
+    else launch_noalloc<8>(ctx, fp, fo, st, launches);
+    CK(cudaGetLastError());
+    uint32_t err_word = 0;
+    uint64_t hs[8] = {0};
+    CK(cudaMemcpyAsync(&err_word, &st.counters[C_ERR], sizeof(err_word), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hs, st.stats, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->stats.rays_closest = hs[2];
+    ctx->stats.rays_shadow = hs[3];
+    ctx->stats.hits_closest = hs[6];
+    ctx->stats.kernel_launches = launches;
+    ctx->stats.device_error = err_word;
+    if (err_word)
+        return fail(ctx, VGB_ERR_DEVICE_LIMIT,
+                    std::string("render_noalloc: device traversal limit hit:") + ((err_word & kErrStack) ? " stack" : "") +
+                        ((err_word & kErrIter) ? " iterations" : ""));
+    return VGB_OK;
+}
