@@ -141,21 +141,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------ CPU legs
-def cpu_sample(scene, cam_id, seconds: float, threads: int):
-    """Times the oracle over bands of rows of the same frame until ~`seconds` of CPU work."""
+def oracle_scene(scene):
     from oracle import oracle
 
     if scene.flat is None:
         scene.flatten()
-    t0 = time.perf_counter()
-    osc = oracle.OracleScene.from_flat(scene.flat, scene.bands.size)
-    build_s = time.perf_counter() - t0
+    return oracle.OracleScene.from_flat(scene.flat, scene.bands.size)
+
+
+def cpu_sample(scene, cam_id, osc, seconds: float, threads: int, start_row=None):
+    """Times the oracle over bands of rows of the same frame until ~`seconds` of CPU work."""
     cam = scene[cam_id].to_c(scene.origin, scene.bands.size)
     lights, nl = scene.c_lights()
     opts = scene.pathtracer.c_options(scene)
     H = cam.height
     rows, total_rays, total_t, spp_px = 0, 0, 0.0, 0
-    r = max(1, H // 2 - 1)
+    r = max(0, H // 2 - 1) if start_row is None else start_row % H
     nrows = 1
     while total_t < seconds and r < H:
         t = time.perf_counter()
@@ -169,9 +170,8 @@ def cpu_sample(scene, cam_id, seconds: float, threads: int):
         r += done
         if dt < seconds / 8:
             nrows = min(H, nrows * 2)
-    osc.close()
     return {"mrays_s": total_rays / total_t / 1e6, "spp_s": spp_px / total_t, "rows": rows, "seconds": total_t,
-            "rays": total_rays, "oracle_bvh_build_s": build_s}
+            "rays": total_rays}
 
 
 def run_reference(args, p, rank, world):
@@ -181,22 +181,25 @@ def run_reference(args, p, rank, world):
 
     scene, cam_id = build_scene(p, device=0)
     threads = oracle.nthreads()
+    osc = oracle_scene(scene)  # the oracle's own BVH, built once outside the timed steps
     per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
     for _ in range(args.warmup):
-        cpu_sample(scene, cam_id, min(per_step, 2.0), threads)
-    vals, spps, rows = [], [], 0
+        cpu_sample(scene, cam_id, osc, min(per_step, 2.0), threads)
+    vals, spps, rows, secs = [], [], 0, 0.0
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        s = cpu_sample(scene, cam_id, per_step, threads)
+    for k in range(args.steps):
+        s = cpu_sample(scene, cam_id, osc, per_step, threads, start_row=scene[cam_id].resolution[1] // 4 + 17 * k)
         vals.append(s["mrays_s"])
         spps.append(s["spp_s"])
         rows = s["rows"]
+        secs += s["seconds"]
+    osc.close()
     elapsed = time.perf_counter() - t0
     v = float(np.mean(vals))
     W = scene[cam_id].resolution[0]
     line = {
         "metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / max(1, args.steps), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm + craters)",
         "impl": "reference",
         "config": {"workload": config_name(p), "parallelism": "host threads"},
@@ -262,6 +265,20 @@ class Renderer:
         return st
 
 
+def reduce_replicas(total_ms: float, rays: float, paths: float, world: int, device):
+    """Whole-job figures of N replicas: the slowest rank's time, the sum of all ranks' work."""
+    if world <= 1:
+        return total_ms, rays, paths
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    w = torch.tensor([rays, paths], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(w[0]), float(w[1])
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -312,13 +329,7 @@ def run_ours(args, p, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     clk = clocks.stop()
     lib.vgb_set_profiling(r.ctx, 0)
-    total_ms = float(sum(ms))
-    if world > 1:
-        t = torch.tensor([total_ms, float(rays), float(paths)], dtype=torch.float64, device=dev)
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax[:1], op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t[1:], op=torch.distributed.ReduceOp.SUM)
-        total_ms, rays, paths = float(tmax[0]), float(t[1]), float(t[2])
+    total_ms, rays, paths = reduce_replicas(float(sum(ms)), float(rays), float(paths), world, dev)
     value = rays / (total_ms / 1000.0) / 1e6
 
     # e2e through the C ABI with host buffers (wall clock around the blocking call)
@@ -338,22 +349,25 @@ def run_ours(args, p, rank, world, local_rank):
     lib.vgb_set_count_pass(r.ctx, 0)
     cst = r.stats()
     s0 = st_list[-1]
-    fam = {"k_extend": (sum(s.ms_extend for s in st_list), sum(s.launches_extend for s in st_list)),
+    fam = {"k_trace": (sum(s.ms_trace for s in st_list), sum(s.launches_trace for s in st_list)),
+           "k_shade": (sum(s.ms_shade for s in st_list), sum(s.launches_shade for s in st_list)),
            "k_shadow": (sum(s.ms_shadow for s in st_list), sum(s.launches_shadow for s in st_list)),
            "k_end_sample": (sum(s.ms_film for s in st_list), sum(s.launches_film for s in st_list))}
     B = scene.bands.size
     nodes_sh = cst.nodes_visited - cst.nodes_closest
     tris_sh = cst.tris_tested - cst.tris_closest
+    # algorithmic bytes of one render, per kernel family
     alg = {
-        "k_extend": cst.nodes_closest * NODE_BYTES + cst.tris_closest * TRI_BYTES + cst.rays_closest * RAY_IO_CLOSEST
-        + cst.hits_closest * shade_bytes(B),
+        "k_trace": cst.nodes_closest * NODE_BYTES + cst.tris_closest * TRI_BYTES + cst.rays_closest * RAY_IO_CLOSEST,
+        "k_shade": cst.hits_closest * shade_bytes(B) + cst.rays_closest * 16,
         "k_shadow": nodes_sh * NODE_BYTES + tris_sh * TRI_BYTES + cst.rays_shadow * (RAY_IO_SHADOW + 4 * B + 8),
         "k_end_sample": r.cam.width * r.cam.height * r.opts.samples * 4 * (4 * B + 2),
     }
+    launches_one = {"k_trace": s0.launches_trace, "k_shade": s0.launches_shade, "k_shadow": s0.launches_shadow,
+                    "k_end_sample": s0.launches_film}
     dominant = max(fam, key=lambda k: fam[k][0])
     dms, dl = fam[dominant]
-    per_launch_bytes = alg[dominant] / max(1, s0.__getattribute__(
-        {"k_extend": "launches_extend", "k_shadow": "launches_shadow", "k_end_sample": "launches_film"}[dominant]))
+    per_launch_bytes = alg[dominant] / max(1, launches_one[dominant])
     per_launch_ms = dms / max(1, dl)
     achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
@@ -377,7 +391,9 @@ def run_ours(args, p, rank, world, local_rank):
         from oracle import oracle
 
         threads = oracle.nthreads()
-        c = cpu_sample(scene, cam_id, args.cpu_seconds, threads)
+        osc = oracle_scene(scene)
+        c = cpu_sample(scene, cam_id, osc, args.cpu_seconds, threads)
+        osc.close()
         cpu = {"value": c["mrays_s"], "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": f"rows {c['rows']} x {r.cam.width} px of the same frame at {r.opts.samples} spp "
                          f"({c['rays']} rays in {c['seconds']:.1f} s; CPU restatement, BVH2 of vira_blas.ipp, not Embree)"}

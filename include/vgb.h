@@ -138,9 +138,10 @@ typedef struct vgb_stats {
     uint32_t kernel_launches;  /* kernels launched by the last render */
     uint32_t device_error;     /* last device error word (0 = none) */
     float ms_last;             /* device time of the last render (CUDA events) */
-    /* profiling mode only (vgb_set_profiling): device time and launches per kernel family */
-    float ms_extend, ms_shadow, ms_film;
-    uint32_t launches_extend, launches_shadow, launches_film;
+    /* profiling mode only (vgb_set_profiling): device time and launches per kernel family:
+     * closest-hit traversal, shading, shadow traversal, film */
+    float ms_trace, ms_shade, ms_shadow, ms_film;
+    uint32_t launches_trace, launches_shade, launches_shadow, launches_film;
 } vgb_stats;
 
 /* ========================= context ============================================= */
@@ -205,8 +206,8 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
  * device or fail.  Same kernels and results as vgb_render, with every byte of scratch taken
  * from one fixed 8 MiB array compiled into the library, which every GPU that loads the library
  * holds until the process exits.  Limits: the film must be device memory, and a frame of
- * P = width*height pixels, B bands and L lights needs about P * 4 * (15 + 6*B + L*(8 + B))
- * bytes of the 8 MiB (about 26,000 pixels at 8 bands and 1 light, 41,000 at 4 bands); larger
+ * P = width*height pixels, B bands and L lights needs about P * 4 * (19 + 6*B + L*(8 + B))
+ * bytes of the 8 MiB (about 25,000 pixels at 8 bands and 1 light, 38,000 at 4 bands); larger
  * frames are rejected with VGB_ERR_INVALID_ARGUMENT and a message naming the sizes.  The
  * first call on a device looks up the array's device address (cudaGetSymbolAddress), so make
  * that first call before any stream capture.  All calls on a device share the array and it
@@ -229,7 +230,7 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* origins, const 
 VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out);
 VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
 /* Per-launch CUDA events around every kernel of vgb_render, summed per kernel family into
- * vgb_stats.ms_extend / ms_shadow / ms_film. */
+ * vgb_stats.ms_trace / ms_shade / ms_shadow / ms_film. */
 VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
 
 #ifdef __cplusplus

@@ -63,7 +63,8 @@ def rel_err(a, b, floor=1e-30):
     b = np.asarray(b, np.float64)
     both_nan = np.isnan(a) & np.isnan(b)
     both_inf = np.isinf(a) & np.isinf(b) & (np.sign(a) == np.sign(b))
-    e = np.abs(a - b) / np.maximum(np.abs(b), floor)
+    with np.errstate(invalid="ignore"):
+        e = np.abs(a - b) / np.maximum(np.abs(b), floor)
     e[both_nan | both_inf] = 0.0
     return e
 

@@ -71,8 +71,9 @@ class Stats(C.Structure):
         ("tris_tested", C.c_uint64), ("nodes_closest", C.c_uint64), ("tris_closest", C.c_uint64),
         ("hits_closest", C.c_uint64), ("bvh_nodes", C.c_uint32), ("bvh_node_bytes", C.c_uint32),
         ("tri_record_bytes", C.c_uint32), ("kernel_launches", C.c_uint32), ("device_error", C.c_uint32),
-        ("ms_last", C.c_float), ("ms_extend", C.c_float), ("ms_shadow", C.c_float), ("ms_film", C.c_float),
-        ("launches_extend", C.c_uint32), ("launches_shadow", C.c_uint32), ("launches_film", C.c_uint32),
+        ("ms_last", C.c_float), ("ms_trace", C.c_float), ("ms_shade", C.c_float), ("ms_shadow", C.c_float),
+        ("ms_film", C.c_float), ("launches_trace", C.c_uint32), ("launches_shade", C.c_uint32),
+        ("launches_shadow", C.c_uint32), ("launches_film", C.c_uint32),
     ]
 
 

@@ -1,10 +1,11 @@
 // vgb_cuda.cu -- wavefront path-tracing kernels for sm_103a and the C ABI around them.
 //
 // Stages of one render (CPUPathTracer::render, cpu_path_tracer.ipp:29-161), per sample:
-//   k_extend  (bounce 0: camera rays over all pixels, 8x4-pixel warp tiles; bounce b>0: the
-//              compacted queue of live paths)  closest-hit traversal + processIntersection:
-//              AOVs, shading point, origin offset, NEE shadow-ray enqueue (one queue per light),
-//              cosine bounce sampling, throughput update, live-path enqueue (warp ballot);
+//   k_trace   (bounce 0: camera rays over all pixels, 8x4-pixel warp tiles; bounce b>0: the
+//              compacted queue of live paths)  closest-hit traversal, one hit record per ray;
+//   k_shade   processIntersection for the same items: AOVs, shading point, origin offset, NEE
+//              shadow-ray enqueue (one queue per light), cosine bounce sampling, throughput
+//              update, live-path enqueue (warp ballot);
 //   k_shadow  (one launch per light)  occlusion traversal of the queued shadow rays, adding
 //              each unoccluded contribution to the path's per-bounce radiance;
 //   k_end_sample  per pixel: folds the last bounce's radiance into the path and the path into
@@ -65,6 +66,7 @@ struct DevState {
     float* sq_tmax[VGB_MAX_LIGHTS];  // [P]
     uint32_t* sq_slot[VGB_MAX_LIGHTS];
     float* sq_con[VGB_MAX_LIGHTS];   // [B][P]
+    float4* hit;         // [P] closest-hit record per queue item: (t, id bits, w(v1), w(v2))
     uint32_t* counters;  // see C_* below
     uint64_t* stats;     // [0] nodes, [1] tris, [2] closest rays, [3] shadow rays
     size_t P;            // plane stride
@@ -202,26 +204,96 @@ __device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float
         if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
 }
 
-// ------------------------------------------------------------------ k_extend
-template <int NB, bool COUNT>
-__global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
-                                                uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
+// Camera::pixelToRay for the pixel of bounce-0 item `item` (8x4-pixel warp tiles).
+__device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item, uint32_t sample, uint32_t& slot,
+                                           F3& ro, F3& rd) {
+    const uint32_t tile = item >> 5, ln = item & 31u;
+    const uint32_t tx = tile % fp.tiles_x, ty = tile / fp.tiles_x;
+    const uint32_t pi = tx * 8u + (ln & 7u), pj = ty * 4u + (ln >> 3);
+    if (pi >= fp.cam.width || pj >= fp.cam.height) return false;
+    slot = pj * fp.cam.width + pi;
+    float X = (float)pi, Y = (float)pj;
+    if (sample != 0) {
+        U4 jr = philox(U4{slot, sample, fp.opt.frame, kSlotJitter}, (uint32_t)fp.opt.seed, (uint32_t)(fp.opt.seed >> 32));
+        X = X + u01(jr.x);
+        Y = Y + u01(jr.y);
+    }
+    const float* K = fp.cam.kinv;
+    float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
+    float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
+    F3 dc{hx, fp.cam.z_dir * hy, fp.cam.z_dir};
+    const float* R = fp.cam.rotation;
+    F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
+          (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
+    rd = normalize(dw);
+    ro = F3{fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]};
+    return true;
+}
+
+// ------------------------------------------------------------------ k_trace (closest hit)
+// Scene::intersect for every live path: camera rays at bounce 0, queued continuation rays
+// after.  Writes one 16-byte hit record per queue item; kept lean so that enough warps are
+// resident to hide the latency of the node and triangle fetches.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
+                                               uint32_t bounce, uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
+    const size_t P = st.P;
+    const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
+    const uint32_t* in_queue = st.pq[in_q];
+    uint32_t err = 0, nclosest = 0;
+    Counters cnt{0, 0};
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n_items; item += gridDim.x * blockDim.x) {
+        uint32_t slot = 0;
+        F3 ro, rd;
+        if (bounce == 0) {
+            if (!camera_ray(fp, item, sample, slot, ro, rd)) continue;
+        } else {
+            slot = in_queue[item];
+            ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
+            rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
+        }
+        HitOut h;
+        h.U = h.V = h.W = 0.f; h.det = 1.f;
+        const WRay wr = make_wray(ro, rd);
+        traverse<false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+        nclosest++;
+        float w0 = 0.f, w1 = 0.f;
+        if (h.id != VGB_NO_HIT) {
+            const float rcp = 1.0f / h.det;
+            w0 = h.V * rcp;
+            w1 = h.W * rcp;
+        }
+        st.hit[item] = make_float4(h.t, __uint_as_float(h.id), w0, w1);
+    }
+    if (err) atomicOr(&st.counters[C_ERR], err);
+    warp_reduce_add(&st.stats[2], nclosest);
+    if (COUNT) {
+        warp_reduce_add(&st.stats[0], cnt.nodes);
+        warp_reduce_add(&st.stats[1], cnt.tris);
+        warp_reduce_add(&st.stats[4], cnt.nodes);
+        warp_reduce_add(&st.stats[5], cnt.tris);
+    }
+}
+
+// ------------------------------------------------------------------ k_shade
+// processIntersection for every item of k_trace: AOVs, shading point, NEE shadow-ray enqueue,
+// BSDF-sampled continuation and live-path enqueue (warp-aggregated appends).
+template <int NB>
+__global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
+                                               uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const uint32_t nb = fp.nb;
     const size_t P = st.P;
-    const uint32_t W = fp.cam.width, H = fp.cam.height;
     const int lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
     uint32_t* out_count = &st.counters[(in_q ^ 1u)];
     uint32_t* out_q = st.pq[in_q ^ 1u];
     const uint32_t* in_queue = st.pq[in_q];
-    uint32_t err = 0;
-    Counters cnt{0, 0};
-    uint32_t nclosest = 0, nhits = 0;
+    uint32_t nhits = 0;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n_items; base += stride) {
         const uint32_t item = base + lane;
         bool active = item < n_items;
-        uint32_t slot = 0, pi = 0, pj = 0;
+        uint32_t slot = 0;
         F3 ro{0, 0, 0}, rd{0, 0, 1};
         float thr[NB];
         float prad[NB];
@@ -229,29 +301,8 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
         for (int k = 0; k < NB; ++k) { thr[k] = 1.f; prad[k] = 0.f; }
         if (active) {
             if (bounce == 0) {
-                const uint32_t tile = item >> 5, ln = item & 31u;
-                const uint32_t tx = tile % fp.tiles_x, ty = tile / fp.tiles_x;
-                pi = tx * 8u + (ln & 7u);
-                pj = ty * 4u + (ln >> 3);
-                active = (pi < W) && (pj < H);
-                slot = pj * W + pi;
+                active = camera_ray(fp, item, sample, slot, ro, rd);
                 if (active) {
-                    float X = (float)pi, Y = (float)pj;
-                    if (sample != 0) {
-                        U4 jr = philox(U4{slot, sample, fp.opt.frame, kSlotJitter}, (uint32_t)fp.opt.seed,
-                                       (uint32_t)(fp.opt.seed >> 32));
-                        X = X + u01(jr.x);
-                        Y = Y + u01(jr.y);
-                    }
-                    const float* K = fp.cam.kinv;
-                    float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
-                    float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-                    F3 dc{hx, fp.cam.z_dir * hy, fp.cam.z_dir};
-                    const float* R = fp.cam.rotation;
-                    F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
-                          (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
-                    rd = normalize(dw);
-                    ro = F3{fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]};
                     if (sample == 0) {
 #pragma unroll
                         for (int k = 0; k < NB; ++k)
@@ -281,15 +332,11 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
                 st.pend[slot] = 0u;
             }
         }
-        // ---- closest hit
-        HitOut h;
-        h.t = __int_as_float(0x7f800000); h.id = VGB_NO_HIT; h.U = h.V = h.W = 0.f; h.det = 1.f;
-        WRay wr = make_wray(ro, rd);
-        if (active) {
-            traverse<false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
-            nclosest++;
-        }
-        bool hit = active && h.id != VGB_NO_HIT;
+        // ---- closest hit, from k_trace
+        float4 hr = make_float4(__int_as_float(0x7f800000), __uint_as_float(VGB_NO_HIT), 0.f, 0.f);
+        if (active) hr = st.hit[item];
+        const uint32_t hid = __float_as_uint(hr.y);
+        bool hit = active && hid != VGB_NO_HIT;
         nhits += hit ? 1u : 0u;
         bool cont = false;
         bool lit = false;  // hit and simulate_lighting: NEE runs for this lane
@@ -322,11 +369,10 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
         F3 tg{1, 0, 0}, bt{0, 1, 0};
         if (hit) {
             // ---- processIntersection (cpu_path_tracer.ipp:280-469)
-            const uint32_t t = h.id;
-            const float rcp = 1.0f / h.det;
+            const uint32_t t = hid;
             float w[3];
-            w[0] = h.V * rcp;
-            w[1] = h.W * rcp;
+            w[0] = hr.z;
+            w[1] = hr.w;
             w[2] = 1.0f - w[0] - w[1];
             const uint32_t i0 = __ldg(&s.idx[3 * t]), i1 = __ldg(&s.idx[3 * t + 1]), i2 = __ldg(&s.idx[3 * t + 2]);
             const uint32_t vi[3] = {i1, i2, i0};
@@ -369,7 +415,7 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
                 for (int k = 0; k < NB; ++k)
                     if (k < (int)nb) st.aalb[k * P + slot] += alb[k];
                 st.anrm[slot] += N.x; st.anrm[P + slot] += N.y; st.anrm[2 * P + slot] += N.z;
-                st.adep[slot] += h.t;
+                st.adep[slot] += hr.x;
                 st.acnt[slot] += 1u;
             }
             if (fp.opt.simulate_lighting) {
@@ -473,15 +519,7 @@ __global__ void __launch_bounds__(256) k_extend(const DevScene s, DevState st, c
         const uint32_t pqi = warp_append(out_count, cont);
         if (cont) out_q[pqi] = slot;
     }
-    if (err) atomicOr(&st.counters[C_ERR], err);
-    warp_reduce_add(&st.stats[2], nclosest);
     warp_reduce_add(&st.stats[6], nhits);
-    if (COUNT) {
-        warp_reduce_add(&st.stats[0], cnt.nodes);
-        warp_reduce_add(&st.stats[1], cnt.tris);
-        warp_reduce_add(&st.stats[4], cnt.nodes);
-        warp_reduce_add(&st.stats[5], cnt.tris);
-    }
 }
 
 // ------------------------------------------------------------------ k_shadow
@@ -677,7 +715,7 @@ struct vgb_context {
     bool count_pass = false;
     bool profiling = false;
     std::vector<cudaEvent_t> prof_events;   // pairs around each launch
-    std::vector<int> prof_family;           // 0 extend, 1 shadow, 2 film
+    std::vector<int> prof_family;           // 0 closest-hit trace, 1 shadow, 2 film, 3 shade
     size_t prof_used = 0;
 };
 
@@ -756,6 +794,7 @@ vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
     AL(st.arad, B * P * f); AL(st.adir, B * P * f); AL(st.aalb, B * P * f); AL(st.anrm, 3 * P * f);
     AL(st.adep, P * f); AL(st.acnt, P * u); AL(st.atri, P * u);
     AL(st.pq[0], P * u); AL(st.pq[1], P * u);
+    AL(st.hit, P * sizeof(float4));
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
         if (l < L) {
             AL(st.sq_org[l], 3 * P * f); AL(st.sq_dir[l], 3 * P * f); AL(st.sq_tmax[l], P * f);
@@ -824,9 +863,13 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
             {
                 Prof p(ctx, 0);
-                k_extend<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                k_trace<COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
-            launches++;
+            {
+                Prof p(ctx, 3);
+                k_shade<NB><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            }
+            launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
                 Prof p(ctx, 1);
                 k_shadow<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
@@ -1126,11 +1169,12 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     ctx->stats.tris_tested = 0;
     ctx->stats.nodes_closest = 0;
     ctx->stats.tris_closest = 0;
-    ctx->stats.ms_extend = ctx->stats.ms_shadow = ctx->stats.ms_film = 0.f;
-    ctx->stats.launches_extend = ctx->stats.launches_shadow = ctx->stats.launches_film = 0;
+    ctx->stats.ms_trace = ctx->stats.ms_shadow = ctx->stats.ms_film = ctx->stats.ms_shade = 0.f;
+    ctx->stats.launches_trace = ctx->stats.launches_shadow = ctx->stats.launches_film = ctx->stats.launches_shade = 0;
     if (ctx->profiling) {
-        float* fam_ms[3] = {&ctx->stats.ms_extend, &ctx->stats.ms_shadow, &ctx->stats.ms_film};
-        uint32_t* fam_n[3] = {&ctx->stats.launches_extend, &ctx->stats.launches_shadow, &ctx->stats.launches_film};
+        float* fam_ms[4] = {&ctx->stats.ms_trace, &ctx->stats.ms_shadow, &ctx->stats.ms_film, &ctx->stats.ms_shade};
+        uint32_t* fam_n[4] = {&ctx->stats.launches_trace, &ctx->stats.launches_shadow, &ctx->stats.launches_film,
+                              &ctx->stats.launches_shade};
         for (size_t k = 0; k < ctx->prof_used; k += 2) {
             float e = 0.f;
             cudaEventElapsedTime(&e, ctx->prof_events[k], ctx->prof_events[k + 1]);
@@ -1250,7 +1294,7 @@ inline size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t noalloc_bytes(size_t P, size_t B, size_t L) {
     const size_t f = 4;
     size_t n = 2 * 256;  // counters, statistics
-    const size_t planes[] = {3, 3, B, B, B, 1, B, B, B, 3, 1, 1, 1, 1, 1};
+    const size_t planes[] = {3, 3, B, B, B, 1, B, B, B, 3, 1, 1, 1, 1, 1, 4};
     for (size_t k : planes) n += up256(k * P * f);
     n += L * (up256(3 * P * f) + up256(3 * P * f) + up256(P * f) + up256(P * f) + up256(B * P * f));
     return n;
@@ -1267,8 +1311,9 @@ void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film
         for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
             cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
             cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
-            k_extend<NB, false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
-            launches++;
+            k_trace<false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            k_shade<NB><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
                 k_shadow<NB, false><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
@@ -1337,6 +1382,7 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     st.arad = (float*)take(B * P * f); st.adir = (float*)take(B * P * f); st.aalb = (float*)take(B * P * f);
     st.anrm = (float*)take(3 * P * f); st.adep = (float*)take(P * f); st.acnt = (uint32_t*)take(P * f);
     st.atri = (uint32_t*)take(P * f); st.pq[0] = (uint32_t*)take(P * f); st.pq[1] = (uint32_t*)take(P * f);
+    st.hit = (float4*)take(4 * P * f);
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
         if (l < std::max<uint32_t>(1, nlights)) {
             st.sq_org[l] = (float*)take(3 * P * f); st.sq_dir[l] = (float*)take(3 * P * f);
