@@ -36,7 +36,6 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-NODE_BYTES = 64
 TRI_BYTES = 48
 RAY_IO_CLOSEST = 32 + 16
 RAY_IO_SHADOW = 32 + 4
@@ -60,6 +59,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample time")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-direct", action="store_true", help="skip the extra plain-direct line item")
+    ap.add_argument("--layout", type=int, choices=[2, 8], default=2, help="device BVH node layout")
     return ap.parse_args()
 
 
@@ -295,6 +295,7 @@ def run_ours(args, p, rank, world, local_rank):
     t0 = time.perf_counter()
     scene, cam_id = build_scene(p, device=local_rank)
     scene.pathtracer.options.frame = rank  # replicas render distinct sample streams
+    scene.bvh_options.layout = args.layout
     t1 = time.perf_counter()
     scene.build_tlas()
     t2 = time.perf_counter()
@@ -354,13 +355,14 @@ def run_ours(args, p, rank, world, local_rank):
            "k_shadow": (sum(s.ms_shadow for s in st_list), sum(s.launches_shadow for s in st_list)),
            "k_end_sample": (sum(s.ms_film for s in st_list), sum(s.launches_film for s in st_list))}
     B = scene.bands.size
+    node_bytes = cst.bvh_node_bytes
     nodes_sh = cst.nodes_visited - cst.nodes_closest
     tris_sh = cst.tris_tested - cst.tris_closest
     # algorithmic bytes of one render, per kernel family
     alg = {
-        "k_trace": cst.nodes_closest * NODE_BYTES + cst.tris_closest * TRI_BYTES + cst.rays_closest * RAY_IO_CLOSEST,
+        "k_trace": cst.nodes_closest * node_bytes + cst.tris_closest * TRI_BYTES + cst.rays_closest * RAY_IO_CLOSEST,
         "k_shade": cst.hits_closest * shade_bytes(B) + cst.rays_closest * 16,
-        "k_shadow": nodes_sh * NODE_BYTES + tris_sh * TRI_BYTES + cst.rays_shadow * (RAY_IO_SHADOW + 4 * B + 8),
+        "k_shadow": nodes_sh * node_bytes + tris_sh * TRI_BYTES + cst.rays_shadow * (RAY_IO_SHADOW + 4 * B + 8),
         "k_end_sample": r.cam.width * r.cam.height * r.opts.samples * 4 * (4 * B + 2),
     }
     launches_one = {"k_trace": s0.launches_trace, "k_shade": s0.launches_shade, "k_shadow": s0.launches_shadow,
@@ -384,7 +386,7 @@ def run_ours(args, p, rank, world, local_rank):
 
     direct = None
     if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
-        direct = plain_direct_item(torch, dev)
+        direct = plain_direct_item(torch, dev, args.layout)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -408,6 +410,12 @@ def run_ours(args, p, rank, world, local_rank):
                        "image": [r.cam.width, r.cam.height], "spp": int(r.opts.samples),
                        "bounces": int(r.opts.bounces), "rr_after_bounce": int(r.opts.rr_depth), "bands": B,
                        "l2": "flushed between timed renders (256 MB write); scene working set also exceeds L2",
+                       "bvh": {"layout": f"{args.layout}-wide" if args.layout == 8 else "binary",
+                               "nodes": int(cst.bvh_nodes), "node_bytes": int(cst.bvh_node_bytes)},
+                       "traversal_counts_per_frame": {"nodes_closest": int(cst.nodes_closest),
+                                                      "tris_closest": int(cst.tris_closest),
+                                                      "nodes_shadow": int(cst.nodes_visited - cst.nodes_closest),
+                                                      "tris_shadow": int(cst.tris_tested - cst.tris_closest)},
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "spectral_path_samples_per_s": paths / (total_ms / 1000.0),
             "rays_per_step": rays / args.steps / max(1, world),
@@ -429,11 +437,12 @@ def run_ours(args, p, rank, world, local_rank):
     scene.close()
 
 
-def plain_direct_item(torch, dev):
+def plain_direct_item(torch, dev, layout=8):
     """The 513^2 / 1024^2 direct-lighting frame: Mrays/s (primary + shadow) on the same GPU."""
     from vira_gb300 import workloads
 
     scene, cam_id = workloads.plain_direct(device=dev.index)
+    scene.bvh_options.layout = layout
     scene.build_tlas()
     stream = torch.cuda.Stream(device=dev)
     r = Renderer(scene, cam_id, torch, stream)

@@ -70,7 +70,7 @@ def test_gpu_matches_golden(gpu, path):
         th, tw = (t.shape[0], t.shape[1]) if t is not None else (0, 0)
         capi.check(lib.vgb_scene_upload(ctx, capi.ptr(arrs[0]), arrs[0].shape[0], capi.ptr(idx), idx.shape[0], B,
                                         capi.ptr(arrs[1]), capi.ptr(arrs[2]), capi.ptr(arrs[3]), capi.ptr(t), tw, th), ctx)
-        capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 0, 0))), ctx)
+        capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 0, 0, 0))), ctx)
         H, W = cam.height, cam.width
         om = np.empty((H, W), np.float32)
         capi.check(lib.vgb_pixel_solid_angle(ctx, C.byref(cam), capi.ptr(om), 0), ctx)

@@ -24,9 +24,10 @@ def _trace_gpu(scene, o, d, any_hit=False, tmax=None):
     return scene.intersect(o, d, any_hit=any_hit, tmax=tmax)
 
 
-@pytest.fixture(scope="module")
-def direct_scene(gpu):
+@pytest.fixture(scope="module", params=[8, 2], ids=["bvh8", "bvh2"])
+def direct_scene(gpu, request):
     scene, cam_id = workloads.plain_direct(posts=257, resolution=256)
+    scene.bvh_options.layout = request.param
     scene.build_tlas()
     yield scene, cam_id
     scene.close()

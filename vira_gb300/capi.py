@@ -62,7 +62,8 @@ class Film(C.Structure):
 
 
 class BvhOptions(C.Structure):
-    _fields_ = [("max_leaf_size", C.c_uint32), ("builder", C.c_uint32), ("threads", C.c_uint32)]
+    _fields_ = [("max_leaf_size", C.c_uint32), ("builder", C.c_uint32), ("threads", C.c_uint32),
+                ("layout", C.c_uint32)]
 
 
 class Stats(C.Structure):

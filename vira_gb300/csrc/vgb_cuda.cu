@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/vgb.h"
@@ -28,19 +29,34 @@ using namespace vgbd;
 
 #define VGB_MAX_LIGHTS 8
 
+// Minimum resident blocks per SM requested from the register allocator (occupancy knobs).
+// Defaults from a sweep on the path-traced workload (GB300, 256-thread blocks).
+#ifndef VGB_TRACE_MINB
+#define VGB_TRACE_MINB 5
+#endif
+#ifndef VGB_SHADE_MINB
+#define VGB_SHADE_MINB 4
+#endif
+#ifndef VGB_SHADOW_MINB
+#define VGB_SHADOW_MINB 6
+#endif
+
 namespace {
 
 // ------------------------------------------------------------------ device data
 struct DevScene {
-    const float4* nodes;
+    const uint4* nodes;    // binary (4 words per node) or compressed 8-wide (5 words per node)
     const float4* tris;
     const uint32_t* idx;   // 3 per triangle, caller order
     const float4* vpos;    // xyz
     const float4* vnrm;    // xyz
     const float2* vuv;
-    const float* valb;     // B per vertex
-    const float* tex;      // [th][tw][B]
+    const float* valb;     // B per vertex (unused when albedo_uniform)
+    const float* tex;      // [th][tw][B], or [th][tw] when tex_mono
     uint32_t tw, th;
+    uint32_t albedo_uniform;          // every vertex has the albedo `albedo_value`
+    uint32_t tex_mono;                // every texel has the same value in all bands
+    float albedo_value[VGB_MAX_BANDS];
 };
 
 struct DevState {
@@ -194,11 +210,20 @@ __device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float
     x0 = min(x0, (int)s.tw - 1); y0 = min(y0, (int)s.th - 1);
     int x1 = min(x0 + 1, (int)s.tw - 1), y1 = min(y0 + 1, (int)s.th - 1);
     float dx = px - (float)x0, dy = py - (float)y0;
+    float a = (1.f - dx) * (1.f - dy), b = dx * (1.f - dy), c = (1.f - dx) * dy, e = dx * dy;
+    if (s.tex_mono) {
+        // the bands of every texel are equal: one fetch per texel, the same per-band arithmetic
+        const float t00 = __ldg(&s.tex[(size_t)y0 * s.tw + x0]), t10 = __ldg(&s.tex[(size_t)y0 * s.tw + x1]);
+        const float t01 = __ldg(&s.tex[(size_t)y1 * s.tw + x0]), t11 = __ldg(&s.tex[(size_t)y1 * s.tw + x1]);
+        const float val = ((a * t00 + b * t10) + c * t01) + e * t11;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) out[k] = val;
+        return;
+    }
     const float* p00 = &s.tex[((size_t)y0 * s.tw + x0) * nb];
     const float* p10 = &s.tex[((size_t)y0 * s.tw + x1) * nb];
     const float* p01 = &s.tex[((size_t)y1 * s.tw + x0) * nb];
     const float* p11 = &s.tex[((size_t)y1 * s.tw + x1) * nb];
-    float a = (1.f - dx) * (1.f - dy), b = dx * (1.f - dy), c = (1.f - dx) * dy, e = dx * dy;
 #pragma unroll
     for (int k = 0; k < NB; ++k)
         if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
@@ -234,8 +259,8 @@ __device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item,
 // Scene::intersect for every live path: camera rays at bounce 0, queued continuation rays
 // after.  Writes one 16-byte hit record per queue item; kept lean so that enough warps are
 // resident to hide the latency of the node and triangle fetches.
-template <bool COUNT>
-__global__ void __launch_bounds__(256) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
+template <int L, bool COUNT>
+__global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
                                                uint32_t bounce, uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const size_t P = st.P;
     const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
@@ -255,7 +280,7 @@ __global__ void __launch_bounds__(256) k_trace(const DevScene s, DevState st, co
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
         const WRay wr = make_wray(ro, rd);
-        traverse<false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+        traverse_any_layout<L, false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
         nclosest++;
         float w0 = 0.f, w1 = 0.f;
         if (h.id != VGB_NO_HIT) {
@@ -279,7 +304,7 @@ __global__ void __launch_bounds__(256) k_trace(const DevScene s, DevState st, co
 // processIntersection for every item of k_trace: AOVs, shading point, NEE shadow-ray enqueue,
 // BSDF-sampled continuation and live-path enqueue (warp-aggregated appends).
 template <int NB>
-__global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
+__global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
                                                uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const uint32_t nb = fp.nb;
     const size_t P = st.P;
@@ -296,9 +321,8 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
         uint32_t slot = 0;
         F3 ro{0, 0, 0}, rd{0, 0, 1};
         float thr[NB];
-        float prad[NB];
 #pragma unroll
-        for (int k = 0; k < NB; ++k) { thr[k] = 1.f; prad[k] = 0.f; }
+        for (int k = 0; k < NB; ++k) thr[k] = 1.f;
         if (active) {
             if (bounce == 0) {
                 active = camera_ray(fp, item, sample, slot, ro, rd);
@@ -311,20 +335,22 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
                         st.adep[slot] = 0.f; st.acnt[slot] = 0u; st.atri[slot] = VGB_NO_HIT;
                     }
                     st.pend[slot] = 0u;
+#pragma unroll
+                    for (int k = 0; k < NB; ++k)
+                        if (k < (int)nb) st.prad[k * P + slot] = 0.f;
                 }
             } else {
                 slot = in_queue[item];
-                ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
-                rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
+                // the incoming ray stays in the path state; it is read below only for a miss.
+                // Fold the previous bounce's radiance into the path now, so that the path
+                // radiance is not live through the shading.
                 const uint32_t pend = st.pend[slot];
+                if (pend) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    if (k < (int)nb) {
-                        thr[k] = st.thr[k * P + slot];
-                        prad[k] = st.prad[k * P + slot];
-                        if (pend) {
+                    for (int k = 0; k < NB; ++k) {
+                        if (k < (int)nb) {
                             const float br = st.brad[k * P + slot];
-                            prad[k] += br;
+                            st.prad[k * P + slot] = st.prad[k * P + slot] + br;
                             if (pend == 1u) st.adir[k * P + slot] += br;
                         }
                     }
@@ -348,6 +374,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
         const uint32_t k0 = (uint32_t)fp.opt.seed, k1 = (uint32_t)(fp.opt.seed >> 32);
         if (active && !hit) {
             if (fp.opt.simulate_lighting && fp.opt.show_background) {
+                if (bounce != 0) rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
                 float x = rd.x, y = rd.y, z = rd.z;
                 float u = atan2f(y, x) / (2 * kPi);
                 float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
@@ -361,7 +388,8 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
                     if (k < (int)nb) {
                         const float bgv = fp.opt.background[k];
                         float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
-                        prad[k] += thr[k] * (bg * 1.f);
+                        const float tk = (bounce == 0) ? 1.f : st.thr[k * P + slot];
+                        st.prad[k * P + slot] = st.prad[k * P + slot] + tk * (bg * 1.f);
                     }
                 }
             }
@@ -396,8 +424,14 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
 #pragma unroll
             for (int k = 0; k < NB; ++k) {
                 if (k < (int)nb) {
-                    float va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
-                               w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
+                    float va;
+                    if (s.albedo_uniform) {
+                        const float c = s.albedo_value[k];
+                        va = (w[0] * c + w[1] * c) + w[2] * c;
+                    } else {
+                        va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
+                             w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
+                    }
                     alb[k] = va * texv[k];
                 }
             }
@@ -420,6 +454,11 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
             }
             if (fp.opt.simulate_lighting) {
                 lit = true;
+                if (bounce != 0) {
+#pragma unroll
+                    for (int k = 0; k < NB; ++k)
+                        if (k < (int)nb) thr[k] = st.thr[k * P + slot];
+                }
                 Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
 #pragma unroll
                 for (int k = 0; k < NB; ++k) {
@@ -467,6 +506,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
             }
         }
         // ---- BSDF-sampled continuation
+        bool new_ray = false;
         if (lit && bounce < fp.opt.bounces) {
             F3 ls = cosine_sample(u01(r0.z), u01(r0.w));
             const float mpdf = ls.z * kInvPi;
@@ -486,6 +526,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
                     if (k < (int)nb) thr[k] *= bsdf * cos_t * wgt / mpdf;
                 }
                 ro = Pp; rd = nd;
+                new_ray = true;
                 if (fp.opt.rr_depth != 0 && bounce + 1 >= fp.opt.rr_depth) {
                     float q = 0.f;
 #pragma unroll
@@ -504,14 +545,14 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
         }
         // ---- write path state and append live paths
         if (active) {
-#pragma unroll
-            for (int k = 0; k < NB; ++k) {
-                if (k < (int)nb) {
-                    st.prad[k * P + slot] = prad[k];
-                    if (cont) st.thr[k * P + slot] = thr[k];
-                }
-            }
             if (cont) {
+#pragma unroll
+                for (int k = 0; k < NB; ++k)
+                    if (k < (int)nb) st.thr[k * P + slot] = thr[k];
+            }
+            // a path that keeps its incoming ray (sampled pdf 0) already has it in the state,
+            // except a camera ray
+            if (cont && (new_ray || bounce == 0)) {
                 st.org[slot] = ro.x; st.org[P + slot] = ro.y; st.org[2 * P + slot] = ro.z;
                 st.dir[slot] = rd.x; st.dir[P + slot] = rd.y; st.dir[2 * P + slot] = rd.z;
             }
@@ -523,8 +564,8 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene s, DevState st, co
 }
 
 // ------------------------------------------------------------------ k_shadow
-template <int NB, bool COUNT>
-__global__ void __launch_bounds__(256) k_shadow(const DevScene s, DevState st, uint32_t light, uint32_t nb) {
+template <int NB, int L, bool COUNT>
+__global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene s, DevState st, uint32_t light, uint32_t nb) {
     const size_t P = st.P;
     const uint32_t n = st.counters[C_SQ + light];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -536,7 +577,7 @@ __global__ void __launch_bounds__(256) k_shadow(const DevScene s, DevState st, u
         const float tmax = st.sq_tmax[light][i];
         WRay wr = make_wray(o, d);
         HitOut h;
-        traverse<true, COUNT>(s.nodes, s.tris, wr, tmax, h, err, cnt);
+        traverse_any_layout<L, true, COUNT>(s.nodes, s.tris, wr, tmax, h, err, cnt);
         nsh++;
         if (h.id == VGB_NO_HIT) {
             const uint32_t slot = st.sq_slot[light][i];
@@ -639,8 +680,8 @@ __global__ void k_pixel_solid_angle(const vgb_camera cam, float* out) {
 }
 
 // ------------------------------------------------------------------ batch trace (TLAS::intersect seam)
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(256) k_trace(const DevScene s, const float* org, const float* dir, const float* tmax,
+template <int L, bool ANY, bool COUNT>
+__global__ void __launch_bounds__(256) k_trace_batch(const DevScene s, const float* org, const float* dir, const float* tmax,
                                                uint32_t n, uint32_t* tri, float* tout, float* bary,
                                                uint32_t* counters, uint64_t* stats) {
     uint32_t err = 0;
@@ -651,7 +692,7 @@ __global__ void __launch_bounds__(256) k_trace(const DevScene s, const float* or
         WRay wr = make_wray(o, d);
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
-        traverse<ANY, COUNT>(s.nodes, s.tris, wr, tmax ? tmax[i] : __int_as_float(0x7f800000), h, err, cnt);
+        traverse_any_layout<L, ANY, COUNT>(s.nodes, s.tris, wr, tmax ? tmax[i] : __int_as_float(0x7f800000), h, err, cnt);
         tri[i] = h.id;
         if (tout) tout[i] = h.t;
         if (bary) {
@@ -692,12 +733,15 @@ struct vgb_context {
     uint32_t* d_idx = nullptr;
     float* d_tex = nullptr;
     uint32_t tw = 1, th = 1;
+    uint32_t albedo_uniform = 0, tex_mono = 0;
+    float albedo_value[VGB_MAX_BANDS] = {0};
     std::vector<float> h_pos;   // kept for the BVH build
     std::vector<uint32_t> h_idx;
     // BVH
-    float4* d_nodes = nullptr;
+    uint4* d_nodes = nullptr;
     float4* d_tris = nullptr;
     uint32_t nnodes = 0;
+    uint32_t bvh_layout = 2;
     bool bvh_ready = false;
     // render scratch
     size_t cap_P = 0;
@@ -815,6 +859,8 @@ DevScene dev_scene(const vgb_context* ctx) {
     DevScene s;
     s.nodes = ctx->d_nodes; s.tris = ctx->d_tris; s.idx = ctx->d_idx; s.vpos = ctx->d_vpos; s.vnrm = ctx->d_vnrm;
     s.vuv = ctx->d_vuv; s.valb = ctx->d_valb; s.tex = ctx->d_tex; s.tw = ctx->tw; s.th = ctx->th;
+    s.albedo_uniform = ctx->albedo_uniform; s.tex_mono = ctx->tex_mono;
+    for (int k = 0; k < VGB_MAX_BANDS; ++k) s.albedo_value[k] = ctx->albedo_value[k];
     return s;
 }
 
@@ -848,7 +894,7 @@ struct Prof {
     }
 };
 
-template <int NB, bool COUNT>
+template <int NB, int L, bool COUNT>
 void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
     const DevScene s = dev_scene(ctx);
     DevState st = ctx->st;
@@ -863,7 +909,7 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
             {
                 Prof p(ctx, 0);
-                k_trace<COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                k_trace<L, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             {
                 Prof p(ctx, 3);
@@ -872,7 +918,7 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
                 Prof p(ctx, 1);
-                k_shadow<NB, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                k_shadow<NB, L, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
@@ -885,11 +931,17 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
     }
 }
 
+template <int L, bool COUNT>
+void dispatch_render_l(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
+    if (fp.nb <= 1) launch_render<1, L, COUNT>(ctx, fp, film, launches);
+    else if (fp.nb <= 4) launch_render<4, L, COUNT>(ctx, fp, film, launches);
+    else launch_render<8, L, COUNT>(ctx, fp, film, launches);
+}
+
 template <bool COUNT>
 void dispatch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
-    if (fp.nb <= 1) launch_render<1, COUNT>(ctx, fp, film, launches);
-    else if (fp.nb <= 4) launch_render<4, COUNT>(ctx, fp, film, launches);
-    else launch_render<8, COUNT>(ctx, fp, film, launches);
+    if (ctx->bvh_layout == 8) dispatch_render_l<8, COUNT>(ctx, fp, film, launches);
+    else dispatch_render_l<2, COUNT>(ctx, fp, film, launches);
 }
 
 }  // namespace
@@ -996,19 +1048,38 @@ VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t
     if (!valb) { alb.assign((size_t)nverts * nbands, 1.f); valb = alb.data(); }
     std::vector<float> one;
     if (!tex) { one.assign(nbands, 1.f); tex = one.data(); tw = th = 1; }
+    // Uniform inputs are folded into constants: same expressions, fewer gathers.
+    bool uniform = true;
+    for (size_t v = 1; v < nverts && uniform; ++v)
+        for (uint32_t k = 0; k < nbands; ++k)
+            if (std::memcmp(&valb[v * nbands + k], &valb[k], 4) != 0) { uniform = false; break; }
+    bool mono = true;
+    const size_t ntex = (size_t)tw * th;
+    for (size_t t = 0; t < ntex && mono; ++t)
+        for (uint32_t k = 1; k < nbands; ++k)
+            if (std::memcmp(&tex[t * nbands + k], &tex[t * nbands], 4) != 0) { mono = false; break; }
+    ctx->albedo_uniform = uniform ? 1u : 0u;
+    ctx->tex_mono = mono ? 1u : 0u;
+    for (uint32_t k = 0; k < VGB_MAX_BANDS; ++k) ctx->albedo_value[k] = k < nbands ? valb[k] : 0.f;
+    std::vector<float> mono_tex;
+    if (mono) {
+        mono_tex.resize(ntex);
+        for (size_t t = 0; t < ntex; ++t) mono_tex[t] = tex[t * nbands];
+    }
     vgb_status s;
     if ((s = dalloc(ctx, &ctx->d_vpos, sizeof(float4) * nverts)) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_vnrm, sizeof(float4) * nverts)) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_vuv, sizeof(float2) * nverts)) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_valb, sizeof(float) * nverts * (size_t)nbands)) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_idx, sizeof(uint32_t) * 3 * (size_t)ntris)) != VGB_OK) return s;
-    if ((s = dalloc(ctx, &ctx->d_tex, sizeof(float) * (size_t)tw * th * nbands)) != VGB_OK) return s;
+    const size_t tex_floats = mono ? ntex : ntex * nbands;
+    if ((s = dalloc(ctx, &ctx->d_tex, sizeof(float) * tex_floats)) != VGB_OK) return s;
     CK(cudaMemcpy(ctx->d_vpos, p4.data(), sizeof(float4) * nverts, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_vnrm, n4.data(), sizeof(float4) * nverts, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_vuv, uv2.data(), sizeof(float2) * nverts, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_valb, valb, sizeof(float) * nverts * (size_t)nbands, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_idx, idx, sizeof(uint32_t) * 3 * (size_t)ntris, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_tex, tex, sizeof(float) * (size_t)tw * th * nbands, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_tex, mono ? mono_tex.data() : tex, sizeof(float) * tex_floats, cudaMemcpyHostToDevice));
     ctx->tw = tw; ctx->th = th;
     ctx->h_pos.assign(pos, pos + 3 * (size_t)nverts);
     ctx->h_idx.assign(idx, idx + 3 * (size_t)ntris);
@@ -1019,23 +1090,27 @@ VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) 
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "bvh_build: no scene uploaded");
     uint32_t leaf = opts ? opts->max_leaf_size : 0, threads = opts ? opts->threads : 0;
+    uint32_t layout = (opts && opts->layout) ? opts->layout : 2;
     if (opts && opts->builder != 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: unknown builder");
-    if (leaf > vgb::kMaxLeaf) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8");
+    if (layout != 2 && layout != 8) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: layout must be 2 or 8");
+    if (leaf > (layout == 8 ? vgb::kMaxLeaf8 : vgb::kMaxLeaf))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8 (binary) or <= 3 (8-wide)");
     vgb::BvhHost bvh;
     const char* why = "";
-    if (!vgb::build_bvh2(ctx->h_pos.data(), ctx->nverts, ctx->h_idx.data(), ctx->ntris, leaf, threads, bvh, &why))
+    if (!vgb::build_bvh(ctx->h_pos.data(), ctx->nverts, ctx->h_idx.data(), ctx->ntris, leaf, threads, layout, bvh, &why))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("bvh_build: ") + why);
     cudaSetDevice(ctx->device);
     free_bvh(ctx);
     vgb_status s;
-    if ((s = dalloc(ctx, &ctx->d_nodes, bvh.nodes.size() * sizeof(float))) != VGB_OK) return s;
+    if ((s = dalloc(ctx, &ctx->d_nodes, bvh.nodes.size() * sizeof(uint32_t))) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_tris, bvh.tris.size() * sizeof(float))) != VGB_OK) return s;
-    CK(cudaMemcpy(ctx->d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice));
     ctx->nnodes = bvh.num_nodes;
+    ctx->bvh_layout = layout;
     ctx->bvh_ready = true;
     ctx->stats.bvh_nodes = bvh.num_nodes;
-    ctx->stats.bvh_node_bytes = 64;
+    ctx->stats.bvh_node_bytes = layout == 8 ? 80 : 64;
     ctx->stats.tri_record_bytes = 48;
     return VGB_OK;
 }
@@ -1237,13 +1312,18 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     const int g = grid_for(ctx, n);
-    if (any_hit) {
-        if (ctx->count_pass) k_trace<true, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
-        else k_trace<true, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
-    } else {
-        if (ctx->count_pass) k_trace<false, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
-        else k_trace<false, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
-    }
+    auto launch = [&](auto lc) {
+        constexpr int L = decltype(lc)::value;
+        if (any_hit) {
+            if (ctx->count_pass) k_trace_batch<L, true, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+            else k_trace_batch<L, true, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+        } else {
+            if (ctx->count_pass) k_trace_batch<L, false, true><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+            else k_trace_batch<L, false, false><<<g, 256, 0, ctx->stream>>>(sc, dorg, ddir, dtmax, n, dtri, dt, db, ctx->d_counters, ctx->d_stats);
+        }
+    };
+    if (ctx->bvh_layout == 8) launch(std::integral_constant<int, 8>{});
+    else launch(std::integral_constant<int, 2>{});
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!on_device) {
@@ -1300,7 +1380,7 @@ size_t noalloc_bytes(size_t P, size_t B, size_t L) {
     return n;
 }
 
-template <int NB>
+template <int NB, int L>
 void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, uint32_t& launches) {
     const DevScene s = dev_scene(ctx);
     const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
@@ -1311,11 +1391,11 @@ void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film
         for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
             cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
             cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
-            k_trace<false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            k_trace<L, false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             k_shade<NB><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
-                k_shadow<NB, false><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                k_shadow<NB, L, false><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
@@ -1411,9 +1491,15 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     CK(cudaMemsetAsync(st.counters, 0, 256, ctx->stream));
     CK(cudaMemsetAsync(st.stats, 0, 256, ctx->stream));
     uint32_t launches = 0;
-    if (B <= 1) launch_noalloc<1>(ctx, fp, fo, st, launches);
-    else if (B <= 4) launch_noalloc<4>(ctx, fp, fo, st, launches);
-    else launch_noalloc<8>(ctx, fp, fo, st, launches);
+    if (ctx->bvh_layout == 8) {
+        if (B <= 1) launch_noalloc<1, 8>(ctx, fp, fo, st, launches);
+        else if (B <= 4) launch_noalloc<4, 8>(ctx, fp, fo, st, launches);
+        else launch_noalloc<8, 8>(ctx, fp, fo, st, launches);
+    } else {
+        if (B <= 1) launch_noalloc<1, 2>(ctx, fp, fo, st, launches);
+        else if (B <= 4) launch_noalloc<4, 2>(ctx, fp, fo, st, launches);
+        else launch_noalloc<8, 2>(ctx, fp, fo, st, launches);
+    }
     CK(cudaGetLastError());
     uint32_t err_word = 0;
     uint64_t hs[8] = {0};

@@ -212,4 +212,112 @@ __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const
     }
 }
 
+// ------------------------------------------------------------------ compressed 8-wide traversal
+// Node (80 bytes, five 16-byte words): origin p, biased exponents and internal-child mask,
+// first internal child, first triangle, eight meta bytes and six arrays of eight 8-bit
+// quantised bounds.  The child in slot s is the nearest for rays whose direction-sign octant
+// is s; a ray of octant o visits slots o^0, o^1, ..., o^7.  The stack holds node groups: the
+// first child index, the internal-child mask and the not-yet-visited hit slots in visiting order.
+constexpr int kStack8 = 32;
+
+__device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t o) {
+    // bit k of the result = bit (o ^ k) of m
+    if (o & 1u) m = ((m & 0x55u) << 1) | ((m & 0xAAu) >> 1);
+    if (o & 2u) m = ((m & 0x33u) << 2) | ((m & 0xCCu) >> 2);
+    if (o & 4u) m = ((m & 0x0Fu) << 4) | ((m & 0xF0u) >> 4);
+    return m;
+}
+
+__device__ __forceinline__ float q8(uint32_t w, int byte) { return (float)((w >> (8 * byte)) & 0xFFu); }
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+    const float widen = 1.0f + 0x1p-20f;
+    const uint32_t oct = (r.d.x < 0.f ? 1u : 0u) | (r.d.y < 0.f ? 2u : 0u) | (r.d.z < 0.f ? 4u : 0u);
+    uint2 stack[kStack8];
+    int sp = 0;
+    uint32_t node = 0;
+    float best = ANY ? tmax : __int_as_float(0x7f800000);
+    h.t = __int_as_float(0x7f800000);
+    h.id = VGB_NO_HIT;
+    uint32_t iter = 0;
+    const float ox = r.o.x, oy = r.o.y, oz = r.o.z, ix = r.ix, iy = r.iy, iz = r.iz;
+    while (true) {
+        if (++iter > kIterCap) { err |= kErrIter; return; }
+        const uint4 w0 = __ldg(&nodes[5 * node + 0]);
+        const uint4 w1 = __ldg(&nodes[5 * node + 1]);
+        const uint4 w2 = __ldg(&nodes[5 * node + 2]);
+        const uint4 w3 = __ldg(&nodes[5 * node + 3]);
+        const uint4 w4 = __ldg(&nodes[5 * node + 4]);
+        if (COUNT) cnt.nodes++;
+        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        const float sx = __uint_as_float((w0.w & 0xFFu) << 23);
+        const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23);
+        const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23);
+        const uint32_t imask = w0.w >> 24;
+        const uint32_t child_base = w1.x, tri_base = w1.y;
+        uint32_t ihits = 0, tbits = 0;
+#pragma unroll
+        for (int sl = 0; sl < 8; ++sl) {
+            const uint32_t meta = ((sl < 4 ? w1.z : w1.w) >> (8 * (sl & 3))) & 0xFFu;
+            const int b = sl & 3;
+            const uint32_t lx = sl < 4 ? w2.x : w2.y, ly = sl < 4 ? w2.z : w2.w, lz = sl < 4 ? w3.x : w3.y;
+            const uint32_t hx = sl < 4 ? w3.z : w3.w, hy = sl < 4 ? w4.x : w4.y, hz = sl < 4 ? w4.z : w4.w;
+            const float a0 = (fmaf(sx, q8(lx, b), px) - ox) * ix, a1 = (fmaf(sx, q8(hx, b), px) - ox) * ix;
+            const float b0 = (fmaf(sy, q8(ly, b), py) - oy) * iy, b1 = (fmaf(sy, q8(hy, b), py) - oy) * iy;
+            const float c0 = (fmaf(sz, q8(lz, b), pz) - oz) * iz, c1 = (fmaf(sz, q8(hz, b), pz) - oz) * iz;
+            const float tn = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
+            const float tf = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), best)) * widen;
+            if (meta != 0u && tn <= tf) {
+                if (imask & (1u << sl)) ihits |= 1u << sl;
+                else tbits |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+            }
+        }
+        // triangles of the hit leaves of this node
+        while (tbits) {
+            const uint32_t k = __ffs(tbits) - 1;
+            tbits &= tbits - 1;
+            const uint32_t ti = tri_base + k;
+            const float4 t0 = __ldg(&tris[3 * ti + 0]);
+            const float4 t1 = __ldg(&tris[3 * ti + 1]);
+            const float4 t2 = __ldg(&tris[3 * ti + 2]);
+            if (COUNT) cnt.tris++;
+            float tt, U, V, W, det;
+            if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
+                const uint32_t id = __float_as_uint(t0.w);
+                if (ANY) {
+                    if (tt <= tmax) { h.t = tt; h.id = id; return; }
+                } else if (tt < h.t || (tt == h.t && id < h.id)) {
+                    h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
+                    best = tt;
+                }
+            }
+        }
+        // next node: the nearest remaining hit child of this node, else of the stacked groups
+        uint32_t pending = octant_order(ihits, oct), base = child_base, im = imask;
+        if (!pending) {
+            if (sp == 0) return;
+            const uint2 g = stack[--sp];
+            base = g.x; pending = g.y & 0xFFu; im = g.y >> 8;
+        }
+        const uint32_t k = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t slot = oct ^ k;
+        node = base + __popc(im & ((1u << slot) - 1u));
+        if (pending) {
+            if (sp >= kStack8) { err |= kErrStack; return; }
+            stack[sp++] = make_uint2(base, pending | (im << 8));
+        }
+    }
+}
+
+// Dispatch on the node layout (2: binary, 8: compressed 8-wide).
+template <int LAYOUT, bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse_any_layout(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                    const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+    if (LAYOUT == 8) traverse8<ANY, COUNT>(nodes, tris, r, tmax, h, err, cnt);
+    else traverse<ANY, COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, h, err, cnt);
+}
+
 }  // namespace vgbd

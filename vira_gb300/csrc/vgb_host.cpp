@@ -264,10 +264,12 @@ uint32_t build_rec(const Ctx& c, Arena& ar, uint32_t arena_id, uint32_t first, u
 
 }  // namespace
 
-bool build_bvh2(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, uint32_t max_leaf,
-                uint32_t threads, BvhHost& out, const char** err) {
-    if (max_leaf == 0) max_leaf = 4;
+bool build_bvh(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t ntris, uint32_t max_leaf,
+               uint32_t threads, uint32_t layout, BvhHost& out, const char** err) {
+    if (layout != 2 && layout != 8) { *err = "unknown BVH layout"; return false; }
+    if (max_leaf == 0) max_leaf = (layout == 8) ? kMaxLeaf8 : 4;
     if (max_leaf > kMaxLeaf) max_leaf = kMaxLeaf;
+    if (layout == 8 && max_leaf > kMaxLeaf8) max_leaf = kMaxLeaf8;
     if (threads == 0) threads = std::max(1u, std::thread::hardware_concurrency());
     if (ntris == 0) { *err = "scene has no triangles"; return false; }
     if ((uint64_t)ntris >= (1ull << (31 - kLeafShift))) { *err = "too many triangles for the leaf encoding"; return false; }
@@ -366,62 +368,206 @@ bool build_bvh2(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t
         max_depth += md + 1;
     }
 
-    // Flatten depth first into the device layout.
     out.nodes.clear(); out.tris.clear();
     out.tris.reserve(12 * (size_t)ntris);
-    std::vector<float>& nodes = out.nodes;
+    out.layout = layout;
+    out.max_depth = max_depth;
     auto get = [&](int64_t ref) -> const BNode& { return arenas[(size_t)(ref >> 32)].nodes[(uint32_t)ref]; };
-    auto emit_tris = [&](const BNode& n) -> int32_t {
-        uint32_t start = (uint32_t)(out.tris.size() / 12);
-        for (uint32_t i = 0; i < n.count; ++i) {
-            uint32_t t = order[n.first + i];
-            for (int k = 0; k < 3; ++k) {
-                const float* p = &pos[3 * (size_t)idx[3 * (size_t)t + k]];
-                out.tris.push_back(p[0]); out.tris.push_back(p[1]); out.tris.push_back(p[2]);
-                uint32_t w = (k == 0) ? t : 0u;
-                float wf; std::memcpy(&wf, &w, 4);
-                out.tris.push_back(wf);
-            }
+    auto emit_tri = [&](uint32_t t) {
+        for (int k = 0; k < 3; ++k) {
+            const float* p = &pos[3 * (size_t)idx[3 * (size_t)t + k]];
+            out.tris.push_back(p[0]); out.tris.push_back(p[1]); out.tris.push_back(p[2]);
+            uint32_t w = (k == 0) ? t : 0u;
+            float wf; std::memcpy(&wf, &w, 4);
+            out.tris.push_back(wf);
         }
-        return ~(int32_t)((start << kLeafShift) | (n.count - 1));
     };
-    // iterative DFS: allocate a node, fill children later
-    struct Item { int64_t ref; uint32_t slot; };
-    std::vector<Item> stack;
     const BNode& root = get(enc(0, 0));
     for (int k = 0; k < 3; ++k) { out.root_lo[k] = root.box.lo[k]; out.root_hi[k] = root.box.hi[k]; }
-    auto alloc = [&]() { uint32_t s = (uint32_t)(nodes.size() / 16); nodes.resize(nodes.size() + 16, 0.f); return s; };
-    auto put_child = [&](uint32_t slot, int side, const Box& b, int32_t link) {
-        float* n = &nodes[16 * (size_t)slot];
-        if (side == 0) { n[0] = b.lo[0]; n[1] = b.hi[0]; n[2] = b.lo[1]; n[3] = b.hi[1]; n[8] = b.lo[2]; n[9] = b.hi[2]; }
-        else { n[4] = b.lo[0]; n[5] = b.hi[0]; n[6] = b.lo[1]; n[7] = b.hi[1]; n[10] = b.lo[2]; n[11] = b.hi[2]; }
-        std::memcpy(&n[12 + side], &link, 4);
-    };
-    uint32_t root_slot = alloc();
-    if (root.leaf) {
-        put_child(root_slot, 0, root.box, emit_tris(root));
-        Box empty;
-        put_child(root_slot, 1, empty, ~(int32_t)0);  // never entered: the box is inverted
-    } else {
-        stack.push_back(Item{enc(0, 0), root_slot});
-        while (!stack.empty()) {
-            Item it = stack.back(); stack.pop_back();
-            const BNode& n = get(it.ref);
-            for (int side = 0; side < 2; ++side) {
-                int64_t cr = n.child[side];
-                const BNode& ch = get(cr);
-                if (ch.leaf) {
-                    put_child(it.slot, side, ch.box, emit_tris(ch));
-                } else {
-                    uint32_t s = alloc();
-                    put_child(it.slot, side, ch.box, (int32_t)s);
-                    stack.push_back(Item{cr, s});
+    std::vector<uint32_t>& words = out.nodes;
+
+    if (layout == 2) {
+        // ---- binary layout, depth first
+        auto emit_leaf = [&](const BNode& n) -> int32_t {
+            uint32_t start = (uint32_t)(out.tris.size() / 12);
+            for (uint32_t i = 0; i < n.count; ++i) emit_tri(order[n.first + i]);
+            return ~(int32_t)((start << kLeafShift) | (n.count - 1));
+        };
+        struct Item { int64_t ref; uint32_t slot; };
+        std::vector<Item> stack;
+        auto alloc = [&]() { uint32_t sl = (uint32_t)(words.size() / 16); words.resize(words.size() + 16, 0u); return sl; };
+        auto fbits = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
+        auto put_child = [&](uint32_t slot, int side, const Box& b, int32_t link) {
+            uint32_t* n = &words[16 * (size_t)slot];
+            if (side == 0) {
+                n[0] = fbits(b.lo[0]); n[1] = fbits(b.hi[0]); n[2] = fbits(b.lo[1]); n[3] = fbits(b.hi[1]);
+                n[8] = fbits(b.lo[2]); n[9] = fbits(b.hi[2]);
+            } else {
+                n[4] = fbits(b.lo[0]); n[5] = fbits(b.hi[0]); n[6] = fbits(b.lo[1]); n[7] = fbits(b.hi[1]);
+                n[10] = fbits(b.lo[2]); n[11] = fbits(b.hi[2]);
+            }
+            n[12 + side] = (uint32_t)link;
+        };
+        uint32_t root_slot = alloc();
+        if (root.leaf) {
+            // both children are the root leaf: tested twice, found once
+            int32_t link = emit_leaf(root);
+            put_child(root_slot, 0, root.box, link);
+            put_child(root_slot, 1, root.box, link);
+        } else {
+            stack.push_back(Item{enc(0, 0), root_slot});
+            while (!stack.empty()) {
+                Item it = stack.back(); stack.pop_back();
+                const BNode& n = get(it.ref);
+                for (int side = 0; side < 2; ++side) {
+                    int64_t cr = n.child[side];
+                    const BNode& ch = get(cr);
+                    if (ch.leaf) {
+                        put_child(it.slot, side, ch.box, emit_leaf(ch));
+                    } else {
+                        uint32_t sl = alloc();
+                        put_child(it.slot, side, ch.box, (int32_t)sl);
+                        stack.push_back(Item{cr, sl});
+                    }
                 }
             }
         }
+        out.num_nodes = (uint32_t)(words.size() / 16);
+        return true;
     }
-    out.num_nodes = (uint32_t)(nodes.size() / 16);
-    out.max_depth = max_depth;
+
+    // ---- 8-wide compressed layout (20 words per node), breadth first
+    // w0..2 origin p (float), w3 biased exponents ex|ey<<8|ez<<16 and the internal-child mask <<24,
+    // w4 first internal child, w5 first triangle, w6..7 meta bytes (0 empty, 0x80 internal,
+    // count<<5|offset for a leaf of 1..3 triangles), w8..19 qlo_x, qlo_y, qlo_z, qhi_x, qhi_y,
+    // qhi_z (8 bytes each).  Child boxes dequantise to p + 2^e * q, rounded outward so that the
+    // FP32 evaluation contains the exact box.
+    auto fbits = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
+    std::vector<std::pair<int64_t, uint32_t>> queue;  // (build node, device node index)
+    queue.reserve(ntris / 4 + 16);
+    words.resize(20, 0u);
+    queue.push_back({enc(0, 0), 0u});
+    for (size_t qi = 0; qi < queue.size(); ++qi) {
+        const int64_t ref = queue[qi].first;
+        const uint32_t slot_index = queue[qi].second;
+        const BNode& bn = get(ref);
+        // collapse: open the largest internal child until there are 8
+        std::vector<int64_t> ch;
+        if (bn.leaf) ch.push_back(ref);
+        else { ch.push_back(bn.child[0]); ch.push_back(bn.child[1]); }
+        while (ch.size() < 8) {
+            int best = -1; float best_area = -1.f;
+            for (size_t c = 0; c < ch.size(); ++c) {
+                const BNode& cn = get(ch[c]);
+                if (cn.leaf) continue;
+                float a = cn.box.half_area();
+                if (a > best_area) { best_area = a; best = (int)c; }
+            }
+            if (best < 0) break;
+            const BNode& op = get(ch[best]);
+            int64_t l = op.child[0], r = op.child[1];
+            ch[best] = l;
+            ch.push_back(r);
+        }
+        const size_t nc = ch.size();
+        Box nb;
+        for (int64_t c : ch) nb.grow(get(c).box);
+        // octant slots: the child in slot s is the nearest one for rays whose direction signs
+        // are s (bit 0: x < 0, bit 1: y < 0, bit 2: z < 0); greedy assignment on
+        // cost(c, s) = dot(centroid_c - centroid_node, D(s)), D(s) = (+-1, +-1, +-1)
+        float pc[3];
+        for (int k = 0; k < 3; ++k) pc[k] = 0.5f * nb.lo[k] + 0.5f * nb.hi[k];
+        float cost[8][8];
+        for (size_t c = 0; c < nc; ++c) {
+            const Box& b = get(ch[c]).box;
+            float d[3];
+            for (int k = 0; k < 3; ++k) d[k] = (0.5f * b.lo[k] + 0.5f * b.hi[k]) - pc[k];
+            for (int sl = 0; sl < 8; ++sl)
+                cost[c][sl] = ((sl & 1) ? -d[0] : d[0]) + ((sl & 2) ? -d[1] : d[1]) + ((sl & 4) ? -d[2] : d[2]);
+        }
+        int slot_of[8];
+        bool used_c[8] = {false}, used_s[8] = {false};
+        for (size_t round = 0; round < nc; ++round) {
+            int bc = -1, bs = -1; float bv = INFINITY;
+            for (size_t c = 0; c < nc; ++c) {
+                if (used_c[c]) continue;
+                for (int sl = 0; sl < 8; ++sl)
+                    if (!used_s[sl] && cost[c][sl] < bv) { bv = cost[c][sl]; bc = (int)c; bs = sl; }
+            }
+            used_c[bc] = true; used_s[bs] = true; slot_of[bc] = bs;
+        }
+        int64_t at_slot[8];
+        for (int sl = 0; sl < 8; ++sl) at_slot[sl] = -1;
+        for (size_t c = 0; c < nc; ++c) at_slot[slot_of[c]] = ch[c];
+        // children records
+        uint32_t imask = 0, n_internal = 0;
+        for (int sl = 0; sl < 8; ++sl)
+            if (at_slot[sl] >= 0 && !get(at_slot[sl]).leaf) { imask |= 1u << sl; n_internal++; }
+        const uint32_t child_base = (uint32_t)(words.size() / 20);
+        words.resize(words.size() + 20 * (size_t)n_internal, 0u);
+        const uint32_t tri_base = (uint32_t)(out.tris.size() / 12);
+        uint8_t meta[8] = {0};
+        uint32_t off = 0, ci = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            if (at_slot[sl] < 0) continue;
+            const BNode& cn = get(at_slot[sl]);
+            if (cn.leaf) {
+                meta[sl] = (uint8_t)((cn.count << 5) | off);
+                for (uint32_t i = 0; i < cn.count; ++i) emit_tri(order[cn.first + i]);
+                off += cn.count;
+            } else {
+                meta[sl] = 0x80;
+                queue.push_back({at_slot[sl], child_base + ci});
+                ci++;
+            }
+        }
+        // quantisation
+        uint8_t qlo[3][8], qhi[3][8];
+        int ebias[3];
+        float p[3];
+        for (int a = 0; a < 3; ++a) {
+            p[a] = nb.lo[a];
+            const double ext = (double)nb.hi[a] - (double)nb.lo[a];
+            int e = -126;
+            if (ext > 0) {
+                int ex;
+                std::frexp(ext / 255.0, &ex);  // ext/255 < 2^ex
+                e = std::max(-126, std::min(127, ex));
+            }
+            for (;; ++e) {
+                const float scale = std::ldexp(1.0f, e);
+                bool ok = (float)(p[a] + scale * 255.0f) >= nb.hi[a];
+                for (int sl = 0; sl < 8 && ok; ++sl) {
+                    if (at_slot[sl] < 0) { qlo[a][sl] = 0; qhi[a][sl] = 0; continue; }
+                    const Box& b = get(at_slot[sl]).box;
+                    double lo_q = std::floor(((double)b.lo[a] - (double)p[a]) / (double)scale);
+                    double hi_q = std::ceil(((double)b.hi[a] - (double)p[a]) / (double)scale);
+                    int lq = (int)std::max(0.0, std::min(255.0, lo_q));
+                    int hq = (int)std::max(0.0, std::min(255.0, hi_q));
+                    while (lq > 0 && (float)(p[a] + scale * (float)lq) > b.lo[a]) lq--;
+                    while (hq < 255 && (float)(p[a] + scale * (float)hq) < b.hi[a]) hq++;
+                    if ((float)(p[a] + scale * (float)lq) > b.lo[a] || (float)(p[a] + scale * (float)hq) < b.hi[a]) ok = false;
+                    qlo[a][sl] = (uint8_t)lq; qhi[a][sl] = (uint8_t)hq;
+                }
+                if (ok || e >= 127) break;
+            }
+            ebias[a] = e + 127;
+        }
+        uint32_t* w = &words[20 * (size_t)slot_index];
+        w[0] = fbits(p[0]); w[1] = fbits(p[1]); w[2] = fbits(p[2]);
+        w[3] = (uint32_t)ebias[0] | ((uint32_t)ebias[1] << 8) | ((uint32_t)ebias[2] << 16) | (imask << 24);
+        w[4] = child_base;
+        w[5] = tri_base;
+        w[6] = (uint32_t)meta[0] | ((uint32_t)meta[1] << 8) | ((uint32_t)meta[2] << 16) | ((uint32_t)meta[3] << 24);
+        w[7] = (uint32_t)meta[4] | ((uint32_t)meta[5] << 8) | ((uint32_t)meta[6] << 16) | ((uint32_t)meta[7] << 24);
+        auto pack8 = [](const uint8_t* q, uint32_t& lo, uint32_t& hi) {
+            lo = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
+            hi = (uint32_t)q[4] | ((uint32_t)q[5] << 8) | ((uint32_t)q[6] << 16) | ((uint32_t)q[7] << 24);
+        };
+        pack8(qlo[0], w[8], w[9]); pack8(qlo[1], w[10], w[11]); pack8(qlo[2], w[12], w[13]);
+        pack8(qhi[0], w[14], w[15]); pack8(qhi[1], w[16], w[17]); pack8(qhi[2], w[18], w[19]);
+    }
+    out.num_nodes = (uint32_t)(words.size() / 20);
     return true;
 }
 

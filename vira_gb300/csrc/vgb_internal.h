@@ -6,7 +6,9 @@
 //   w2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
 //   w3 = (child0, child1, 0, 0) as int32: >= 0 inner node index, < 0 leaf ~(first << 3 | count-1)
 // A leaf holds 1..8 consecutive triangle records.  The root is node 0; a scene whose root
-// is a leaf gets one inner node whose second child is empty (an inverted box).
+// is a leaf gets one inner node whose two children are that leaf.
+//
+// Device BVH (compressed 8-wide): one node is five 16-byte words, see vgb_host.cpp.
 //
 // Triangle record (watertight test input), three 16-byte words in leaf order:
 //   (v0.x, v0.y, v0.z, id as bits), (v1.xyz, 0), (v2.xyz, 0)
@@ -19,18 +21,21 @@ namespace vgb {
 
 constexpr int kLeafShift = 3;
 constexpr uint32_t kMaxLeaf = 8;
+constexpr uint32_t kMaxLeaf8 = 3;   // triangles per leaf child of an 8-wide node
 
 struct BvhHost {
-    std::vector<float> nodes;      // 16 floats per node
+    uint32_t layout = 2;           // 2: binary (16 words per node), 8: compressed 8-wide (20 words)
+    std::vector<uint32_t> nodes;
     std::vector<float> tris;       // 12 floats per triangle record
     uint32_t num_nodes = 0;
     uint32_t max_depth = 0;
     float root_lo[3] = {0, 0, 0}, root_hi[3] = {0, 0, 0};
 };
 
-// Binned-SAH build over the triangles of (positions, indices).  Deterministic for a given
-// input and leaf size, whatever the thread count.
-bool build_bvh2(const float* positions, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
-                uint32_t max_leaf, uint32_t threads, BvhHost& out, const char** err);
+// Binned-SAH build over the triangles of (positions, indices), emitted in the binary layout or
+// collapsed into the compressed 8-wide layout.  Deterministic for a given input, leaf size and
+// layout, whatever the thread count.
+bool build_bvh(const float* positions, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
+               uint32_t max_leaf, uint32_t threads, uint32_t layout, BvhHost& out, const char** err);
 
 }  // namespace vgb

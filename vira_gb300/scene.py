@@ -351,7 +351,7 @@ class Scene:
         self.ambient = None
         self.background = np.zeros(bands.size, np.float32)
         self.pathtracer = PathTracer()
-        self.bvh_options = capi.BvhOptions(0, 0, 0)
+        self.bvh_options = capi.BvhOptions(0, 0, 0, 0)
         self._ctx = None
         self._dirty = True
         self._omega_cache = {}
