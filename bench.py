@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-direct", action="store_true", help="skip the extra plain-direct line item")
     ap.add_argument("--layout", type=int, choices=[2, 8], default=2, help="device BVH node layout")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-trajectory line item")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint line item")
     return ap.parse_args()
 
 
@@ -387,6 +389,14 @@ def run_ours(args, p, rank, world, local_rank):
     direct = None
     if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
         direct = plain_direct_item(torch, dev, args.layout)
+    batched = None
+    if not args.no_batched and p["kind"] == "path_traced" and rank == 0:
+        scene.close()
+        batched = batched_item(torch, dev, args.layout)
+    adjoint = None
+    if not args.no_adjoint and p["kind"] == "path_traced" and rank == 0:
+        scene.close()
+        adjoint = adjoint_item(torch, dev, args.layout)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -431,13 +441,151 @@ def run_ours(args, p, rank, world, local_rank):
         }
         if direct is not None:
             line["plain_direct"] = direct
+        if batched is not None:
+            line["batched"] = batched
+        if adjoint is not None:
+            line["adjoint"] = adjoint
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
     scene.close()
 
 
-def plain_direct_item(torch, dev, layout=8):
+def batched_item(torch, dev, layout=2, nframes=256, reps=2):
+    """The trajectory workload: 256 frames of uneven size and spp in one persistent launch
+    (autotuned, CUDA-graph replay) against per-frame vgb_render calls of the same frames."""
+    from vira_gb300 import capi, workloads
+
+    scene, frames = workloads.trajectory(nframes=nframes, device=dev.index)
+    scene.bvh_options.layout = layout
+    scene.build_tlas()
+    lib = capi.load()
+    ctx = scene.context()
+    B = scene.bands.size
+    arr = (capi.Frame * len(frames))()
+    films = []
+    for i, fr in enumerate(frames):
+        cam = fr.camera.to_c(scene.origin, B)
+        W, H = fr.camera.resolution
+        om = scene._batch_omega(fr.camera, cam)
+        planes = {"total_radiance": torch.empty((B, H, W), device=dev), "received_power": torch.empty((B, H, W), device=dev),
+                  "triangle_id": torch.empty((H, W), dtype=torch.int32, device=dev)}
+        f = arr[i]
+        f.camera = cam
+        L = scene.lights[0]
+        p = (np.asarray(fr.light_positions[0]) - scene.origin).astype(np.float32)
+        for a in range(3):
+            f.lights[0].position[a] = float(p[a])
+        f.lights[0].radius = float(L.radius)
+        for b in range(B):
+            f.lights[0].radiance[b] = float(L.radiance[b])
+        f.nlights = 1
+        f.samples = fr.samples
+        f.frame = fr.frame
+        for k, t in planes.items():
+            setattr(f.film, k, t.data_ptr())
+        f.film.pixel_solid_angle = om.data_ptr()
+        f.film.on_device = 1
+        films.append(planes)
+    opts = scene.pathtracer.c_options(scene)
+
+    def checksum():
+        torch.cuda.synchronize(dev)
+        return [float(p["total_radiance"].double().sum()) + float(p["triangle_id"].double().sum()) for p in films]
+
+    torch.cuda.synchronize(dev)
+    tune = capi.BatchOptions(1, 1, 0, 0, 0)
+    capi.check(lib.vgb_render_batch(ctx, arr, len(frames), C.byref(opts), C.byref(tune)), ctx, "render_batch")
+    bo = capi.BatchOptions(0, 1, 0, 0, 0)
+    bt, rays = [], 0
+    for _ in range(reps):
+        t = time.perf_counter()
+        capi.check(lib.vgb_render_batch(ctx, arr, len(frames), C.byref(opts), C.byref(bo)), ctx, "render_batch")
+        bt.append(time.perf_counter() - t)
+        st = capi.Stats()
+        lib.vgb_get_stats(ctx, C.byref(st))
+        rays = st.rays_closest + st.rays_shadow
+    sums_batch = checksum()
+    # per-frame launches of the plain renderer, same frames
+    pt, pr = [], 0
+    for _ in range(reps):
+        t = time.perf_counter()
+        pr = 0
+        for i in range(len(frames)):
+            f = arr[i]
+            o = capi.PtOptions.from_buffer_copy(bytes(opts))
+            o.samples, o.frame = f.samples, f.frame
+            lights = (capi.Light * 1)(f.lights[0])
+            film = capi.Film.from_buffer_copy(bytes(f.film))
+            capi.check(lib.vgb_render(ctx, C.byref(f.camera), lights, 1, C.byref(o), C.byref(film)), ctx, "render")
+            st = capi.Stats()
+            lib.vgb_get_stats(ctx, C.byref(st))
+            pr += st.rays_closest + st.rays_shadow
+        pt.append(time.perf_counter() - t)
+    sums_plain = checksum()
+    th, bps, grab = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    lib.vgb_batch_tuning(ctx, C.byref(th), C.byref(bps), C.byref(grab))
+    samples = sum(int(f.samples) * f.camera.width * f.camera.height for f in arr)
+    scene.close()
+    tb, tp = min(bt), min(pt)
+    return {"workload": f"trajectory_{len(frames)}frames_dem513_8band_direct", "path_samples": samples,
+            "rays": int(rays), "batched_s": tb, "per_frame_s": tp, "speedup": tp / tb,
+            "batched_mrays_s": rays / tb / 1e6, "per_frame_mrays_s": pr / tp / 1e6,
+            "batched_path_samples_per_s": samples / tb,
+            "identical_per_pixel": sums_batch == sums_plain and rays == pr,
+            "tuned": {"block_threads": th.value, "blocks_per_sm": bps.value, "tiles_per_grab": grab.value},
+            "timing": "wall clock around the blocking C-ABI calls, best of %d" % reps}
+
+
+def adjoint_item(torch, dev, layout=2, reps=2):
+    """The inversion workload: 16 views of a 1025^2 crater DEM, albedo texels and vertex heights as
+    parameters; one forward (all views) and one backward (path-replay adjoint, all views)."""
+    from vira_gb300 import workloads
+    from vira_gb300.autograd import _apply_parameters, adjoint_views, forward_views
+
+    scene, views = workloads.inversion(device=dev.index)
+    scene.bvh_options.layout = layout
+    mesh = scene.meshes[0]
+    base_tex = mesh.albedo_map.copy()
+    base_z = mesh.positions[:, 2].copy()
+    rng = np.random.default_rng(4)
+    tgt_tex = (base_tex * (1.0 + 0.05 * rng.standard_normal(base_tex.shape[:2]))[:, :, None]).astype(np.float32)
+    tgt_z = (base_z + rng.normal(0.0, 0.5, base_z.shape)).astype(np.float32)
+    _apply_parameters(scene, torch.tensor(tgt_tex), torch.tensor(tgt_z))
+    targets = forward_views(scene, views, dev)
+    _apply_parameters(scene, torch.tensor(base_tex), torch.tensor(base_z))
+    imgs = forward_views(scene, views, dev)  # warm-up
+    grads = [2.0 * (i - t) for i, t in zip(imgs, targets)]
+    adjoint_views(scene, views, grads, dev)  # warm-up
+    fw, bw = [], []
+    for _ in range(reps):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        imgs = forward_views(scene, views, dev)
+        torch.cuda.synchronize(dev)
+        fw.append(time.perf_counter() - t)
+        grads = [2.0 * (i - t_) for i, t_ in zip(imgs, targets)]
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        gt, gz = adjoint_views(scene, views, grads, dev)
+        torch.cuda.synchronize(dev)
+        bw.append(time.perf_counter() - t)
+    loss = float(sum(((i - t_) ** 2).double().sum() for i, t_ in zip(imgs, targets)))
+    ntexel = base_tex.shape[0] * base_tex.shape[1]
+    nz = base_z.shape[0]
+    res = views[0].camera.resolution
+    out = {"workload": f"inversion_dem{int(round(nz ** 0.5))}_tex{base_tex.shape[0]}_{len(views)}views_{res[0]}px_"
+                       f"{scene.pathtracer.options.samples}spp_{scene.pathtracer.options.bounces}b_4band",
+           "parameters": ntexel + nz, "texels": ntexel, "heights": nz,
+           "forward_s": min(fw), "backward_s": min(bw), "backward_over_forward": min(bw) / min(fw),
+           "backward_passes_per_s": 1.0 / min(bw), "loss": loss,
+           "grad_norm": {"texture": float(gt.double().norm()), "heights": float(gz.double().norm())},
+           "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
+    scene.close()
+    return out
+
+
+def plain_direct_item(torch, dev, layout=2):
     """The 513^2 / 1024^2 direct-lighting frame: Mrays/s (primary + shadow) on the same GPU."""
     from vira_gb300 import workloads
 

@@ -216,6 +216,53 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
  * the GPU -- two contexts or two streams rendering at once on one device -- race. */
 VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                                       uint32_t nlights, const vgb_pt_options* opts, vgb_film* film);
+/* ---- batched trajectory rendering -------------------------------------------------
+ * Many frames (cameras, lights, resolutions and sample counts of their own) rendered by one
+ * persistent kernel: warps claim (frame, 8x4-pixel tile) items from a queue, the most expensive
+ * frames first, and keep each tile's samples in registers and shared memory.  Per-pixel results
+ * are those of vgb_render for the same frame (same arithmetic and random streams).  No
+ * counterpart in the reference, which renders one frame per call. */
+typedef struct vgb_frame {
+    vgb_camera camera;
+    vgb_light lights[8];
+    uint32_t nlights;
+    uint32_t samples;          /* this frame's samples per pixel */
+    uint32_t frame;            /* RNG key word of this frame (vgb_pt_options.frame for vgb_render) */
+    vgb_film film;             /* device planes (on_device must be 1) */
+} vgb_frame;
+
+typedef struct vgb_batch_options {
+    uint32_t autotune;         /* 1: time launch shapes on a 1/16 sample of the tiles, keep the best */
+    uint32_t use_graph;        /* 1: replay the batch from a captured CUDA graph */
+    uint32_t block_threads;    /* 0: default or tuned (64, 128 or 256) */
+    uint32_t blocks_per_sm;    /* 0: default or tuned */
+    uint32_t tiles_per_grab;   /* work items claimed per queue access; 0: default or tuned */
+} vgb_batch_options;
+
+/* Renders `nframes` frames with the options in `opts` (samples and frame are taken from each
+ * vgb_frame).  Frames' film planes are written as by vgb_render. */
+VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame* frames, uint32_t nframes,
+                                    const vgb_pt_options* opts, const vgb_batch_options* bopts);
+/* The launch shape chosen by the last autotuned batch (0s before the first one). */
+VGB_API vgb_status vgb_batch_tuning(vgb_context* ctx, uint32_t* block_threads, uint32_t* blocks_per_sm,
+                                    uint32_t* tiles_per_grab);
+
+/* ---- adjoint (differentiable rendering; no counterpart in the reference) -------------
+ * Given dL/dI for the total-radiance planes ([B][H][W]) of a frame rendered with the same
+ * camera, lights and options, ADDS into d_texture ([tex_h][tex_w][B], the albedo texture's
+ * layout) and d_height (one per vertex: the derivative with respect to the vertex's z in the
+ * scene frame); NULL skips one.  Paths are replayed from their random streams, nothing is stored
+ * by the forward render.  Height gradients go through the hit triangle's face normal in every
+ * next-event term and through the motion of the hit point on the triangle (barycentrics, hence
+ * texture coordinates and interpolated albedo); they need flat shading.  Excluded: visibility
+ * (shadow and silhouette edges), the rotation of the sampled continuation direction with the
+ * normal, the motion of the shading point, Russian roulette decisions.  At most 3 bounces. */
+VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                               uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
+                               float* d_texture, float* d_height, int on_device);
+/* Replaces the albedo texture (same size) without re-uploading the mesh or rebuilding the BVH. */
+VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h);
+
 /* TLAS::intersect(Ray&) seam (include/vira/rendering/acceleration/tlas.hpp:24): a batch of
  * rays, closest hit (any_hit = 0) or occlusion (any_hit = 1, tmax per ray or +inf).
  * origins/dirs: 3 floats per ray.  tri_out: VGB_NO_HIT on a miss; t_out: +inf on a miss;

@@ -51,6 +51,7 @@ def load():
         "oracle_trace": (C.c_int, [P, P, P, P, U32, C.c_int, C.c_int, P, P, P, C.c_int, P, P]),
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
                                     C.POINTER(capi.Film), U32, U32, C.c_int, P]),
+        "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -157,6 +158,19 @@ class OracleScene:
                                    int(any_hit), mode, tri.ctypes.data, t.ctypes.data, w.ctypes.data,
                                    threads or nthreads(), C.byref(nodes), C.byref(tris)) == 0
         return tri, t, w
+
+    def adjoint(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, dldi, tex_shape=None,
+                nverts=None, threads=None):
+        """FP64 gradients of sum(dL/dI * I): (d_texture [th][tw][B] or None, d_height [nverts] or None)."""
+        d = np.ascontiguousarray(dldi, np.float32)
+        gt = np.zeros(tex_shape, np.float64) if tex_shape is not None else None
+        gz = np.zeros(nverts, np.float64) if nverts is not None else None
+        rc = load().oracle_adjoint(self.h, C.byref(cam), C.cast(lights, C.c_void_p) if nlights else None, nlights,
+                                   C.byref(opts), d.ctypes.data, None if gt is None else gt.ctypes.data,
+                                   None if gz is None else gz.ctypes.data, threads or nthreads())
+        if rc != 0:
+            raise ValueError("oracle_adjoint rejected its arguments")
+        return gt, gz
 
     def render(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, omega=None, rows=None,
                threads=None):

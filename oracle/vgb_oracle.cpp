@@ -1020,3 +1020,260 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
     }
     return 0;
 }
+
+
+// ==================================================================== FP64 adjoint (path replay)
+// The same sampled paths as oracle_render (FP32, identical arithmetic), with the gradient of
+// sum_k g_k I_k (g = dL/dI / spp) formed in FP64: albedo through the suffix radiance / albedo
+// of every path vertex, heights through the hit triangle's face normal in every NEE term and
+// through the hit-point motion on the triangle (barycentrics -> uv -> bilinear texture and
+// interpolated vertex albedo).  Visibility, the rotation of sampled directions with the normal
+// and the motion of the shading point are excluded, as in the product's vgb_adjoint.
+namespace {
+
+struct AVtx {
+    uint32_t tri;
+    float w0, w1, uvx, uvy;
+    double m1, m2, gn[3];
+    float alb[VGB_MAX_BANDS], va[VGB_MAX_BANDS], tex[VGB_MAX_BANDS], rad[VGB_MAX_BANDS];
+};
+
+static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light* lights, uint32_t nlights,
+                          const vgb_pt_options& o, uint32_t i, uint32_t j, const double* g, double* gtex, double* gz) {
+    const uint32_t B = s.nbands;
+    Rng rng{(uint32_t)o.seed, (uint32_t)(o.seed >> 32), j * cam.width + i, 0, o.frame};
+    V3 org{cam.origin[0], cam.origin[1], cam.origin[2]};
+    for (uint32_t sample = 0; sample < o.samples; ++sample) {
+        rng.sample = sample;
+        float X = (float)i, Y = (float)j;
+        if (sample != 0) {
+            U4 jr = rng.draw(0, SLOT_JITTER);
+            X = X + u01(jr.v[0]);
+            Y = Y + u01(jr.v[1]);
+        }
+        const float* K = cam.kinv;
+        float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
+        float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
+        V3 dir = normalize(mat3_mul(cam.rotation, V3{hx, cam.z_dir * hy, cam.z_dir}));
+        V3 ro = org;
+        float thr[VGB_MAX_BANDS], bgc[VGB_MAX_BANDS] = {0};
+        for (uint32_t k = 0; k < B; ++k) thr[k] = 1.f;
+        AVtx vx[4];
+        int nv = 0;
+        for (uint32_t bounce = 0; bounce < o.bounces + 1 && nv < 4; ++bounce) {
+            Hit h = trace(s, ro, dir, INF_F, false, 0);
+            if (std::isinf(h.t)) {
+                if (o.simulate_lighting && o.show_background) {
+                    float x = dir.x, y = dir.y, z = dir.z;
+                    float u = std::atan2(y, x) / (2 * PI_F);
+                    float v = std::atan2(std::sqrt(x * x + y * y), z) / PI_F;
+                    float px = std::fmod(u * 1.f, 1.f), py = std::fmod(v * 1.f, 1.f);
+                    if (px < 0) px += 1.f;
+                    if (py < 0) py += 1.f;
+                    float a = (1.f - px) * (1.f - py), b = px * (1.f - py), c = (1.f - px) * py, e = px * py;
+                    for (uint32_t k = 0; k < B; ++k) {
+                        float bgv = o.background[k];
+                        bgc[k] = thr[k] * ((((a * bgv + b * bgv) + c * bgv) + e * bgv) * 1.f);
+                    }
+                }
+                break;
+            }
+            AVtx& V = vx[nv++];
+            const uint32_t t = h.tri;
+            const uint32_t i0 = s.idx[3 * t], i1 = s.idx[3 * t + 1], i2 = s.idx[3 * t + 2];
+            const uint32_t vi[3] = {i1, i2, i0};
+            const float* w = h.w;
+            V.tri = t; V.w0 = w[0]; V.w1 = w[1];
+            {
+                const float* a = &s.uv[2 * vi[0]]; const float* b = &s.uv[2 * vi[1]]; const float* c = &s.uv[2 * vi[2]];
+                V.uvx = (w[0] * a[0] + w[1] * b[0]) + w[2] * c[0];
+                V.uvy = (w[0] * a[1] + w[1] * b[1]) + w[2] * c[1];
+            }
+            V3 p0 = s.pos[i0], p1 = s.pos[i1], p2 = s.pos[i2];
+            V3 fnn = normalize(cross(p0 - p1, p2 - p0));
+            V3 fnrm{-fnn.x, -fnn.y, -fnn.z};
+            V3 N_local = fnrm;
+            if (o.smooth_shading) N_local = normalize((w[0] * s.nrm[vi[0]] + w[1] * s.nrm[vi[1]]) + w[2] * s.nrm[vi[2]]);
+            V3 N = N_local;
+            V3 arb = (std::fabs(N.x) < 0.9f) ? V3{1, 0, 0} : V3{0, 1, 0};
+            V3 tangent = normalize(cross(arb, N));
+            V3 bitangent = cross(N, tangent);
+            sample_uvs(s, V.uvx, V.uvy, V.tex);
+            for (uint32_t k = 0; k < B; ++k) {
+                V.va[k] = (w[0] * s.albedo[(size_t)vi[0] * B + k] + w[1] * s.albedo[(size_t)vi[1] * B + k]) +
+                          w[2] * s.albedo[(size_t)vi[2] * B + k];
+                V.alb[k] = V.va[k] * V.tex[k];
+            }
+            // M^-1 e_z for the hit-point motion, FP64 (caller order A=v0, B=v1, C=v2)
+            {
+                V3d A{p0.x, p0.y, p0.z}, Bv{p1.x, p1.y, p1.z}, Cv{p2.x, p2.y, p2.z}, d{dir.x, dir.y, dir.z};
+                V3d c1 = A - Bv, c2 = A - Cv, ez{0, 0, 1};
+                double det = dotd(d, crossd(c1, c2));
+                V.m1 = det != 0 ? dotd(d, crossd(ez, c2)) / det : 0.0;
+                V.m2 = det != 0 ? dotd(d, crossd(c1, ez)) / det : 0.0;
+            }
+            V.gn[0] = V.gn[1] = V.gn[2] = 0.0;
+            for (uint32_t k = 0; k < B; ++k) V.rad[k] = 0.f;
+            V3 P = (w[0] * s.pos[vi[0]] + w[1] * s.pos[vi[1]]) + w[2] * s.pos[vi[2]];
+            {
+                V3 q[3];
+                for (int k = 0; k < 3; ++k) { V3 vp = s.pos[vi[k]], vn = s.nrm[vi[k]]; q[k] = P - dot(P - vp, vn) * vn; }
+                V3 sp = (q[0] * w[0] + q[1] * w[1]) + q[2] * w[2];
+                if (dot(sp - P, N_local) > 0) P = sp;
+            }
+            if (!o.simulate_lighting) break;
+            P = V3{off1(P.x, fnrm.x), off1(P.y, fnrm.y), off1(P.z, fnrm.z)};
+            if (bounce == 0 && o.has_ambient)
+                for (uint32_t k = 0; k < B; ++k) V.rad[k] += thr[k] * (o.ambient[k] * V.alb[k]);
+            U4 r0 = rng.draw(bounce, SLOT_MAIN);
+            for (uint32_t l = 0; l < nlights; ++l) {
+                float ru1, ru2;
+                if (l == 0) { ru1 = u01(r0.v[0]); ru2 = u01(r0.v[1]); }
+                else { U4 rl = rng.draw(bounce, 1 + l); ru1 = u01(rl.v[0]); ru2 = u01(rl.v[1]); }
+                V3 Ld; float dist, lpdf = 0;
+                light_sample(lights[l], P, o.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                if (!(lpdf > 0)) continue;
+                Hit sh = trace(s, P, Ld, dist, true, 0);
+                if (!(sh.t > dist)) continue;
+                float nl = dot(N, Ld);
+                float cos_t = std::max(0.0f, dot(Ld, N));
+                float mpdf = (nl <= 0.f) ? 0.f : nl * INV_PI_F;
+                float wgt = power_heuristic(lpdf, mpdf);
+                double gc = 0;
+                for (uint32_t k = 0; k < B; ++k) {
+                    float bsdf = V.alb[k] * INV_PI_F * std::max(nl, 0.f);
+                    float con = thr[k] * bsdf * lights[l].radiance[k] * cos_t * wgt / lpdf;
+                    V.rad[k] += con;
+                    gc += g[k] * (double)con;
+                }
+                if (nl > 0.f && wgt > 0.f) {
+                    double m = (double)nl / 3.141592653589793238462;
+                    double lp = lpdf;
+                    double dw_over_w = -2.0 * m / 3.141592653589793238462 / (lp * lp + m * m);
+                    double sc = gc * (2.0 / nl + dw_over_w);
+                    V.gn[0] += sc * Ld.x; V.gn[1] += sc * Ld.y; V.gn[2] += sc * Ld.z;
+                }
+            }
+            if (bounce >= o.bounces) break;
+            V3 ls = cosine_sample(u01(r0.v[2]), u01(r0.v[3]));
+            float mpdf = ls.z * INV_PI_F;
+            V3 nd{(tangent.x * ls.x + bitangent.x * ls.y) + N.x * ls.z, (tangent.y * ls.x + bitangent.y * ls.y) + N.y * ls.z,
+                  (tangent.z * ls.x + bitangent.z * ls.y) + N.z * ls.z};
+            if (mpdf > 0) {
+                float nl = dot(N, nd);
+                float cos_t = std::max(0.0f, dot(nd, N));
+                float lp = 0;
+                for (uint32_t l = 0; l < nlights; ++l) lp += light_pdf(lights[l], P, nd);
+                lp /= (float)nlights;
+                float wgt = power_heuristic(mpdf, lp);
+                for (uint32_t k = 0; k < B; ++k) {
+                    float bsdf = V.alb[k] * INV_PI_F * std::max(nl, 0.f);
+                    thr[k] *= bsdf * cos_t * wgt / mpdf;
+                }
+                ro = P; dir = nd;
+                if (o.rr_depth != 0 && bounce + 1 >= o.rr_depth) {
+                    float q = 0.f;
+                    for (uint32_t k = 0; k < B; ++k) q = std::max(q, thr[k]);
+                    q = std::min(q, 1.0f);
+                    U4 rr = rng.draw(bounce, SLOT_RR);
+                    if (u01(rr.v[0]) >= q) break;
+                    for (uint32_t k = 0; k < B; ++k) thr[k] = thr[k] / q;
+                }
+            }
+        }
+        double S[VGB_MAX_BANDS];
+        for (uint32_t k = 0; k < B; ++k) S[k] = bgc[k];
+        for (int b = nv - 1; b >= 0; --b) {
+            const AVtx& V = vx[b];
+            double ga[VGB_MAX_BANDS];
+            for (uint32_t k = 0; k < B; ++k) {
+                S[k] += V.rad[k];
+                ga[k] = V.alb[k] != 0.f ? g[k] * S[k] / (double)V.alb[k] : 0.0;
+            }
+            float rx = (float)s.tw, ry = (float)s.th;
+            float px = std::fmod(V.uvx * rx, rx), py = std::fmod(V.uvy * ry, ry);
+            if (px < 0) px += rx;
+            if (py < 0) py += ry;
+            int x0 = std::min((int)std::floor(px), (int)s.tw - 1), y0 = std::min((int)std::floor(py), (int)s.th - 1);
+            int x1 = std::min(x0 + 1, (int)s.tw - 1), y1 = std::min(y0 + 1, (int)s.th - 1);
+            double dx = px - (float)x0, dy = py - (float)y0;
+            double wt[4] = {(1 - dx) * (1 - dy), dx * (1 - dy), (1 - dx) * dy, dx * dy};
+            size_t tx[4] = {(size_t)y0 * s.tw + x0, (size_t)y0 * s.tw + x1, (size_t)y1 * s.tw + x0, (size_t)y1 * s.tw + x1};
+            if (gtex)
+                for (uint32_t k = 0; k < B; ++k)
+                    for (int q = 0; q < 4; ++q) gtex[tx[q] * B + k] += ga[k] * V.va[k] * wt[q];
+            if (gz) {
+                uint32_t ia = s.idx[3 * V.tri], ib = s.idx[3 * V.tri + 1], ic = s.idx[3 * V.tri + 2];
+                V3d A{s.pos[ia].x, s.pos[ia].y, s.pos[ia].z}, Bv{s.pos[ib].x, s.pos[ib].y, s.pos[ib].z};
+                V3d Cv{s.pos[ic].x, s.pos[ic].y, s.pos[ic].z};
+                V3d a = A - Bv, bb = Cv - A;
+                V3d n = crossd(a, bb);
+                double ln = std::sqrt(dotd(n, n));
+                V3d nh{n.x / ln, n.y / ln, n.z / ln};
+                V3d dn[3] = {V3d{-bb.y - a.y, bb.x + a.x, 0}, V3d{bb.y, -bb.x, 0}, V3d{a.y, -a.x, 0}};
+                const float* uvA = &s.uv[2 * ia]; const float* uvB = &s.uv[2 * ib]; const float* uvC = &s.uv[2 * ic];
+                double d0 = 0, d1 = 0;
+                for (uint32_t k = 0; k < B; ++k) {
+                    double t00 = s.tex[tx[0] * B + k], t10 = s.tex[tx[1] * B + k], t01 = s.tex[tx[2] * B + k], t11 = s.tex[tx[3] * B + k];
+                    double dtdx = (1 - dy) * (t10 - t00) + dy * (t11 - t01);
+                    double dtdy = (1 - dx) * (t01 - t00) + dx * (t11 - t10);
+                    double dt0 = dtdx * rx * ((double)uvB[0] - uvA[0]) + dtdy * ry * ((double)uvB[1] - uvA[1]);
+                    double dt1 = dtdx * rx * ((double)uvC[0] - uvA[0]) + dtdy * ry * ((double)uvC[1] - uvA[1]);
+                    double aA = s.albedo[(size_t)ia * B + k], aB = s.albedo[(size_t)ib * B + k], aC = s.albedo[(size_t)ic * B + k];
+                    d0 += ga[k] * ((aB - aA) * V.tex[k] + (double)V.va[k] * dt0);
+                    d1 += ga[k] * ((aC - aA) * V.tex[k] + (double)V.va[k] * dt1);
+                }
+                double wv[3] = {1.0 - (double)V.w0 - (double)V.w1, V.w0, V.w1};
+                uint32_t vid[3] = {ia, ib, ic};
+                for (int q = 0; q < 3; ++q) {
+                    double nd = dotd(nh, dn[q]);
+                    double dN[3] = {-(dn[q].x - nh.x * nd) / ln, -(dn[q].y - nh.y * nd) / ln, -(dn[q].z - nh.z * nd) / ln};
+                    double gq = V.gn[0] * dN[0] + V.gn[1] * dN[1] + V.gn[2] * dN[2];
+                    gq += (d0 * V.m1 + d1 * V.m2) * wv[q];
+                    gz[vid[q]] += gq;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// Adds the FP64 gradients of sum(dL/dI * I) into gtex ([th][tw][B]) and gz (per vertex).
+OAPI int oracle_adjoint(void* h, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                        const vgb_pt_options* opts, const float* dldi, double* gtex, double* gz, int nthreads) {
+    if (!h || !cam || !opts || !dldi || opts->samples == 0) return 1;
+    const Scene& s = *static_cast<Scene*>(h);
+    if (opts->nbands != s.nbands || opts->bounces > 3) return 1;
+    const uint32_t W = cam->width, H = cam->height, B = s.nbands;
+    const size_t npix = (size_t)W * H, ntex = (size_t)s.tw * s.th * B;
+    int nt = std::max(1, nthreads);
+    std::vector<std::vector<double>> tb(nt), zb(nt);
+    std::atomic<uint32_t> next{0};
+    auto work = [&](int tid) {
+        if (gtex) tb[tid].assign(ntex, 0.0);
+        if (gz) zb[tid].assign(s.nverts, 0.0);
+        while (true) {
+            uint32_t j = next.fetch_add(1);
+            if (j >= H) break;
+            for (uint32_t i = 0; i < W; ++i) {
+                double g[VGB_MAX_BANDS];
+                bool any = false;
+                for (uint32_t k = 0; k < B; ++k) {
+                    g[k] = (double)dldi[k * npix + (size_t)j * W + i] / (double)(float)opts->samples;
+                    any |= g[k] != 0.0;
+                }
+                if (any) adjoint_pixel(s, *cam, lights, nlights, *opts, i, j, g, gtex ? tb[tid].data() : nullptr,
+                                       gz ? zb[tid].data() : nullptr);
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) th.emplace_back(work, t);
+    for (auto& x : th) x.join();
+    for (int t = 0; t < nt; ++t) {
+        if (gtex) for (size_t q = 0; q < ntex; ++q) gtex[q] += tb[t][q];
+        if (gz) for (size_t q = 0; q < s.nverts; ++q) gz[q] += zb[t][q];
+    }
+    return 0;
+}

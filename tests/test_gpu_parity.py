@@ -210,3 +210,21 @@ def test_render_errors(gpu):
     opts.nbands = 4
     assert lib.vgb_render(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(f)) == 0
     scene.close()
+
+
+def test_small_frame_after_large_frame(gpu):
+    """Scratch keeps the largest frame's size; film planes must still use each frame's own size."""
+    import torch
+
+    scene, cam_id = workloads.plain_direct(posts=65, resolution=96)
+    big = gpu_render_host(scene, cam_id)
+    scene[cam_id].set_resolution(40, 40)
+    small = gpu_render_host(scene, cam_id)
+    scene.close()
+    fresh_scene, fresh_id = workloads.plain_direct(posts=65, resolution=96)
+    fresh_scene[fresh_id].set_resolution(40, 40)
+    fresh = gpu_render_host(fresh_scene, fresh_id)
+    fresh_scene.close()
+    for k in fresh:
+        assert same_bits(small[k], fresh[k]) if k != "triangle_id" else np.array_equal(small[k], fresh[k])
+    assert big["total_radiance"].shape[1] == 96

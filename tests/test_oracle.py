@@ -247,3 +247,41 @@ def test_synthetic_generators():
     assert np.allclose(np.linalg.norm(v, axis=1), 1.0)
     n = synthetic.real_sh_noise(v, 8, seed=5)
     assert n.shape == (v.shape[0],) and np.isfinite(n).all() and n.std() > 0
+
+
+def test_oracle_adjoint_albedo_euler_identity():
+    """Direct lighting is linear (degree 1) in the albedo texels, so sum_t alb_t dI/dalb_t = I
+    (Euler's theorem); with g = dL/dI the FP64 adjoint must satisfy sum alb * grad = sum g * I."""
+    from helpers import oracle_render
+
+    scene, cam_id = workloads.path_traced(posts=65, tex=32, resolution=24, spp=2, bounces=0, rr_depth=0, seed=5)
+    f = scene.flatten()
+    cam = scene[cam_id].to_c(scene.origin, 8)
+    lights, nl = scene.c_lights()
+    opts = scene.pathtracer.c_options(scene)
+    osc = oracle.OracleScene.from_flat(f, 8)
+    planes, _ = osc.render(cam, lights, nl, opts)
+    I = planes["total_radiance"].astype(np.float64)
+    g = np.random.default_rng(2).standard_normal(I.shape).astype(np.float32)
+    gt, _ = osc.adjoint(cam, lights, nl, opts, g, tex_shape=f["texture"].shape)
+    osc.close()
+    lhs = float(np.sum(f["texture"].astype(np.float64) * gt))
+    rhs = float(np.sum(g.astype(np.float64) * I))
+    assert abs(lhs - rhs) <= 1e-5 * abs(rhs)
+
+
+def test_oracle_adjoint_heights_translation_invariance():
+    """Moving every vertex up by the same amount does not change face normals, and hit points
+    slide along with the surface: the sum of the normal terms of each triangle vanishes."""
+    scene, cam_id = workloads.path_traced(posts=33, tex=32, resolution=16, spp=1, bounces=0, rr_depth=0, seed=6)
+    scene.meshes[0].albedo_map = None  # uniform albedo: only the normal terms remain
+    f = scene.flatten()
+    cam = scene[cam_id].to_c(scene.origin, 8)
+    lights, nl = scene.c_lights()
+    opts = scene.pathtracer.c_options(scene)
+    osc = oracle.OracleScene.from_flat(f, 8)
+    g = np.ones((8, 16, 16), np.float32)
+    _, gz = osc.adjoint(cam, lights, nl, opts, g, nverts=f["positions"].shape[0])
+    osc.close()
+    assert np.abs(gz).max() > 0
+    assert abs(gz.sum()) <= 1e-9 * np.abs(gz).sum() + 1e-12

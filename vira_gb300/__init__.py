@@ -6,10 +6,10 @@ as hand-written CUDA kernels behind the C ABI of include/vgb.h (libvgb.so).  Thi
 the host side: scene, FP64 poses and ephemeris, rebasing, and the reference-shaped API.
 """
 from . import capi, spectral, synthetic
-from .scene import Camera, Instance, Mesh, PathTracer, PathTracerOptions, RenderPasses, Scene, SphereLight
+from .scene import BatchFrame, Camera, Instance, Mesh, PathTracer, PathTracerOptions, RenderPasses, Scene, SphereLight
 from .spectral import EIGHT_BAND, FOUR_BAND, SpectralBands, black_body_radiance
 
 __all__ = [
-    "capi", "spectral", "synthetic", "Camera", "Instance", "Mesh", "PathTracer", "PathTracerOptions",
+    "capi", "spectral", "synthetic", "BatchFrame", "Camera", "Instance", "Mesh", "PathTracer", "PathTracerOptions",
     "RenderPasses", "Scene", "SphereLight", "SpectralBands", "black_body_radiance", "FOUR_BAND", "EIGHT_BAND",
 ]

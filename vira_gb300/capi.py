@@ -61,6 +61,16 @@ class Film(C.Structure):
     ]
 
 
+class Frame(C.Structure):
+    _fields_ = [("camera", Camera), ("lights", Light * 8), ("nlights", C.c_uint32), ("samples", C.c_uint32),
+                ("frame", C.c_uint32), ("film", Film)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("autotune", C.c_uint32), ("use_graph", C.c_uint32), ("block_threads", C.c_uint32),
+                ("blocks_per_sm", C.c_uint32), ("tiles_per_grab", C.c_uint32)]
+
+
 class BvhOptions(C.Structure):
     _fields_ = [("max_leaf_size", C.c_uint32), ("builder", C.c_uint32), ("threads", C.c_uint32),
                 ("layout", C.c_uint32)]
@@ -98,6 +108,10 @@ SIGNATURES = {
     "vgb_render": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
     "vgb_render_noalloc": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
     "vgb_trace_rays": (C.c_int, [_P, _P, _P, _P, _U32, C.c_int, _P, _P, _P, C.c_int]),
+    "vgb_render_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), C.POINTER(BatchOptions)]),
+    "vgb_batch_tuning": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
+    "vgb_adjoint": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_texture_update": (C.c_int, [_P, _P, _U32, _U32]),
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),

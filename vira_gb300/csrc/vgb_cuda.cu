@@ -88,7 +88,7 @@ struct DevState {
     size_t P;            // plane stride
 };
 
-enum { C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_ERR = 2 + VGB_MAX_LIGHTS, C_COUNT = 3 + VGB_MAX_LIGHTS };
+enum { C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_ERR = 2 + VGB_MAX_LIGHTS, C_BATCH = 3 + VGB_MAX_LIGHTS, C_COUNT = 4 + VGB_MAX_LIGHTS };
 
 struct FrameParams {
     vgb_camera cam;
@@ -227,6 +227,125 @@ __device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float
 #pragma unroll
     for (int k = 0; k < NB; ++k)
         if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
+}
+
+// processIntersection up to the shading point (cpu_path_tracer.ipp:295-346): uv, face and
+// shading normals, tangent frame, albedo (vertex albedo x texture), interpolated position and
+// computeShadingPoint (:494-511).  The normal matrix is the identity in the flattened frame.
+template <int NB>
+__device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool smooth, uint32_t t, float w0f,
+                                           float w1f, F3& Pp, F3& N, F3& fnrm, F3& tg, F3& bt, float* alb,
+                                           float* va_out = nullptr, float* tex_out = nullptr, float* uv_out = nullptr) {
+    float w[3];
+    w[0] = w0f;
+    w[1] = w1f;
+    w[2] = 1.0f - w[0] - w[1];
+    const uint32_t i0 = __ldg(&s.idx[3 * t]), i1 = __ldg(&s.idx[3 * t + 1]), i2 = __ldg(&s.idx[3 * t + 2]);
+    const uint32_t vi[3] = {i1, i2, i0};
+    F3 vp[3], vn[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { vp[k] = ld3(__ldg(&s.vpos[vi[k]])); vn[k] = ld3(__ldg(&s.vnrm[vi[k]])); }
+    const float2 uva = __ldg(&s.vuv[vi[0]]), uvb = __ldg(&s.vuv[vi[1]]), uvc = __ldg(&s.vuv[vi[2]]);
+    const float uvx = (w[0] * uva.x + w[1] * uvb.x) + w[2] * uvc.x;
+    const float uvy = (w[0] * uva.y + w[1] * uvb.y) + w[2] * uvc.y;
+    // Triangle::init face normal from the caller's vertex order (v0, v1, v2) = (vp[2], vp[0], vp[1])
+    F3 fnn = normalize(cross(vp[2] - vp[0], vp[1] - vp[2]));
+    fnrm = F3{-fnn.x, -fnn.y, -fnn.z};
+    F3 Nl = fnrm;
+    if (smooth) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
+    N = Nl;
+    F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
+    tg = normalize(cross(arb, N));
+    bt = cross(N, tg);
+    float texv[NB];
+    sample_uvs<NB>(s, nb, uvx, uvy, texv);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        if (k < (int)nb) {
+            float va;
+            if (s.albedo_uniform) {
+                const float c = s.albedo_value[k];
+                va = (w[0] * c + w[1] * c) + w[2] * c;
+            } else {
+                va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
+                     w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
+            }
+            alb[k] = va * texv[k];
+            if (va_out) va_out[k] = va;
+            if (tex_out) tex_out[k] = texv[k];
+        } else {
+            alb[k] = 0.f;
+        }
+    }
+    if (uv_out) { uv_out[0] = uvx; uv_out[1] = uvy; }
+    Pp = (w[0] * vp[0] + w[1] * vp[1]) + w[2] * vp[2];
+    F3 q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) q[k] = Pp - dot(Pp - vp[k], vn[k]) * vn[k];
+    F3 sp = (q[0] * w[0] + q[1] * w[1]) + q[2] * w[2];
+    if (dot(sp - Pp, Nl) > 0) Pp = sp;
+}
+
+// Direct lighting from one light (cpu_path_tracer.ipp:399-428): samples the light and returns
+// whether a shadow ray is needed, its direction and length, and the contribution per band if
+// the shadow ray is unoccluded.
+template <int NB>
+__device__ __forceinline__ bool nee_light(const vgb_light& L, F3 Pp, F3 N, const float* alb, const float* thr,
+                                          uint32_t nb, bool det, float ru1, float ru2, F3& Ld, float& dist,
+                                          float* con) {
+    float lpdf = 0.f;
+    light_sample(L, Pp, det, ru1, ru2, Ld, dist, lpdf);
+    if (!(lpdf > 0)) return false;
+    const float nl = dot(N, Ld);
+    const float cos_t = smax(0.0f, dot(Ld, N));
+    const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+    const float wgt = power_heuristic(lpdf, mpdf);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+        con[k] = (k < (int)nb) ? thr[k] * bsdf * L.radiance[k] * cos_t * wgt / lpdf : 0.f;
+    }
+    return true;
+}
+
+// BSDF-sampled continuation (cpu_path_tracer.ipp:431-461) with optional Russian roulette.
+// Returns whether the path continues; new_ray is false when the sampled pdf is 0 (the reference
+// then keeps the incoming ray and throughput).
+template <int NB>
+__device__ __forceinline__ bool continue_path(const vgb_light* lights, uint32_t nlights, const vgb_pt_options& opt,
+                                              uint32_t nb, F3 Pp, F3 N, F3 tg, F3 bt, const float* alb, float* thr,
+                                              U4 r0, uint32_t slot, uint32_t sample, uint32_t frame, uint32_t bounce,
+                                              F3& nd, bool& new_ray) {
+    new_ray = false;
+    F3 ls = cosine_sample(u01(r0.z), u01(r0.w));
+    const float mpdf = ls.z * kInvPi;
+    nd = F3{(tg.x * ls.x + bt.x * ls.y) + N.x * ls.z, (tg.y * ls.x + bt.y * ls.y) + N.y * ls.z,
+            (tg.z * ls.x + bt.z * ls.y) + N.z * ls.z};
+    if (!(mpdf > 0)) return true;
+    const float nl = dot(N, nd);
+    const float cos_t = smax(0.0f, dot(nd, N));
+    float lp = 0;
+    for (uint32_t l = 0; l < nlights; ++l) lp += light_pdf(lights[l], Pp, nd);
+    lp /= (float)nlights;
+    const float wgt = power_heuristic(mpdf, lp);
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+        if (k < (int)nb) thr[k] *= bsdf * cos_t * wgt / mpdf;
+    }
+    new_ray = true;
+    if (opt.rr_depth != 0 && bounce + 1 >= opt.rr_depth) {
+        float q = 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) if (k < (int)nb) q = smax(q, thr[k]);
+        q = smin(q, 1.0f);
+        const U4 rr = philox(U4{slot, sample, frame, (bounce << 8) | kSlotRR}, (uint32_t)opt.seed,
+                             (uint32_t)(opt.seed >> 32));
+        if (u01(rr.x) >= q) return false;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) if (k < (int)nb) thr[k] = thr[k] / q;
+    }
+    return true;
 }
 
 // Camera::pixelToRay for the pixel of bounce-0 item `item` (8x4-pixel warp tiles).
@@ -398,51 +517,8 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         if (hit) {
             // ---- processIntersection (cpu_path_tracer.ipp:280-469)
             const uint32_t t = hid;
-            float w[3];
-            w[0] = hr.z;
-            w[1] = hr.w;
-            w[2] = 1.0f - w[0] - w[1];
-            const uint32_t i0 = __ldg(&s.idx[3 * t]), i1 = __ldg(&s.idx[3 * t + 1]), i2 = __ldg(&s.idx[3 * t + 2]);
-            const uint32_t vi[3] = {i1, i2, i0};
-            F3 vp[3], vn[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) { vp[k] = ld3(__ldg(&s.vpos[vi[k]])); vn[k] = ld3(__ldg(&s.vnrm[vi[k]])); }
-            const float2 uva = __ldg(&s.vuv[vi[0]]), uvb = __ldg(&s.vuv[vi[1]]), uvc = __ldg(&s.vuv[vi[2]]);
-            const float uvx = (w[0] * uva.x + w[1] * uvb.x) + w[2] * uvc.x;
-            const float uvy = (w[0] * uva.y + w[1] * uvb.y) + w[2] * uvc.y;
-            // Triangle::init face normal from the caller's vertex order (v0, v1, v2) = (vp[2], vp[0], vp[1])
-            F3 fnn = normalize(cross(vp[2] - vp[0], vp[1] - vp[2]));
-            F3 fnrm{-fnn.x, -fnn.y, -fnn.z};
-            F3 Nl = fnrm;
-            if (fp.opt.smooth_shading) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
-            N = Nl;
-            F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
-            tg = normalize(cross(arb, N));
-            bt = cross(N, tg);
-            float texv[NB];
-            sample_uvs<NB>(s, nb, uvx, uvy, texv);
-#pragma unroll
-            for (int k = 0; k < NB; ++k) {
-                if (k < (int)nb) {
-                    float va;
-                    if (s.albedo_uniform) {
-                        const float c = s.albedo_value[k];
-                        va = (w[0] * c + w[1] * c) + w[2] * c;
-                    } else {
-                        va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
-                             w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
-                    }
-                    alb[k] = va * texv[k];
-                }
-            }
-            Pp = (w[0] * vp[0] + w[1] * vp[1]) + w[2] * vp[2];
-            {
-                F3 q[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) q[k] = Pp - dot(Pp - vp[k], vn[k]) * vn[k];
-                F3 sp = (q[0] * w[0] + q[1] * w[1]) + q[2] * w[2];
-                if (dot(sp - Pp, Nl) > 0) Pp = sp;
-            }
+            F3 fnrm;
+            surface_at<NB>(s, nb, fp.opt.smooth_shading != 0, t, hr.z, hr.w, Pp, N, fnrm, tg, bt, alb);
             if (bounce == 0) {
                 if (st.atri[slot] == VGB_NO_HIT) st.atri[slot] = t;
 #pragma unroll
@@ -473,7 +549,8 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         for (uint32_t l = 0; l < fp.nlights; ++l) {
             bool pred = false;
             F3 Ld{0, 0, 1};
-            float dist = 0.f, lpdf = 0.f, nl = 0.f, cos_t = 0.f, wgt = 0.f;
+            float dist = 0.f;
+            float con[NB];
             if (lit) {
                 float ru1, ru2;
                 if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
@@ -481,14 +558,8 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                     U4 rl = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | (1u + l)}, k0, k1);
                     ru1 = u01(rl.x); ru2 = u01(rl.y);
                 }
-                light_sample(fp.lights[l], Pp, fp.opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
-                if (lpdf > 0) {
-                    pred = true;
-                    nl = dot(N, Ld);
-                    cos_t = smax(0.0f, dot(Ld, N));
-                    const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
-                    wgt = power_heuristic(lpdf, mpdf);
-                }
+                pred = nee_light<NB>(fp.lights[l], Pp, N, alb, thr, nb, fp.opt.deterministic_light != 0, ru1, ru2, Ld,
+                                     dist, con);
             }
             const uint32_t qi = warp_append(&st.counters[C_SQ + l], pred);
             if (pred) {
@@ -497,51 +568,18 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                 st.sq_tmax[l][qi] = dist;
                 st.sq_slot[l][qi] = slot;
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    if (k < (int)nb) {
-                        const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
-                        st.sq_con[l][k * P + qi] = thr[k] * bsdf * fp.lights[l].radiance[k] * cos_t * wgt / lpdf;
-                    }
-                }
+                for (int k = 0; k < NB; ++k)
+                    if (k < (int)nb) st.sq_con[l][k * P + qi] = con[k];
             }
         }
         // ---- BSDF-sampled continuation
         bool new_ray = false;
         if (lit && bounce < fp.opt.bounces) {
-            F3 ls = cosine_sample(u01(r0.z), u01(r0.w));
-            const float mpdf = ls.z * kInvPi;
-            F3 nd{(tg.x * ls.x + bt.x * ls.y) + N.x * ls.z, (tg.y * ls.x + bt.y * ls.y) + N.y * ls.z,
-                  (tg.z * ls.x + bt.z * ls.y) + N.z * ls.z};
-            cont = true;
-            if (mpdf > 0) {
-                const float nl = dot(N, nd);
-                const float cos_t = smax(0.0f, dot(nd, N));
-                float lp = 0;
-                for (uint32_t l = 0; l < fp.nlights; ++l) lp += light_pdf(fp.lights[l], Pp, nd);
-                lp /= (float)fp.nlights;
-                const float wgt = power_heuristic(mpdf, lp);
-#pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
-                    if (k < (int)nb) thr[k] *= bsdf * cos_t * wgt / mpdf;
-                }
-                ro = Pp; rd = nd;
-                new_ray = true;
-                if (fp.opt.rr_depth != 0 && bounce + 1 >= fp.opt.rr_depth) {
-                    float q = 0.f;
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) if (k < (int)nb) q = smax(q, thr[k]);
-                    q = smin(q, 1.0f);
-                    const U4 rr = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | kSlotRR}, k0, k1);
-                    if (u01(rr.x) >= q) {
-                        cont = false;
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) if (k < (int)nb) thr[k] = thr[k] / q;
-                    }
-                }
-            }
-            // mpdf == 0: the reference keeps the incoming ray and throughput
+            F3 nd;
+            cont = continue_path<NB>(fp.lights, fp.nlights, fp.opt, nb, Pp, N, tg, bt, alb, thr, r0, slot, sample,
+                                     fp.opt.frame, bounce, nd, new_ray);
+            if (new_ray) { ro = Pp; rd = nd; }
+            // pdf 0: the reference keeps the incoming ray and throughput
         }
         // ---- write path state and append live paths
         if (active) {
@@ -597,9 +635,10 @@ __global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene 
 // ------------------------------------------------------------------ k_end_sample
 template <int NB>
 __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_constant__ FrameParams fp, uint32_t last, FilmOut f) {
-    const size_t P = st.P;
+    const size_t P = st.P;                       // plane stride of the scratch state
     const uint32_t nb = fp.nb;
     const uint32_t npix = fp.cam.width * fp.cam.height;
+    const size_t FP = npix;                      // plane stride of the caller's film
     const float sf = (float)fp.opt.samples;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint32_t pend = st.pend[p];
@@ -626,16 +665,16 @@ __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_co
             if (k < (int)nb) {
                 const float total = tot[k] / sf;
                 const float direct = st.adir[k * P + p] / sf;
-                if (f.total) f.total[k * P + p] = total;
-                if (f.direct) f.direct[k * P + p] = direct;
-                if (f.indirect) f.indirect[k * P + p] = total - direct;
-                if (f.albedo) f.albedo[k * P + p] = st.aalb[k * P + p] / sf;
-                if (f.power) f.power[k * P + p] = (fp.cam.power_scale[k] * f.omega[p]) * total;
+                if (f.total) f.total[k * FP + p] = total;
+                if (f.direct) f.direct[k * FP + p] = direct;
+                if (f.indirect) f.indirect[k * FP + p] = total - direct;
+                if (f.albedo) f.albedo[k * FP + p] = st.aalb[k * P + p] / sf;
+                if (f.power) f.power[k * FP + p] = (fp.cam.power_scale[k] * f.omega[p]) * total;
             }
         }
         if (f.normal) {
             F3 n = normalize(F3{st.anrm[p], st.anrm[P + p], st.anrm[2 * P + p]});
-            f.normal[p] = n.x; f.normal[P + p] = n.y; f.normal[2 * P + p] = n.z;
+            f.normal[p] = n.x; f.normal[FP + p] = n.y; f.normal[2 * FP + p] = n.z;
         }
         if (f.depth) f.depth[p] = (count == 0) ? __int_as_float(0x7f800000) : st.adep[p] / (float)count;
         if (f.alpha) f.alpha[p] = (float)count / sf;
@@ -761,6 +800,14 @@ struct vgb_context {
     std::vector<cudaEvent_t> prof_events;   // pairs around each launch
     std::vector<int> prof_family;           // 0 closest-hit trace, 1 shadow, 2 film, 3 shade
     size_t prof_used = 0;
+    // batched rendering
+    void* d_frames = nullptr;                // DevFrame table
+    size_t cap_frames = 0;
+    void* h_frames = nullptr;                // pinned staging of the table
+    uint32_t tuned_threads = 0, tuned_bps = 0, tuned_grab = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_key = 0;
+    unsigned char graph_params_probe[1024] = {0};   // kernel parameters the graph was captured with
 };
 
 namespace {
@@ -988,6 +1035,9 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     free_scene(ctx); free_bvh(ctx); free_scratch(ctx); free_staging(ctx);
     dfree(ctx->d_counters); dfree(ctx->d_stats);
     for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    dfree(ctx->d_frames);
+    if (ctx->h_frames) cudaFreeHost(ctx->h_frames);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1515,5 +1565,738 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
         return fail(ctx, VGB_ERR_DEVICE_LIMIT,
                     std::string("render_noalloc: device traversal limit hit:") + ((err_word & kErrStack) ? " stack" : "") +
                         ((err_word & kErrIter) ? " iterations" : ""));
+    return VGB_OK;
+}
+
+
+// ====================================================================== batched trajectory
+namespace {
+
+struct DevFrame {
+    vgb_camera cam;
+    vgb_light lights[VGB_MAX_LIGHTS];
+    uint32_t nlights, samples, frame, tiles_x, tile_begin, pad[3];
+    FilmOut film;
+};
+
+struct BatchParams {
+    vgb_pt_options opt;
+    uint32_t nframes, nb, total_tiles, grab, tile_stride;
+};
+
+__device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ frames, uint32_t n, uint32_t t) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (frames[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One persistent launch over every (frame, tile) item.  A warp owns a tile and loops over its
+// samples and bounces; accumulation order and random streams are those of the wavefront path.
+template <int NB, int L>
+__global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, const __grid_constant__ BatchParams bp,
+                        uint32_t* counter, uint32_t* errw, uint64_t* stats) {
+    extern __shared__ float sm_acc[];
+    constexpr int PL = 5 * NB + 4;  // arad[NB] adir[NB] aalb[NB] anrm[3] adep | prad[NB] brad[NB]
+    const int lane = threadIdx.x & 31;
+    float* acc = sm_acc + (size_t)(threadIdx.x >> 5) * PL * 32;
+#define ACC(pl) acc[(pl) * 32 + lane]
+    const uint32_t nb = bp.nb;
+    const vgb_pt_options& opt = bp.opt;
+    const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
+    const uint32_t n_items = (bp.total_tiles + bp.tile_stride - 1) / bp.tile_stride;
+    uint32_t err = 0, nclosest = 0, nshadow = 0;
+    Counters cnt{0, 0};
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, bp.grab);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_items) break;
+        const uint32_t end = min(base + bp.grab, n_items);
+        for (uint32_t it = base; it < end; ++it) {
+            const uint32_t t = it * bp.tile_stride;
+            const DevFrame& F = frames[find_frame(frames, bp.nframes, t)];
+            const uint32_t tile = t - F.tile_begin;
+            const uint32_t tx = tile % F.tiles_x, ty = tile / F.tiles_x;
+            const uint32_t pi = tx * 8u + (lane & 7u), pj = ty * 4u + (lane >> 3);
+            const uint32_t W = F.cam.width, H = F.cam.height;
+            if (pi >= W || pj >= H) continue;
+            const uint32_t slot = pj * W + pi;
+#pragma unroll
+            for (int p = 0; p < PL; ++p) acc[p * 32 + lane] = 0.f;
+            uint32_t first_tri = VGB_NO_HIT;
+            uint32_t count = 0;
+            for (uint32_t sample = 0; sample < F.samples; ++sample) {
+                // camera ray (camera_ray with this frame's camera and key)
+                float X = (float)pi, Y = (float)pj;
+                if (sample != 0) {
+                    U4 jr = philox(U4{slot, sample, F.frame, kSlotJitter}, k0, k1);
+                    X = X + u01(jr.x);
+                    Y = Y + u01(jr.y);
+                }
+                const float* K = F.cam.kinv;
+                const float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
+                const float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
+                const F3 dc{hx, F.cam.z_dir * hy, F.cam.z_dir};
+                const float* R = F.cam.rotation;
+                const F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
+                            (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
+                F3 rd = normalize(dw);
+                F3 ro{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
+                float thr[NB], alb[NB];
+#define PRAD(k) acc[(3 * NB + 4 + (k)) * 32 + lane]
+#define BRAD(k) acc[(4 * NB + 4 + (k)) * 32 + lane]
+#pragma unroll
+                for (int k = 0; k < NB; ++k) { thr[k] = 1.f; PRAD(k) = 0.f; BRAD(k) = 0.f; }
+                uint32_t pend = 0;
+                for (uint32_t bounce = 0; bounce <= opt.bounces; ++bounce) {
+                    if (pend) {
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) {
+                            PRAD(k) += BRAD(k);
+                            if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                        }
+                        pend = 0;
+                    }
+                    HitOut h;
+                    h.U = h.V = h.W = 0.f; h.det = 1.f;
+                    const WRay wr = make_wray(ro, rd);
+                    traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+                    nclosest++;
+                    if (h.id == VGB_NO_HIT) {
+                        if (opt.simulate_lighting && opt.show_background) {
+                            float x = rd.x, y = rd.y, z = rd.z;
+                            float u = atan2f(y, x) / (2 * kPi);
+                            float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+                            float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+                            if (px < 0) px += 1.f;
+                            if (py < 0) py += 1.f;
+                            float ddx = px - 0.f, ddy = py - 0.f;
+                            float a = (1.f - ddx) * (1.f - ddy), b = ddx * (1.f - ddy), c = (1.f - ddx) * ddy, e = ddx * ddy;
+#pragma unroll
+                            for (int k = 0; k < NB; ++k) {
+                                const float bgv = opt.background[k];
+                                float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
+                                PRAD(k) = PRAD(k) + thr[k] * (bg * 1.f);
+                            }
+                        }
+                        break;
+                    }
+                    const float rcp = 1.0f / h.det;
+                    const float w0 = h.V * rcp, w1 = h.W * rcp;
+                    F3 Pp, N, fnrm, tg, bt;
+                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
+                    if (bounce == 0) {
+                        if (first_tri == VGB_NO_HIT) first_tri = h.id;
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
+                        ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
+                        ACC(3 * NB + 3) += h.t;
+                        count += 1u;
+                    }
+                    if (!opt.simulate_lighting) break;
+                    Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                    for (int k = 0; k < NB; ++k)
+                        BRAD(k) = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * alb[k]) : 0.f;
+                    pend = (bounce == 0) ? 1u : 2u;
+                    const U4 r0 = philox(U4{slot, sample, F.frame, (bounce << 8) | kSlotMain}, k0, k1);
+                    for (uint32_t l = 0; l < F.nlights; ++l) {
+                        float ru1, ru2;
+                        if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                        else {
+                            U4 rl = philox(U4{slot, sample, F.frame, (bounce << 8) | (1u + l)}, k0, k1);
+                            ru1 = u01(rl.x); ru2 = u01(rl.y);
+                        }
+                        // nee_light, with the contribution formed only once the shadow ray is clear
+                        F3 Ld; float dist, lpdf = 0.f;
+                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                        if (lpdf > 0) {
+                            HitOut hs;
+                            const WRay ws = make_wray(Pp, Ld);
+                            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+                            nshadow++;
+                            if (hs.id == VGB_NO_HIT) {
+                                const float nl = dot(N, Ld);
+                                const float cos_t = smax(0.0f, dot(Ld, N));
+                                const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                                const float wgt = power_heuristic(lpdf, mpdf);
+#pragma unroll
+                                for (int k = 0; k < NB; ++k) {
+                                    const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+                                    const float con = (k < (int)nb) ? thr[k] * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                                    BRAD(k) += con;
+                                }
+                            }
+                        }
+                    }
+                    if (bounce >= opt.bounces) break;
+                    bool new_ray = false;
+                    F3 nd;
+                    const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0, slot,
+                                                        sample, F.frame, bounce, nd, new_ray);
+                    if (!cont) break;
+                    if (new_ray) { ro = Pp; rd = nd; }
+                }
+                if (pend) {
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) {
+                        PRAD(k) += BRAD(k);
+                        if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
+#undef PRAD
+#undef BRAD
+            }
+            // RenderPasses::updateImages for this pixel
+            const size_t P = (size_t)W * H;
+            const float sf = (float)F.samples;
+            const FilmOut& f = F.film;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k < (int)nb) {
+                    const float total = ACC(k) / sf;
+                    const float direct = ACC(NB + k) / sf;
+                    if (f.total) f.total[k * P + slot] = total;
+                    if (f.direct) f.direct[k * P + slot] = direct;
+                    if (f.indirect) f.indirect[k * P + slot] = total - direct;
+                    if (f.albedo) f.albedo[k * P + slot] = ACC(2 * NB + k) / sf;
+                    if (f.power) f.power[k * P + slot] = (F.cam.power_scale[k] * f.omega[slot]) * total;
+                }
+            }
+            if (f.normal) {
+                F3 n = normalize(F3{ACC(3 * NB + 0), ACC(3 * NB + 1), ACC(3 * NB + 2)});
+                f.normal[slot] = n.x; f.normal[P + slot] = n.y; f.normal[2 * P + slot] = n.z;
+            }
+            if (f.depth) f.depth[slot] = (count == 0) ? __int_as_float(0x7f800000) : ACC(3 * NB + 3) / (float)count;
+            if (f.alpha) f.alpha[slot] = (float)count / sf;
+            if (f.tri) f.tri[slot] = first_tri;
+        }
+    }
+#undef ACC
+    if (err) atomicOr(errw, err);
+    warp_reduce_add(&stats[2], nclosest);
+    warp_reduce_add(&stats[3], nshadow);
+}
+
+template <int NB, int L>
+cudaError_t launch_batch(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
+                         uint32_t bps) {
+    const size_t smem = (size_t)(threads / 32) * (5 * NB + 4) * 32 * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_batch<NB, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_batch<NB, L>, (int)threads, smem);
+    const uint32_t b = std::max<uint32_t>(1, std::min<uint32_t>(bps, (uint32_t)std::max(1, maxb)));
+    cudaMemsetAsync(&ctx->d_counters[C_ERR + 1], 0, sizeof(uint32_t), ctx->stream);
+    k_batch<NB, L><<<b * ctx->num_sms, threads, smem, ctx->stream>>>(dev_scene(ctx), d_frames, bp, &ctx->d_counters[C_ERR + 1],
+                                                                      &ctx->d_counters[C_ERR], ctx->d_stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_any(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
+                             uint32_t bps) {
+    if (ctx->bvh_layout == 8) {
+        if (bp.nb <= 1) return launch_batch<1, 8>(ctx, d_frames, bp, threads, bps);
+        if (bp.nb <= 4) return launch_batch<4, 8>(ctx, d_frames, bp, threads, bps);
+        return launch_batch<8, 8>(ctx, d_frames, bp, threads, bps);
+    }
+    if (bp.nb <= 1) return launch_batch<1, 2>(ctx, d_frames, bp, threads, bps);
+    if (bp.nb <= 4) return launch_batch<4, 2>(ctx, d_frames, bp, threads, bps);
+    return launch_batch<8, 2>(ctx, d_frames, bp, threads, bps);
+}
+
+}  // namespace
+
+extern "C" VGB_API vgb_status vgb_batch_tuning(vgb_context* ctx, uint32_t* threads, uint32_t* bps, uint32_t* grab) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (threads) *threads = ctx->tuned_threads;
+    if (bps) *bps = ctx->tuned_bps;
+    if (grab) *grab = ctx->tuned_grab;
+    return VGB_OK;
+}
+
+extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame* frames, uint32_t nframes,
+                                               const vgb_pt_options* opts, const vgb_batch_options* bo) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!frames || nframes == 0 || !opts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: no frames or options");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_batch: build the BVH first");
+    if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: nbands differs from the scene");
+    // schedule: frames by decreasing samples per pixel (cost per tile), then by index
+    std::vector<uint32_t> order(nframes);
+    for (uint32_t f = 0; f < nframes; ++f) {
+        const vgb_frame& fr = frames[f];
+        if (fr.samples == 0 || fr.camera.width == 0 || fr.camera.height == 0 || fr.nlights > VGB_MAX_LIGHTS ||
+            !fr.film.on_device || (fr.film.received_power && !fr.film.pixel_solid_angle))
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: frame " + std::to_string(f) +
+                                                           ": samples/resolution/lights/film invalid (film must be device memory)");
+        order[f] = f;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return frames[a].samples > frames[b].samples; });
+    cudaSetDevice(ctx->device);
+    if (nframes > ctx->cap_frames) {
+        dfree(ctx->d_frames);
+        if (ctx->h_frames) cudaFreeHost(ctx->h_frames);
+        ctx->d_frames = nullptr; ctx->h_frames = nullptr; ctx->cap_frames = 0;
+        vgb_status s = dalloc(ctx, &ctx->d_frames, sizeof(DevFrame) * nframes);
+        if (s != VGB_OK) return s;
+        CK(cudaMallocHost(&ctx->h_frames, sizeof(DevFrame) * nframes));
+        ctx->cap_frames = nframes;
+        if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));  // the pinned table may still feed a previous copy
+    DevFrame* hf = static_cast<DevFrame*>(ctx->h_frames);
+    uint64_t total_tiles = 0;
+    for (uint32_t i = 0; i < nframes; ++i) {
+        const vgb_frame& fr = frames[order[i]];
+        DevFrame& d = hf[i];
+        std::memset(&d, 0, sizeof(d));
+        d.cam = fr.camera;
+        for (uint32_t l = 0; l < fr.nlights; ++l) d.lights[l] = fr.lights[l];
+        d.nlights = fr.nlights;
+        d.samples = fr.samples;
+        d.frame = fr.frame;
+        d.tiles_x = (fr.camera.width + 7) / 8;
+        d.tile_begin = (uint32_t)total_tiles;
+        total_tiles += (uint64_t)d.tiles_x * ((fr.camera.height + 3) / 4);
+        d.film.total = fr.film.total_radiance; d.film.direct = fr.film.direct_radiance;
+        d.film.indirect = fr.film.indirect_radiance; d.film.power = fr.film.received_power;
+        d.film.albedo = fr.film.albedo; d.film.normal = fr.film.normal_global; d.film.depth = fr.film.depth;
+        d.film.alpha = fr.film.alpha; d.film.tri = fr.film.triangle_id; d.film.omega = fr.film.pixel_solid_angle;
+    }
+    if (total_tiles >= (1ull << 31)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: too many pixels");
+    CK(cudaMemcpyAsync(ctx->d_frames, hf, sizeof(DevFrame) * nframes, cudaMemcpyHostToDevice, ctx->stream));
+    BatchParams bp;
+    std::memset(&bp, 0, sizeof(bp));
+    bp.opt = *opts;
+    bp.nframes = nframes;
+    bp.nb = ctx->nbands;
+    bp.total_tiles = (uint32_t)total_tiles;
+    const DevFrame* dfr = static_cast<const DevFrame*>(ctx->d_frames);
+    uint32_t threads = bo && bo->block_threads ? bo->block_threads : (ctx->tuned_threads ? ctx->tuned_threads : 128);
+    uint32_t bps = bo && bo->blocks_per_sm ? bo->blocks_per_sm : (ctx->tuned_bps ? ctx->tuned_bps : 4);
+    uint32_t grab = bo && bo->tiles_per_grab ? bo->tiles_per_grab : (ctx->tuned_grab ? ctx->tuned_grab : 1);
+    if (threads != 64 && threads != 128 && threads != 256)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: block_threads must be 64, 128 or 256");
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+    if (bo && bo->autotune) {
+        // autotuner: time candidate launch shapes on every 16th tile, keep the fastest
+        const uint32_t cand_t[] = {64, 128, 256};
+        const uint32_t cand_b[] = {2, 4, 8, 16};
+        const uint32_t cand_g[] = {1, 4};
+        float best = INFINITY;
+        BatchParams probe = bp;
+        probe.tile_stride = 16;
+        for (uint32_t ct : cand_t)
+            for (uint32_t cb : cand_b)
+                for (uint32_t cg : cand_g) {
+                    probe.grab = cg;
+                    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+                    CK(launch_batch_any(ctx, dfr, probe, ct, cb));
+                    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+                    CK(cudaEventSynchronize(ctx->ev1));
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+                    if (ms < best) { best = ms; threads = ct; bps = cb; grab = cg; }
+                }
+        ctx->tuned_threads = threads; ctx->tuned_bps = bps; ctx->tuned_grab = grab;
+        CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+        vgb_status es = check_device_error(ctx);
+        if (es != VGB_OK) return es;
+    }
+    bp.grab = grab;
+    bp.tile_stride = 1;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (bo && bo->use_graph) {
+        const uint64_t key = ((uint64_t)nframes << 40) ^ ((uint64_t)total_tiles << 8) ^ ((uint64_t)threads << 4) ^ bps ^
+                             ((uint64_t)grab << 56) ^ ((uint64_t)ctx->nbands << 60) ^ ((uint64_t)ctx->bvh_layout << 20) ^
+                             ((uint64_t)opts->bounces << 24) ^ ((uint64_t)opts->samples << 28);
+        static_assert(sizeof(BatchParams) < 4096, "kernel parameters");
+        // the graph holds the launch with these parameters; rebuild it when they change
+        if (!ctx->graph_exec || ctx->graph_key != key ||
+            std::memcmp(&ctx->graph_params_probe, &bp, sizeof(bp)) != 0) {
+            if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t le = launch_batch_any(ctx, dfr, bp, threads, bps);
+            cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+            CK(le);
+            CK(ce);
+            cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            CK(ie);
+            ctx->graph_key = key;
+            std::memcpy(&ctx->graph_params_probe, &bp, sizeof(bp));
+        }
+        CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    } else {
+        CK(launch_batch_any(ctx, dfr, bp, threads, bps));
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    uint64_t hs[8];
+    CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    ctx->stats.rays_closest = hs[2];
+    ctx->stats.rays_shadow = hs[3];
+    ctx->stats.kernel_launches = 1;
+    ctx->stats.ms_last = ms;
+    return check_device_error(ctx);
+}
+
+
+// ====================================================================== adjoint (path replay)
+// Gradients of the loss L(I) with respect to the albedo texels and the vertex heights (z),
+// given dL/dI for the total-radiance planes of a frame.  Each pixel sample's path is replayed
+// from its random stream (nothing is stored between the forward render and this pass), its
+// vertices are kept in registers/local memory for the length of the path, and the gradients
+// are scattered with atomics:
+//   albedo   every contribution at or after vertex b is linear in alb_b, so
+//            dI/d alb_b = (suffix radiance from b) / alb_b, then through alb = va * bilinear(tex)
+//   heights  the shading normal (flat shading: the hit triangle's face normal) in every NEE term,
+//            d C / d(N.L) = C (2 / (N.L) + w'/w), and the motion of the hit point on the triangle
+//            (barycentrics, hence uv and the interpolated albedo) for a fixed ray,
+//            d[t, b1, b2]/dz_i = b_i * M^-1 e_z with M = [d | A-B | A-C].
+// Excluded and stated: visibility (shadow and silhouette edges), the rotation of the sampled
+// continuation direction with the normal, the motion of the shading point (light direction and
+// shadow-ray origin), and Russian roulette decisions.
+namespace {
+
+constexpr int kAdjMaxVerts = 4;
+
+template <int NB>
+struct AdjVtx {
+    uint32_t tri;
+    float w0, w1;
+    float m1, m2;       // M^-1 e_z, barycentric components
+    float uvx, uvy;
+    float gnx, gny, gnz;  // dL/dN at this vertex (already weighted by dL/dI)
+    float alb[NB], va[NB], tex[NB], rad[NB];
+};
+
+template <int NB, int L>
+__global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const __grid_constant__ FrameParams fp,
+                                                 const float* __restrict__ dldi, float* __restrict__ gtex,
+                                                 float* __restrict__ gz, uint32_t* errw, uint64_t* stats) {
+    const uint32_t nb = fp.nb;
+    const vgb_pt_options& opt = fp.opt;
+    const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
+    const uint32_t npix = fp.cam.width * fp.cam.height;
+    const uint32_t n_items = fp.tiles_x * fp.tiles_y * 32u;
+    const float sf = (float)opt.samples;
+    uint32_t err = 0, nrays = 0;
+    Counters cnt{0, 0};
+    for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n_items; item += gridDim.x * blockDim.x) {
+        uint32_t slot;
+        F3 ro0, rd0;
+        if (!camera_ray(fp, item, 0, slot, ro0, rd0)) continue;
+        float g[NB];
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            g[k] = (k < (int)nb) ? dldi[(size_t)k * npix + slot] / sf : 0.f;
+            any |= g[k] != 0.f;
+        }
+        if (!any) continue;
+        for (uint32_t sample = 0; sample < opt.samples; ++sample) {
+            F3 ro, rd;
+            camera_ray(fp, item, sample, slot, ro, rd);
+            AdjVtx<NB> vx[kAdjMaxVerts];
+            float thr[NB], bgc[NB];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) { thr[k] = 1.f; bgc[k] = 0.f; }
+            int nv = 0;
+            for (uint32_t bounce = 0; bounce <= opt.bounces && nv < kAdjMaxVerts; ++bounce) {
+                HitOut h;
+                h.U = h.V = h.W = 0.f; h.det = 1.f;
+                const WRay wr = make_wray(ro, rd);
+                traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+                nrays++;
+                if (h.id == VGB_NO_HIT) {
+                    if (opt.simulate_lighting && opt.show_background) {
+                        float x = rd.x, y = rd.y, z = rd.z;
+                        float u = atan2f(y, x) / (2 * kPi);
+                        float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+                        float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+                        if (px < 0) px += 1.f;
+                        if (py < 0) py += 1.f;
+                        float a = (1.f - px) * (1.f - py), b = px * (1.f - py), c = (1.f - px) * py, e = px * py;
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) {
+                            const float bgv = opt.background[k];
+                            bgc[k] = thr[k] * ((((a * bgv + b * bgv) + c * bgv) + e * bgv) * 1.f);
+                        }
+                    }
+                    break;
+                }
+                AdjVtx<NB>& V = vx[nv++];
+                const float rcp = 1.0f / h.det;
+                V.tri = h.id;
+                V.w0 = h.V * rcp;
+                V.w1 = h.W * rcp;
+                F3 Pp, N, fnrm, tg, bt;
+                float uv[2];
+                surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, V.w0, V.w1, Pp, N, fnrm, tg, bt, V.alb, V.va, V.tex, uv);
+                V.uvx = uv[0]; V.uvy = uv[1];
+                // M^-1 e_z for the hit-point motion (caller order A=v0, B=v1, C=v2)
+                {
+                    const uint32_t ia = __ldg(&s.idx[3 * h.id]), ib = __ldg(&s.idx[3 * h.id + 1]), ic = __ldg(&s.idx[3 * h.id + 2]);
+                    const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
+                    const F3 c1 = A - B, c2 = A - C;
+                    const float det = dot(rd, cross(c1, c2));
+                    // Cramer: x1 = det[d, e_z, c2] / det, x2 = det[d, c1, e_z] / det
+                    const F3 ez{0.f, 0.f, 1.f};
+                    V.m1 = (det != 0.f) ? dot(rd, cross(ez, c2)) / det : 0.f;
+                    V.m2 = (det != 0.f) ? dot(rd, cross(c1, ez)) / det : 0.f;
+                }
+                V.gnx = V.gny = V.gnz = 0.f;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) V.rad[k] = 0.f;
+                if (!opt.simulate_lighting) break;
+                Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                for (int k = 0; k < NB; ++k)
+                    V.rad[k] = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * V.alb[k]) : 0.f;
+                const U4 r0 = philox(U4{slot, sample, opt.frame, (bounce << 8) | kSlotMain}, k0, k1);
+                for (uint32_t l = 0; l < fp.nlights; ++l) {
+                    float ru1, ru2;
+                    if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                    else {
+                        U4 rl = philox(U4{slot, sample, opt.frame, (bounce << 8) | (1u + l)}, k0, k1);
+                        ru1 = u01(rl.x); ru2 = u01(rl.y);
+                    }
+                    F3 Ld; float dist, lpdf = 0.f;
+                    light_sample(fp.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                    if (!(lpdf > 0)) continue;
+                    HitOut hs;
+                    const WRay ws = make_wray(Pp, Ld);
+                    traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+                    nrays++;
+                    if (hs.id != VGB_NO_HIT) continue;
+                    const float nl = dot(N, Ld);
+                    const float cos_t = smax(0.0f, dot(Ld, N));
+                    const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                    const float wgt = power_heuristic(lpdf, mpdf);
+                    float gc = 0.f;
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) {
+                        const float bsdf = V.alb[k] * kInvPi * smax(nl, 0.f);
+                        const float con = (k < (int)nb) ? thr[k] * bsdf * fp.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                        V.rad[k] += con;
+                        gc += g[k] * con;
+                    }
+                    if (nl > 0.f && wgt > 0.f) {
+                        // d/dc of c^2 w(c) with w = lp^2 / (lp^2 + (c/pi)^2)
+                        const float m = nl * kInvPi;
+                        const float dw_over_w = -2.f * m * kInvPi / (lpdf * lpdf + m * m);
+                        const float s_c = gc * (2.f / nl + dw_over_w);
+                        V.gnx += s_c * Ld.x; V.gny += s_c * Ld.y; V.gnz += s_c * Ld.z;
+                    }
+                }
+                if (bounce >= opt.bounces) break;
+                bool new_ray = false;
+                F3 nd;
+                const bool cont = continue_path<NB>(fp.lights, fp.nlights, opt, nb, Pp, N, tg, bt, V.alb, thr, r0, slot,
+                                                    sample, opt.frame, bounce, nd, new_ray);
+                if (!cont) break;
+                if (new_ray) { ro = Pp; rd = nd; }
+                (void)fnrm;
+            }
+            // backward over the recorded vertices: suffix radiance, then scatter
+            float S[NB];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) S[k] = bgc[k];
+            for (int b = nv - 1; b >= 0; --b) {
+                AdjVtx<NB>& V = vx[b];
+                float ga[NB];
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    S[k] += V.rad[k];
+                    ga[k] = (k < (int)nb && V.alb[k] != 0.f) ? g[k] * S[k] / V.alb[k] : 0.f;
+                }
+                // texel weights of sample_uvs at (uvx, uvy)
+                const float rx = (float)s.tw, ry = (float)s.th;
+                float px = fmodf(V.uvx * rx, rx), py = fmodf(V.uvy * ry, ry);
+                if (px < 0) px += rx;
+                if (py < 0) py += ry;
+                int x0 = min((int)floorf(px), (int)s.tw - 1), y0 = min((int)floorf(py), (int)s.th - 1);
+                int x1 = min(x0 + 1, (int)s.tw - 1), y1 = min(y0 + 1, (int)s.th - 1);
+                const float dx = px - (float)x0, dy = py - (float)y0;
+                const float wt[4] = {(1.f - dx) * (1.f - dy), dx * (1.f - dy), (1.f - dx) * dy, dx * dy};
+                const size_t tx[4] = {(size_t)y0 * s.tw + x0, (size_t)y0 * s.tw + x1, (size_t)y1 * s.tw + x0,
+                                      (size_t)y1 * s.tw + x1};
+                if (gtex) {
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) {
+                        if (k >= (int)nb || ga[k] == 0.f) continue;
+                        const float base = ga[k] * V.va[k];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (wt[q] != 0.f) atomicAdd(&gtex[tx[q] * nb + k], base * wt[q]);
+                    }
+                }
+                if (gz) {
+                    const uint32_t ia = __ldg(&s.idx[3 * V.tri]), ib = __ldg(&s.idx[3 * V.tri + 1]), ic = __ldg(&s.idx[3 * V.tri + 2]);
+                    const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
+                    // face normal N = -n/|n|, n = cross(A-B, C-A)
+                    const F3 a = A - B, bb = C - A;
+                    const F3 n = cross(a, bb);
+                    const float ln = length(n);
+                    const F3 nh = n * (1.f / ln);
+                    const F3 dn[3] = {F3{-bb.y - a.y, bb.x + a.x, 0.f}, F3{bb.y, -bb.x, 0.f}, F3{a.y, -a.x, 0.f}};
+                    const F3 gN{V.gnx, V.gny, V.gnz};
+                    // hit-point motion: d(albedo)/d(barycentrics)
+                    const float2 uvA = __ldg(&s.vuv[ia]), uvB = __ldg(&s.vuv[ib]), uvC = __ldg(&s.vuv[ic]);
+                    float dalb_dw0 = 0.f, dalb_dw1 = 0.f;  // sum_k ga[k] * d alb_k / d w0, / d w1
+                    {
+                        // texture derivative with respect to (px, py)
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) {
+                            if (k >= (int)nb || ga[k] == 0.f) continue;
+                            float t00, t10, t01, t11;
+                            if (s.tex_mono) {
+                                t00 = __ldg(&s.tex[tx[0]]); t10 = __ldg(&s.tex[tx[1]]);
+                                t01 = __ldg(&s.tex[tx[2]]); t11 = __ldg(&s.tex[tx[3]]);
+                            } else {
+                                t00 = __ldg(&s.tex[tx[0] * nb + k]); t10 = __ldg(&s.tex[tx[1] * nb + k]);
+                                t01 = __ldg(&s.tex[tx[2] * nb + k]); t11 = __ldg(&s.tex[tx[3] * nb + k]);
+                            }
+                            const float dtdx = (1.f - dy) * (t10 - t00) + dy * (t11 - t01);
+                            const float dtdy = (1.f - dx) * (t01 - t00) + dx * (t11 - t10);
+                            // d px / d w0 = rx * (uvB - uvA).x, ... (Interaction order: w0 ~ B, w1 ~ C)
+                            const float dt_dw0 = dtdx * rx * (uvB.x - uvA.x) + dtdy * ry * (uvB.y - uvA.y);
+                            const float dt_dw1 = dtdx * rx * (uvC.x - uvA.x) + dtdy * ry * (uvC.y - uvA.y);
+                            float dva_dw0 = 0.f, dva_dw1 = 0.f;
+                            if (!s.albedo_uniform) {
+                                const float aA = __ldg(&s.valb[(size_t)ia * nb + k]), aB = __ldg(&s.valb[(size_t)ib * nb + k]);
+                                const float aC = __ldg(&s.valb[(size_t)ic * nb + k]);
+                                dva_dw0 = aB - aA; dva_dw1 = aC - aA;
+                            }
+                            dalb_dw0 += ga[k] * (dva_dw0 * V.tex[k] + V.va[k] * dt_dw0);
+                            dalb_dw1 += ga[k] * (dva_dw1 * V.tex[k] + V.va[k] * dt_dw1);
+                        }
+                    }
+                    const float wv[3] = {1.0f - V.w0 - V.w1, V.w0, V.w1};  // weights of A, B, C
+                    const uint32_t vid[3] = {ia, ib, ic};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        // normal term: dN = -(dn - nh (nh . dn)) / |n|
+                        const float nd = dot(nh, dn[q]);
+                        const F3 dN = (dn[q] - nh * nd) * (-1.f / ln);
+                        float gq = dot(gN, dN);
+                        // motion term
+                        gq += (dalb_dw0 * V.m1 + dalb_dw1 * V.m2) * wv[q];
+                        if (gq != 0.f) atomicAdd(&gz[vid[q]], gq);
+                    }
+                }
+            }
+        }
+    }
+    if (err) atomicOr(errw, err);
+    warp_reduce_add(&stats[2], nrays);
+}
+
+template <int NB, int L>
+void launch_adjoint(vgb_context* ctx, const FrameParams& fp, const float* dldi, float* gtex, float* gz) {
+    const uint32_t n = fp.tiles_x * fp.tiles_y * 32u;
+    const int g = grid_for(ctx, n, 16);
+    k_adjoint<NB, L><<<g, 128, 0, ctx->stream>>>(dev_scene(ctx), fp, dldi, gtex, gz, &ctx->d_counters[C_ERR], ctx->d_stats);
+}
+
+}  // namespace
+
+extern "C" VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                          uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
+                                          float* d_texture, float* d_height, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!cam || !opts || !dL_dradiance) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: null camera/options/gradient");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "adjoint: build the BVH first");
+    if (opts->samples == 0 || opts->nbands != ctx->nbands || nlights > VGB_MAX_LIGHTS || (nlights && !lights))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: samples, nbands or lights invalid");
+    if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: at most 3 bounces");
+    if (d_height && opts->smooth_shading)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: height gradients need flat shading (face normals)");
+    cudaSetDevice(ctx->device);
+    FrameParams fp;
+    std::memset(&fp, 0, sizeof(fp));
+    fp.cam = *cam;
+    fp.opt = *opts;
+    for (uint32_t l = 0; l < nlights; ++l) fp.lights[l] = lights[l];
+    fp.nlights = nlights;
+    fp.nb = ctx->nbands;
+    fp.tiles_x = (cam->width + 7) / 8;
+    fp.tiles_y = (cam->height + 3) / 4;
+    const size_t npix = (size_t)cam->width * cam->height;
+    const size_t ntex = (size_t)ctx->tw * ctx->th * ctx->nbands;
+    const float* dl = dL_dradiance;
+    float *gt = d_texture, *gh = d_height;
+    vgb_status s;
+    if (!on_device) {
+        const size_t need = npix * ctx->nbands + (d_texture ? ntex : 0) + (d_height ? ctx->nverts : 0);
+        if ((s = ensure_staging(ctx, need * sizeof(float))) != VGB_OK) return s;
+        float* cur = (float*)ctx->staging_base;
+        CK(cudaMemcpyAsync(cur, dL_dradiance, npix * ctx->nbands * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        dl = cur; cur += npix * ctx->nbands;
+        if (d_texture) { gt = cur; CK(cudaMemcpyAsync(gt, d_texture, ntex * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); cur += ntex; }
+        if (d_height) { gh = cur; CK(cudaMemcpyAsync(gh, d_height, ctx->nverts * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); }
+    }
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const bool l8 = ctx->bvh_layout == 8;
+    if (ctx->nbands <= 1) { if (l8) launch_adjoint<1, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<1, 2>(ctx, fp, dl, gt, gh); }
+    else if (ctx->nbands <= 4) { if (l8) launch_adjoint<4, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<4, 2>(ctx, fp, dl, gt, gh); }
+    else { if (l8) launch_adjoint<8, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<8, 2>(ctx, fp, dl, gt, gh); }
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!on_device) {
+        if (d_texture) CK(cudaMemcpyAsync(d_texture, gt, ntex * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (d_height) CK(cudaMemcpyAsync(d_height, gh, ctx->nverts * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    uint64_t hs[8];
+    CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    ctx->stats.rays_closest = hs[2];
+    ctx->stats.rays_shadow = 0;
+    ctx->stats.kernel_launches = 1;
+    ctx->stats.ms_last = ms;
+    return check_device_error(ctx);
+}
+
+// Albedo texture update without re-uploading the mesh or rebuilding the BVH.
+extern "C" VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!texture || tex_w != ctx->tw || tex_h != ctx->th)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "texture_update: size differs from the uploaded texture");
+    if (ctx->nverts == 0) return fail(ctx, VGB_ERR_NOT_READY, "texture_update: no scene uploaded");
+    cudaSetDevice(ctx->device);
+    const size_t ntex = (size_t)tex_w * tex_h;
+    const uint32_t B = ctx->nbands;
+    bool mono = true;
+    for (size_t t = 0; t < ntex && mono; ++t)
+        for (uint32_t k = 1; k < B; ++k)
+            if (std::memcmp(&texture[t * B + k], &texture[t * B], 4) != 0) { mono = false; break; }
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (mono != (ctx->tex_mono != 0)) {
+        dfree(ctx->d_tex);
+        ctx->d_tex = nullptr;
+        vgb_status s = dalloc(ctx, &ctx->d_tex, sizeof(float) * (mono ? ntex : ntex * B));
+        if (s != VGB_OK) return s;
+        ctx->tex_mono = mono ? 1u : 0u;
+    }
+    if (mono) {
+        std::vector<float> m(ntex);
+        for (size_t t = 0; t < ntex; ++t) m[t] = texture[t * B];
+        CK(cudaMemcpy(ctx->d_tex, m.data(), ntex * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+        CK(cudaMemcpy(ctx->d_tex, texture, ntex * B * sizeof(float), cudaMemcpyHostToDevice));
+    }
     return VGB_OK;
 }

@@ -332,6 +332,17 @@ class PathTracer:
         return rp
 
 
+@dataclass
+class BatchFrame:
+    """One frame of a batched render: its camera, samples per pixel, RNG frame key and, optionally,
+    its own light positions (FP64, scene frame) in the order of Scene.lights."""
+
+    camera: Camera
+    samples: int = 1
+    frame: int = 0
+    light_positions: list | None = None
+
+
 # ============================================================================ scene
 class Scene:
     """Scene (include/vira/scene.hpp) reduced to what the path tracer reads.
@@ -514,6 +525,81 @@ class Scene:
             ctx = self.context()
             capi.check(capi.load().vgb_pixel_solid_angle(ctx, C.byref(cam_c), capi.ptr(om), 1), ctx, "pixel_solid_angle")
             self._omega_cache = {key: om}
+        return om
+
+    # --- batched trajectory rendering
+    def render_batch(self, frames: list, autotune: bool = True, use_graph: bool = False,
+                     planes=("total_radiance", "received_power", "triangle_id", "depth")):
+        """Renders many frames in one persistent launch (vgb_render_batch).  Returns one dict of
+        torch CUDA planes per frame.  Per-pixel results equal those of rendering each frame with
+        PathTracer.render and options.samples/frame set to the frame's values."""
+        import torch
+
+        self.build_tlas()
+        ctx = self.context()
+        lib = capi.load()
+        B = self.bands.size
+        dev = torch.device("cuda", self.device)
+        arr = (capi.Frame * len(frames))()
+        outs = []
+        keep = []
+        for i, fr in enumerate(frames):
+            cam = fr.camera.to_c(self.origin, B)
+            W, H = fr.camera.resolution
+            omega = self._batch_omega(fr.camera, cam)
+            keep.append(omega)
+            out = {}
+            for name in planes:
+                if name in ("depth", "alpha"):
+                    out[name] = torch.empty((H, W), dtype=torch.float32, device=dev)
+                elif name == "triangle_id":
+                    out[name] = torch.empty((H, W), dtype=torch.int32, device=dev)
+                elif name == "normal_global":
+                    out[name] = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+                else:
+                    out[name] = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+            outs.append(out)
+            f = arr[i]
+            f.camera = cam
+            pos = fr.light_positions if fr.light_positions is not None else [L.position for L in self.lights]
+            for k, L in enumerate(self.lights):
+                p = (np.asarray(pos[k], np.float64) - self.origin).astype(np.float32)
+                for a in range(3):
+                    f.lights[k].position[a] = float(p[a])
+                f.lights[k].radius = float(L.radius)
+                for b in range(B):
+                    f.lights[k].radiance[b] = float(L.radiance[b])
+            f.nlights = len(self.lights)
+            f.samples = int(fr.samples)
+            f.frame = int(fr.frame)
+            for name, t in out.items():
+                setattr(f.film, name, t.data_ptr())
+            f.film.pixel_solid_angle = omega.data_ptr()
+            f.film.on_device = 1
+        opts = self.pathtracer.c_options(self)
+        bo = capi.BatchOptions(int(autotune), int(use_graph), 0, 0, 0)
+        torch.cuda.current_stream(dev).synchronize()
+        capi.check(lib.vgb_render_batch(ctx, arr, len(frames), C.byref(opts), C.byref(bo)), ctx, "render_batch")
+        st = capi.Stats()
+        lib.vgb_get_stats(ctx, C.byref(st))
+        self.pathtracer.last_stats = st
+        return outs
+
+    def _batch_omega(self, camera: Camera, cam_c):
+        import torch
+
+        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir))
+        cache = getattr(self, "_omega_batch", None)
+        if cache is None:
+            cache = self._omega_batch = {}
+        om = cache.get(key)
+        if om is None:
+            W, H = camera.resolution
+            om = torch.empty((H, W), dtype=torch.float32, device=torch.device("cuda", self.device))
+            torch.cuda.current_stream(om.device).synchronize()
+            ctx = self.context()
+            capi.check(capi.load().vgb_pixel_solid_angle(ctx, C.byref(cam_c), capi.ptr(om), 1), ctx, "pixel_solid_angle")
+            cache[key] = om
         return om
 
     # --- renders (scene.ipp:840-915)
