@@ -1,0 +1,317 @@
+// vgb.hpp -- C++ host API over the C ABI of vgb.h, shaped like Vira's scene / camera / path tracer.
+//
+// Vira's renderer object is CPUPathTracer with public `options`, `renderPasses` and
+// render(Camera&, Scene&) (include/vira/rendering/cpu_path_tracer.hpp:46-58); Scene owns it as
+// `pathtracer` and calls it from pathtraceRender (include/implementation/scene.ipp:840-845).
+// vgb::GpuPathTracer keeps those names.  Poses, the sun position and the scene origin are FP64;
+// everything is rebased into the local scene frame in FP64 before the FP32 cast.  Errors from
+// the C ABI become vgb::Error (a std::runtime_error), as the reference reports errors.
+#pragma once
+
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "vgb.h"
+
+namespace vgb {
+
+struct Error : std::runtime_error {
+    vgb_status status;
+    Error(vgb_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(vgb_status s, const vgb_context* ctx, const char* what) {
+    if (s != VGB_OK) throw Error(s, std::string(what) + ": " + (ctx ? vgb_last_error(ctx) : "error"));
+}
+
+using Vec3 = std::array<double, 3>;
+using Mat3 = std::array<double, 9>;  // column-major
+
+inline Vec3 sub(const Vec3& a, const Vec3& b) { return {a[0] - b[0], a[1] - b[1], a[2] - b[2]}; }
+inline Vec3 cross(const Vec3& a, const Vec3& b) {
+    return {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
+}
+inline double dot(const Vec3& a, const Vec3& b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline Vec3 normalized(const Vec3& a) {
+    const double s = 1.0 / std::sqrt(dot(a, a));
+    return {a[0] * s, a[1] * s, a[2] * s};
+}
+
+// Band edges in metres, FP32 as SpectralData stores them (spectral_data.ipp:65-132).
+struct SpectralBands {
+    std::vector<float> lo, hi;
+    static SpectralBands bounds(const std::vector<std::array<float, 2>>& nm) {
+        SpectralBands b;
+        for (auto& p : nm) {
+            b.lo.push_back(std::fmin(p[0], p[1]) * 1e-9f);
+            b.hi.push_back(std::fmax(p[0], p[1]) * 1e-9f);
+        }
+        return b;
+    }
+    static SpectralBands uniform(int n, float lo_nm, float hi_nm) {
+        SpectralBands b;
+        const float step = (hi_nm - lo_nm) / (float)n;
+        for (int i = 0; i < n; ++i) {
+            const float a = lo_nm + (float)i * step, c = lo_nm + (float)(i + 1) * step;
+            b.lo.push_back(std::fmin(a, c) * 1e-9f);
+            b.hi.push_back(std::fmax(a, c) * 1e-9f);
+        }
+        return b;
+    }
+    uint32_t size() const { return (uint32_t)lo.size(); }
+};
+
+// blackBodyRadiance (spectral_data.ipp:613-629): trapezoid of Planck's law in FP64 per band.
+inline std::vector<float> blackBodyRadiance(const SpectralBands& bands, double T, uint32_t steps = 1000) {
+    const double c = 299792458.0, h = 6.62607015e-34, kB = 1.380649e-23;
+    std::vector<float> out;
+    for (uint32_t i = 0; i < bands.size(); ++i) {
+        const double mn = bands.lo[i], mx = bands.hi[i], step = (mx - mn) / (double)(steps - 1);
+        double area = 0, prev_l = mn, prev_r = 0;
+        for (uint32_t k = 0; k < steps; ++k) {
+            const double l = mn + (double)k * step;
+            const double r = 2 * h * c * c / std::pow(l, 5.) * 1. / (std::exp(h * c / (l * kB * T)) - 1.);
+            if (k) area += (l - prev_l) * (prev_r + r) / 2.;
+            prev_l = l; prev_r = r;
+        }
+        out.push_back((float)area);
+    }
+    return out;
+}
+
+// Camera (camera.hpp:220-235 defaults), FP64 pose.
+class Camera {
+public:
+    float focal_length = 0.05f, f_stop = 2.8f, aperture_diameter = 0.05f / 2.8f;
+    uint32_t width = 1920, height = 1080;
+    float sensor_x = 0.036f, sensor_y = 0.02025f;
+    bool square_pixel = true, blender_frame = false;
+    Vec3 position{0, 0, 0};
+    Mat3 rotation{1, 0, 0, 0, 1, 0, 0, 0, 1};
+    std::vector<float> optical_efficiency{1.f};
+
+    void setFocalLength(double f) { focal_length = (float)f; f_stop = (float)f / aperture_diameter; }
+    void setFStop(double f) { f_stop = (float)f; aperture_diameter = focal_length / f_stop; }
+    void setSensorSize(double x) {
+        sensor_x = (float)x;
+        sensor_y = (float)((double)height * (x / (double)width));
+        square_pixel = true;
+    }
+    void setSensorSize(double x, double y) { sensor_x = (float)x; sensor_y = (float)y; square_pixel = false; }
+    void setResolution(uint32_t x, uint32_t y) {
+        width = x; height = y;
+        if (square_pixel) setSensorSize(sensor_x);
+    }
+    void setFieldOfView(double deg) { setFocalLength(sensor_x / 2.0 / std::tan(deg * (M_PI / 180.0) / 2.0)); }
+    void setLocalPosition(double x, double y, double z) { position = {x, y, z}; }
+    void lookAt(const Vec3& target, Vec3 up = {0, 0, 1}) { lookInDirection(sub(target, position), up); }
+    // Camera::lookInDirection (camera.ipp:1455-1500), FP64
+    void lookInDirection(Vec3 d, Vec3 up = {0, 0, 1}) {
+        up = normalized(up);
+        d = normalized(d);
+        if (std::fabs(dot(d, up)) > 0.999) {
+            const Vec3 cand[3] = {{0, 1, 0}, {0, 0, 1}, {1, 0, 0}};
+            for (auto& c : cand)
+                if (std::fabs(dot(d, c)) < 0.999) { up = c; break; }
+        }
+        Vec3 y = blender_frame ? up : Vec3{-up[0], -up[1], -up[2]};
+        Vec3 z = blender_frame ? Vec3{-d[0], -d[1], -d[2]} : d;
+        Vec3 x = normalized(cross(y, z));
+        y = normalized(cross(z, x));
+        z = normalized(z);
+        rotation = {x[0], x[1], x[2], y[0], y[1], y[2], z[0], z[1], z[2]};
+    }
+    vgb_camera toC(const Vec3& origin, uint32_t nbands) const {
+        vgb_camera c{};
+        c.width = width; c.height = height;
+        for (int k = 0; k < 3; ++k) c.origin[k] = (float)(position[k] - origin[k]);
+        for (int k = 0; k < 9; ++k) c.rotation[k] = (float)rotation[k];
+        c.z_dir = blender_frame ? -1.f : 1.f;
+        check(vgb_camera_intrinsics(focal_length, sensor_x, sensor_y, width, height, INFINITY, INFINITY, 0.f, 0.f,
+                                    c.z_dir, c.kinv), nullptr, "camera_intrinsics");
+        const float d = focal_length / f_stop, r = d / 2.f, area = 3.14159265358979323846f * r * r;
+        for (uint32_t k = 0; k < nbands; ++k)
+            c.power_scale[k] = optical_efficiency[optical_efficiency.size() == 1 ? 0 : k] * area;
+        return c;
+    }
+};
+
+struct SphereLight {
+    std::vector<float> radiance;
+    float radius = 696000000.f;
+    Vec3 position{0, 0, 0};
+};
+
+struct Mesh {
+    std::vector<float> positions;   // 3 per vertex, mesh frame
+    std::vector<uint32_t> indices;  // 3 per triangle
+    std::vector<float> albedo;      // B per vertex (empty: 1)
+    std::vector<float> uv;          // 2 per vertex (empty: 0)
+    std::vector<float> albedo_map;  // [h][w][B] (empty: 1x1 of 1.0)
+    uint32_t map_w = 0, map_h = 0;
+    bool smooth_shading = false;
+
+    // DEM::makeMesh with the non-OGR projection (dem.ipp:138-211)
+    static Mesh fromDEM(const std::vector<float>& heights, uint32_t w, uint32_t h, double posting, float albedo,
+                        uint32_t nbands) {
+        Mesh m;
+        m.positions.resize(3 * (size_t)w * h);
+        m.indices.resize(6 * (size_t)(w - 1) * (h - 1));
+        uint32_t nt = 0;
+        check(vgb_dem_triangulate(heights.data(), w, h, posting, posting, m.positions.data(), m.indices.data(), &nt),
+              nullptr, "dem_triangulate");
+        m.indices.resize(3 * (size_t)nt);
+        m.albedo.assign((size_t)w * h * nbands, albedo);
+        return m;
+    }
+};
+
+struct CPUPathTracerOptions {  // cpu_path_tracer.hpp:30-43, plus the RNG key and two additions
+    size_t samples = 1;
+    size_t bounces = 0;
+    bool show_background = false;
+    uint64_t seed = 0;
+    uint32_t frame = 0;
+    bool deterministic_light = false;
+    uint32_t rr_depth = 0;
+};
+
+struct RenderPasses {  // passes.hpp:51-95, planar [B][H][W]
+    bool simulate_lighting = false;
+    uint32_t width = 0, height = 0, bands = 0;
+    std::vector<float> total_radiance, direct_radiance, indirect_radiance, received_power, albedo, normal_global,
+        depth, alpha;
+    std::vector<uint32_t> triangle_id;
+};
+
+class Scene;
+
+class GpuPathTracer {
+public:
+    CPUPathTracerOptions options;
+    RenderPasses renderPasses;
+    void render(Camera& camera, Scene& scene);
+};
+
+class Scene {
+public:
+    explicit Scene(SpectralBands b, int device = 0) : bands(std::move(b)) {
+        check(vgb_context_create(&ctx_, device), nullptr, "context_create");
+        background.assign(bands.size(), 0.f);
+    }
+    ~Scene() { if (ctx_) vgb_context_destroy(ctx_); }
+    Scene(const Scene&) = delete;
+    Scene& operator=(const Scene&) = delete;
+
+    SpectralBands bands;
+    Vec3 origin{0, 0, 0};
+    std::vector<Mesh> meshes;
+    std::vector<SphereLight> lights;
+    std::vector<float> ambient, background;
+    GpuPathTracer pathtracer;
+
+    size_t addMesh(Mesh m) { meshes.push_back(std::move(m)); dirty_ = true; return meshes.size() - 1; }
+    size_t newSun(double temperature = 5800.0) {  // Group::newSun (scene/group.ipp:585-591)
+        SphereLight s;
+        s.radiance = blackBodyRadiance(bands, temperature, 1000);
+        lights.push_back(s);
+        return lights.size() - 1;
+    }
+    void setSunDirection(size_t id, double az_deg, double el_deg, double distance = 149597870700.0) {
+        const double az = az_deg * (M_PI / 180.0), el = el_deg * (M_PI / 180.0);
+        lights[id].position = {origin[0] + distance * std::cos(el) * std::cos(az),
+                               origin[1] + distance * std::cos(el) * std::sin(az), origin[2] + distance * std::sin(el)};
+    }
+    void markDirty() { dirty_ = true; }
+
+    // Scene::buildTLAS (scene.ipp:712-812): the first mesh is uploaded in the scene frame.
+    void buildTLAS() {
+        if (!dirty_) return;
+        if (meshes.empty()) throw Error(VGB_ERR_INVALID_ARGUMENT, "buildTLAS: no mesh");
+        const Mesh& m = meshes[0];
+        const uint32_t nv = (uint32_t)(m.positions.size() / 3), nt = (uint32_t)(m.indices.size() / 3);
+        std::vector<float> p(m.positions.size());
+        for (size_t v = 0; v < nv; ++v)
+            for (int k = 0; k < 3; ++k) p[3 * v + k] = (float)((double)m.positions[3 * v + k] - origin[k]);
+        check(vgb_scene_upload(ctx_, p.data(), nv, m.indices.data(), nt, bands.size(),
+                               m.albedo.empty() ? nullptr : m.albedo.data(), nullptr,
+                               m.uv.empty() ? nullptr : m.uv.data(), m.albedo_map.empty() ? nullptr : m.albedo_map.data(),
+                               m.map_w, m.map_h), ctx_, "scene_upload");
+        vgb_bvh_options o{0, 0, 0, 0};
+        check(vgb_bvh_build(ctx_, &o), ctx_, "bvh_build");
+        dirty_ = false;
+    }
+
+    std::vector<vgb_light> cLights() const {
+        std::vector<vgb_light> out;
+        for (auto& L : lights) {
+            vgb_light l{};
+            for (int k = 0; k < 3; ++k) l.position[k] = (float)(L.position[k] - origin[k]);
+            l.radius = L.radius;
+            for (uint32_t b = 0; b < bands.size(); ++b) l.radiance[b] = L.radiance[b];
+            out.push_back(l);
+        }
+        return out;
+    }
+
+    // Scene::pathtraceRender (scene.ipp:840-845) without the sensor chain: the received power.
+    const std::vector<float>& pathtraceRender(Camera& camera) {
+        pathtracer.render(camera, *this);
+        return pathtracer.renderPasses.received_power;
+    }
+
+    vgb_context* context() { return ctx_; }
+
+private:
+    vgb_context* ctx_ = nullptr;
+    bool dirty_ = true;
+};
+
+inline void GpuPathTracer::render(Camera& camera, Scene& scene) {
+    scene.buildTLAS();
+    vgb_context* ctx = scene.context();
+    const uint32_t B = scene.bands.size(), W = camera.width, H = camera.height;
+    const size_t P = (size_t)W * H;
+    vgb_camera cam = camera.toC(scene.origin, B);
+    std::vector<vgb_light> lights = scene.cLights();
+    vgb_pt_options o{};
+    o.samples = (uint32_t)options.samples;
+    o.bounces = (uint32_t)options.bounces;
+    o.show_background = options.show_background;
+    o.simulate_lighting = renderPasses.simulate_lighting;
+    o.smooth_shading = scene.meshes.empty() ? 0 : scene.meshes[0].smooth_shading;
+    o.deterministic_light = options.deterministic_light;
+    o.rr_depth = options.rr_depth;
+    o.seed = options.seed;
+    o.frame = options.frame;
+    o.nbands = B;
+    if (!scene.ambient.empty()) {
+        o.has_ambient = 1;
+        for (uint32_t b = 0; b < B; ++b) o.ambient[b] = scene.ambient[b];
+    }
+    for (uint32_t b = 0; b < B; ++b) o.background[b] = scene.background[b];
+    RenderPasses& rp = renderPasses;
+    rp.width = W; rp.height = H; rp.bands = B;
+    std::vector<float> omega(P);
+    check(vgb_pixel_solid_angle(ctx, &cam, omega.data(), 0), ctx, "pixel_solid_angle");
+    rp.depth.assign(P, 0.f); rp.alpha.assign(P, 0.f); rp.albedo.assign(B * P, 0.f); rp.normal_global.assign(3 * P, 0.f);
+    rp.triangle_id.assign(P, VGB_NO_HIT);
+    vgb_film f{};
+    f.depth = rp.depth.data(); f.alpha = rp.alpha.data(); f.albedo = rp.albedo.data();
+    f.normal_global = rp.normal_global.data(); f.triangle_id = rp.triangle_id.data();
+    if (rp.simulate_lighting) {
+        rp.total_radiance.assign(B * P, 0.f); rp.direct_radiance.assign(B * P, 0.f);
+        rp.indirect_radiance.assign(B * P, 0.f); rp.received_power.assign(B * P, 0.f);
+        f.total_radiance = rp.total_radiance.data(); f.direct_radiance = rp.direct_radiance.data();
+        f.indirect_radiance = rp.indirect_radiance.data(); f.received_power = rp.received_power.data();
+        f.pixel_solid_angle = omega.data();
+    }
+    f.on_device = 0;
+    check(vgb_render(ctx, &cam, lights.data(), (uint32_t)lights.size(), &o, &f), ctx, "render");
+}
+
+}  // namespace vgb
