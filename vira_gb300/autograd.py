@@ -65,6 +65,7 @@ def forward_views(scene: Scene, views: list, device):
     """Renders every view; returns a list of [B][H][W] total-radiance tensors."""
     import torch
 
+    scene.build_tlas()
     lib = capi.load()
     ctx = scene.context()
     B = scene.bands.size
@@ -89,6 +90,7 @@ def adjoint_views(scene: Scene, views: list, grads: list, device, want_texture=T
     """Sums the adjoint of every view: returns (d_texture [th][tw][B], d_heights [nverts])."""
     import torch
 
+    scene.build_tlas()
     lib = capi.load()
     ctx = scene.context()
     B = scene.bands.size

@@ -37,8 +37,13 @@ using namespace vgbd;
 #ifndef VGB_SHADE_MINB
 #define VGB_SHADE_MINB 4
 #endif
+// k_batch without bounces: 3 blocks of 256 threads cap it at 80 registers (a few spills outside
+// the traversal loop), measured faster on the trajectory workload than 128 registers.
+#ifndef VGB_BATCH_DIRECT_MINB
+#define VGB_BATCH_DIRECT_MINB 3
+#endif
 #ifndef VGB_SHADOW_MINB
-#define VGB_SHADOW_MINB 6
+#define VGB_SHADOW_MINB 5
 #endif
 
 namespace {
@@ -229,6 +234,13 @@ __device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float
         if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
 }
 
+// The tangent frame of the shading normal (cpu_path_tracer.ipp:318-321).
+__device__ __forceinline__ void tangent_frame(F3 N, F3& tg, F3& bt) {
+    F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
+    tg = normalize(cross(arb, N));
+    bt = cross(N, tg);
+}
+
 // processIntersection up to the shading point (cpu_path_tracer.ipp:295-346): uv, face and
 // shading normals, tangent frame, albedo (vertex albedo x texture), interpolated position and
 // computeShadingPoint (:494-511).  The normal matrix is the identity in the flattened frame.
@@ -254,9 +266,7 @@ __device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool 
     F3 Nl = fnrm;
     if (smooth) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
     N = Nl;
-    F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
-    tg = normalize(cross(arb, N));
-    bt = cross(N, tg);
+    tangent_frame(N, tg, bt);
     float texv[NB];
     sample_uvs<NB>(s, nb, uvx, uvy, texv);
 #pragma unroll
@@ -1593,16 +1603,30 @@ __device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ fram
     return lo;
 }
 
-// One persistent launch over every (frame, tile) item.  A warp owns a tile and loops over its
-// samples and bounces; accumulation order and random streams are those of the wavefront path.
-template <int NB, int L>
-__global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, const __grid_constant__ BatchParams bp,
+// Shared-memory planes per lane of k_batch: arad[NB] adir[NB] aalb[NB] anrm[3] adep (the
+// pixel's sums over samples) | brad[NB] con[NB] alb[NB] prad[NB] (the current sample) | thr[NB]
+// (paths with bounces only).
+__host__ __device__ constexpr int batch_planes(int nb, bool direct) { return 7 * nb + 4 + (direct ? 0 : nb); }
+
+// One persistent launch over every (frame, tile) item.  A warp owns an 8x4-pixel tile and each
+// lane runs its pixel's samples as a small state machine: camera ray -> closest hit -> one
+// occlusion ray per light -> continuation ray -> ...  Whatever state its lane is in, every ray of
+// the warp goes through the one traversal loop of the kernel, so a lane that finished its sample
+// early traces its next camera ray while its neighbours trace occlusion rays.  Accumulation
+// order and random streams are those of the wavefront path, so the film is bit-identical.
+template <int NB, int L, bool DIRECT>
+__global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_batch(const DevScene s, const DevFrame* __restrict__ frames, const __grid_constant__ BatchParams bp,
                         uint32_t* counter, uint32_t* errw, uint64_t* stats) {
     extern __shared__ float sm_acc[];
-    constexpr int PL = 5 * NB + 4;  // arad[NB] adir[NB] aalb[NB] anrm[3] adep | prad[NB] brad[NB]
+    constexpr int PL = batch_planes(NB, DIRECT);
     const int lane = threadIdx.x & 31;
     float* acc = sm_acc + (size_t)(threadIdx.x >> 5) * PL * 32;
 #define ACC(pl) acc[(pl) * 32 + lane]
+#define BRAD(k) ACC(3 * NB + 4 + (k))
+#define CON(k) ACC(4 * NB + 4 + (k))
+#define ALB(k) ACC(5 * NB + 4 + (k))
+#define PRAD(k) ACC(6 * NB + 4 + (k))
+#define THR(k) (DIRECT ? 1.f : ACC(7 * NB + 4 + (k)))
     const uint32_t nb = bp.nb;
     const vgb_pt_options& opt = bp.opt;
     const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
@@ -1622,14 +1646,17 @@ __global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, c
             const uint32_t tx = tile % F.tiles_x, ty = tile / F.tiles_x;
             const uint32_t pi = tx * 8u + (lane & 7u), pj = ty * 4u + (lane >> 3);
             const uint32_t W = F.cam.width, H = F.cam.height;
-            if (pi >= W || pj >= H) continue;
+            const bool valid = pi < W && pj < H;
             const uint32_t slot = pj * W + pi;
 #pragma unroll
-            for (int p = 0; p < PL; ++p) acc[p * 32 + lane] = 0.f;
-            uint32_t first_tri = VGB_NO_HIT;
-            uint32_t count = 0;
-            for (uint32_t sample = 0; sample < F.samples; ++sample) {
-                // camera ray (camera_ray with this frame's camera and key)
+            for (int p = 0; p < 3 * NB + 4; ++p) acc[p * 32 + lane] = 0.f;
+            uint32_t first_tri = VGB_NO_HIT, count = 0;
+            uint32_t sample = 0, bounce = 0, l = 0, pend = 0;
+            bool active = valid && F.samples > 0, shadow = false;
+            F3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 1.f}, Pp{0.f, 0.f, 0.f}, N{0.f, 0.f, 1.f}, Ld{0.f, 0.f, 1.f};
+            float dist = 0.f;
+            // a new sample: camera_ray with this frame's camera and key, unit throughput
+            auto start_sample = [&]() {
                 float X = (float)pi, Y = (float)pj;
                 if (sample != 0) {
                     U4 jr = philox(U4{slot, sample, F.frame, kSlotJitter}, k0, k1);
@@ -1643,27 +1670,33 @@ __global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, c
                 const float* R = F.cam.rotation;
                 const F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
                             (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
-                F3 rd = normalize(dw);
-                F3 ro{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
-                float thr[NB], alb[NB];
-#define PRAD(k) acc[(3 * NB + 4 + (k)) * 32 + lane]
-#define BRAD(k) acc[(4 * NB + 4 + (k)) * 32 + lane]
+                rd = normalize(dw);
+                ro = F3{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
 #pragma unroll
-                for (int k = 0; k < NB; ++k) { thr[k] = 1.f; PRAD(k) = 0.f; BRAD(k) = 0.f; }
-                uint32_t pend = 0;
-                for (uint32_t bounce = 0; bounce <= opt.bounces; ++bounce) {
-                    if (pend) {
+                for (int k = 0; k < NB; ++k) {
+                    PRAD(k) = 0.f;
+                    if (!DIRECT) ACC(7 * NB + 4 + k) = 1.f;
+                }
+                bounce = 0;
+                pend = 0;
+                shadow = false;
+            };
+            if (active) start_sample();
+            while (__any_sync(0xffffffffu, active)) {
+                if (!active) continue;
+                HitOut h;
+                h.U = h.V = h.W = 0.f; h.det = 1.f;
+                const WRay wr = make_wray(shadow ? Pp : ro, shadow ? Ld : rd);
+                traverse_layout_rt<L, false>(s.nodes, s.tris, wr, shadow ? dist : 0.f, shadow, h, err, cnt);
+                bool sample_done = false;
+                if (shadow) {
+                    nshadow++;
+                    if (h.id == VGB_NO_HIT) {
 #pragma unroll
-                        for (int k = 0; k < NB; ++k) {
-                            PRAD(k) += BRAD(k);
-                            if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
-                        }
-                        pend = 0;
+                        for (int k = 0; k < NB; ++k) BRAD(k) += CON(k);
                     }
-                    HitOut h;
-                    h.U = h.V = h.W = 0.f; h.det = 1.f;
-                    const WRay wr = make_wray(ro, rd);
-                    traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+                    ++l;
+                } else {
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
@@ -1679,80 +1712,111 @@ __global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, c
                             for (int k = 0; k < NB; ++k) {
                                 const float bgv = opt.background[k];
                                 float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
-                                PRAD(k) = PRAD(k) + thr[k] * (bg * 1.f);
+                                PRAD(k) = PRAD(k) + THR(k) * (bg * 1.f);
                             }
                         }
-                        break;
-                    }
-                    const float rcp = 1.0f / h.det;
-                    const float w0 = h.V * rcp, w1 = h.W * rcp;
-                    F3 Pp, N, fnrm, tg, bt;
-                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
-                    if (bounce == 0) {
-                        if (first_tri == VGB_NO_HIT) first_tri = h.id;
+                        sample_done = true;
+                    } else {
+                        const float rcp = 1.0f / h.det;
+                        const float w0 = h.V * rcp, w1 = h.W * rcp;
+                        F3 fnrm, tg, bt;
+                        float alb[NB];
+                        surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
+                        if (bounce == 0) {
+                            if (first_tri == VGB_NO_HIT) first_tri = h.id;
 #pragma unroll
-                        for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
-                        ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
-                        ACC(3 * NB + 3) += h.t;
-                        count += 1u;
-                    }
-                    if (!opt.simulate_lighting) break;
-                    Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
-#pragma unroll
-                    for (int k = 0; k < NB; ++k)
-                        BRAD(k) = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * alb[k]) : 0.f;
-                    pend = (bounce == 0) ? 1u : 2u;
-                    const U4 r0 = philox(U4{slot, sample, F.frame, (bounce << 8) | kSlotMain}, k0, k1);
-                    for (uint32_t l = 0; l < F.nlights; ++l) {
-                        float ru1, ru2;
-                        if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
-                        else {
-                            U4 rl = philox(U4{slot, sample, F.frame, (bounce << 8) | (1u + l)}, k0, k1);
-                            ru1 = u01(rl.x); ru2 = u01(rl.y);
+                            for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
+                            ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
+                            ACC(3 * NB + 3) += h.t;
+                            count += 1u;
                         }
-                        // nee_light, with the contribution formed only once the shadow ray is clear
-                        F3 Ld; float dist, lpdf = 0.f;
-                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                        if (!opt.simulate_lighting) {
+                            sample_done = true;
+                        } else {
+                            Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                            for (int k = 0; k < NB; ++k) {
+                                BRAD(k) = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + THR(k) * (opt.ambient[k] * alb[k]) : 0.f;
+                                ALB(k) = alb[k];
+                            }
+                            pend = (bounce == 0) ? 1u : 2u;
+                            l = 0;
+                        }
+                    }
+                }
+                if (!sample_done) {
+                    // the next light that needs an occlusion ray (nee_light, contribution kept
+                    // until the ray is found clear)
+                    shadow = false;
+                    while (l < F.nlights) {
+                        U4 rl = philox(U4{slot, sample, F.frame, (bounce << 8) | (l == 0 ? (uint32_t)kSlotMain : 1u + l)}, k0, k1);
+                        float lpdf = 0.f;
+                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, u01(rl.x), u01(rl.y), Ld, dist, lpdf);
                         if (lpdf > 0) {
-                            HitOut hs;
-                            const WRay ws = make_wray(Pp, Ld);
-                            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
-                            nshadow++;
-                            if (hs.id == VGB_NO_HIT) {
-                                const float nl = dot(N, Ld);
-                                const float cos_t = smax(0.0f, dot(Ld, N));
-                                const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
-                                const float wgt = power_heuristic(lpdf, mpdf);
+                            const float nl = dot(N, Ld);
+                            const float cos_t = smax(0.0f, dot(Ld, N));
+                            const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                            const float wgt = power_heuristic(lpdf, mpdf);
+#pragma unroll
+                            for (int k = 0; k < NB; ++k) {
+                                const float bsdf = ALB(k) * kInvPi * smax(nl, 0.f);
+                                CON(k) = (k < (int)nb) ? THR(k) * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                            }
+                            shadow = true;
+                            break;
+                        }
+                        ++l;
+                    }
+                    if (!shadow) {
+                        // every light of this vertex is done: continue the path or end the sample
+                        if (DIRECT || bounce >= opt.bounces) {
+                            sample_done = true;
+                        } else {
+                            const U4 r0 = philox(U4{slot, sample, F.frame, (bounce << 8) | kSlotMain}, k0, k1);
+                            F3 tg, bt;
+                            tangent_frame(N, tg, bt);
+                            float alb[NB], thr[NB];
+#pragma unroll
+                            for (int k = 0; k < NB; ++k) { alb[k] = ALB(k); thr[k] = THR(k); }
+                            bool new_ray = false;
+                            F3 nd;
+                            const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0,
+                                                                slot, sample, F.frame, bounce, nd, new_ray);
+                            if (!DIRECT) {
+#pragma unroll
+                                for (int k = 0; k < NB; ++k) ACC(7 * NB + 4 + k) = thr[k];
+                            }
+                            if (!cont) {
+                                sample_done = true;
+                            } else {
+                                if (new_ray) { ro = Pp; rd = nd; }
 #pragma unroll
                                 for (int k = 0; k < NB; ++k) {
-                                    const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
-                                    const float con = (k < (int)nb) ? thr[k] * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
-                                    BRAD(k) += con;
+                                    PRAD(k) += BRAD(k);
+                                    if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
                                 }
+                                pend = 0;
+                                ++bounce;
                             }
                         }
                     }
-                    if (bounce >= opt.bounces) break;
-                    bool new_ray = false;
-                    F3 nd;
-                    const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0, slot,
-                                                        sample, F.frame, bounce, nd, new_ray);
-                    if (!cont) break;
-                    if (new_ray) { ro = Pp; rd = nd; }
                 }
-                if (pend) {
+                if (sample_done) {
 #pragma unroll
                     for (int k = 0; k < NB; ++k) {
-                        PRAD(k) += BRAD(k);
-                        if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                        if (pend) {
+                            PRAD(k) += BRAD(k);
+                            if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                        }
+                        if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
                     }
+                    pend = 0;
+                    if (++sample < F.samples) start_sample();
+                    else active = false;
                 }
-#pragma unroll
-                for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
-#undef PRAD
-#undef BRAD
             }
             // RenderPasses::updateImages for this pixel
+            if (!valid) continue;
             const size_t P = (size_t)W * H;
             const float sf = (float)F.samples;
             const FilmOut& f = F.film;
@@ -1777,25 +1841,38 @@ __global__ void k_batch(const DevScene s, const DevFrame* __restrict__ frames, c
             if (f.tri) f.tri[slot] = first_tri;
         }
     }
+#undef THR
+#undef PRAD
+#undef ALB
+#undef CON
+#undef BRAD
 #undef ACC
     if (err) atomicOr(errw, err);
     warp_reduce_add(&stats[2], nclosest);
     warp_reduce_add(&stats[3], nshadow);
 }
 
+template <int NB, int L, bool DIRECT>
+cudaError_t launch_batch_t(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
+                           uint32_t bps) {
+    const size_t smem = (size_t)(threads / 32) * batch_planes(NB, DIRECT) * 32 * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_batch<NB, L, DIRECT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_batch<NB, L, DIRECT>, (int)threads, smem);
+    const uint32_t b = std::max<uint32_t>(1, std::min<uint32_t>(bps, (uint32_t)std::max(1, maxb)));
+    cudaMemsetAsync(&ctx->d_counters[C_BATCH], 0, sizeof(uint32_t), ctx->stream);
+    k_batch<NB, L, DIRECT><<<b * ctx->num_sms, threads, smem, ctx->stream>>>(dev_scene(ctx), d_frames, bp,
+                                                                             &ctx->d_counters[C_BATCH],
+                                                                             &ctx->d_counters[C_ERR], ctx->d_stats);
+    return cudaGetLastError();
+}
+
 template <int NB, int L>
 cudaError_t launch_batch(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
                          uint32_t bps) {
-    const size_t smem = (size_t)(threads / 32) * (5 * NB + 4) * 32 * sizeof(float);
-    cudaError_t e = cudaFuncSetAttribute(k_batch<NB, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int maxb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_batch<NB, L>, (int)threads, smem);
-    const uint32_t b = std::max<uint32_t>(1, std::min<uint32_t>(bps, (uint32_t)std::max(1, maxb)));
-    cudaMemsetAsync(&ctx->d_counters[C_ERR + 1], 0, sizeof(uint32_t), ctx->stream);
-    k_batch<NB, L><<<b * ctx->num_sms, threads, smem, ctx->stream>>>(dev_scene(ctx), d_frames, bp, &ctx->d_counters[C_ERR + 1],
-                                                                      &ctx->d_counters[C_ERR], ctx->d_stats);
-    return cudaGetLastError();
+    if (bp.opt.bounces == 0) return launch_batch_t<NB, L, true>(ctx, d_frames, bp, threads, bps);
+    return launch_batch_t<NB, L, false>(ctx, d_frames, bp, threads, bps);
 }
 
 cudaError_t launch_batch_any(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,

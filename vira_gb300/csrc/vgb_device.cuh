@@ -138,21 +138,67 @@ struct HitOut {
 
 struct Counters { uint32_t nodes, tris; };
 
-// Closest hit (ANY = false; ties in t go to the smaller id) or occlusion (ANY = true, any
-// hit with t <= tmax).  Box tests are conservative: slab distances (lo - o) * (1/d) carry a
-// relative error below 2*gamma(3) (Ize 2013), and the exit distance is widened by 2^-20.
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                         const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Per-ray constants of the slab test.  A plane distance is one fused multiply-add,
+// fma(plane, 1/d, -(o/d) -+ e): with o/d rounded once, its error is a relative part below
+// 2^-23 (the reciprocal and the fma) plus an absolute part below 2^-24 |o/d|, so each axis
+// shifts its near plane down and its far plane up by e = 2^-20 |o/d| (16x that bound), and the
+// exit distance is widened by 2^-20 for the relative part (Ize 2013).  No box that the exact
+// slab test keeps is culled, so the closest hit does not depend on this arithmetic.
+struct SlabRay {
+    float ix, iy, iz, lx, hx, ly, hy, lz, hz;  // reciprocals; offsets of the lo and hi planes
+};
+__device__ __forceinline__ SlabRay make_slab(const WRay& r) {
+    SlabRay q;
+    q.ix = r.ix; q.iy = r.iy; q.iz = r.iz;
+    const float ox = r.o.x * r.ix, oy = r.o.y * r.iy, oz = r.o.z * r.iz;
+    const float ex = fabsf(ox) * 0x1p-20f, ey = fabsf(oy) * 0x1p-20f, ez = fabsf(oz) * 0x1p-20f;
+    q.lx = (r.ix >= 0.f) ? (-ox - ex) : (-ox + ex);
+    q.hx = (r.ix >= 0.f) ? (-ox + ex) : (-ox - ex);
+    q.ly = (r.iy >= 0.f) ? (-oy - ey) : (-oy + ey);
+    q.hy = (r.iy >= 0.f) ? (-oy + ey) : (-oy - ey);
+    q.lz = (r.iz >= 0.f) ? (-oz - ez) : (-oz + ez);
+    q.hz = (r.iz >= 0.f) ? (-oz + ez) : (-oz - ez);
+    return q;
+}
+
+// Entry and exit distances of the box [lo, hi] clipped to [0, tfar] (exit widened).
+__device__ __forceinline__ void slab(const SlabRay& q, float lox, float hix, float loy, float hiy, float loz,
+                                     float hiz, float tfar, float& tn, float& tf) {
     const float widen = 1.0f + 0x1p-20f;
+    const float a0 = fmaf(lox, q.ix, q.lx), a1 = fmaf(hix, q.ix, q.hx);
+    const float b0 = fmaf(loy, q.iy, q.ly), b1 = fmaf(hiy, q.iy, q.hy);
+    const float c0 = fmaf(loz, q.iz, q.lz), c1 = fmaf(hiz, q.iz, q.hz);
+    tn = fmax3(fminf(a0, a1), fminf(b0, b1), fmaxf(fminf(c0, c1), 0.0f));
+    tf = fmin3(fmaxf(a0, a1), fmaxf(b0, b1), fminf(fmaxf(c0, c1), tfar)) * widen;
+}
+
+// Closest hit (any = false; ties in t go to the smaller id) or occlusion (any = true, any
+// hit with t <= tmax).  Box tests are conservative (make_slab).
+// `any` may be a run-time value: a kernel that interleaves closest-hit and occlusion rays in one
+// loop passes it per ray; the templated wrapper below passes a constant.
+template <bool COUNT>
+__device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                            const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
+                                            Counters& cnt) {
     int stack[kStackSize];
     int sp = 0;
     int node = 0;
-    float best = ANY ? tmax : __int_as_float(0x7f800000);
+    float best = any ? tmax : __int_as_float(0x7f800000);
     h.t = __int_as_float(0x7f800000);
     h.id = VGB_NO_HIT;
     uint32_t iter = 0;
-    const float ox = r.o.x, oy = r.o.y, oz = r.o.z, ix = r.ix, iy = r.iy, iz = r.iz;
+    const SlabRay q = make_slab(r);
     while (true) {
         while (node >= 0) {
             if (++iter > kIterCap) { err |= kErrIter; return; }
@@ -161,16 +207,9 @@ __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const
             const float4 n2 = __ldg(&nodes[4 * node + 2]);
             const float4 n3 = __ldg(&nodes[4 * node + 3]);
             if (COUNT) cnt.nodes++;
-            float a0 = (n0.x - ox) * ix, a1 = (n0.y - ox) * ix;
-            float b0 = (n0.z - oy) * iy, b1 = (n0.w - oy) * iy;
-            float c0 = (n2.x - oz) * iz, c1 = (n2.y - oz) * iz;
-            float tn0 = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
-            float tf0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), best)) * widen;
-            float d0 = (n1.x - ox) * ix, d1 = (n1.y - ox) * ix;
-            float e0 = (n1.z - oy) * iy, e1 = (n1.w - oy) * iy;
-            float f0 = (n2.z - oz) * iz, f1 = (n2.w - oz) * iz;
-            float tn1 = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1)), fmaxf(fminf(f0, f1), 0.0f));
-            float tf1 = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1)), fminf(fmaxf(f0, f1), best)) * widen;
+            float tn0, tf0, tn1, tf1;
+            slab(q, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, best, tn0, tf0);
+            slab(q, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, best, tn1, tf1);
             const bool h0 = tn0 <= tf0, h1 = tn1 <= tf1;
             const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
             if (h0 && h1) {
@@ -199,7 +238,7 @@ __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const
             float tt, U, V, W, det;
             if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
                 const uint32_t id = __float_as_uint(t0.w);
-                if (ANY) {
+                if (any) {
                     if (tt <= tmax) { h.t = tt; h.id = id; return; }
                 } else if (tt < h.t || (tt == h.t && id < h.id)) {
                     h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
@@ -210,6 +249,12 @@ __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const
         if (sp == 0) return;
         node = stack[--sp];
     }
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                         const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+    traverse_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt);
 }
 
 // ------------------------------------------------------------------ compressed 8-wide traversal
@@ -230,15 +275,16 @@ __device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t o) {
 
 __device__ __forceinline__ float q8(uint32_t w, int byte) { return (float)((w >> (8 * byte)) & 0xFFu); }
 
-template <bool ANY, bool COUNT>
-__device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+template <bool COUNT>
+__device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                             const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
+                                             Counters& cnt) {
     const float widen = 1.0f + 0x1p-20f;
     const uint32_t oct = (r.d.x < 0.f ? 1u : 0u) | (r.d.y < 0.f ? 2u : 0u) | (r.d.z < 0.f ? 4u : 0u);
     uint2 stack[kStack8];
     int sp = 0;
     uint32_t node = 0;
-    float best = ANY ? tmax : __int_as_float(0x7f800000);
+    float best = any ? tmax : __int_as_float(0x7f800000);
     h.t = __int_as_float(0x7f800000);
     h.id = VGB_NO_HIT;
     uint32_t iter = 0;
@@ -286,7 +332,7 @@ __device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const
             float tt, U, V, W, det;
             if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
                 const uint32_t id = __float_as_uint(t0.w);
-                if (ANY) {
+                if (any) {
                     if (tt <= tmax) { h.t = tt; h.id = id; return; }
                 } else if (tt < h.t || (tt == h.t && id < h.id)) {
                     h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
@@ -312,12 +358,27 @@ __device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const
     }
 }
 
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
+    traverse8_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt);
+}
+
 // Dispatch on the node layout (2: binary, 8: compressed 8-wide).
 template <int LAYOUT, bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse_any_layout(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                                     const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
     if (LAYOUT == 8) traverse8<ANY, COUNT>(nodes, tris, r, tmax, h, err, cnt);
     else traverse<ANY, COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, h, err, cnt);
+}
+
+// The same with the closest-hit / occlusion choice made per ray at run time.
+template <int LAYOUT, bool COUNT>
+__device__ __forceinline__ void traverse_layout_rt(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                   const WRay& r, float tmax, bool any, HitOut& h, uint32_t& err,
+                                                   Counters& cnt) {
+    if (LAYOUT == 8) traverse8_rt<COUNT>(nodes, tris, r, tmax, any, h, err, cnt);
+    else traverse_rt<COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, any, h, err, cnt);
 }
 
 }  // namespace vgbd

@@ -1,0 +1,50 @@
+"""Small cases of each kernel family for profiler captures (a few GB on the device at most).
+
+    python -m vira_gb300.profile_cases path [scale]   # k_trace / k_shade / k_shadow / k_end_sample
+    python -m vira_gb300.profile_cases batch          # k_batch: 24 trajectory frames, 256^2-1024^2
+    python -m vira_gb300.profile_cases adjoint        # k_adjoint: 2 views of a 513^2 crater DEM
+
+``path`` renders the path-traced workload shrunk by ``scale`` (posts, texture and pixels; 4 spp)
+twice; the captures skip the launches of the first render.
+"""
+from __future__ import annotations
+
+import sys
+
+
+def main(argv=None):
+    import torch
+
+    from . import workloads
+
+    argv = sys.argv[1:] if argv is None else argv
+    kind = argv[0] if argv else "path"
+    scale = float(argv[1]) if len(argv) > 1 else 0.25
+    if kind == "path":
+        posts = int(4096 * scale) + 1
+        scene, cam = workloads.path_traced(posts=posts, tex=int(4096 * scale), resolution=int(2048 * scale), spp=4)
+        for _ in range(2):
+            scene.pathtracer.render(scene[cam], scene)
+        torch.cuda.synchronize()
+        print("path", scene.pathtracer.last_stats.ms_last, "ms")
+    elif kind == "batch":
+        scene, frames = workloads.trajectory(nframes=24, resolutions=(256, 512, 1024), spps=(1, 4, 16))
+        for _ in range(2):
+            scene.render_batch(frames, autotune=False, use_graph=False)
+        torch.cuda.synchronize()
+        print("batch", scene.pathtracer.last_stats.ms_last, "ms")
+    elif kind == "adjoint":
+        from .autograd import adjoint_views, forward_views
+
+        scene, views = workloads.inversion(posts=513, tex=512, resolution=256, nviews=2, spp=4)
+        dev = torch.device("cuda", 0)
+        imgs = forward_views(scene, views, dev)
+        gt, gz = adjoint_views(scene, views, [torch.ones_like(i) for i in imgs], dev)
+        torch.cuda.synchronize()
+        print("adjoint", float(gt.abs().sum()))
+    else:
+        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint")
+
+
+if __name__ == "__main__":
+    main()
