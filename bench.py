@@ -34,6 +34,13 @@ from pathlib import Path
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
+
+# ncu capture of the full path-traced frame (dram__bytes_read.sum + dram__bytes_write.sum of the
+# k_trace launches of one sample, averaged over its four bounces); see
+# profiles/traffic_path_traced_dem4097_2048px.md for the command and the per-launch figures.
+MEASURED_TRAFFIC = {
+    ("path_traced_dem4097_tex4096_2048px_64spp_3b_rr2_8band", 2): {"k_trace": 118951936.0},
+}
 sys.path.insert(0, str(ROOT))
 
 TRI_BYTES = 48
@@ -62,6 +69,7 @@ def parse():
     ap.add_argument("--layout", type=int, choices=[2, 8], default=2, help="device BVH node layout")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-trajectory line item")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint line item")
+    ap.add_argument("--no-asteroid", action="store_true", help="skip the fused batched-adjoint asteroid line item")
     return ap.parse_args()
 
 
@@ -375,16 +383,9 @@ def run_ours(args, p, rank, world, local_rank):
     per_launch_ms = dms / max(1, dl)
     achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic_per_launch.json"
-    if tfile.exists():
-        try:
-            tj = json.loads(tfile.read_text())
-            ent = tj.get(config_name(p), {}).get(dominant)
-            if ent:
-                traffic = float(ent)
-        except Exception:
-            traffic = None
+    # DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture of this
+    # workload (profiles/traffic_path_traced_dem4097_2048px.md), or None for other workloads.
+    traffic = MEASURED_TRAFFIC.get((config_name(p), args.layout), {}).get(dominant)
 
     direct = None
     if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
@@ -397,6 +398,10 @@ def run_ours(args, p, rank, world, local_rank):
     if not args.no_adjoint and p["kind"] == "path_traced" and rank == 0:
         scene.close()
         adjoint = adjoint_item(torch, dev, args.layout)
+    asteroid = None
+    if not args.no_asteroid and p["kind"] == "path_traced" and rank == 0:
+        scene.close()
+        asteroid = asteroid_item(torch, dev, args.layout)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -445,6 +450,8 @@ def run_ours(args, p, rank, world, local_rank):
             line["batched"] = batched
         if adjoint is not None:
             line["adjoint"] = adjoint
+        if asteroid is not None:
+            line["batched_adjoint"] = asteroid
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -581,6 +588,56 @@ def adjoint_item(torch, dev, layout=2, reps=2):
            "backward_passes_per_s": 1.0 / min(bw), "loss": loss,
            "grad_norm": {"texture": float(gt.double().norm()), "heights": float(gz.double().norm())},
            "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
+    scene.close()
+    return out
+
+
+def asteroid_item(torch, dev, layout=2, reps=2):
+    """The batched-adjoint asteroid workload: 64 views of uneven size, per-vertex radial offsets as
+    parameters (smooth shading), the fused forward + L2 loss + adjoint of all views in one
+    persistent launch, against per-view forward renders followed by per-view adjoint launches."""
+    from vira_gb300 import workloads
+    from vira_gb300.autograd import _apply_positions, adjoint_views, forward_views, render_adjoint_batch
+
+    t0 = time.perf_counter()
+    scene, views, dirs = workloads.asteroid(device=dev.index)
+    scene.bvh_options.layout = layout
+    mesh = scene.meshes[0]
+    base = torch.tensor(mesh.positions.copy())
+    dr = torch.tensor(dirs)
+    rng = np.random.default_rng(9)
+    off = torch.tensor(rng.normal(0.0, 0.5, dirs.shape[0]), dtype=torch.float32)
+    _apply_positions(scene, None, base + off[:, None] * dr)
+    targets = forward_views(scene, views, dev)
+    _apply_positions(scene, None, base)
+    setup = time.perf_counter() - t0
+    render_adjoint_batch(scene, views, targets, dev, want_texture=False)  # warm-up
+    fused, sep = [], []
+    loss = 0.0
+    gp = None
+    for _ in range(reps):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        loss, _, _, gp = render_adjoint_batch(scene, views, targets, dev, want_texture=False, keep_radiance=False)
+        torch.cuda.synchronize(dev)
+        fused.append(time.perf_counter() - t)
+    for _ in range(reps):
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        imgs = forward_views(scene, views, dev)
+        grads = [2.0 * (i - t_) for i, t_ in zip(imgs, targets)]
+        adjoint_views(scene, views, grads, dev, want_texture=False, want_heights=True, positions=True)
+        torch.cuda.synchronize(dev)
+        sep.append(time.perf_counter() - t)
+    g_off = (gp.cpu() * dr).sum(dim=1)
+    pix = sum(v.camera.resolution[0] * v.camera.resolution[1] for v in views)
+    out = {"workload": f"asteroid_ico9_{mesh.indices.shape[0]}tris_{len(views)}views_256-1024px_"
+                       f"{scene.pathtracer.options.samples}spp_4band_smooth",
+           "parameters": int(dirs.shape[0]), "pixels": int(pix), "loss": loss,
+           "fused_s": min(fused), "per_view_forward_plus_adjoint_s": min(sep),
+           "speedup_over_per_view": min(sep) / min(fused), "gradient_evaluations_per_s": 1.0 / min(fused),
+           "grad_norm_radial": float(g_off.double().norm()), "setup_s": setup,
+           "timing": "wall clock around the blocking C-ABI calls, best of %d" % reps}
     scene.close()
     return out
 

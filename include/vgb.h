@@ -252,14 +252,50 @@ VGB_API vgb_status vgb_batch_tuning(vgb_context* ctx, uint32_t* block_threads, u
  * camera, lights and options, ADDS into d_texture ([tex_h][tex_w][B], the albedo texture's
  * layout) and d_height (one per vertex: the derivative with respect to the vertex's z in the
  * scene frame); NULL skips one.  Paths are replayed from their random streams, nothing is stored
- * by the forward render.  Height gradients go through the hit triangle's face normal in every
- * next-event term and through the motion of the hit point on the triangle (barycentrics, hence
- * texture coordinates and interpolated albedo); they need flat shading.  Excluded: visibility
- * (shadow and silhouette edges), the rotation of the sampled continuation direction with the
- * normal, the motion of the shading point, Russian roulette decisions.  At most 3 bounces. */
+ * by the forward render.  Height gradients go through the shading normal in every next-event
+ * term (flat shading: the hit triangle's face normal; smooth shading: the interpolated vertex
+ * normals, see vgb_adjoint_positions) and through the motion of the hit point on the triangle
+ * (barycentrics, hence texture coordinates, interpolated albedo and interpolated normal).
+ * Excluded: visibility (shadow and silhouette edges), the rotation of the sampled continuation
+ * direction with the normal, the motion of the shading point, Russian roulette decisions.
+ * At most 3 bounces. */
 VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                                uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
                                float* d_texture, float* d_height, int on_device);
+/* As vgb_adjoint, with the gradient with respect to every vertex position: ADDS into
+ * d_position ([nverts][3], scene frame).  With smooth shading the shading normal's gradient goes
+ * back through the vertex normals of each hit triangle to the positions of their 1-rings (the
+ * vertex normals must be those of vgb_compute_vertex_normals); with flat shading through the
+ * face normal.  A per-vertex offset along any direction field (heights: +z; radial offsets:
+ * the unit radial direction) has the gradient dot(d_position[v], direction[v]). */
+VGB_API vgb_status vgb_adjoint_positions(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                         uint32_t nlights, const vgb_pt_options* opts,
+                                         const float* dL_dradiance, float* d_texture, float* d_position,
+                                         int on_device);
+
+/* ---- fused forward + adjoint over many views (no counterpart in the reference) ---------
+ * One persistent launch renders every view, forms the L2 loss against the view's target and
+ * back-propagates it: per pixel, the samples are traced (forward), dL/dI = 2 (I - target) is
+ * formed, and the same samples are replayed for the gradients.  All pointers are device memory. */
+typedef struct vgb_view {
+    vgb_camera camera;
+    vgb_light lights[8];
+    uint32_t nlights;
+    uint32_t samples;          /* this view's samples per pixel */
+    uint32_t frame;            /* RNG key word of this view */
+    uint32_t pad;
+    const float* target;       /* [B][H][W] */
+    float* radiance;           /* [B][H][W] total radiance out (as vgb_render's), or NULL */
+} vgb_view;
+
+/* ADDS the gradients of loss = sum over views, bands and pixels of (I - target)^2 into
+ * d_texture ([tex_h][tex_w][B]) and d_position ([nverts][3]) (either may be NULL) and writes the
+ * loss (FP64 sum) to *loss if loss is not NULL.  The radiance planes equal vgb_render's
+ * total_radiance for the same view (same arithmetic and random streams).  Exclusions as for
+ * vgb_adjoint_positions; at most 3 bounces. */
+VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* views, uint32_t nviews,
+                                            const vgb_pt_options* opts, float* d_texture, float* d_position,
+                                            double* loss);
 /* Replaces the albedo texture (same size) without re-uploading the mesh or rebuilding the BVH. */
 VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h);
 

@@ -52,6 +52,8 @@ def load():
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
                                     C.POINTER(capi.Film), U32, U32, C.c_int, P]),
         "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
+        "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
+                                               C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -171,6 +173,20 @@ class OracleScene:
         if rc != 0:
             raise ValueError("oracle_adjoint rejected its arguments")
         return gt, gz
+
+    def adjoint_positions(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, dldi, tex_shape=None,
+                          nverts=None, threads=None):
+        """FP64 gradients of sum(dL/dI * I): (d_texture [th][tw][B] or None, d_position [nverts][3] or None)."""
+        d = np.ascontiguousarray(dldi, np.float32)
+        gt = np.zeros(tex_shape, np.float64) if tex_shape is not None else None
+        gp = np.zeros((nverts, 3), np.float64) if nverts is not None else None
+        rc = load().oracle_adjoint_positions(self.h, C.byref(cam), C.cast(lights, C.c_void_p) if nlights else None,
+                                             nlights, C.byref(opts), d.ctypes.data,
+                                             None if gt is None else gt.ctypes.data,
+                                             None if gp is None else gp.ctypes.data, threads or nthreads())
+        if rc != 0:
+            raise ValueError("oracle_adjoint_positions rejected its arguments")
+        return gt, gp
 
     def render(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, omega=None, rows=None,
                threads=None):

@@ -1025,21 +1025,32 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
 // ==================================================================== FP64 adjoint (path replay)
 // The same sampled paths as oracle_render (FP32, identical arithmetic), with the gradient of
 // sum_k g_k I_k (g = dL/dI / spp) formed in FP64: albedo through the suffix radiance / albedo
-// of every path vertex, heights through the hit triangle's face normal in every NEE term and
-// through the hit-point motion on the triangle (barycentrics -> uv -> bilinear texture and
-// interpolated vertex albedo).  Visibility, the rotation of sampled directions with the normal
-// and the motion of the shading point are excluded, as in the product's vgb_adjoint.
+// of every path vertex; vertex positions through the shading normal in every NEE term (flat:
+// the hit triangle's face normal; smooth: the interpolated vertex normals, then the normals of
+// the 1-ring faces, vnormal_backward) and through the hit-point motion on the triangle
+// (barycentrics -> uv -> bilinear texture, interpolated vertex albedo and normal).  Visibility,
+// the rotation of sampled directions with the normal and the motion of the shading point are
+// excluded, as in the product's vgb_adjoint_positions.
 namespace {
 
 struct AVtx {
     uint32_t tri;
     float w0, w1, uvx, uvy;
-    double m1, m2, gn[3];
+    double m[3][2], gn[3];   // M^-1 e_a (b1, b2) for a = x, y, z; dL/dN
     float alb[VGB_MAX_BANDS], va[VGB_MAX_BANDS], tex[VGB_MAX_BANDS], rad[VGB_MAX_BANDS];
 };
 
+static inline V3d v3d(V3 a) { return V3d{a.x, a.y, a.z}; }
+static inline V3d addd(V3d a, V3d b) { return V3d{a.x + b.x, a.y + b.y, a.z + b.z}; }
+static inline V3d subd(V3d a, V3d b) { return V3d{a.x - b.x, a.y - b.y, a.z - b.z}; }
+static inline V3d muld(V3d a, double k) { return V3d{a.x * k, a.y * k, a.z * k}; }
+
+// Gradients of sum(g * I) for one pixel, added into gtex ([th][tw][B]), gpos ([nverts][3]) and,
+// with smooth shading, gvn ([nverts][3], the vertex-normal gradients that
+// vnormal_backward carries to the positions).
 static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light* lights, uint32_t nlights,
-                          const vgb_pt_options& o, uint32_t i, uint32_t j, const double* g, double* gtex, double* gz) {
+                          const vgb_pt_options& o, uint32_t i, uint32_t j, const double* g, double* gtex, double* gpos,
+                          double* gvn) {
     const uint32_t B = s.nbands;
     Rng rng{(uint32_t)o.seed, (uint32_t)(o.seed >> 32), j * cam.width + i, 0, o.frame};
     V3 org{cam.origin[0], cam.origin[1], cam.origin[2]};
@@ -1104,13 +1115,16 @@ static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light
                           w[2] * s.albedo[(size_t)vi[2] * B + k];
                 V.alb[k] = V.va[k] * V.tex[k];
             }
-            // M^-1 e_z for the hit-point motion, FP64 (caller order A=v0, B=v1, C=v2)
+            // M^-1 e_a for the hit-point motion, FP64 (caller order A=v0, B=v1, C=v2), M = [d | A-B | A-C]
             {
                 V3d A{p0.x, p0.y, p0.z}, Bv{p1.x, p1.y, p1.z}, Cv{p2.x, p2.y, p2.z}, d{dir.x, dir.y, dir.z};
-                V3d c1 = A - Bv, c2 = A - Cv, ez{0, 0, 1};
+                V3d c1 = A - Bv, c2 = A - Cv;
                 double det = dotd(d, crossd(c1, c2));
-                V.m1 = det != 0 ? dotd(d, crossd(ez, c2)) / det : 0.0;
-                V.m2 = det != 0 ? dotd(d, crossd(c1, ez)) / det : 0.0;
+                for (int a = 0; a < 3; ++a) {
+                    V3d e{a == 0 ? 1.0 : 0.0, a == 1 ? 1.0 : 0.0, a == 2 ? 1.0 : 0.0};
+                    V.m[a][0] = det != 0 ? dotd(d, crossd(e, c2)) / det : 0.0;
+                    V.m[a][1] = det != 0 ? dotd(d, crossd(c1, e)) / det : 0.0;
+                }
             }
             V.gn[0] = V.gn[1] = V.gn[2] = 0.0;
             for (uint32_t k = 0; k < B; ++k) V.rad[k] = 0.f;
@@ -1202,15 +1216,44 @@ static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light
             if (gtex)
                 for (uint32_t k = 0; k < B; ++k)
                     for (int q = 0; q < 4; ++q) gtex[tx[q] * B + k] += ga[k] * V.va[k] * wt[q];
-            if (gz) {
+            if (gpos) {
                 uint32_t ia = s.idx[3 * V.tri], ib = s.idx[3 * V.tri + 1], ic = s.idx[3 * V.tri + 2];
                 V3d A{s.pos[ia].x, s.pos[ia].y, s.pos[ia].z}, Bv{s.pos[ib].x, s.pos[ib].y, s.pos[ib].z};
                 V3d Cv{s.pos[ic].x, s.pos[ic].y, s.pos[ic].z};
-                V3d a = A - Bv, bb = Cv - A;
-                V3d n = crossd(a, bb);
-                double ln = std::sqrt(dotd(n, n));
-                V3d nh{n.x / ln, n.y / ln, n.z / ln};
-                V3d dn[3] = {V3d{-bb.y - a.y, bb.x + a.x, 0}, V3d{bb.y, -bb.x, 0}, V3d{a.y, -a.x, 0}};
+                const V3d gN{V.gn[0], V.gn[1], V.gn[2]};
+                const double wA = 1.0 - (double)V.w0 - (double)V.w1;
+                V3d gp[3] = {V3d{0, 0, 0}, V3d{0, 0, 0}, V3d{0, 0, 0}};   // A, B, C
+                double e0 = 0, e1 = 0;   // dL/dw0, dL/dw1 through the interpolated normal
+                if (!o.smooth_shading) {
+                    // N = -n/|n|, n = cross(a, bb): dL/dn, then dL/da = bb x dL/dn, dL/dbb = dL/dn x a
+                    V3d a = A - Bv, bb = Cv - A;
+                    V3d n = crossd(a, bb);
+                    double ln = std::sqrt(dotd(n, n));
+                    if (ln > 0) {
+                        V3d nh = muld(n, 1.0 / ln);
+                        V3d gn = muld(subd(gN, muld(nh, dotd(nh, gN))), -1.0 / ln);
+                        V3d ga_ = crossd(bb, gn), gb_ = crossd(gn, a);
+                        gp[0] = subd(ga_, gb_); gp[1] = muld(ga_, -1.0); gp[2] = gb_;
+                    }
+                } else {
+                    // N = S/|S|, S = w0 n_B + w1 n_C + wA n_A
+                    V3d nA = v3d(s.nrm[ia]), nB = v3d(s.nrm[ib]), nC = v3d(s.nrm[ic]);
+                    V3d S = addd(addd(muld(nB, V.w0), muld(nC, V.w1)), muld(nA, wA));
+                    double lS = std::sqrt(dotd(S, S));
+                    if (lS > 0) {
+                        V3d Nn = muld(S, 1.0 / lS);
+                        V3d gS = muld(subd(gN, muld(Nn, dotd(Nn, gN))), 1.0 / lS);
+                        e0 = dotd(gS, subd(nB, nA));
+                        e1 = dotd(gS, subd(nC, nA));
+                        const uint32_t vid[3] = {ia, ib, ic};
+                        const double wv[3] = {wA, V.w0, V.w1};
+                        for (int q = 0; q < 3; ++q) {
+                            gvn[3 * (size_t)vid[q] + 0] += wv[q] * gS.x;
+                            gvn[3 * (size_t)vid[q] + 1] += wv[q] * gS.y;
+                            gvn[3 * (size_t)vid[q] + 2] += wv[q] * gS.z;
+                        }
+                    }
+                }
                 const float* uvA = &s.uv[2 * ia]; const float* uvB = &s.uv[2 * ib]; const float* uvC = &s.uv[2 * ic];
                 double d0 = 0, d1 = 0;
                 for (uint32_t k = 0; k < B; ++k) {
@@ -1223,15 +1266,15 @@ static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light
                     d0 += ga[k] * ((aB - aA) * V.tex[k] + (double)V.va[k] * dt0);
                     d1 += ga[k] * ((aC - aA) * V.tex[k] + (double)V.va[k] * dt1);
                 }
-                double wv[3] = {1.0 - (double)V.w0 - (double)V.w1, V.w0, V.w1};
+                d0 += e0;
+                d1 += e1;
+                double wv[3] = {wA, V.w0, V.w1};
                 uint32_t vid[3] = {ia, ib, ic};
-                for (int q = 0; q < 3; ++q) {
-                    double nd = dotd(nh, dn[q]);
-                    double dN[3] = {-(dn[q].x - nh.x * nd) / ln, -(dn[q].y - nh.y * nd) / ln, -(dn[q].z - nh.z * nd) / ln};
-                    double gq = V.gn[0] * dN[0] + V.gn[1] * dN[1] + V.gn[2] * dN[2];
-                    gq += (d0 * V.m1 + d1 * V.m2) * wv[q];
-                    gz[vid[q]] += gq;
-                }
+                for (int q = 0; q < 3; ++q)
+                    for (int a = 0; a < 3; ++a) {
+                        const double gpa = a == 0 ? gp[q].x : (a == 1 ? gp[q].y : gp[q].z);
+                        gpos[3 * (size_t)vid[q] + a] += gpa + (d0 * V.m[a][0] + d1 * V.m[a][1]) * wv[q];
+                    }
             }
         }
     }
@@ -1239,20 +1282,63 @@ static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light
 
 }  // namespace
 
-// Adds the FP64 gradients of sum(dL/dI * I) into gtex ([th][tw][B]) and gz (per vertex).
-OAPI int oracle_adjoint(void* h, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
-                        const vgb_pt_options* opts, const float* dldi, double* gtex, double* gz, int nthreads) {
+// Vertex-normal gradients to position gradients (FP64): n_v = A_v/|A_v|, A_v the sum of the
+// unit normals u_f of the faces of v (vgb_compute_vertex_normals), u_f = c/|c|,
+// c = cross(p1 - p0, p2 - p0).
+static void vnormal_backward(const Scene& s, const double* gvn, double* gpos) {
+    std::vector<V3d> A(s.nverts, V3d{0, 0, 0});
+    auto face = [&](uint32_t t, V3d& e1, V3d& e2, V3d& c, double& lc) {
+        V3d p0 = v3d(s.pos[s.idx[3 * t]]), p1 = v3d(s.pos[s.idx[3 * t + 1]]), p2 = v3d(s.pos[s.idx[3 * t + 2]]);
+        if (std::isinf(p0.x) || std::isinf(p1.x) || std::isinf(p2.x)) return false;
+        e1 = subd(p1, p0); e2 = subd(p2, p0);
+        c = crossd(e1, e2);
+        lc = std::sqrt(dotd(c, c));
+        return lc > 0;
+    };
+    for (uint32_t t = 0; t < s.ntris; ++t) {
+        V3d e1, e2, c; double lc;
+        if (!face(t, e1, e2, c, lc)) continue;
+        for (int q = 0; q < 3; ++q) A[s.idx[3 * t + q]] = addd(A[s.idx[3 * t + q]], muld(c, 1.0 / lc));
+    }
+    for (uint32_t t = 0; t < s.ntris; ++t) {
+        V3d e1, e2, c; double lc;
+        if (!face(t, e1, e2, c, lc)) continue;
+        V3d gu{0, 0, 0};
+        for (int q = 0; q < 3; ++q) {
+            const uint32_t v = s.idx[3 * t + q];
+            double la = std::sqrt(dotd(A[v], A[v]));
+            if (!(la > 0)) continue;
+            V3d n = muld(A[v], 1.0 / la), G{gvn[3 * (size_t)v], gvn[3 * (size_t)v + 1], gvn[3 * (size_t)v + 2]};
+            gu = addd(gu, muld(subd(G, muld(n, dotd(n, G))), 1.0 / la));
+        }
+        V3d u = muld(c, 1.0 / lc);
+        V3d gc = muld(subd(gu, muld(u, dotd(u, gu))), 1.0 / lc);
+        V3d g1 = crossd(e2, gc), g2 = crossd(gc, e1), g0 = muld(addd(g1, g2), -1.0);
+        const V3d gq[3] = {g0, g1, g2};
+        for (int q = 0; q < 3; ++q) {
+            const size_t o = 3 * (size_t)s.idx[3 * t + q];
+            gpos[o] += gq[q].x; gpos[o + 1] += gq[q].y; gpos[o + 2] += gq[q].z;
+        }
+    }
+}
+
+// Adds the FP64 gradients of sum(dL/dI * I) into gtex ([th][tw][B]) and gpos ([nverts][3]).
+OAPI int oracle_adjoint_positions(void* h, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                                  const vgb_pt_options* opts, const float* dldi, double* gtex, double* gpos,
+                                  int nthreads) {
     if (!h || !cam || !opts || !dldi || opts->samples == 0) return 1;
     const Scene& s = *static_cast<Scene*>(h);
     if (opts->nbands != s.nbands || opts->bounces > 3) return 1;
     const uint32_t W = cam->width, H = cam->height, B = s.nbands;
-    const size_t npix = (size_t)W * H, ntex = (size_t)s.tw * s.th * B;
+    const size_t npix = (size_t)W * H, ntex = (size_t)s.tw * s.th * B, n3 = 3 * (size_t)s.nverts;
+    const bool smooth = gpos && opts->smooth_shading;
     int nt = std::max(1, nthreads);
-    std::vector<std::vector<double>> tb(nt), zb(nt);
+    std::vector<std::vector<double>> tb(nt), pb(nt), nb(nt);
     std::atomic<uint32_t> next{0};
     auto work = [&](int tid) {
         if (gtex) tb[tid].assign(ntex, 0.0);
-        if (gz) zb[tid].assign(s.nverts, 0.0);
+        if (gpos) pb[tid].assign(n3, 0.0);
+        if (smooth) nb[tid].assign(n3, 0.0);
         while (true) {
             uint32_t j = next.fetch_add(1);
             if (j >= H) break;
@@ -1264,16 +1350,31 @@ OAPI int oracle_adjoint(void* h, const vgb_camera* cam, const vgb_light* lights,
                     any |= g[k] != 0.0;
                 }
                 if (any) adjoint_pixel(s, *cam, lights, nlights, *opts, i, j, g, gtex ? tb[tid].data() : nullptr,
-                                       gz ? zb[tid].data() : nullptr);
+                                       gpos ? pb[tid].data() : nullptr, smooth ? nb[tid].data() : nullptr);
             }
         }
     };
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t) th.emplace_back(work, t);
     for (auto& x : th) x.join();
+    std::vector<double> gvn(smooth ? n3 : 0, 0.0);
     for (int t = 0; t < nt; ++t) {
         if (gtex) for (size_t q = 0; q < ntex; ++q) gtex[q] += tb[t][q];
-        if (gz) for (size_t q = 0; q < s.nverts; ++q) gz[q] += zb[t][q];
+        if (gpos) for (size_t q = 0; q < n3; ++q) gpos[q] += pb[t][q];
+        if (smooth) for (size_t q = 0; q < n3; ++q) gvn[q] += nb[t][q];
     }
+    if (smooth) vnormal_backward(s, gvn.data(), gpos);
     return 0;
+}
+
+// Adds the FP64 gradients of sum(dL/dI * I) into gtex ([th][tw][B]) and gz (per vertex, z).
+OAPI int oracle_adjoint(void* h, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                        const vgb_pt_options* opts, const float* dldi, double* gtex, double* gz, int nthreads) {
+    if (!h) return 1;
+    const Scene& s = *static_cast<Scene*>(h);
+    std::vector<double> gp(gz ? 3 * (size_t)s.nverts : 0, 0.0);
+    int rc = oracle_adjoint_positions(h, cam, lights, nlights, opts, dldi, gtex, gz ? gp.data() : nullptr, nthreads);
+    if (rc == 0 && gz)
+        for (size_t v = 0; v < s.nverts; ++v) gz[v] += gp[3 * v + 2];
+    return rc;
 }

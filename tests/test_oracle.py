@@ -285,3 +285,72 @@ def test_oracle_adjoint_heights_translation_invariance():
     osc.close()
     assert np.abs(gz).max() > 0
     assert abs(gz.sum()) <= 1e-9 * np.abs(gz).sum() + 1e-12
+
+
+def test_oracle_position_adjoint_translation_invariance():
+    """With uniform albedo and flat shading, translating every vertex by one vector changes no
+    face normal, and a hit point sliding within its triangle keeps its normal: the position
+    gradients of every triangle, and so their sum, vanish in each axis.  (With smooth shading the
+    sliding hit point changes its interpolated normal, so there is no such invariance.)"""
+    for smooth in (False,):
+        scene, cam_id = workloads.path_traced(posts=33, tex=32, resolution=16, spp=1, bounces=0, rr_depth=0, seed=6)
+        scene.meshes[0].albedo_map = None
+        scene.meshes[0].set_smooth_shading(smooth)
+        f = scene.flatten()
+        cam = scene[cam_id].to_c(scene.origin, 8)
+        lights, nl = scene.c_lights()
+        opts = scene.pathtracer.c_options(scene)
+        osc = oracle.OracleScene.from_flat(f, 8)
+        g = np.ones((8, 16, 16), np.float32)
+        _, gp = osc.adjoint_positions(cam, lights, nl, opts, g, nverts=f["positions"].shape[0])
+        _, gz = osc.adjoint(cam, lights, nl, opts, g, nverts=f["positions"].shape[0])
+        osc.close()
+        assert np.abs(gp).max() > 0
+        assert np.all(np.abs(gp.sum(axis=0)) <= 1e-9 * np.abs(gp).sum(axis=0) + 1e-12)
+        assert np.allclose(gz, gp[:, 2], rtol=0, atol=1e-12 * np.abs(gz).max())
+
+
+def test_oracle_position_adjoint_matches_finite_differences():
+    """The FP64 position adjoint of sum(g * I) against central differences of the oracle's FP32
+    renders (step 2e-2 m) for flat and smooth shading; vertices whose step flips a shadow ray
+    (visibility, excluded by design) are the rare outliers."""
+    rng = np.random.default_rng(8)
+    for smooth in (False, True):
+        scene, cam_id = workloads.path_traced(posts=33, tex=32, resolution=24, spp=1, bounces=0, rr_depth=0, seed=7)
+        scene.meshes[0].albedo_map = None
+        scene.meshes[0].set_smooth_shading(smooth)
+        f = scene.flatten()
+        cam = scene[cam_id].to_c(scene.origin, 8)
+        lights, nl = scene.c_lights()
+        opts = scene.pathtracer.c_options(scene)
+        g = rng.uniform(0.5, 1.5, (8, 24, 24)).astype(np.float32)
+        osc = oracle.OracleScene.from_flat(f, 8)
+        _, gp = osc.adjoint_positions(cam, lights, nl, opts, g, nverts=f["positions"].shape[0])
+        osc.close()
+
+        def loss(pos):
+            ff = dict(f)
+            ff["positions"] = pos
+            ff["normals"] = oracle.compute_normals(pos, f["indices"])
+            o = oracle.OracleScene.from_flat(ff, 8)
+            planes, _ = o.render(cam, lights, nl, opts, threads=1)
+            o.close()
+            return float(np.sum(g.astype(np.float64) * planes["total_radiance"]))
+
+        flat_g = np.abs(gp).ravel()
+        cand = np.nonzero(flat_g > np.percentile(flat_g, 97))[0]
+        pick = rng.choice(cand, size=min(8, len(cand)), replace=False)
+        errs = []
+        h = 2e-2
+        for q in pick:
+            v, a = divmod(int(q), 3)
+            pp = f["positions"].copy()
+            pp[v, a] += h
+            lp = loss(pp)
+            pp[v, a] -= 2 * h
+            lm = loss(pp)
+            fd = (lp - lm) / (2 * h)
+            errs.append(abs(fd - gp[v, a]) / max(abs(fd), 1e-12))
+        errs = np.array(errs)
+        print("smooth" if smooth else "flat", "FD relative errors", np.round(errs, 5))
+        assert np.median(errs) <= 2e-2 and np.mean(errs <= 5e-2) >= 0.6, (smooth, np.round(errs, 4))

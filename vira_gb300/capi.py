@@ -66,6 +66,11 @@ class Frame(C.Structure):
                 ("frame", C.c_uint32), ("film", Film)]
 
 
+class View(C.Structure):
+    _fields_ = [("camera", Camera), ("lights", Light * 8), ("nlights", C.c_uint32), ("samples", C.c_uint32),
+                ("frame", C.c_uint32), ("pad", C.c_uint32), ("target", C.c_void_p), ("radiance", C.c_void_p)]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("autotune", C.c_uint32), ("use_graph", C.c_uint32), ("block_threads", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("tiles_per_grab", C.c_uint32)]
@@ -111,6 +116,8 @@ SIGNATURES = {
     "vgb_render_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), C.POINTER(BatchOptions)]),
     "vgb_batch_tuning": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
     "vgb_adjoint": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_adjoint_positions": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_render_adjoint_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), _P, _P, C.POINTER(C.c_double)]),
     "vgb_texture_update": (C.c_int, [_P, _P, _U32, _U32]),
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),

@@ -37,8 +37,8 @@ using namespace vgbd;
 #ifndef VGB_SHADE_MINB
 #define VGB_SHADE_MINB 4
 #endif
-// k_batch without bounces: 3 blocks of 256 threads cap it at 80 registers (a few spills outside
-// the traversal loop), measured faster on the trajectory workload than 128 registers.
+// k_batch without bounces: 3 blocks of 256 threads cap it at 80 registers (spills outside the
+// traversal loop), measured faster on the trajectory workload than 124 registers.
 #ifndef VGB_BATCH_DIRECT_MINB
 #define VGB_BATCH_DIRECT_MINB 3
 #endif
@@ -359,6 +359,27 @@ __device__ __forceinline__ bool continue_path(const vgb_light* lights, uint32_t 
 }
 
 // Camera::pixelToRay for the pixel of bounce-0 item `item` (8x4-pixel warp tiles).
+// Camera::pixelToRay for pixel (pi, pj) = slot: sample 0 through the pixel corner, later
+// samples jittered (camera.ipp:1126-1163, cpu_path_tracer.ipp:182-192).
+__device__ __forceinline__ void pixel_ray(const vgb_camera& cam, uint32_t pi, uint32_t pj, uint32_t slot,
+                                          uint32_t sample, uint32_t frame, uint32_t k0, uint32_t k1, F3& ro, F3& rd) {
+    float X = (float)pi, Y = (float)pj;
+    if (sample != 0) {
+        U4 jr = philox(U4{slot, sample, frame, kSlotJitter}, k0, k1);
+        X = X + u01(jr.x);
+        Y = Y + u01(jr.y);
+    }
+    const float* K = cam.kinv;
+    float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
+    float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
+    F3 dc{hx, cam.z_dir * hy, cam.z_dir};
+    const float* R = cam.rotation;
+    F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
+          (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
+    rd = normalize(dw);
+    ro = F3{cam.origin[0], cam.origin[1], cam.origin[2]};
+}
+
 __device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item, uint32_t sample, uint32_t& slot,
                                            F3& ro, F3& rd) {
     const uint32_t tile = item >> 5, ln = item & 31u;
@@ -366,21 +387,7 @@ __device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item,
     const uint32_t pi = tx * 8u + (ln & 7u), pj = ty * 4u + (ln >> 3);
     if (pi >= fp.cam.width || pj >= fp.cam.height) return false;
     slot = pj * fp.cam.width + pi;
-    float X = (float)pi, Y = (float)pj;
-    if (sample != 0) {
-        U4 jr = philox(U4{slot, sample, fp.opt.frame, kSlotJitter}, (uint32_t)fp.opt.seed, (uint32_t)(fp.opt.seed >> 32));
-        X = X + u01(jr.x);
-        Y = Y + u01(jr.y);
-    }
-    const float* K = fp.cam.kinv;
-    float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
-    float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-    F3 dc{hx, fp.cam.z_dir * hy, fp.cam.z_dir};
-    const float* R = fp.cam.rotation;
-    F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
-          (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
-    rd = normalize(dw);
-    ro = F3{fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]};
+    pixel_ray(fp.cam, pi, pj, slot, sample, fp.opt.frame, (uint32_t)fp.opt.seed, (uint32_t)(fp.opt.seed >> 32), ro, rd);
     return true;
 }
 
@@ -818,6 +825,12 @@ struct vgb_context {
     cudaGraphExec_t graph_exec = nullptr;
     uint64_t graph_key = 0;
     unsigned char graph_params_probe[1024] = {0};   // kernel parameters the graph was captured with
+    // adjoint
+    float* d_adj = nullptr;                  // [nverts][3] vertex-normal gradients, [nverts][3] normal sums,
+    size_t cap_adj = 0;                      //   [nverts][3] position gradients (z-only callers)
+    void* d_views = nullptr;                 // DevView table of vgb_render_adjoint_batch
+    size_t cap_views = 0;
+    double* d_loss = nullptr;
 };
 
 namespace {
@@ -1048,6 +1061,7 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     dfree(ctx->d_frames);
     if (ctx->h_frames) cudaFreeHost(ctx->h_frames);
+    dfree(ctx->d_adj); dfree(ctx->d_views); dfree(ctx->d_loss);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1604,29 +1618,22 @@ __device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ fram
 }
 
 // Shared-memory planes per lane of k_batch: arad[NB] adir[NB] aalb[NB] anrm[3] adep (the
-// pixel's sums over samples) | brad[NB] con[NB] alb[NB] prad[NB] (the current sample) | thr[NB]
-// (paths with bounces only).
-__host__ __device__ constexpr int batch_planes(int nb, bool direct) { return 7 * nb + 4 + (direct ? 0 : nb); }
+// pixel's sums over samples) | prad[NB] brad[NB] (the current sample).
+__host__ __device__ constexpr int batch_planes(int nb, bool) { return 5 * nb + 4; }
 
-// One persistent launch over every (frame, tile) item.  A warp owns an 8x4-pixel tile and each
-// lane runs its pixel's samples as a small state machine: camera ray -> closest hit -> one
-// occlusion ray per light -> continuation ray -> ...  Whatever state its lane is in, every ray of
-// the warp goes through the one traversal loop of the kernel, so a lane that finished its sample
-// early traces its next camera ray while its neighbours trace occlusion rays.  Accumulation
-// order and random streams are those of the wavefront path, so the film is bit-identical.
+// One persistent launch over every (frame, tile) item.  A warp owns an 8x4-pixel tile and loops
+// over its samples and bounces in step: every lane traces its closest-hit ray, then the
+// occlusion rays of its lights, so the lanes of a warp run the same traversal together.
+// Accumulation order and random streams are those of the wavefront path (bit-identical film).
+// DIRECT (no bounces) drops the continuation and its throughput.
 template <int NB, int L, bool DIRECT>
 __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_batch(const DevScene s, const DevFrame* __restrict__ frames, const __grid_constant__ BatchParams bp,
                         uint32_t* counter, uint32_t* errw, uint64_t* stats) {
     extern __shared__ float sm_acc[];
-    constexpr int PL = batch_planes(NB, DIRECT);
+    constexpr int PL = 5 * NB + 4;  // arad[NB] adir[NB] aalb[NB] anrm[3] adep | prad[NB] brad[NB]
     const int lane = threadIdx.x & 31;
     float* acc = sm_acc + (size_t)(threadIdx.x >> 5) * PL * 32;
 #define ACC(pl) acc[(pl) * 32 + lane]
-#define BRAD(k) ACC(3 * NB + 4 + (k))
-#define CON(k) ACC(4 * NB + 4 + (k))
-#define ALB(k) ACC(5 * NB + 4 + (k))
-#define PRAD(k) ACC(6 * NB + 4 + (k))
-#define THR(k) (DIRECT ? 1.f : ACC(7 * NB + 4 + (k)))
     const uint32_t nb = bp.nb;
     const vgb_pt_options& opt = bp.opt;
     const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
@@ -1646,17 +1653,14 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
             const uint32_t tx = tile % F.tiles_x, ty = tile / F.tiles_x;
             const uint32_t pi = tx * 8u + (lane & 7u), pj = ty * 4u + (lane >> 3);
             const uint32_t W = F.cam.width, H = F.cam.height;
-            const bool valid = pi < W && pj < H;
+            if (pi >= W || pj >= H) continue;
             const uint32_t slot = pj * W + pi;
 #pragma unroll
-            for (int p = 0; p < 3 * NB + 4; ++p) acc[p * 32 + lane] = 0.f;
-            uint32_t first_tri = VGB_NO_HIT, count = 0;
-            uint32_t sample = 0, bounce = 0, l = 0, pend = 0;
-            bool active = valid && F.samples > 0, shadow = false;
-            F3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 1.f}, Pp{0.f, 0.f, 0.f}, N{0.f, 0.f, 1.f}, Ld{0.f, 0.f, 1.f};
-            float dist = 0.f;
-            // a new sample: camera_ray with this frame's camera and key, unit throughput
-            auto start_sample = [&]() {
+            for (int p = 0; p < PL; ++p) acc[p * 32 + lane] = 0.f;
+            uint32_t first_tri = VGB_NO_HIT;
+            uint32_t count = 0;
+            for (uint32_t sample = 0; sample < F.samples; ++sample) {
+                // camera ray (camera_ray with this frame's camera and key)
                 float X = (float)pi, Y = (float)pj;
                 if (sample != 0) {
                     U4 jr = philox(U4{slot, sample, F.frame, kSlotJitter}, k0, k1);
@@ -1670,33 +1674,28 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                 const float* R = F.cam.rotation;
                 const F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
                             (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
-                rd = normalize(dw);
-                ro = F3{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
+                F3 rd = normalize(dw);
+                F3 ro{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
+                float thr[NB], alb[NB];
+#define PRAD(k) acc[(3 * NB + 4 + (k)) * 32 + lane]
+#define BRAD(k) acc[(4 * NB + 4 + (k)) * 32 + lane]
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    PRAD(k) = 0.f;
-                    if (!DIRECT) ACC(7 * NB + 4 + k) = 1.f;
-                }
-                bounce = 0;
-                pend = 0;
-                shadow = false;
-            };
-            if (active) start_sample();
-            while (__any_sync(0xffffffffu, active)) {
-                if (!active) continue;
-                HitOut h;
-                h.U = h.V = h.W = 0.f; h.det = 1.f;
-                const WRay wr = make_wray(shadow ? Pp : ro, shadow ? Ld : rd);
-                traverse_layout_rt<L, false>(s.nodes, s.tris, wr, shadow ? dist : 0.f, shadow, h, err, cnt);
-                bool sample_done = false;
-                if (shadow) {
-                    nshadow++;
-                    if (h.id == VGB_NO_HIT) {
+                for (int k = 0; k < NB; ++k) { thr[k] = 1.f; PRAD(k) = 0.f; BRAD(k) = 0.f; }
+                uint32_t pend = 0;
+                const uint32_t last_bounce = DIRECT ? 0u : opt.bounces;
+                for (uint32_t bounce = 0; bounce <= last_bounce; ++bounce) {
+                    if (pend) {
 #pragma unroll
-                        for (int k = 0; k < NB; ++k) BRAD(k) += CON(k);
+                        for (int k = 0; k < NB; ++k) {
+                            PRAD(k) += BRAD(k);
+                            if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                        }
+                        pend = 0;
                     }
-                    ++l;
-                } else {
+                    HitOut h;
+                    h.U = h.V = h.W = 0.f; h.det = 1.f;
+                    const WRay wr = make_wray(ro, rd);
+                    traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
@@ -1712,111 +1711,80 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                             for (int k = 0; k < NB; ++k) {
                                 const float bgv = opt.background[k];
                                 float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
-                                PRAD(k) = PRAD(k) + THR(k) * (bg * 1.f);
+                                PRAD(k) = PRAD(k) + thr[k] * (bg * 1.f);
                             }
                         }
-                        sample_done = true;
-                    } else {
-                        const float rcp = 1.0f / h.det;
-                        const float w0 = h.V * rcp, w1 = h.W * rcp;
-                        F3 fnrm, tg, bt;
-                        float alb[NB];
-                        surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
-                        if (bounce == 0) {
-                            if (first_tri == VGB_NO_HIT) first_tri = h.id;
-#pragma unroll
-                            for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
-                            ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
-                            ACC(3 * NB + 3) += h.t;
-                            count += 1u;
-                        }
-                        if (!opt.simulate_lighting) {
-                            sample_done = true;
-                        } else {
-                            Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
-#pragma unroll
-                            for (int k = 0; k < NB; ++k) {
-                                BRAD(k) = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + THR(k) * (opt.ambient[k] * alb[k]) : 0.f;
-                                ALB(k) = alb[k];
-                            }
-                            pend = (bounce == 0) ? 1u : 2u;
-                            l = 0;
-                        }
+                        break;
                     }
-                }
-                if (!sample_done) {
-                    // the next light that needs an occlusion ray (nee_light, contribution kept
-                    // until the ray is found clear)
-                    shadow = false;
-                    while (l < F.nlights) {
-                        U4 rl = philox(U4{slot, sample, F.frame, (bounce << 8) | (l == 0 ? (uint32_t)kSlotMain : 1u + l)}, k0, k1);
-                        float lpdf = 0.f;
-                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, u01(rl.x), u01(rl.y), Ld, dist, lpdf);
+                    const float rcp = 1.0f / h.det;
+                    const float w0 = h.V * rcp, w1 = h.W * rcp;
+                    F3 Pp, N, fnrm, tg, bt;
+                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
+                    if (bounce == 0) {
+                        if (first_tri == VGB_NO_HIT) first_tri = h.id;
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
+                        ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
+                        ACC(3 * NB + 3) += h.t;
+                        count += 1u;
+                    }
+                    if (!opt.simulate_lighting) break;
+                    Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                    for (int k = 0; k < NB; ++k)
+                        BRAD(k) = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * alb[k]) : 0.f;
+                    pend = (bounce == 0) ? 1u : 2u;
+                    const U4 r0 = philox(U4{slot, sample, F.frame, (bounce << 8) | kSlotMain}, k0, k1);
+                    for (uint32_t l = 0; l < F.nlights; ++l) {
+                        float ru1, ru2;
+                        if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                        else {
+                            U4 rl = philox(U4{slot, sample, F.frame, (bounce << 8) | (1u + l)}, k0, k1);
+                            ru1 = u01(rl.x); ru2 = u01(rl.y);
+                        }
+                        // nee_light, with the contribution formed only once the shadow ray is clear
+                        F3 Ld; float dist, lpdf = 0.f;
+                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
                         if (lpdf > 0) {
-                            const float nl = dot(N, Ld);
-                            const float cos_t = smax(0.0f, dot(Ld, N));
-                            const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
-                            const float wgt = power_heuristic(lpdf, mpdf);
-#pragma unroll
-                            for (int k = 0; k < NB; ++k) {
-                                const float bsdf = ALB(k) * kInvPi * smax(nl, 0.f);
-                                CON(k) = (k < (int)nb) ? THR(k) * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
-                            }
-                            shadow = true;
-                            break;
-                        }
-                        ++l;
-                    }
-                    if (!shadow) {
-                        // every light of this vertex is done: continue the path or end the sample
-                        if (DIRECT || bounce >= opt.bounces) {
-                            sample_done = true;
-                        } else {
-                            const U4 r0 = philox(U4{slot, sample, F.frame, (bounce << 8) | kSlotMain}, k0, k1);
-                            F3 tg, bt;
-                            tangent_frame(N, tg, bt);
-                            float alb[NB], thr[NB];
-#pragma unroll
-                            for (int k = 0; k < NB; ++k) { alb[k] = ALB(k); thr[k] = THR(k); }
-                            bool new_ray = false;
-                            F3 nd;
-                            const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0,
-                                                                slot, sample, F.frame, bounce, nd, new_ray);
-                            if (!DIRECT) {
-#pragma unroll
-                                for (int k = 0; k < NB; ++k) ACC(7 * NB + 4 + k) = thr[k];
-                            }
-                            if (!cont) {
-                                sample_done = true;
-                            } else {
-                                if (new_ray) { ro = Pp; rd = nd; }
+                            HitOut hs;
+                            const WRay ws = make_wray(Pp, Ld);
+                            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+                            nshadow++;
+                            if (hs.id == VGB_NO_HIT) {
+                                const float nl = dot(N, Ld);
+                                const float cos_t = smax(0.0f, dot(Ld, N));
+                                const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                                const float wgt = power_heuristic(lpdf, mpdf);
 #pragma unroll
                                 for (int k = 0; k < NB; ++k) {
-                                    PRAD(k) += BRAD(k);
-                                    if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
+                                    const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+                                    const float con = (k < (int)nb) ? thr[k] * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                                    BRAD(k) += con;
                                 }
-                                pend = 0;
-                                ++bounce;
                             }
                         }
                     }
+                    if (DIRECT || bounce >= opt.bounces) break;
+                    bool new_ray = false;
+                    F3 nd;
+                    const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0, slot,
+                                                        sample, F.frame, bounce, nd, new_ray);
+                    if (!cont) break;
+                    if (new_ray) { ro = Pp; rd = nd; }
                 }
-                if (sample_done) {
+                if (pend) {
 #pragma unroll
                     for (int k = 0; k < NB; ++k) {
-                        if (pend) {
-                            PRAD(k) += BRAD(k);
-                            if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
-                        }
-                        if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
+                        PRAD(k) += BRAD(k);
+                        if (pend == 1u && k < (int)nb) ACC(NB + k) += BRAD(k);
                     }
-                    pend = 0;
-                    if (++sample < F.samples) start_sample();
-                    else active = false;
                 }
+#pragma unroll
+                for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
+#undef PRAD
+#undef BRAD
             }
             // RenderPasses::updateImages for this pixel
-            if (!valid) continue;
             const size_t P = (size_t)W * H;
             const float sf = (float)F.samples;
             const FilmOut& f = F.film;
@@ -1841,11 +1809,6 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
             if (f.tri) f.tri[slot] = first_tri;
         }
     }
-#undef THR
-#undef PRAD
-#undef ALB
-#undef CON
-#undef BRAD
 #undef ACC
     if (err) atomicOr(errw, err);
     warp_reduce_add(&stats[2], nclosest);
@@ -1954,7 +1917,7 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
     bp.nb = ctx->nbands;
     bp.total_tiles = (uint32_t)total_tiles;
     const DevFrame* dfr = static_cast<const DevFrame*>(ctx->d_frames);
-    uint32_t threads = bo && bo->block_threads ? bo->block_threads : (ctx->tuned_threads ? ctx->tuned_threads : 128);
+    uint32_t threads = bo && bo->block_threads ? bo->block_threads : (ctx->tuned_threads ? ctx->tuned_threads : 256);
     uint32_t bps = bo && bo->blocks_per_sm ? bo->blocks_per_sm : (ctx->tuned_bps ? ctx->tuned_bps : 4);
     uint32_t grab = bo && bo->tiles_per_grab ? bo->tiles_per_grab : (ctx->tuned_grab ? ctx->tuned_grab : 1);
     if (threads != 64 && threads != 128 && threads != 256)
@@ -2028,17 +1991,18 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
 
 
 // ====================================================================== adjoint (path replay)
-// Gradients of the loss L(I) with respect to the albedo texels and the vertex heights (z),
-// given dL/dI for the total-radiance planes of a frame.  Each pixel sample's path is replayed
-// from its random stream (nothing is stored between the forward render and this pass), its
-// vertices are kept in registers/local memory for the length of the path, and the gradients
-// are scattered with atomics:
-//   albedo   every contribution at or after vertex b is linear in alb_b, so
-//            dI/d alb_b = (suffix radiance from b) / alb_b, then through alb = va * bilinear(tex)
-//   heights  the shading normal (flat shading: the hit triangle's face normal) in every NEE term,
-//            d C / d(N.L) = C (2 / (N.L) + w'/w), and the motion of the hit point on the triangle
-//            (barycentrics, hence uv and the interpolated albedo) for a fixed ray,
-//            d[t, b1, b2]/dz_i = b_i * M^-1 e_z with M = [d | A-B | A-C].
+// Gradients of the loss L(I) with respect to the albedo texels and the vertex positions, given
+// dL/dI for the total-radiance planes.  Each pixel sample's path is replayed from its random
+// stream (nothing is stored between the forward render and this pass), its vertices are kept
+// in local memory for the length of the path, and the gradients are scattered with atomics:
+//   albedo     every contribution at or after vertex b is linear in alb_b, so
+//              dI/d alb_b = (suffix radiance from b) / alb_b, then through alb = va * bilinear(tex)
+//   positions  the shading normal N in every NEE term, d C / d(N.L) = C (2 / (N.L) + w'/w),
+//              back through the face normal (flat shading) or through N = normalize(sum w_i n_i)
+//              to the vertex normals n_i (smooth shading; k_vnormal_backward carries those to
+//              the positions of each vertex's 1-ring); and the motion of the hit point on the
+//              triangle for a fixed ray, d[t, b1, b2]/dp_q = w_q M^-1 (M = [d | A-B | A-C]),
+//              which moves the texture coordinates, the interpolated albedo and normal.
 // Excluded and stated: visibility (shadow and silhouette edges), the rotation of the sampled
 // continuation direction with the normal, the motion of the shading point (light direction and
 // shadow-ray origin), and Russian roulette decisions.
@@ -2050,28 +2014,270 @@ template <int NB>
 struct AdjVtx {
     uint32_t tri;
     float w0, w1;
-    float m1, m2;       // M^-1 e_z, barycentric components
+    float m[3][2];        // M^-1 e_a for a = x, y, z: the barycentric components (b1, b2)
     float uvx, uvy;
     float gnx, gny, gnz;  // dL/dN at this vertex (already weighted by dL/dI)
     float alb[NB], va[NB], tex[NB], rad[NB];
 };
 
+struct AdjOut {
+    float* gtex;        // [th][tw][B] or null
+    float* gpos;        // [nverts][3] or null
+    float* gvn;         // [nverts][3] vertex-normal gradients (smooth shading) or null
+};
+
+// Replays one pixel sample and records its path vertices; returns their number.  `g` (dL/dI
+// per band, already divided by the sample count) may be null: no normal gradients are formed.
+// prad receives the sample's path radiance, summed in the order of the forward renderer.
+template <int NB, int L>
+__device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& cam, const vgb_light* lights,
+                                          uint32_t nlights, const vgb_pt_options& opt, uint32_t nb, uint32_t pi,
+                                          uint32_t pj, uint32_t slot, uint32_t sample, uint32_t frame,
+                                          const float* g, AdjVtx<NB>* vx, float* bgc, float* prad,
+                                          uint32_t& err, uint32_t& nrays) {
+    const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
+    Counters cnt{0, 0};
+    F3 ro, rd;
+    pixel_ray(cam, pi, pj, slot, sample, frame, k0, k1, ro, rd);
+    float thr[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) { thr[k] = 1.f; bgc[k] = 0.f; prad[k] = 0.f; }
+    int nv = 0;
+    for (uint32_t bounce = 0; bounce <= opt.bounces && nv < kAdjMaxVerts; ++bounce) {
+        HitOut h;
+        h.U = h.V = h.W = 0.f; h.det = 1.f;
+        const WRay wr = make_wray(ro, rd);
+        traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+        nrays++;
+        if (h.id == VGB_NO_HIT) {
+            if (opt.simulate_lighting && opt.show_background) {
+                float x = rd.x, y = rd.y, z = rd.z;
+                float u = atan2f(y, x) / (2 * kPi);
+                float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+                float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+                if (px < 0) px += 1.f;
+                if (py < 0) py += 1.f;
+                float a = (1.f - px) * (1.f - py), b = px * (1.f - py), c = (1.f - px) * py, e = px * py;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    const float bgv = opt.background[k];
+                    bgc[k] = thr[k] * ((((a * bgv + b * bgv) + c * bgv) + e * bgv) * 1.f);
+                    prad[k] = prad[k] + bgc[k];
+                }
+            }
+            break;
+        }
+        AdjVtx<NB>& V = vx[nv++];
+        const float rcp = 1.0f / h.det;
+        V.tri = h.id;
+        V.w0 = h.V * rcp;
+        V.w1 = h.W * rcp;
+        F3 Pp, N, fnrm, tg, bt;
+        float uv[2];
+        surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, V.w0, V.w1, Pp, N, fnrm, tg, bt, V.alb, V.va, V.tex, uv);
+        V.uvx = uv[0]; V.uvy = uv[1];
+        if (g) {
+            // M^-1 e_a for the hit-point motion (caller order A=v0, B=v1, C=v2), by Cramer's rule:
+            // b1 = det[d, e_a, c2] / det, b2 = det[d, c1, e_a] / det
+            const uint32_t ia = __ldg(&s.idx[3 * h.id]), ib = __ldg(&s.idx[3 * h.id + 1]), ic = __ldg(&s.idx[3 * h.id + 2]);
+            const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
+            const F3 c1 = A - B, c2 = A - C;
+            const float det = dot(rd, cross(c1, c2));
+            const float idet = (det != 0.f) ? 1.f / det : 0.f;
+            const F3 u1 = cross(c2, rd), u2 = cross(rd, c1);  // det[d, e_a, c2] = e_a . (c2 x d)
+            V.m[0][0] = u1.x * idet; V.m[1][0] = u1.y * idet; V.m[2][0] = u1.z * idet;
+            V.m[0][1] = u2.x * idet; V.m[1][1] = u2.y * idet; V.m[2][1] = u2.z * idet;
+        }
+        V.gnx = V.gny = V.gnz = 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) V.rad[k] = 0.f;
+        if (!opt.simulate_lighting) break;
+        Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+        for (int k = 0; k < NB; ++k)
+            V.rad[k] = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * V.alb[k]) : 0.f;
+        const U4 r0 = philox(U4{slot, sample, frame, (bounce << 8) | kSlotMain}, k0, k1);
+        for (uint32_t l = 0; l < nlights; ++l) {
+            float ru1, ru2;
+            if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+            else {
+                U4 rl = philox(U4{slot, sample, frame, (bounce << 8) | (1u + l)}, k0, k1);
+                ru1 = u01(rl.x); ru2 = u01(rl.y);
+            }
+            F3 Ld; float dist, lpdf = 0.f;
+            light_sample(lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+            if (!(lpdf > 0)) continue;
+            HitOut hs;
+            const WRay ws = make_wray(Pp, Ld);
+            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+            nrays++;
+            if (hs.id != VGB_NO_HIT) continue;
+            const float nl = dot(N, Ld);
+            const float cos_t = smax(0.0f, dot(Ld, N));
+            const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+            const float wgt = power_heuristic(lpdf, mpdf);
+            float gc = 0.f;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                const float bsdf = V.alb[k] * kInvPi * smax(nl, 0.f);
+                const float con = (k < (int)nb) ? thr[k] * bsdf * lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                V.rad[k] += con;
+                if (g) gc += g[k] * con;
+            }
+            if (g && nl > 0.f && wgt > 0.f) {
+                // d/dc of c^2 w(c) with w = lp^2 / (lp^2 + (c/pi)^2)
+                const float m = nl * kInvPi;
+                const float dw_over_w = -2.f * m * kInvPi / (lpdf * lpdf + m * m);
+                const float s_c = gc * (2.f / nl + dw_over_w);
+                V.gnx += s_c * Ld.x; V.gny += s_c * Ld.y; V.gnz += s_c * Ld.z;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NB; ++k) prad[k] = prad[k] + V.rad[k];
+        if (bounce >= opt.bounces) break;
+        bool new_ray = false;
+        F3 nd;
+        const bool cont = continue_path<NB>(lights, nlights, opt, nb, Pp, N, tg, bt, V.alb, thr, r0, slot, sample,
+                                            frame, bounce, nd, new_ray);
+        if (!cont) break;
+        if (new_ray) { ro = Pp; rd = nd; }
+    }
+    return nv;
+}
+
+// Backward over the recorded vertices of one sample: suffix radiance, then the scatter.
+template <int NB>
+__device__ __forceinline__ void adj_scatter(const DevScene& s, uint32_t nb, bool smooth, const AdjVtx<NB>* vx,
+                                            int nv, const float* bgc, const float* g, const AdjOut& out) {
+    float S[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) S[k] = bgc[k];
+    for (int b = nv - 1; b >= 0; --b) {
+        const AdjVtx<NB>& V = vx[b];
+        float ga[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            S[k] += V.rad[k];
+            ga[k] = (k < (int)nb && V.alb[k] != 0.f) ? g[k] * S[k] / V.alb[k] : 0.f;
+        }
+        // texel weights of sample_uvs at (uvx, uvy)
+        const float rx = (float)s.tw, ry = (float)s.th;
+        float px = fmodf(V.uvx * rx, rx), py = fmodf(V.uvy * ry, ry);
+        if (px < 0) px += rx;
+        if (py < 0) py += ry;
+        int x0 = min((int)floorf(px), (int)s.tw - 1), y0 = min((int)floorf(py), (int)s.th - 1);
+        int x1 = min(x0 + 1, (int)s.tw - 1), y1 = min(y0 + 1, (int)s.th - 1);
+        const float dx = px - (float)x0, dy = py - (float)y0;
+        const float wt[4] = {(1.f - dx) * (1.f - dy), dx * (1.f - dy), (1.f - dx) * dy, dx * dy};
+        const size_t tx[4] = {(size_t)y0 * s.tw + x0, (size_t)y0 * s.tw + x1, (size_t)y1 * s.tw + x0,
+                              (size_t)y1 * s.tw + x1};
+        if (out.gtex) {
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k >= (int)nb || ga[k] == 0.f) continue;
+                const float base = ga[k] * V.va[k];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (wt[q] != 0.f) atomicAdd(&out.gtex[tx[q] * nb + k], base * wt[q]);
+            }
+        }
+        if (!out.gpos) continue;
+        const uint32_t ia = __ldg(&s.idx[3 * V.tri]), ib = __ldg(&s.idx[3 * V.tri + 1]), ic = __ldg(&s.idx[3 * V.tri + 2]);
+        const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
+        const F3 gN{V.gnx, V.gny, V.gnz};
+        // dL/d(w0, w1) through the albedo (vertex albedo and texture coordinates)
+        const float2 uvA = __ldg(&s.vuv[ia]), uvB = __ldg(&s.vuv[ib]), uvC = __ldg(&s.vuv[ic]);
+        float gw0 = 0.f, gw1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k >= (int)nb || ga[k] == 0.f) continue;
+            float t00, t10, t01, t11;
+            if (s.tex_mono) {
+                t00 = __ldg(&s.tex[tx[0]]); t10 = __ldg(&s.tex[tx[1]]);
+                t01 = __ldg(&s.tex[tx[2]]); t11 = __ldg(&s.tex[tx[3]]);
+            } else {
+                t00 = __ldg(&s.tex[tx[0] * nb + k]); t10 = __ldg(&s.tex[tx[1] * nb + k]);
+                t01 = __ldg(&s.tex[tx[2] * nb + k]); t11 = __ldg(&s.tex[tx[3] * nb + k]);
+            }
+            const float dtdx = (1.f - dy) * (t10 - t00) + dy * (t11 - t01);
+            const float dtdy = (1.f - dx) * (t01 - t00) + dx * (t11 - t10);
+            // d px / d w0 = rx * (uvB - uvA).x, ... (Interaction order: w0 ~ B, w1 ~ C)
+            const float dt_dw0 = dtdx * rx * (uvB.x - uvA.x) + dtdy * ry * (uvB.y - uvA.y);
+            const float dt_dw1 = dtdx * rx * (uvC.x - uvA.x) + dtdy * ry * (uvC.y - uvA.y);
+            float dva_dw0 = 0.f, dva_dw1 = 0.f;
+            if (!s.albedo_uniform) {
+                const float aA = __ldg(&s.valb[(size_t)ia * nb + k]), aB = __ldg(&s.valb[(size_t)ib * nb + k]);
+                const float aC = __ldg(&s.valb[(size_t)ic * nb + k]);
+                dva_dw0 = aB - aA; dva_dw1 = aC - aA;
+            }
+            gw0 += ga[k] * (dva_dw0 * V.tex[k] + V.va[k] * dt_dw0);
+            gw1 += ga[k] * (dva_dw1 * V.tex[k] + V.va[k] * dt_dw1);
+        }
+        F3 gp[3] = {F3{0.f, 0.f, 0.f}, F3{0.f, 0.f, 0.f}, F3{0.f, 0.f, 0.f}};  // A, B, C
+        const float wA = 1.0f - V.w0 - V.w1;
+        if (!smooth) {
+            // face normal N = -n/|n|, n = cross(a, bb), a = A-B, bb = C-A
+            const F3 a = A - B, bb = C - A;
+            const F3 n = cross(a, bb);
+            const float ln = length(n);
+            if (ln > 0.f) {
+                const F3 nh = n * (1.f / ln);
+                const F3 gn = (gN - nh * dot(nh, gN)) * (-1.f / ln);   // dL/dn
+                const F3 ga_ = cross(bb, gn), gb_ = cross(gn, a);       // dL/da, dL/dbb
+                gp[0] = ga_ - gb_; gp[1] = F3{0.f, 0.f, 0.f} - ga_; gp[2] = gb_;
+            }
+        } else {
+            // N = S/|S|, S = w0 n_B + w1 n_C + wA n_A (surface_at's order)
+            const F3 nA = ld3(__ldg(&s.vnrm[ia])), nB = ld3(__ldg(&s.vnrm[ib])), nC = ld3(__ldg(&s.vnrm[ic]));
+            const F3 Sv = (V.w0 * nB + V.w1 * nC) + wA * nA;
+            const float lS = length(Sv);
+            if (lS > 0.f && out.gvn) {
+                const F3 Nn = Sv * (1.f / lS);
+                const F3 gS = (gN - Nn * dot(Nn, gN)) * (1.f / lS);
+                gw0 += dot(gS, nB - nA);
+                gw1 += dot(gS, nC - nA);
+                const uint32_t vid[3] = {ia, ib, ic};
+                const float wv[3] = {wA, V.w0, V.w1};
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    if (wv[q] == 0.f) continue;
+                    atomicAdd(&out.gvn[3 * (size_t)vid[q] + 0], wv[q] * gS.x);
+                    atomicAdd(&out.gvn[3 * (size_t)vid[q] + 1], wv[q] * gS.y);
+                    atomicAdd(&out.gvn[3 * (size_t)vid[q] + 2], wv[q] * gS.z);
+                }
+            }
+        }
+        // hit-point motion: dL/dp_q,a = w_q (gw0 m_a1 + gw1 m_a2)
+        const F3 gm{gw0 * V.m[0][0] + gw1 * V.m[0][1], gw0 * V.m[1][0] + gw1 * V.m[1][1],
+                    gw0 * V.m[2][0] + gw1 * V.m[2][1]};
+        const uint32_t vid[3] = {ia, ib, ic};
+        const float wv[3] = {wA, V.w0, V.w1};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const F3 t = gp[q] + gm * wv[q];
+            if (t.x != 0.f) atomicAdd(&out.gpos[3 * (size_t)vid[q] + 0], t.x);
+            if (t.y != 0.f) atomicAdd(&out.gpos[3 * (size_t)vid[q] + 1], t.y);
+            if (t.z != 0.f) atomicAdd(&out.gpos[3 * (size_t)vid[q] + 2], t.z);
+        }
+    }
+}
+
 template <int NB, int L>
 __global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const __grid_constant__ FrameParams fp,
-                                                 const float* __restrict__ dldi, float* __restrict__ gtex,
-                                                 float* __restrict__ gz, uint32_t* errw, uint64_t* stats) {
+                                                 const float* __restrict__ dldi, const AdjOut out, uint32_t* errw,
+                                                 uint64_t* stats) {
     const uint32_t nb = fp.nb;
     const vgb_pt_options& opt = fp.opt;
-    const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
     const uint32_t npix = fp.cam.width * fp.cam.height;
     const uint32_t n_items = fp.tiles_x * fp.tiles_y * 32u;
     const float sf = (float)opt.samples;
+    const bool smooth = opt.smooth_shading != 0;
     uint32_t err = 0, nrays = 0;
-    Counters cnt{0, 0};
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n_items; item += gridDim.x * blockDim.x) {
-        uint32_t slot;
-        F3 ro0, rd0;
-        if (!camera_ray(fp, item, 0, slot, ro0, rd0)) continue;
+        const uint32_t tile = item >> 5, ln = item & 31u;
+        const uint32_t pi = (tile % fp.tiles_x) * 8u + (ln & 7u), pj = (tile / fp.tiles_x) * 4u + (ln >> 3);
+        if (pi >= fp.cam.width || pj >= fp.cam.height) continue;
+        const uint32_t slot = pj * fp.cam.width + pi;
         float g[NB];
         bool any = false;
 #pragma unroll
@@ -2081,224 +2287,249 @@ __global__ void __launch_bounds__(128) k_adjoint(const DevScene s, const __grid_
         }
         if (!any) continue;
         for (uint32_t sample = 0; sample < opt.samples; ++sample) {
-            F3 ro, rd;
-            camera_ray(fp, item, sample, slot, ro, rd);
             AdjVtx<NB> vx[kAdjMaxVerts];
-            float thr[NB], bgc[NB];
-#pragma unroll
-            for (int k = 0; k < NB; ++k) { thr[k] = 1.f; bgc[k] = 0.f; }
-            int nv = 0;
-            for (uint32_t bounce = 0; bounce <= opt.bounces && nv < kAdjMaxVerts; ++bounce) {
-                HitOut h;
-                h.U = h.V = h.W = 0.f; h.det = 1.f;
-                const WRay wr = make_wray(ro, rd);
-                traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
-                nrays++;
-                if (h.id == VGB_NO_HIT) {
-                    if (opt.simulate_lighting && opt.show_background) {
-                        float x = rd.x, y = rd.y, z = rd.z;
-                        float u = atan2f(y, x) / (2 * kPi);
-                        float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
-                        float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
-                        if (px < 0) px += 1.f;
-                        if (py < 0) py += 1.f;
-                        float a = (1.f - px) * (1.f - py), b = px * (1.f - py), c = (1.f - px) * py, e = px * py;
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) {
-                            const float bgv = opt.background[k];
-                            bgc[k] = thr[k] * ((((a * bgv + b * bgv) + c * bgv) + e * bgv) * 1.f);
-                        }
-                    }
-                    break;
-                }
-                AdjVtx<NB>& V = vx[nv++];
-                const float rcp = 1.0f / h.det;
-                V.tri = h.id;
-                V.w0 = h.V * rcp;
-                V.w1 = h.W * rcp;
-                F3 Pp, N, fnrm, tg, bt;
-                float uv[2];
-                surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, V.w0, V.w1, Pp, N, fnrm, tg, bt, V.alb, V.va, V.tex, uv);
-                V.uvx = uv[0]; V.uvy = uv[1];
-                // M^-1 e_z for the hit-point motion (caller order A=v0, B=v1, C=v2)
-                {
-                    const uint32_t ia = __ldg(&s.idx[3 * h.id]), ib = __ldg(&s.idx[3 * h.id + 1]), ic = __ldg(&s.idx[3 * h.id + 2]);
-                    const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
-                    const F3 c1 = A - B, c2 = A - C;
-                    const float det = dot(rd, cross(c1, c2));
-                    // Cramer: x1 = det[d, e_z, c2] / det, x2 = det[d, c1, e_z] / det
-                    const F3 ez{0.f, 0.f, 1.f};
-                    V.m1 = (det != 0.f) ? dot(rd, cross(ez, c2)) / det : 0.f;
-                    V.m2 = (det != 0.f) ? dot(rd, cross(c1, ez)) / det : 0.f;
-                }
-                V.gnx = V.gny = V.gnz = 0.f;
-#pragma unroll
-                for (int k = 0; k < NB; ++k) V.rad[k] = 0.f;
-                if (!opt.simulate_lighting) break;
-                Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
-#pragma unroll
-                for (int k = 0; k < NB; ++k)
-                    V.rad[k] = (bounce == 0 && opt.has_ambient && k < (int)nb) ? 0.f + thr[k] * (opt.ambient[k] * V.alb[k]) : 0.f;
-                const U4 r0 = philox(U4{slot, sample, opt.frame, (bounce << 8) | kSlotMain}, k0, k1);
-                for (uint32_t l = 0; l < fp.nlights; ++l) {
-                    float ru1, ru2;
-                    if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
-                    else {
-                        U4 rl = philox(U4{slot, sample, opt.frame, (bounce << 8) | (1u + l)}, k0, k1);
-                        ru1 = u01(rl.x); ru2 = u01(rl.y);
-                    }
-                    F3 Ld; float dist, lpdf = 0.f;
-                    light_sample(fp.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
-                    if (!(lpdf > 0)) continue;
-                    HitOut hs;
-                    const WRay ws = make_wray(Pp, Ld);
-                    traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
-                    nrays++;
-                    if (hs.id != VGB_NO_HIT) continue;
-                    const float nl = dot(N, Ld);
-                    const float cos_t = smax(0.0f, dot(Ld, N));
-                    const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
-                    const float wgt = power_heuristic(lpdf, mpdf);
-                    float gc = 0.f;
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) {
-                        const float bsdf = V.alb[k] * kInvPi * smax(nl, 0.f);
-                        const float con = (k < (int)nb) ? thr[k] * bsdf * fp.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
-                        V.rad[k] += con;
-                        gc += g[k] * con;
-                    }
-                    if (nl > 0.f && wgt > 0.f) {
-                        // d/dc of c^2 w(c) with w = lp^2 / (lp^2 + (c/pi)^2)
-                        const float m = nl * kInvPi;
-                        const float dw_over_w = -2.f * m * kInvPi / (lpdf * lpdf + m * m);
-                        const float s_c = gc * (2.f / nl + dw_over_w);
-                        V.gnx += s_c * Ld.x; V.gny += s_c * Ld.y; V.gnz += s_c * Ld.z;
-                    }
-                }
-                if (bounce >= opt.bounces) break;
-                bool new_ray = false;
-                F3 nd;
-                const bool cont = continue_path<NB>(fp.lights, fp.nlights, opt, nb, Pp, N, tg, bt, V.alb, thr, r0, slot,
-                                                    sample, opt.frame, bounce, nd, new_ray);
-                if (!cont) break;
-                if (new_ray) { ro = Pp; rd = nd; }
-                (void)fnrm;
-            }
-            // backward over the recorded vertices: suffix radiance, then scatter
-            float S[NB];
-#pragma unroll
-            for (int k = 0; k < NB; ++k) S[k] = bgc[k];
-            for (int b = nv - 1; b >= 0; --b) {
-                AdjVtx<NB>& V = vx[b];
-                float ga[NB];
-#pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    S[k] += V.rad[k];
-                    ga[k] = (k < (int)nb && V.alb[k] != 0.f) ? g[k] * S[k] / V.alb[k] : 0.f;
-                }
-                // texel weights of sample_uvs at (uvx, uvy)
-                const float rx = (float)s.tw, ry = (float)s.th;
-                float px = fmodf(V.uvx * rx, rx), py = fmodf(V.uvy * ry, ry);
-                if (px < 0) px += rx;
-                if (py < 0) py += ry;
-                int x0 = min((int)floorf(px), (int)s.tw - 1), y0 = min((int)floorf(py), (int)s.th - 1);
-                int x1 = min(x0 + 1, (int)s.tw - 1), y1 = min(y0 + 1, (int)s.th - 1);
-                const float dx = px - (float)x0, dy = py - (float)y0;
-                const float wt[4] = {(1.f - dx) * (1.f - dy), dx * (1.f - dy), (1.f - dx) * dy, dx * dy};
-                const size_t tx[4] = {(size_t)y0 * s.tw + x0, (size_t)y0 * s.tw + x1, (size_t)y1 * s.tw + x0,
-                                      (size_t)y1 * s.tw + x1};
-                if (gtex) {
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) {
-                        if (k >= (int)nb || ga[k] == 0.f) continue;
-                        const float base = ga[k] * V.va[k];
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            if (wt[q] != 0.f) atomicAdd(&gtex[tx[q] * nb + k], base * wt[q]);
-                    }
-                }
-                if (gz) {
-                    const uint32_t ia = __ldg(&s.idx[3 * V.tri]), ib = __ldg(&s.idx[3 * V.tri + 1]), ic = __ldg(&s.idx[3 * V.tri + 2]);
-                    const F3 A = ld3(__ldg(&s.vpos[ia])), B = ld3(__ldg(&s.vpos[ib])), C = ld3(__ldg(&s.vpos[ic]));
-                    // face normal N = -n/|n|, n = cross(A-B, C-A)
-                    const F3 a = A - B, bb = C - A;
-                    const F3 n = cross(a, bb);
-                    const float ln = length(n);
-                    const F3 nh = n * (1.f / ln);
-                    const F3 dn[3] = {F3{-bb.y - a.y, bb.x + a.x, 0.f}, F3{bb.y, -bb.x, 0.f}, F3{a.y, -a.x, 0.f}};
-                    const F3 gN{V.gnx, V.gny, V.gnz};
-                    // hit-point motion: d(albedo)/d(barycentrics)
-                    const float2 uvA = __ldg(&s.vuv[ia]), uvB = __ldg(&s.vuv[ib]), uvC = __ldg(&s.vuv[ic]);
-                    float dalb_dw0 = 0.f, dalb_dw1 = 0.f;  // sum_k ga[k] * d alb_k / d w0, / d w1
-                    {
-                        // texture derivative with respect to (px, py)
-#pragma unroll
-                        for (int k = 0; k < NB; ++k) {
-                            if (k >= (int)nb || ga[k] == 0.f) continue;
-                            float t00, t10, t01, t11;
-                            if (s.tex_mono) {
-                                t00 = __ldg(&s.tex[tx[0]]); t10 = __ldg(&s.tex[tx[1]]);
-                                t01 = __ldg(&s.tex[tx[2]]); t11 = __ldg(&s.tex[tx[3]]);
-                            } else {
-                                t00 = __ldg(&s.tex[tx[0] * nb + k]); t10 = __ldg(&s.tex[tx[1] * nb + k]);
-                                t01 = __ldg(&s.tex[tx[2] * nb + k]); t11 = __ldg(&s.tex[tx[3] * nb + k]);
-                            }
-                            const float dtdx = (1.f - dy) * (t10 - t00) + dy * (t11 - t01);
-                            const float dtdy = (1.f - dx) * (t01 - t00) + dx * (t11 - t10);
-                            // d px / d w0 = rx * (uvB - uvA).x, ... (Interaction order: w0 ~ B, w1 ~ C)
-                            const float dt_dw0 = dtdx * rx * (uvB.x - uvA.x) + dtdy * ry * (uvB.y - uvA.y);
-                            const float dt_dw1 = dtdx * rx * (uvC.x - uvA.x) + dtdy * ry * (uvC.y - uvA.y);
-                            float dva_dw0 = 0.f, dva_dw1 = 0.f;
-                            if (!s.albedo_uniform) {
-                                const float aA = __ldg(&s.valb[(size_t)ia * nb + k]), aB = __ldg(&s.valb[(size_t)ib * nb + k]);
-                                const float aC = __ldg(&s.valb[(size_t)ic * nb + k]);
-                                dva_dw0 = aB - aA; dva_dw1 = aC - aA;
-                            }
-                            dalb_dw0 += ga[k] * (dva_dw0 * V.tex[k] + V.va[k] * dt_dw0);
-                            dalb_dw1 += ga[k] * (dva_dw1 * V.tex[k] + V.va[k] * dt_dw1);
-                        }
-                    }
-                    const float wv[3] = {1.0f - V.w0 - V.w1, V.w0, V.w1};  // weights of A, B, C
-                    const uint32_t vid[3] = {ia, ib, ic};
-#pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        // normal term: dN = -(dn - nh (nh . dn)) / |n|
-                        const float nd = dot(nh, dn[q]);
-                        const F3 dN = (dn[q] - nh * nd) * (-1.f / ln);
-                        float gq = dot(gN, dN);
-                        // motion term
-                        gq += (dalb_dw0 * V.m1 + dalb_dw1 * V.m2) * wv[q];
-                        if (gq != 0.f) atomicAdd(&gz[vid[q]], gq);
-                    }
-                }
-            }
+            float bgc[NB], prad[NB];
+            const int nv = adj_replay<NB, L>(s, fp.cam, fp.lights, fp.nlights, opt, nb, pi, pj, slot, sample,
+                                             opt.frame, g, vx, bgc, prad, err, nrays);
+            adj_scatter<NB>(s, nb, smooth, vx, nv, bgc, g, out);
         }
     }
     if (err) atomicOr(errw, err);
     warp_reduce_add(&stats[2], nrays);
 }
 
-template <int NB, int L>
-void launch_adjoint(vgb_context* ctx, const FrameParams& fp, const float* dldi, float* gtex, float* gz) {
-    const uint32_t n = fp.tiles_x * fp.tiles_y * 32u;
-    const int g = grid_for(ctx, n, 16);
-    k_adjoint<NB, L><<<g, 128, 0, ctx->stream>>>(dev_scene(ctx), fp, dldi, gtex, gz, &ctx->d_counters[C_ERR], ctx->d_stats);
+// Sums of the unit face normals per vertex (vgb_compute_vertex_normals before its normalisation).
+__global__ void k_vnormal_sums(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t ntris,
+                               float* __restrict__ sums) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntris; t += gridDim.x * blockDim.x) {
+        const uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+        const F3 p0 = ld3(vpos[i0]), p1 = ld3(vpos[i1]), p2 = ld3(vpos[i2]);
+        if (isinf(p0.x) || isinf(p1.x) || isinf(p2.x)) continue;
+        const F3 c = cross(p1 - p0, p2 - p0);
+        const float lc = length(c);
+        if (!(lc > 0.f)) continue;
+        const F3 u = c * (1.f / lc);
+        const uint32_t v[3] = {i0, i1, i2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            atomicAdd(&sums[3 * (size_t)v[q] + 0], u.x);
+            atomicAdd(&sums[3 * (size_t)v[q] + 1], u.y);
+            atomicAdd(&sums[3 * (size_t)v[q] + 2], u.z);
+        }
+    }
 }
 
-}  // namespace
+// Vertex-normal gradients to position gradients.  n_v = A_v/|A_v|, A_v = sum of the unit face
+// normals u_f = c_f/|c_f|, c_f = cross(p1 - p0, p2 - p0) over the faces of v:
+// dL/dA_v = (G_v - n_v (n_v.G_v)) / |A_v|; per face dL/du_f = sum of dL/dA_v of its vertices,
+// dL/dc_f = (dL/du_f - u_f (u_f.dL/du_f)) / |c_f|, dL/de1 = e2 x dL/dc, dL/de2 = dL/dc x e1.
+__global__ void k_vnormal_backward(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t ntris,
+                                   const float* __restrict__ sums, const float* __restrict__ gvn,
+                                   float* __restrict__ gpos) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntris; t += gridDim.x * blockDim.x) {
+        const uint32_t v[3] = {idx[3 * t], idx[3 * t + 1], idx[3 * t + 2]};
+        const F3 p0 = ld3(vpos[v[0]]), p1 = ld3(vpos[v[1]]), p2 = ld3(vpos[v[2]]);
+        if (isinf(p0.x) || isinf(p1.x) || isinf(p2.x)) continue;
+        const F3 e1 = p1 - p0, e2 = p2 - p0;
+        const F3 c = cross(e1, e2);
+        const float lc = length(c);
+        if (!(lc > 0.f)) continue;
+        F3 gu{0.f, 0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const size_t o = 3 * (size_t)v[q];
+            const F3 Av{sums[o], sums[o + 1], sums[o + 2]};
+            const F3 G{gvn[o], gvn[o + 1], gvn[o + 2]};
+            const float la = length(Av);
+            if (!(la > 0.f)) continue;
+            const F3 n = Av * (1.f / la);
+            gu = gu + (G - n * dot(n, G)) * (1.f / la);
+        }
+        const F3 u = c * (1.f / lc);
+        const F3 gc = (gu - u * dot(u, gu)) * (1.f / lc);
+        const F3 g1 = cross(e2, gc), g2 = cross(gc, e1);
+        const F3 g0 = F3{0.f, 0.f, 0.f} - (g1 + g2);
+        const F3 gq[3] = {g0, g1, g2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const size_t o = 3 * (size_t)v[q];
+            if (gq[q].x != 0.f) atomicAdd(&gpos[o + 0], gq[q].x);
+            if (gq[q].y != 0.f) atomicAdd(&gpos[o + 1], gq[q].y);
+            if (gq[q].z != 0.f) atomicAdd(&gpos[o + 2], gq[q].z);
+        }
+    }
+}
 
-extern "C" VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
-                                          uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
-                                          float* d_texture, float* d_height, int on_device) {
+// z components of a [n][3] array added into a [n] array.
+__global__ void k_add_z(const float* __restrict__ xyz, uint32_t n, float* __restrict__ z) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] += xyz[3 * (size_t)i + 2];
+}
+
+// ---------------------------------------------------------------- fused forward + adjoint
+struct DevView {
+    vgb_camera cam;
+    vgb_light lights[VGB_MAX_LIGHTS];
+    uint32_t nlights, samples, frame, tiles_x, tile_begin, pad[3];
+    const float* target;
+    float* radiance;
+};
+
+struct AdjBatchParams {
+    vgb_pt_options opt;
+    uint32_t nviews, nb, total_tiles;
+};
+
+// One persistent launch over every (view, 8x4-pixel tile) item; a lane owns a pixel: its
+// samples are traced (forward radiance, in the forward renderer's order), dL/dI = 2 (I - T)
+// is formed and the samples are replayed for the gradients.
+template <int NB, int L>
+__global__ void __launch_bounds__(128) k_adjoint_batch(const DevScene s, const DevView* __restrict__ views,
+                                                       const __grid_constant__ AdjBatchParams bp, const AdjOut out,
+                                                       uint32_t* counter, double* loss, uint32_t* errw,
+                                                       uint64_t* stats) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nb = bp.nb;
+    const vgb_pt_options& opt = bp.opt;
+    const bool smooth = opt.smooth_shading != 0;
+    uint32_t err = 0, nrays = 0;
+    double lsum = 0.0;
+    while (true) {
+        uint32_t it = 0;
+        if (lane == 0) it = atomicAdd(counter, 1u);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= bp.total_tiles) break;
+        uint32_t lo = 0, hi = bp.nviews - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (views[mid].tile_begin <= it) lo = mid; else hi = mid - 1;
+        }
+        const DevView& Vw = views[lo];
+        const uint32_t tile = it - Vw.tile_begin;
+        const uint32_t pi = (tile % Vw.tiles_x) * 8u + (lane & 7u), pj = (tile / Vw.tiles_x) * 4u + (lane >> 3);
+        const uint32_t W = Vw.cam.width, H = Vw.cam.height;
+        if (pi >= W || pj >= H) continue;
+        const uint32_t slot = pj * W + pi;
+        const size_t P = (size_t)W * H;
+        const float sf = (float)Vw.samples;
+        float acc[NB], g[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) acc[k] = 0.f;
+        for (uint32_t pass = 0; pass < 2; ++pass) {
+            if (pass == 1) {
+                // RenderPasses::updateImages, then the L2 loss and its gradient for this pixel
+                bool any = false;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    g[k] = 0.f;
+                    if (k < (int)nb) {
+                        const float I = acc[k] / sf;
+                        if (Vw.radiance) Vw.radiance[k * P + slot] = I;
+                        const float d = I - __ldg(&Vw.target[k * P + slot]);
+                        lsum += (double)d * (double)d;
+                        g[k] = (2.f * d) / sf;
+                        any |= g[k] != 0.f;
+                    }
+                }
+                if (!any || (!out.gtex && !out.gpos)) break;
+            }
+            for (uint32_t sample = 0; sample < Vw.samples; ++sample) {
+                AdjVtx<NB> vx[kAdjMaxVerts];
+                float bgc[NB], prad[NB];
+                const int nv = adj_replay<NB, L>(s, Vw.cam, Vw.lights, Vw.nlights, opt, nb, pi, pj, slot, sample,
+                                                 Vw.frame, pass ? g : nullptr, vx, bgc, prad, err, nrays);
+                if (pass == 0) {
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) if (k < (int)nb) acc[k] = acc[k] + prad[k];
+                } else {
+                    adj_scatter<NB>(s, nb, smooth, vx, nv, bgc, g, out);
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+    if (lane == 0 && lsum != 0.0) atomicAdd(loss, lsum);
+    if (err) atomicOr(errw, err);
+    warp_reduce_add(&stats[2], nrays);
+}
+
+template <int NB, int L>
+void launch_adjoint(vgb_context* ctx, const FrameParams& fp, const float* dldi, const AdjOut& out) {
+    const uint32_t n = fp.tiles_x * fp.tiles_y * 32u;
+    const int g = grid_for(ctx, n, 16);
+    k_adjoint<NB, L><<<g, 128, 0, ctx->stream>>>(dev_scene(ctx), fp, dldi, out, &ctx->d_counters[C_ERR], ctx->d_stats);
+}
+
+template <int NB, int L>
+void launch_adjoint_batch(vgb_context* ctx, const DevView* views, const AdjBatchParams& bp, const AdjOut& out) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_batch<NB, L>, 128, 0);
+    const uint32_t blocks = (uint32_t)std::max(1, per_sm) * (uint32_t)ctx->num_sms;
+    k_adjoint_batch<NB, L><<<blocks, 128, 0, ctx->stream>>>(dev_scene(ctx), views, bp, out, &ctx->d_counters[C_BATCH],
+                                                            ctx->d_loss, &ctx->d_counters[C_ERR], ctx->d_stats);
+}
+
+template <typename F>
+void dispatch_nb_layout(vgb_context* ctx, F&& f) {
+    const bool l8 = ctx->bvh_layout == 8;
+    if (ctx->nbands <= 1) { if (l8) f(std::integral_constant<int, 1>{}, std::integral_constant<int, 8>{}); else f(std::integral_constant<int, 1>{}, std::integral_constant<int, 2>{}); }
+    else if (ctx->nbands <= 4) { if (l8) f(std::integral_constant<int, 4>{}, std::integral_constant<int, 8>{}); else f(std::integral_constant<int, 4>{}, std::integral_constant<int, 2>{}); }
+    else { if (l8) f(std::integral_constant<int, 8>{}, std::integral_constant<int, 8>{}); else f(std::integral_constant<int, 8>{}, std::integral_constant<int, 2>{}); }
+}
+
+// Position-gradient scratch: vertex-normal gradients, normal sums and (for z-only callers)
+// full position gradients, [nverts][3] each.
+vgb_status ensure_adj_scratch(vgb_context* ctx) {
+    const size_t need = 9 * (size_t)ctx->nverts * sizeof(float);
+    if (need <= ctx->cap_adj) return VGB_OK;
+    dfree(ctx->d_adj);
+    ctx->d_adj = nullptr;
+    ctx->cap_adj = 0;
+    vgb_status s = dalloc(ctx, &ctx->d_adj, need);
+    if (s != VGB_OK) return s;
+    ctx->cap_adj = need;
+    return VGB_OK;
+}
+
+// Runs `body(out)` with the position outputs set up; gpos: caller's [nverts][3] or null,
+// gz: caller's [nverts] (z only) or null.  Smooth shading adds the vertex-normal pass.
+template <typename Body>
+vgb_status run_adjoint(vgb_context* ctx, bool smooth, float* gtex, float* gpos, float* gz, Body&& body) {
+    AdjOut out{gtex, nullptr, nullptr};
+    const size_t n3 = 3 * (size_t)ctx->nverts;
+    if (gpos || gz) {
+        vgb_status s = ensure_adj_scratch(ctx);
+        if (s != VGB_OK) return s;
+        float* gvn = ctx->d_adj;
+        float* sums = ctx->d_adj + n3;
+        float* full = ctx->d_adj + 2 * n3;
+        out.gpos = gpos ? gpos : full;
+        if (!gpos) CK(cudaMemsetAsync(full, 0, n3 * sizeof(float), ctx->stream));
+        if (smooth) {
+            out.gvn = gvn;
+            CK(cudaMemsetAsync(gvn, 0, 2 * n3 * sizeof(float), ctx->stream));
+            k_vnormal_sums<<<grid_for(ctx, ctx->ntris), 256, 0, ctx->stream>>>(ctx->d_vpos, ctx->d_idx, ctx->ntris, sums);
+        }
+    }
+    body(out);
+    CK(cudaGetLastError());
+    if (out.gvn)
+        k_vnormal_backward<<<grid_for(ctx, ctx->ntris), 256, 0, ctx->stream>>>(ctx->d_vpos, ctx->d_idx, ctx->ntris,
+                                                                               ctx->d_adj + n3, out.gvn, out.gpos);
+    if (gz) k_add_z<<<grid_for(ctx, ctx->nverts), 256, 0, ctx->stream>>>(out.gpos, ctx->nverts, gz);
+    CK(cudaGetLastError());
+    return VGB_OK;
+}
+
+vgb_status adjoint_common(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                          const vgb_pt_options* opts, const float* dL_dradiance, float* d_texture, float* d_pos,
+                          bool xyz, int on_device, const char* what) {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
-    if (!cam || !opts || !dL_dradiance) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: null camera/options/gradient");
-    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "adjoint: build the BVH first");
+    const std::string w(what);
+    if (!cam || !opts || !dL_dradiance) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": null camera/options/gradient");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, w + ": build the BVH first");
     if (opts->samples == 0 || opts->nbands != ctx->nbands || nlights > VGB_MAX_LIGHTS || (nlights && !lights))
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: samples, nbands or lights invalid");
-    if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: at most 3 bounces");
-    if (d_height && opts->smooth_shading)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "adjoint: height gradients need flat shading (face normals)");
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": samples, nbands or lights invalid");
+    if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": at most 3 bounces");
     cudaSetDevice(ctx->device);
     FrameParams fp;
     std::memset(&fp, 0, sizeof(fp));
@@ -2311,31 +2542,120 @@ extern "C" VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* ca
     fp.tiles_y = (cam->height + 3) / 4;
     const size_t npix = (size_t)cam->width * cam->height;
     const size_t ntex = (size_t)ctx->tw * ctx->th * ctx->nbands;
+    const size_t npos = (xyz ? 3 : 1) * (size_t)ctx->nverts;
     const float* dl = dL_dradiance;
-    float *gt = d_texture, *gh = d_height;
+    float *gt = d_texture, *gp = d_pos;
     vgb_status s;
     if (!on_device) {
-        const size_t need = npix * ctx->nbands + (d_texture ? ntex : 0) + (d_height ? ctx->nverts : 0);
+        const size_t need = npix * ctx->nbands + (d_texture ? ntex : 0) + (d_pos ? npos : 0);
         if ((s = ensure_staging(ctx, need * sizeof(float))) != VGB_OK) return s;
         float* cur = (float*)ctx->staging_base;
         CK(cudaMemcpyAsync(cur, dL_dradiance, npix * ctx->nbands * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         dl = cur; cur += npix * ctx->nbands;
         if (d_texture) { gt = cur; CK(cudaMemcpyAsync(gt, d_texture, ntex * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); cur += ntex; }
-        if (d_height) { gh = cur; CK(cudaMemcpyAsync(gh, d_height, ctx->nverts * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); }
+        if (d_pos) { gp = cur; CK(cudaMemcpyAsync(gp, d_pos, npos * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); }
     }
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    const bool l8 = ctx->bvh_layout == 8;
-    if (ctx->nbands <= 1) { if (l8) launch_adjoint<1, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<1, 2>(ctx, fp, dl, gt, gh); }
-    else if (ctx->nbands <= 4) { if (l8) launch_adjoint<4, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<4, 2>(ctx, fp, dl, gt, gh); }
-    else { if (l8) launch_adjoint<8, 8>(ctx, fp, dl, gt, gh); else launch_adjoint<8, 2>(ctx, fp, dl, gt, gh); }
-    CK(cudaGetLastError());
+    s = run_adjoint(ctx, opts->smooth_shading != 0, gt, xyz ? gp : nullptr, xyz ? nullptr : gp, [&](const AdjOut& out) {
+        dispatch_nb_layout(ctx, [&](auto nbc, auto lc) { launch_adjoint<decltype(nbc)::value, decltype(lc)::value>(ctx, fp, dl, out); });
+    });
+    if (s != VGB_OK) return s;
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!on_device) {
         if (d_texture) CK(cudaMemcpyAsync(d_texture, gt, ntex * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-        if (d_height) CK(cudaMemcpyAsync(d_height, gh, ctx->nverts * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (d_pos) CK(cudaMemcpyAsync(d_pos, gp, npos * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    uint64_t hs[8];
+    CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
+    ctx->stats.rays_closest = hs[2];
+    ctx->stats.rays_shadow = 0;
+    ctx->stats.kernel_launches = 1;
+    ctx->stats.ms_last = ms;
+    return check_device_error(ctx);
+}
+
+}  // namespace
+
+extern "C" VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                          uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
+                                          float* d_texture, float* d_height, int on_device) {
+    return adjoint_common(ctx, cam, lights, nlights, opts, dL_dradiance, d_texture, d_height, false, on_device, "adjoint");
+}
+
+extern "C" VGB_API vgb_status vgb_adjoint_positions(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
+                                                    uint32_t nlights, const vgb_pt_options* opts,
+                                                    const float* dL_dradiance, float* d_texture, float* d_position,
+                                                    int on_device) {
+    return adjoint_common(ctx, cam, lights, nlights, opts, dL_dradiance, d_texture, d_position, true, on_device,
+                          "adjoint_positions");
+}
+
+extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* views, uint32_t nviews,
+                                                       const vgb_pt_options* opts, float* d_texture, float* d_position,
+                                                       double* loss) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!views || nviews == 0 || !opts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: no views or options");
+    if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_adjoint_batch: build the BVH first");
+    if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: nbands differs from the scene");
+    if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: at most 3 bounces");
+    cudaSetDevice(ctx->device);
+    std::vector<DevView> hv(nviews);
+    uint32_t tiles = 0;
+    for (uint32_t i = 0; i < nviews; ++i) {
+        const vgb_view& v = views[i];
+        if (v.samples == 0 || v.nlights > VGB_MAX_LIGHTS || !v.target || v.camera.width == 0 || v.camera.height == 0)
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: view " + std::to_string(i) + " invalid");
+        DevView& d = hv[i];
+        std::memset(&d, 0, sizeof(d));
+        d.cam = v.camera;
+        for (uint32_t l = 0; l < v.nlights; ++l) d.lights[l] = v.lights[l];
+        d.nlights = v.nlights;
+        d.samples = v.samples;
+        d.frame = v.frame;
+        d.tiles_x = (v.camera.width + 7) / 8;
+        d.tile_begin = tiles;
+        d.target = v.target;
+        d.radiance = v.radiance;
+        const uint64_t t = (uint64_t)tiles + (uint64_t)d.tiles_x * ((v.camera.height + 3) / 4);
+        if (t > 0xFFFFFFFFull) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: too many tiles");
+        tiles = (uint32_t)t;
+    }
+    vgb_status s;
+    if (nviews * sizeof(DevView) > ctx->cap_views) {
+        dfree(ctx->d_views);
+        ctx->d_views = nullptr;
+        ctx->cap_views = 0;
+        if ((s = dalloc(ctx, &ctx->d_views, nviews * sizeof(DevView))) != VGB_OK) return s;
+        ctx->cap_views = nviews * sizeof(DevView);
+    }
+    if (!ctx->d_loss && (s = dalloc(ctx, &ctx->d_loss, sizeof(double))) != VGB_OK) return s;
+    CK(cudaMemcpyAsync(ctx->d_views, hv.data(), nviews * sizeof(DevView), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_loss, 0, sizeof(double), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->d_counters[C_BATCH], 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
+    AdjBatchParams bp;
+    std::memset(&bp, 0, sizeof(bp));
+    bp.opt = *opts;
+    bp.nviews = nviews;
+    bp.nb = ctx->nbands;
+    bp.total_tiles = tiles;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    s = run_adjoint(ctx, opts->smooth_shading != 0, d_texture, d_position, nullptr, [&](const AdjOut& out) {
+        dispatch_nb_layout(ctx, [&](auto nbc, auto lc) {
+            launch_adjoint_batch<decltype(nbc)::value, decltype(lc)::value>(ctx, (const DevView*)ctx->d_views, bp, out);
+        });
+    });
+    if (s != VGB_OK) return s;
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    double hl = 0.0;
+    CK(cudaMemcpyAsync(&hl, ctx->d_loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (loss) *loss = hl;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     uint64_t hs[8];

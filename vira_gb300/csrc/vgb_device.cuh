@@ -185,8 +185,7 @@ __device__ __forceinline__ void slab(const SlabRay& q, float lox, float hix, flo
 
 // Closest hit (any = false; ties in t go to the smaller id) or occlusion (any = true, any
 // hit with t <= tmax).  Box tests are conservative (make_slab).
-// `any` may be a run-time value: a kernel that interleaves closest-hit and occlusion rays in one
-// loop passes it per ray; the templated wrapper below passes a constant.
+// One body for both kinds of ray; the templated wrapper below passes `any` as a constant.
 template <bool COUNT>
 __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                             const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
@@ -370,15 +369,6 @@ __device__ __forceinline__ void traverse_any_layout(const uint4* __restrict__ no
                                                     const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
     if (LAYOUT == 8) traverse8<ANY, COUNT>(nodes, tris, r, tmax, h, err, cnt);
     else traverse<ANY, COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, h, err, cnt);
-}
-
-// The same with the closest-hit / occlusion choice made per ray at run time.
-template <int LAYOUT, bool COUNT>
-__device__ __forceinline__ void traverse_layout_rt(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                   const WRay& r, float tmax, bool any, HitOut& h, uint32_t& err,
-                                                   Counters& cnt) {
-    if (LAYOUT == 8) traverse8_rt<COUNT>(nodes, tris, r, tmax, any, h, err, cnt);
-    else traverse_rt<COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, any, h, err, cnt);
 }
 
 }  // namespace vgbd

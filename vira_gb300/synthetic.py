@@ -121,36 +121,48 @@ def icosphere(subdivisions: int):
 
 
 def real_sh_noise(dirs: np.ndarray, lmax: int, seed: int) -> np.ndarray:
-    """Sum over l <= lmax of random real spherical harmonics with amplitude ~ l^-2, evaluated at
-    unit directions; uses the associated Legendre recurrence in FP64."""
+    """Sum over 1 <= l <= lmax of random real spherical harmonics with amplitude ~ l^-2, evaluated
+    at unit directions; uses the associated Legendre recurrence in FP64.  For each order m the
+    l-sums of the cos(m phi) and sin(m phi) terms are formed first, so the azimuthal factors are
+    evaluated once per m."""
     rng = np.random.default_rng(seed)
     x, y, z = dirs[:, 0], dirs[:, 1], dirs[:, 2]
-    theta = np.arccos(np.clip(z, -1, 1))
-    phi = np.arctan2(y, x)
-    ct = np.cos(theta)
+    ct = np.clip(z, -1.0, 1.0)
     st = np.sqrt(np.maximum(0.0, 1 - ct * ct))
+    phi = np.arctan2(y, x)
     out = np.zeros_like(x)
+    cs = np.empty_like(x)
+    sn = np.empty_like(x)
+    tmp = np.empty_like(x)
     # P_m^m, then upward in l
     pmm = np.ones_like(x)
     for m in range(0, lmax + 1):
         if m > 0:
-            pmm = pmm * (-(2 * m - 1)) * st
+            pmm *= st
+            pmm *= -(2 * m - 1)
+        cs.fill(0.0)
+        sn.fill(0.0)
         p_prev, p_cur = None, pmm
         for l in range(m, lmax + 1):
             if l == m:
                 p = pmm
             elif l == m + 1:
-                p = ct * (2 * m + 1) * pmm
+                p = ct * ((2 * m + 1) * pmm)
             else:
-                p = (ct * (2 * l - 1) * p_cur - (l + m - 1) * p_prev) / (l - m)
+                p = (ct * ((2 * l - 1) * p_cur) - (l + m - 1) * p_prev) / (l - m)
             if l > m:
                 p_prev, p_cur = p_cur, p
             if l >= 1:
                 norm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.exp(math.lgamma(l - m + 1) - math.lgamma(l + m + 1)))
                 amp = float(l) ** -2.0
                 ca, sa = rng.standard_normal(2)
-                if m == 0:
-                    out += amp * ca * norm * p
-                else:
-                    out += amp * norm * p * math.sqrt(2) * (ca * np.cos(m * phi) + sa * np.sin(m * phi))
+                np.multiply(p, amp * norm * ca, out=tmp)
+                cs += tmp
+                if m > 0:
+                    np.multiply(p, amp * norm * sa, out=tmp)
+                    sn += tmp
+        if m == 0:
+            out += cs
+        else:
+            out += math.sqrt(2) * (cs * np.cos(m * phi) + sn * np.sin(m * phi))
     return out

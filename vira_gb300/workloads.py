@@ -13,6 +13,11 @@
                    plain_direct terrain; per-frame resolution drawn from {256^2, 512^2, 1024^2,
                    2048^2} and spp from {1, 4, 16, 64}; the sun slews 0.1 deg per frame; 8 bands;
                    direct lighting.
+``asteroid``       icosphere subdivision 9 (5.2M triangles) with radial spherical-harmonic relief
+                   up to degree 32 (amplitude ~ l^-2, 20 m RMS, mean radius 250 m), uniform albedo
+                   0.05, smooth shading; 64 views of 256^2-1024^2 at 1-3 km range under phase
+                   angles 0-90 deg; 4 bands, 8 spp, direct lighting; per-vertex radial offsets are
+                   the parameters (fused forward + adjoint of every view in one launch).
 Each takes sizes that shrink posts, pixels or frames for tests.
 """
 from __future__ import annotations
@@ -163,3 +168,49 @@ def inversion(posts: int = 1025, tex: int = 1024, resolution: int = 512, nviews:
     pt.options.seed = seed
     pt.render_passes.simulate_lighting = True
     return scene, views
+
+
+def asteroid(subdivisions: int = 9, lmax: int = 32, nviews: int = 64, resolutions=(256, 512, 1024), spp: int = 8,
+             bounces: int = 0, seed: int = 9, device: int = 0, radius: float = 250.0, relief_rms: float = 20.0):
+    """The batched-adjoint asteroid workload: returns (scene, views, radial_dirs [nverts][3] float32).
+    Vertex v sits at radial_dirs[v] * (radius + relief_v); an offset field o moves it to
+    radial_dirs[v] * (radius + relief_v + o_v)."""
+    from .autograd import View
+
+    dirs, faces = synthetic.icosphere(subdivisions)
+    relief = synthetic.real_sh_noise(dirs, lmax, seed=seed)
+    relief *= relief_rms / max(1e-12, float(np.sqrt(np.mean(relief * relief))))
+    pos = (dirs * (radius + relief)[:, None]).astype(np.float32)
+    B = FOUR_BAND.size
+    scene = Scene(FOUR_BAND, device=device)
+    mesh = Mesh(positions=pos, indices=faces, albedo=np.full((pos.shape[0], B), 0.05, np.float32))
+    mesh.set_smooth_shading(True)
+    scene.add_mesh(mesh)
+    scene.new_instance(("mesh", 0))
+    scene.new_sun(temperature=5778.0)
+    rng = np.random.default_rng(seed + 1)
+    views = []
+    for v in range(nviews):
+        res = int(rng.choice(resolutions))
+        cam = Camera()
+        cam.set_resolution(res, res)
+        cam.set_sensor_size(36.0 / 1000.0)
+        cam.set_field_of_view(30.0)
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        rr = rng.uniform(1000.0, 3000.0)
+        cam.set_local_position(*(rr * d))
+        cam.look_at((0.0, 0.0, 0.0))
+        # sun direction at phase angle alpha from the view direction (seen from the body)
+        alpha = math.radians(rng.uniform(0.0, 90.0))
+        a = rng.standard_normal(3)
+        a -= d * float(a @ d)
+        a /= np.linalg.norm(a)
+        s_dir = math.cos(alpha) * d + math.sin(alpha) * a
+        views.append(View(camera=cam, sun_position=scene.origin + 149597870700.0 * s_dir, frame=v, samples=spp))
+    pt = scene.pathtracer
+    pt.options.samples = spp
+    pt.options.bounces = bounces
+    pt.options.seed = seed
+    pt.render_passes.simulate_lighting = True
+    return scene, views, dirs.astype(np.float32)
