@@ -228,3 +228,37 @@ def test_small_frame_after_large_frame(gpu):
     for k in fresh:
         assert same_bits(small[k], fresh[k]) if k != "triangle_id" else np.array_equal(small[k], fresh[k])
     assert big["total_radiance"].shape[1] == 96
+
+
+def test_plane_subsets_equal_full_film(gpu):
+    """The per-pixel sums a film does not request are skipped; requested planes must not change.
+    Path-traced frame with bounces, background and ambient (every fold of the path radiance)."""
+    scene, cam_id = workloads.path_traced(posts=65, tex=64, resolution=40, spp=3, bounces=2, rr_depth=1, seed=3)
+    scene.set_ambient(0.02)
+    scene.set_background_emission(0.3)
+    scene.pathtracer.options.show_background = True
+    full = gpu_render_host(scene, cam_id)
+    lib = capi.load()
+    ctx = scene.context()
+    cam = scene[cam_id].to_c(scene.origin, 8)
+    lights, nl = scene.c_lights()
+    opts = scene.pathtracer.c_options(scene)
+    W, H, B = cam.width, cam.height, 8
+    shapes = {"total_radiance": (B, H, W), "direct_radiance": (B, H, W), "indirect_radiance": (B, H, W),
+              "albedo": (B, H, W), "normal_global": (3, H, W), "depth": (H, W), "alpha": (H, W)}
+    subsets = [("total_radiance",), ("direct_radiance",), ("indirect_radiance", "alpha"), ("albedo", "depth"),
+               ("normal_global", "triangle_id")]
+    for sub in subsets:
+        f = capi.Film()
+        out = {}
+        for k in sub:
+            out[k] = np.empty((H, W), np.uint32) if k == "triangle_id" else np.empty(shapes[k], np.float32)
+            setattr(f, k, out[k].ctypes.data)
+        f.on_device = 0
+        capi.check(lib.vgb_render(ctx, C.byref(cam), lights, nl, C.byref(opts), C.byref(f)), ctx)
+        for k, v in out.items():
+            if k == "triangle_id":
+                assert np.array_equal(v, full[k]), sub
+            else:
+                assert same_bits(v, full[k]), (sub, k)
+    scene.close()

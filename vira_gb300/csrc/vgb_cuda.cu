@@ -102,13 +102,30 @@ struct FrameParams {
     uint32_t nlights;
     uint32_t nb;
     uint32_t tiles_x, tiles_y;
+    uint32_t aux;   // AUX_* bits: the per-pixel sums the requested film planes need
 };
+
+// Per-pixel sums kept over the samples only when a requested film plane reads them (the total
+// radiance sum is always kept): albedo, normal, direct radiance (direct and indirect planes),
+// depth and hit count (depth and alpha planes), first triangle.
+enum : uint32_t { AUX_ALB = 1u, AUX_NRM = 2u, AUX_DIR = 4u, AUX_DEP = 8u, AUX_TRI = 16u };
+
+// Fold state of a pixel's path (DevState::pend): bits 0-1 what the bounce radiance holds
+// (0 nothing, 1 bounce-0 radiance, 2 a later bounce's), bit 2 set while the path radiance has
+// not been written this sample (it reads as 0).
+constexpr uint32_t kPendMask = 3u, kPradEmpty = 4u;
 
 struct FilmOut {
     float *total, *direct, *indirect, *power, *albedo, *normal, *depth, *alpha;
     uint32_t* tri;
     const float* omega;
 };
+
+// The AUX_* sums that the planes of a film read.
+inline uint32_t aux_for(const FilmOut& f) {
+    return (f.albedo ? AUX_ALB : 0u) | (f.normal ? AUX_NRM : 0u) | ((f.direct || f.indirect) ? AUX_DIR : 0u) |
+           ((f.depth || f.alpha) ? AUX_DEP : 0u) | (f.tri ? AUX_TRI : 0u);
+}
 
 __device__ __forceinline__ void warp_reduce_add(uint64_t* dst, uint32_t v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -459,21 +476,26 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         float thr[NB];
 #pragma unroll
         for (int k = 0; k < NB; ++k) thr[k] = 1.f;
+        const uint32_t aux = fp.aux;
+        uint32_t pendv = 0u;  // this item's fold state, written once below
         if (active) {
             if (bounce == 0) {
                 active = camera_ray(fp, item, sample, slot, ro, rd);
                 if (active) {
                     if (sample == 0) {
 #pragma unroll
-                        for (int k = 0; k < NB; ++k)
-                            if (k < (int)nb) { st.arad[k * P + slot] = 0.f; st.adir[k * P + slot] = 0.f; st.aalb[k * P + slot] = 0.f; }
-                        st.anrm[slot] = 0.f; st.anrm[P + slot] = 0.f; st.anrm[2 * P + slot] = 0.f;
-                        st.adep[slot] = 0.f; st.acnt[slot] = 0u; st.atri[slot] = VGB_NO_HIT;
+                        for (int k = 0; k < NB; ++k) {
+                            if (k < (int)nb) {
+                                st.arad[k * P + slot] = 0.f;
+                                if (aux & AUX_DIR) st.adir[k * P + slot] = 0.f;
+                                if (aux & AUX_ALB) st.aalb[k * P + slot] = 0.f;
+                            }
+                        }
+                        if (aux & AUX_NRM) { st.anrm[slot] = 0.f; st.anrm[P + slot] = 0.f; st.anrm[2 * P + slot] = 0.f; }
+                        if (aux & AUX_DEP) { st.adep[slot] = 0.f; st.acnt[slot] = 0u; }
+                        if (aux & AUX_TRI) st.atri[slot] = VGB_NO_HIT;
                     }
-                    st.pend[slot] = 0u;
-#pragma unroll
-                    for (int k = 0; k < NB; ++k)
-                        if (k < (int)nb) st.prad[k * P + slot] = 0.f;
+                    pendv = kPradEmpty;  // the path radiance starts at 0 without being written
                 }
             } else {
                 slot = in_queue[item];
@@ -481,17 +503,20 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                 // Fold the previous bounce's radiance into the path now, so that the path
                 // radiance is not live through the shading.
                 const uint32_t pend = st.pend[slot];
-                if (pend) {
+                if (pend & kPendMask) {
 #pragma unroll
                     for (int k = 0; k < NB; ++k) {
                         if (k < (int)nb) {
                             const float br = st.brad[k * P + slot];
-                            st.prad[k * P + slot] = st.prad[k * P + slot] + br;
-                            if (pend == 1u) st.adir[k * P + slot] += br;
+                            const float pr = (pend & kPradEmpty) ? 0.f : st.prad[k * P + slot];
+                            st.prad[k * P + slot] = pr + br;
+                            if ((pend & kPendMask) == 1u && (aux & AUX_DIR)) st.adir[k * P + slot] += br;
                         }
                     }
+                    pendv = 0u;
+                } else {
+                    pendv = pend & kPradEmpty;
                 }
-                st.pend[slot] = 0u;
             }
         }
         // ---- closest hit, from k_trace
@@ -525,9 +550,11 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                         const float bgv = fp.opt.background[k];
                         float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
                         const float tk = (bounce == 0) ? 1.f : st.thr[k * P + slot];
-                        st.prad[k * P + slot] = st.prad[k * P + slot] + tk * (bg * 1.f);
+                        const float pr = (pendv & kPradEmpty) ? 0.f : st.prad[k * P + slot];
+                        st.prad[k * P + slot] = pr + tk * (bg * 1.f);
                     }
                 }
+                pendv = 0u;
             }
         }
         F3 tg{1, 0, 0}, bt{0, 1, 0};
@@ -537,13 +564,14 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
             F3 fnrm;
             surface_at<NB>(s, nb, fp.opt.smooth_shading != 0, t, hr.z, hr.w, Pp, N, fnrm, tg, bt, alb);
             if (bounce == 0) {
-                if (st.atri[slot] == VGB_NO_HIT) st.atri[slot] = t;
+                if ((aux & AUX_TRI) && st.atri[slot] == VGB_NO_HIT) st.atri[slot] = t;
+                if (aux & AUX_ALB) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k)
-                    if (k < (int)nb) st.aalb[k * P + slot] += alb[k];
-                st.anrm[slot] += N.x; st.anrm[P + slot] += N.y; st.anrm[2 * P + slot] += N.z;
-                st.adep[slot] += hr.x;
-                st.acnt[slot] += 1u;
+                    for (int k = 0; k < NB; ++k)
+                        if (k < (int)nb) st.aalb[k * P + slot] += alb[k];
+                }
+                if (aux & AUX_NRM) { st.anrm[slot] += N.x; st.anrm[P + slot] += N.y; st.anrm[2 * P + slot] += N.z; }
+                if (aux & AUX_DEP) { st.adep[slot] += hr.x; st.acnt[slot] += 1u; }
             }
             if (fp.opt.simulate_lighting) {
                 lit = true;
@@ -558,7 +586,7 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                     if (k < (int)nb)
                         st.brad[k * P + slot] = (bounce == 0 && fp.opt.has_ambient) ? 0.f + thr[k] * (fp.opt.ambient[k] * alb[k]) : 0.f;
                 }
-                st.pend[slot] = (bounce == 0) ? 1u : 2u;
+                pendv = (pendv & kPradEmpty) | ((bounce == 0) ? 1u : 2u);
                 r0 = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | kSlotMain}, k0, k1);
             }
         }
@@ -600,6 +628,7 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         }
         // ---- write path state and append live paths
         if (active) {
+            st.pend[slot] = pendv;
             if (cont) {
 #pragma unroll
                 for (int k = 0; k < NB; ++k)
@@ -659,29 +688,30 @@ __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_co
     const float sf = (float)fp.opt.samples;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const uint32_t pend = st.pend[p];
+        const bool want_dir = (fp.aux & AUX_DIR) != 0;
         float tot[NB];
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
             if (k < (int)nb) {
-                float pr = st.prad[k * P + p];
-                if (pend) {
+                float pr = (pend & kPradEmpty) ? 0.f : st.prad[k * P + p];
+                if (pend & kPendMask) {
                     const float br = st.brad[k * P + p];
                     pr += br;
-                    if (pend == 1u) st.adir[k * P + p] += br;
+                    if ((pend & kPendMask) == 1u && want_dir) st.adir[k * P + p] += br;
                 }
                 tot[k] = st.arad[k * P + p] + pr;
                 st.arad[k * P + p] = tot[k];
             }
         }
-        st.pend[p] = 0u;
+        // (the fold state is rewritten for every pixel by the next sample's camera rays)
         if (!last) continue;
         // unidirectional (cpu_path_tracer.ipp:229-240) + RenderPasses::updateImages (passes.ipp:82-128)
-        const uint32_t count = st.acnt[p];
+        const uint32_t count = (fp.aux & AUX_DEP) ? st.acnt[p] : 0u;
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
             if (k < (int)nb) {
                 const float total = tot[k] / sf;
-                const float direct = st.adir[k * P + p] / sf;
+                const float direct = want_dir ? st.adir[k * P + p] / sf : 0.f;
                 if (f.total) f.total[k * FP + p] = total;
                 if (f.direct) f.direct[k * FP + p] = direct;
                 if (f.indirect) f.indirect[k * FP + p] = total - direct;
@@ -1292,6 +1322,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     }
     f.total = df[0]; f.direct = df[1]; f.indirect = df[2]; f.power = df[3]; f.albedo = df[4];
     f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
+    fp.aux = aux_for(f);
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     uint32_t launches = 0;
     ctx->prof_used = 0;
@@ -1560,6 +1591,7 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     fo.total = film->total_radiance; fo.direct = film->direct_radiance; fo.indirect = film->indirect_radiance;
     fo.power = film->received_power; fo.albedo = film->albedo; fo.normal = film->normal_global;
     fo.depth = film->depth; fo.alpha = film->alpha; fo.tri = film->triangle_id; fo.omega = film->pixel_solid_angle;
+    fp.aux = aux_for(fo);
     // The array keeps the last call's contents: the counters, statistics and error word must
     // start at zero; every other region is written before it is read.
     CK(cudaMemsetAsync(st.counters, 0, 256, ctx->stream));
