@@ -98,6 +98,15 @@ typedef struct vgb_pt_options {
     uint32_t nbands;             /* B */
     float ambient[VGB_MAX_BANDS];
     float background[VGB_MAX_BANDS];
+    /* adaptive sampling (cpu_path_tracer.ipp:198-226): after sample s (s > 0), a pixel stops
+     * when s is a multiple of samples_to_detect_miss and no sample has hit yet, or s is a
+     * multiple of samples_per_batch and the 95% interval of the path-radiance magnitude is within
+     * sampling_tolerance of its mean (or every magnitude was 0); the pixel's planes are then
+     * divided by s, as the reference does.  0 = off (reference default). */
+    uint32_t adaptive_sampling;
+    uint32_t samples_per_batch;      /* options.samples_per_batch (reference default 30) */
+    float sampling_tolerance;        /* options.sampling_tolerance (reference default 0.05) */
+    uint32_t samples_to_detect_miss; /* options.samples_to_detect_miss (reference default 30) */
 } vgb_pt_options;
 
 /* ---- film: RenderPasses planes (caller-owned; NULL = pass not written) ----------

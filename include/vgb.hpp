@@ -178,6 +178,10 @@ struct CPUPathTracerOptions {  // cpu_path_tracer.hpp:30-43, plus the RNG key an
     uint32_t frame = 0;
     bool deterministic_light = false;
     uint32_t rr_depth = 0;
+    bool adaptive_sampling = false;
+    size_t samples_per_batch = 30;
+    float sampling_tolerance = 0.05f;
+    size_t samples_to_detect_miss = 30;
 };
 
 struct RenderPasses {  // passes.hpp:51-95, planar [B][H][W]
@@ -289,6 +293,10 @@ inline void GpuPathTracer::render(Camera& camera, Scene& scene) {
     o.seed = options.seed;
     o.frame = options.frame;
     o.nbands = B;
+    o.adaptive_sampling = options.adaptive_sampling;
+    o.samples_per_batch = (uint32_t)options.samples_per_batch;
+    o.sampling_tolerance = options.sampling_tolerance;
+    o.samples_to_detect_miss = (uint32_t)options.samples_to_detect_miss;
     if (!scene.ambient.empty()) {
         o.has_ambient = 1;
         for (uint32_t b = 0; b < B; ++b) o.ambient[b] = scene.ambient[b];

@@ -605,6 +605,7 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
     float depth = 0;
     uint32_t count = 0, tri_first = VGB_NO_HIT;
     bool first_hit = true;
+    float s1 = 0.f, s2 = 0.f;   // adaptive sampling sums
     V3 org{cam.origin[0], cam.origin[1], cam.origin[2]};
     uint32_t sample;
     for (sample = 0; sample < o.samples; ++sample) {
@@ -761,7 +762,28 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
             for (uint32_t k = 0; k < B; ++k) path[k] += rad[k];
         }
         for (uint32_t k = 0; k < B; ++k) radiance[k] += path[k];
+        if (o.adaptive_sampling) {
+            // unidirectional's adaptive stop (cpu_path_tracer.ipp:198-226); illum = magnitude()
+            // (spectral_data.ipp:280-287)
+            float sq = 0;
+            for (uint32_t k = 0; k < B; ++k) sq += path[k] * path[k];
+            float illum = std::sqrt(sq);
+            s1 += illum;
+            s2 += (illum * illum);
+            if (sample % o.samples_to_detect_miss == 0 && sample != 0) {
+                if (depth == 0) break;
+            }
+            if (sample % o.samples_per_batch == 0 && sample != 0) {
+                if (s1 == 0) break;
+                float n = static_cast<float>(sample) + 1.f;
+                float mu = s1 / n;
+                float variance = (1.f / (n - 1.f)) * (s2 - (s1 * s1) / n);
+                float I = 1.96f * std::sqrt(variance / n);
+                if (I <= o.sampling_tolerance * mu) break;
+            }
+        }
     }
+    // after a break `sample` is the index of the last sample taken: the reference divides by it
     float sf = (float)sample;
     for (uint32_t k = 0; k < B; ++k) {
         out.total[k] = radiance[k] / sf;
@@ -974,6 +996,7 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
                        uint32_t row_end, int nthreads, uint64_t* ray_counts_out) {
     if (!h || !cam || !opts || !film) return 1;
     if (opts->samples == 0 || (nlights && !lights)) return 1;
+    if (opts->adaptive_sampling && (opts->samples_per_batch == 0 || opts->samples_to_detect_miss == 0)) return 1;
     const Scene& s = *static_cast<Scene*>(h);
     if (opts->nbands != s.nbands) return 1;
     const uint32_t W = cam->width, H = cam->height, B = s.nbands;

@@ -32,12 +32,33 @@ def test_library_exports_every_declared_symbol():
     assert b"sm_103a" in lib.vgb_version()
 
 
-def test_struct_layouts_match_the_header():
-    # sizes of the plain-data structs as a C compiler lays them out
-    assert C.sizeof(capi.Camera) == 4 * (2 + 3 + 9 + 6 + 1 + 8)
-    assert C.sizeof(capi.Light) == 4 * (3 + 1 + 8)
-    assert C.sizeof(capi.PtOptions) == 4 * 8 + 8 + 4 * 2 + 4 * 16
-    assert C.sizeof(capi.Film) == 8 * 10 + 8
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes struct has the size and field offsets a C compiler gives the header's struct."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"vgb_camera": capi.Camera, "vgb_light": capi.Light, "vgb_pt_options": capi.PtOptions,
+             "vgb_film": capi.Film, "vgb_frame": capi.Frame, "vgb_view": capi.View,
+             "vgb_batch_options": capi.BatchOptions, "vgb_bvh_options": capi.BvhOptions, "vgb_stats": capi.Stats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vgb.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')
+        for f in py._fields_:
+            lines.append(f'    printf("{cname}.{f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parents[1] / "include"
+    subprocess.run([cc, "-std=c99", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for cname, py in pairs.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f in py._fields_:
+            assert int(got[f"{cname}.{f[0]}"]) == getattr(py, f[0]).offset, f"{cname}.{f[0]}"
 
 
 def test_context_without_gpu_fails_cleanly():

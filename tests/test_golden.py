@@ -22,7 +22,9 @@ def _load(path):
     cam = capi.Camera.from_buffer_copy(d["camera"].tobytes())
     nl = int(d["nlights"])
     lights = (capi.Light * max(1, nl)).from_buffer_copy(d["lights"].tobytes().ljust(C.sizeof(capi.Light) * max(1, nl), b"\0"))
-    opts = capi.PtOptions.from_buffer_copy(d["options"].tobytes())
+    # fixtures written before the adaptive-sampling fields were appended hold the shorter struct;
+    # the appended fields are zero (adaptive sampling off, as in the reference's defaults)
+    opts = capi.PtOptions.from_buffer_copy(d["options"].tobytes().ljust(C.sizeof(capi.PtOptions), b"\0"))
     tex = d["texture"] if d["texture"].size else None
     return d, cam, lights, nl, opts, tex
 

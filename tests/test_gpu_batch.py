@@ -69,3 +69,31 @@ def test_batch_graph_replay_picks_up_new_frames(gpu):
         assert np.array_equal(x["total_radiance"].cpu().numpy(), r["total_radiance"])
     assert any(not torch.equal(x["total_radiance"], f0) for x, f0 in zip(b, first))
     scene.close()
+
+
+@pytest.mark.parametrize("bounces", [0, 1])
+def test_adaptive_batch_equals_per_frame(gpu, bounces):
+    """Adaptive sampling (cpu_path_tracer.ipp:198-226): the persistent kernel stops each pixel at
+    the same sample as the wavefront renderer and divides by the same count."""
+    import torch
+
+    scene, frames = workloads.trajectory(nframes=6, posts=129, resolutions=(24, 40), spps=(24, 33), seed=4,
+                                         alt_top=3000.0, alt_bottom=800.0)
+    opt = scene.pathtracer.options
+    opt.bounces = bounces
+    opt.adaptive_sampling = True
+    opt.samples_per_batch = 4
+    opt.samples_to_detect_miss = 6
+    opt.sampling_tolerance = 0.2
+    batch = scene.render_batch(frames, autotune=False, use_graph=False)
+    torch.cuda.synchronize()
+    ref = _per_frame(scene, frames)
+    for i, (b, r) in enumerate(zip(batch, ref)):
+        for k in r:
+            assert np.array_equal(b[k].cpu().numpy().view(np.uint32), r[k].view(np.uint32)), (i, k)
+    opt.adaptive_sampling = False
+    full = _per_frame(scene, frames)
+    changed = sum(int((~np.isclose(r["total_radiance"], f["total_radiance"], rtol=0, atol=0)).any(axis=0).sum())
+                  for r, f in zip(ref, full))
+    assert changed > 0, "no pixel stopped early"
+    scene.close()

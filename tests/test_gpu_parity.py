@@ -262,3 +262,28 @@ def test_plane_subsets_equal_full_film(gpu):
             else:
                 assert same_bits(v, full[k]), (sub, k)
     scene.close()
+
+
+def test_adaptive_sampling_matches_oracle(gpu):
+    """Adaptive sampling with deterministic light sampling: every stopping decision depends on
+    float sums that the kernels and the oracle form identically, so the planes are bit-exact,
+    including the reference's division by the index of the last sample and the early stop of
+    pixels that see only sky."""
+    scene, cam_id = workloads.plain_direct(posts=129, resolution=48)
+    cam = scene[cam_id]
+    cam.look_in_direction((0.454, 0.0, -0.891))  # part of the view is sky
+    opt = scene.pathtracer.options
+    opt.samples = 40
+    opt.adaptive_sampling = True
+    opt.samples_per_batch = 8
+    opt.samples_to_detect_miss = 5
+    opt.sampling_tolerance = 0.03
+    g = gpu_render_host(scene, cam_id)
+    o, _ = oracle_render(scene, cam_id)
+    for k in ("total_radiance", "direct_radiance", "albedo", "depth", "alpha"):
+        assert same_bits(g[k], o[k]), k
+    assert np.array_equal(g["triangle_id"], o["triangle_id"])
+    alpha = g["alpha"]
+    assert (alpha == 0).any(), "no sky pixel"
+    assert (alpha > 1.0).any(), "no pixel stopped early (alpha = hits / last index exceeds 1)"
+    scene.close()

@@ -354,3 +354,38 @@ def test_oracle_position_adjoint_matches_finite_differences():
         errs = np.array(errs)
         print("smooth" if smooth else "flat", "FD relative errors", np.round(errs, 5))
         assert np.median(errs) <= 2e-2 and np.mean(errs <= 5e-2) >= 0.6, (smooth, np.round(errs, 4))
+
+
+def test_oracle_adaptive_sampling_rule():
+    """cpu_path_tracer.ipp:198-226 restated: with a tolerance no interval can miss, every lit pixel
+    stops at the first batch check (sample index = samples_per_batch) and is divided by that index,
+    so its radiance is the sum of samples_per_batch + 1 samples over samples_per_batch; sky pixels
+    stop at the first miss check."""
+    from helpers import oracle_render
+
+    scene, cam_id = workloads.plain_direct(posts=65, resolution=16)
+    scene[cam_id].look_in_direction((0.454, 0.0, -0.891))
+    opt = scene.pathtracer.options
+    opt.samples = 7
+    ref, _ = oracle_render(scene, cam_id)                 # fixed 7 samples
+    opt.samples = 50
+    opt.adaptive_sampling = True
+    opt.samples_per_batch = 6
+    opt.samples_to_detect_miss = 4
+    opt.sampling_tolerance = 1e30
+    ada, _ = oracle_render(scene, cam_id)
+    lit = ref["alpha"] > 0
+    sky = ref["alpha"] == 0
+    assert lit.any() and sky.any()
+    # lit: 7 samples summed, divided by 6 instead of 7
+    assert np.allclose(ada["total_radiance"][:, lit], ref["total_radiance"][:, lit] * 7.0 / 6.0, rtol=2e-6, atol=0)
+    assert np.allclose(ada["alpha"][lit], ref["alpha"][lit] * 7.0 / 6.0, rtol=1e-6)
+    assert np.all(ada["alpha"][sky] == 0) and np.all(np.isinf(ada["depth"][sky]))
+    # tolerance 0 with random light sampling: no early batch stop while the variance is positive
+    opt.sampling_tolerance = 0.0
+    opt.deterministic_light = False
+    opt.samples = 13
+    ada0, _ = oracle_render(scene, cam_id)
+    opt.adaptive_sampling = False
+    full, _ = oracle_render(scene, cam_id)
+    assert np.array_equal(ada0["total_radiance"][:, lit], full["total_radiance"][:, lit])

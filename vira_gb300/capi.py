@@ -49,6 +49,8 @@ class PtOptions(C.Structure):
         ("deterministic_light", C.c_uint32), ("rr_depth", C.c_uint32), ("has_ambient", C.c_uint32),
         ("seed", C.c_uint64), ("frame", C.c_uint32), ("nbands", C.c_uint32),
         ("ambient", C.c_float * MAX_BANDS), ("background", C.c_float * MAX_BANDS),
+        ("adaptive_sampling", C.c_uint32), ("samples_per_batch", C.c_uint32), ("sampling_tolerance", C.c_float),
+        ("samples_to_detect_miss", C.c_uint32),
     ]
 
 

@@ -88,6 +88,11 @@ struct DevState {
     uint32_t* sq_slot[VGB_MAX_LIGHTS];
     float* sq_con[VGB_MAX_LIGHTS];   // [B][P]
     float4* hit;         // [P] closest-hit record per queue item: (t, id bits, w(v1), w(v2))
+    // adaptive sampling: per pixel the sums of the path-radiance magnitude and of its square,
+    // and the sample index at which the pixel stopped (0 while it samples on)
+    float* as1;
+    float* as2;
+    uint32_t* anum;
     uint32_t* counters;  // see C_* below
     uint64_t* stats;     // [0] nodes, [1] tris, [2] closest rays, [3] shadow rays
     size_t P;            // plane stride
@@ -425,6 +430,7 @@ __global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s,
         F3 ro, rd;
         if (bounce == 0) {
             if (!camera_ray(fp, item, sample, slot, ro, rd)) continue;
+            if (fp.opt.adaptive_sampling && sample != 0 && st.anum[slot]) continue;  // pixel has stopped
         } else {
             slot = in_queue[item];
             ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
@@ -481,6 +487,10 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         if (active) {
             if (bounce == 0) {
                 active = camera_ray(fp, item, sample, slot, ro, rd);
+                if (active && fp.opt.adaptive_sampling) {
+                    if (sample == 0) { st.as1[slot] = 0.f; st.as2[slot] = 0.f; st.anum[slot] = 0u; }
+                    else if (st.anum[slot]) active = false;  // the pixel has stopped sampling
+                }
                 if (active) {
                     if (sample == 0) {
 #pragma unroll
@@ -680,32 +690,70 @@ __global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene 
 
 // ------------------------------------------------------------------ k_end_sample
 template <int NB>
-__global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_constant__ FrameParams fp, uint32_t last, FilmOut f) {
+__global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_constant__ FrameParams fp, uint32_t smp,
+                                                    uint32_t last, FilmOut f) {
     const size_t P = st.P;                       // plane stride of the scratch state
     const uint32_t nb = fp.nb;
     const uint32_t npix = fp.cam.width * fp.cam.height;
     const size_t FP = npix;                      // plane stride of the caller's film
-    const float sf = (float)fp.opt.samples;
+    const float sf_all = (float)fp.opt.samples;
+    const bool adaptive = fp.opt.adaptive_sampling != 0;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
-        const uint32_t pend = st.pend[p];
         const bool want_dir = (fp.aux & AUX_DIR) != 0;
+        uint32_t stopped = adaptive ? st.anum[p] : 0u;
         float tot[NB];
+        if (!stopped) {
+            const uint32_t pend = st.pend[p];
+            float prs[NB];
 #pragma unroll
-        for (int k = 0; k < NB; ++k) {
-            if (k < (int)nb) {
-                float pr = (pend & kPradEmpty) ? 0.f : st.prad[k * P + p];
-                if (pend & kPendMask) {
-                    const float br = st.brad[k * P + p];
-                    pr += br;
-                    if ((pend & kPendMask) == 1u && want_dir) st.adir[k * P + p] += br;
+            for (int k = 0; k < NB; ++k) {
+                prs[k] = 0.f;
+                if (k < (int)nb) {
+                    float pr = (pend & kPradEmpty) ? 0.f : st.prad[k * P + p];
+                    if (pend & kPendMask) {
+                        const float br = st.brad[k * P + p];
+                        pr += br;
+                        if ((pend & kPendMask) == 1u && want_dir) st.adir[k * P + p] += br;
+                    }
+                    prs[k] = pr;
+                    tot[k] = st.arad[k * P + p] + pr;
+                    st.arad[k * P + p] = tot[k];
                 }
-                tot[k] = st.arad[k * P + p] + pr;
-                st.arad[k * P + p] = tot[k];
             }
+            // (the fold state is rewritten for every pixel by the next sample's camera rays)
+            if (adaptive) {
+                // unidirectional's stopping rule (cpu_path_tracer.ipp:198-226)
+                float sq = 0.f;
+#pragma unroll
+                for (int k = 0; k < NB; ++k) if (k < (int)nb) sq += prs[k] * prs[k];
+                const float illum = sqrtf(sq);
+                const float s1 = st.as1[p] + illum, s2 = st.as2[p] + illum * illum;
+                st.as1[p] = s1;
+                st.as2[p] = s2;
+                bool stop = false;
+                if (smp != 0 && smp % fp.opt.samples_to_detect_miss == 0 && st.adep[p] == 0.f) {
+                    stop = true;
+                } else if (smp != 0 && smp % fp.opt.samples_per_batch == 0) {
+                    if (s1 == 0.f) {
+                        stop = true;
+                    } else {
+                        const float n = (float)smp + 1.f;
+                        const float mu = s1 / n;
+                        const float variance = (1.f / (n - 1.f)) * (s2 - (s1 * s1) / n);
+                        const float I = 1.96f * sqrtf(variance / n);
+                        stop = I <= fp.opt.sampling_tolerance * mu;
+                    }
+                }
+                if (stop) { st.anum[p] = smp; stopped = smp; }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NB; ++k) tot[k] = (k < (int)nb) ? st.arad[k * P + p] : 0.f;
         }
-        // (the fold state is rewritten for every pixel by the next sample's camera rays)
         if (!last) continue;
-        // unidirectional (cpu_path_tracer.ipp:229-240) + RenderPasses::updateImages (passes.ipp:82-128)
+        // unidirectional (cpu_path_tracer.ipp:229-240) + RenderPasses::updateImages (passes.ipp:82-128);
+        // a pixel that stopped early divides by the index of its last sample, as the reference does
+        const float sf = stopped ? (float)stopped : sf_all;
         const uint32_t count = (fp.aux & AUX_DEP) ? st.acnt[p] : 0u;
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
@@ -939,6 +987,7 @@ vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
     AL(st.adep, P * f); AL(st.acnt, P * u); AL(st.atri, P * u);
     AL(st.pq[0], P * u); AL(st.pq[1], P * u);
     AL(st.hit, P * sizeof(float4));
+    AL(st.as1, P * f); AL(st.as2, P * f); AL(st.anum, P * u);
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
         if (l < L) {
             AL(st.sq_org[l], 3 * P * f); AL(st.sq_dir[l], 3 * P * f); AL(st.sq_tmax[l], P * f);
@@ -1025,7 +1074,7 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
         }
         {
             Prof p(ctx, 2);
-            k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+            k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
         }
         launches++;
     }
@@ -1274,6 +1323,8 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: null camera/options/film");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render: build the BVH first");
     if (opts->samples == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: options.samples must be >= 1");
+    if (opts->adaptive_sampling && (opts->samples_per_batch == 0 || opts->samples_to_detect_miss == 0))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: adaptive sampling needs samples_per_batch and samples_to_detect_miss >= 1");
     if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: nbands differs from the scene");
     if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: at most 8 lights");
@@ -1322,7 +1373,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     }
     f.total = df[0]; f.direct = df[1]; f.indirect = df[2]; f.power = df[3]; f.albedo = df[4];
     f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
-    fp.aux = aux_for(f);
+    fp.aux = aux_for(f) | (opts->adaptive_sampling ? AUX_DEP : 0u);  // the miss test reads the depth sum
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     uint32_t launches = 0;
     ctx->prof_used = 0;
@@ -1505,7 +1556,7 @@ void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film
             }
             q ^= 1u;
         }
-        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
         launches++;
     }
 }
@@ -1520,6 +1571,8 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     if (!film->on_device)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: film planes must be device memory (on_device = 1)");
     if (opts->samples == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: options.samples must be >= 1");
+    if (opts->adaptive_sampling)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: adaptive sampling keeps per-pixel statistics the fixed array has no room for; use vgb_render");
     if (opts->nbands != ctx->nbands)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: nbands differs from the scene");
     if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
@@ -1625,6 +1678,18 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
 }
 
 
+// Out-of-line traversal for the kernels that trace both ray kinds in one large body (k_batch,
+// the adjoint replay): one copy of the loop, called for closest-hit and occlusion rays, keeps
+// those kernels' instruction footprint small (instruction fetch was their leading stall; the
+// batch kernel ran 12 % and the adjoint 28 % faster than with both loops inlined).
+template <int L>
+__device__ __noinline__ void trace_ool(const uint4* __restrict__ nodes, const float4* __restrict__ tris, WRay r,
+                                       float tmax, bool any, HitOut& h, uint32_t& err) {
+    Counters c{0, 0};
+    if (L == 8) traverse8_rt<false>(nodes, tris, r, tmax, any, h, err, c);
+    else traverse_rt<false>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, any, h, err, c);
+}
+
 // ====================================================================== batched trajectory
 namespace {
 
@@ -1671,7 +1736,6 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
     const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
     const uint32_t n_items = (bp.total_tiles + bp.tile_stride - 1) / bp.tile_stride;
     uint32_t err = 0, nclosest = 0, nshadow = 0;
-    Counters cnt{0, 0};
     while (true) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(counter, bp.grab);
@@ -1691,6 +1755,8 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
             for (int p = 0; p < PL; ++p) acc[p * 32 + lane] = 0.f;
             uint32_t first_tri = VGB_NO_HIT;
             uint32_t count = 0;
+            float s1 = 0.f, s2 = 0.f;   // adaptive sampling: magnitude sums
+            uint32_t stopped = 0;       // adaptive sampling: sample index at which the pixel stopped
             for (uint32_t sample = 0; sample < F.samples; ++sample) {
                 // camera ray (camera_ray with this frame's camera and key)
                 float X = (float)pi, Y = (float)pj;
@@ -1727,7 +1793,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     HitOut h;
                     h.U = h.V = h.W = 0.f; h.det = 1.f;
                     const WRay wr = make_wray(ro, rd);
-                    traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+                    trace_ool<L>(s.nodes, s.tris, wr, 0.f, false, h, err);
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
@@ -1780,7 +1846,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                         if (lpdf > 0) {
                             HitOut hs;
                             const WRay ws = make_wray(Pp, Ld);
-                            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+                            trace_ool<L>(s.nodes, s.tris, ws, dist, true, hs, err);
                             nshadow++;
                             if (hs.id == VGB_NO_HIT) {
                                 const float nl = dot(N, Ld);
@@ -1813,12 +1879,36 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                 }
 #pragma unroll
                 for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
+                if (opt.adaptive_sampling) {
+                    // unidirectional's stopping rule (cpu_path_tracer.ipp:198-226)
+                    float sq = 0.f;
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) if (k < (int)nb) sq += PRAD(k) * PRAD(k);
+                    const float illum = sqrtf(sq);
+                    s1 = s1 + illum;
+                    s2 = s2 + illum * illum;
+                    bool stop = false;
+                    if (sample != 0 && sample % opt.samples_to_detect_miss == 0 && ACC(3 * NB + 3) == 0.f) {
+                        stop = true;
+                    } else if (sample != 0 && sample % opt.samples_per_batch == 0) {
+                        if (s1 == 0.f) {
+                            stop = true;
+                        } else {
+                            const float n = (float)sample + 1.f;
+                            const float mu = s1 / n;
+                            const float variance = (1.f / (n - 1.f)) * (s2 - (s1 * s1) / n);
+                            const float I = 1.96f * sqrtf(variance / n);
+                            stop = I <= opt.sampling_tolerance * mu;
+                        }
+                    }
+                    if (stop) { stopped = sample; break; }
+                }
 #undef PRAD
 #undef BRAD
             }
             // RenderPasses::updateImages for this pixel
             const size_t P = (size_t)W * H;
-            const float sf = (float)F.samples;
+            const float sf = stopped ? (float)stopped : (float)F.samples;  // the reference divides by the last index
             const FilmOut& f = F.film;
 #pragma unroll
             for (int k = 0; k < NB; ++k) {
@@ -1898,6 +1988,8 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
     if (!frames || nframes == 0 || !opts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: no frames or options");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_batch: build the BVH first");
     if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: nbands differs from the scene");
+    if (opts->adaptive_sampling && (opts->samples_per_batch == 0 || opts->samples_to_detect_miss == 0))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: adaptive sampling needs samples_per_batch and samples_to_detect_miss >= 1");
     // schedule: frames by decreasing samples per pixel (cost per tile), then by index
     std::vector<uint32_t> order(nframes);
     for (uint32_t f = 0; f < nframes; ++f) {
@@ -2068,7 +2160,6 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
                                           const float* g, AdjVtx<NB>* vx, float* bgc, float* prad,
                                           uint32_t& err, uint32_t& nrays) {
     const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
-    Counters cnt{0, 0};
     F3 ro, rd;
     pixel_ray(cam, pi, pj, slot, sample, frame, k0, k1, ro, rd);
     float thr[NB];
@@ -2079,7 +2170,7 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
         const WRay wr = make_wray(ro, rd);
-        traverse_any_layout<L, false, false>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+        trace_ool<L>(s.nodes, s.tris, wr, 0.f, false, h, err);
         nrays++;
         if (h.id == VGB_NO_HIT) {
             if (opt.simulate_lighting && opt.show_background) {
@@ -2141,7 +2232,7 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
             if (!(lpdf > 0)) continue;
             HitOut hs;
             const WRay ws = make_wray(Pp, Ld);
-            traverse_any_layout<L, true, false>(s.nodes, s.tris, ws, dist, hs, err, cnt);
+            trace_ool<L>(s.nodes, s.tris, ws, dist, true, hs, err);
             nrays++;
             if (hs.id != VGB_NO_HIT) continue;
             const float nl = dot(N, Ld);
@@ -2561,6 +2652,8 @@ vgb_status adjoint_common(vgb_context* ctx, const vgb_camera* cam, const vgb_lig
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, w + ": build the BVH first");
     if (opts->samples == 0 || opts->nbands != ctx->nbands || nlights > VGB_MAX_LIGHTS || (nlights && !lights))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": samples, nbands or lights invalid");
+    if (opts->adaptive_sampling)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": adaptive sampling is not differentiated (render with fixed samples)");
     if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": at most 3 bounces");
     cudaSetDevice(ctx->device);
     FrameParams fp;
@@ -2635,6 +2728,8 @@ extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const v
     if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: nbands differs from the scene");
     if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: at most 3 bounces");
+    if (opts->adaptive_sampling)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: adaptive sampling is not differentiated");
     cudaSetDevice(ctx->device);
     std::vector<DevView> hv(nviews);
     uint32_t tiles = 0;

@@ -243,6 +243,10 @@ class PathTracerOptions:
     frame: int = 0
     deterministic_light: bool = False
     rr_depth: int = 0
+    adaptive_sampling: bool = False
+    samples_per_batch: int = 30
+    sampling_tolerance: float = 0.05
+    samples_to_detect_miss: int = 30
 
 
 @dataclass
@@ -284,6 +288,10 @@ class PathTracer:
         o.rr_depth = int(opt.rr_depth)
         o.seed, o.frame = int(opt.seed), int(opt.frame)
         o.nbands = scene.bands.size
+        o.adaptive_sampling = int(bool(opt.adaptive_sampling))
+        o.samples_per_batch = int(opt.samples_per_batch)
+        o.sampling_tolerance = float(opt.sampling_tolerance)
+        o.samples_to_detect_miss = int(opt.samples_to_detect_miss)
         if scene.ambient is not None:
             o.has_ambient = 1
             for k in range(scene.bands.size):
