@@ -84,6 +84,16 @@ typedef struct vgb_light {
 
 /* ---- path tracer options: CPUPathTracerOptions + RenderPasses switches ----------
  * include/vira/rendering/cpu_path_tracer.hpp:30-43, include/vira/rendering/passes.hpp:72-84. */
+/* ---- EATWT denoiser options (rendering/cpu_denoise.hpp:10-19, EATWTOptions) ---------- */
+typedef struct vgb_denoise_options {
+    uint32_t levels_direct;      /* MAX_LEVELS_DIRECT (5) */
+    uint32_t levels_indirect;    /* MAX_LEVELS_INDIRECT (5) */
+    float depth_threshold;       /* DEPTH_THRESHOLD (0.2) */
+    float normal_threshold;      /* NORMAL_THRESHOLD (0.5) */
+    float min_normal_weight;     /* MIN_NORMAL_WEIGHT (0.3) */
+    float epsilon;               /* EPSILON (1e-6) */
+} vgb_denoise_options;
+
 typedef struct vgb_pt_options {
     uint32_t samples;            /* options.samples (>= 1) */
     uint32_t bounces;            /* options.bounces */
@@ -107,6 +117,12 @@ typedef struct vgb_pt_options {
     uint32_t samples_per_batch;      /* options.samples_per_batch (reference default 30) */
     float sampling_tolerance;        /* options.sampling_tolerance (reference default 0.05) */
     uint32_t samples_to_detect_miss; /* options.samples_to_detect_miss (reference default 30) */
+    /* options.denoise (cpu_path_tracer.ipp:124-134): after the samples, the direct and indirect
+     * radiance are filtered by the edge-avoiding a-trous wavelet transform guided by albedo,
+     * depth and normal, the total radiance becomes their sum and the received power follows
+     * from it.  0 = off (reference default). */
+    uint32_t denoise;
+    vgb_denoise_options denoiser;    /* zero-filled: the reference's EATWTOptions defaults */
 } vgb_pt_options;
 
 /* ---- film: RenderPasses planes (caller-owned; NULL = pass not written) ----------
@@ -305,6 +321,15 @@ typedef struct vgb_view {
 VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* views, uint32_t nviews,
                                             const vgb_pt_options* opts, float* d_texture, float* d_position,
                                             double* loss);
+/* denoiseSpectralRadianceEATWT (rendering/cpu_denoise.ipp:9-214) on caller planes: direct and
+ * indirect ([B][H][W], filtered in place), albedo ([B][H][W]), depth ([H][W]) and normal_global
+ * ([3][H][W]).  o may be NULL (reference defaults).  The reference indexes its images as
+ * (y, x), that is transposed, so each level filters along columns first and rows second; for
+ * square images this equals the reference, for other sizes the reference reads out of range and
+ * this applies the same column-then-row order.  All planes device memory if on_device else host. */
+VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
+                               const float* depth, const float* normal, uint32_t width, uint32_t height,
+                               uint32_t nbands, const vgb_denoise_options* o, int on_device);
 /* Replaces the albedo texture (same size) without re-uploading the mesh or rebuilding the BVH. */
 VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h);
 

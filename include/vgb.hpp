@@ -178,6 +178,7 @@ struct CPUPathTracerOptions {  // cpu_path_tracer.hpp:30-43, plus the RNG key an
     uint32_t frame = 0;
     bool deterministic_light = false;
     uint32_t rr_depth = 0;
+    bool denoise = false;                  // EATWT with the reference's default options
     bool adaptive_sampling = false;
     size_t samples_per_batch = 30;
     float sampling_tolerance = 0.05f;
@@ -297,6 +298,7 @@ inline void GpuPathTracer::render(Camera& camera, Scene& scene) {
     o.samples_per_batch = (uint32_t)options.samples_per_batch;
     o.sampling_tolerance = options.sampling_tolerance;
     o.samples_to_detect_miss = (uint32_t)options.samples_to_detect_miss;
+    o.denoise = options.denoise;
     if (!scene.ambient.empty()) {
         o.has_ambient = 1;
         for (uint32_t b = 0; b < B; ++b) o.ambient[b] = scene.ambient[b];

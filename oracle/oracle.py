@@ -52,6 +52,8 @@ def load():
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
                                     C.POINTER(capi.Film), U32, U32, C.c_int, P]),
         "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
+        "oracle_denoise": (C.c_int, [P, P, P, P, P, U32, U32, U32, U32, U32, C.c_float, C.c_float, C.c_float,
+                                     C.c_float]),
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
                                                C.c_int]),
     }
@@ -108,6 +110,23 @@ def pixel_solid_angle(cam: capi.Camera):
 
 def blackbody_band(T, lmin_m, lmax_m, steps=1000):
     return load().oracle_blackbody_band(T, lmin_m, lmax_m, steps)
+
+
+def denoise(direct, indirect, albedo, depth, normal, levels_direct=5, levels_indirect=5, depth_threshold=0.2,
+            normal_threshold=0.5, min_normal_weight=0.3, epsilon=1e-6):
+    """EATWT denoiser restated (square images): returns filtered (direct, indirect) planes [B][H][W]."""
+    d = np.array(direct, np.float32, order="C", copy=True)
+    i = np.array(indirect, np.float32, order="C", copy=True)
+    a = np.ascontiguousarray(albedo, np.float32)
+    z = np.ascontiguousarray(depth, np.float32)
+    n = np.ascontiguousarray(normal, np.float32)
+    B, H, W = d.shape
+    rc = load().oracle_denoise(d.ctypes.data, i.ctypes.data, a.ctypes.data, z.ctypes.data, n.ctypes.data, W, H, B,
+                               levels_direct, levels_indirect, depth_threshold, normal_threshold, min_normal_weight,
+                               epsilon)
+    if rc != 0:
+        raise ValueError("oracle_denoise rejected its arguments (square images only)")
+    return d, i
 
 
 class OracleScene:

@@ -1401,3 +1401,90 @@ OAPI int oracle_adjoint(void* h, const vgb_camera* cam, const vgb_light* lights,
         for (size_t v = 0; v < s.nverts; ++v) gz[v] += gp[3 * v + 2];
     return rc;
 }
+
+// ==================================================================== EATWT denoiser
+// denoiseSpectralRadianceEATWT (include/implementation/rendering/cpu_denoise.ipp:9-214) with the
+// reference's image indexing restated: Image(i, j) is data[i + j * width] (image.ipp:134-140) and
+// the denoiser calls Image(y, x), so every access below is at(y, x) = y + x * width.  That is
+// only in range for square images, so other sizes are rejected.  Planes are planar ([B][H][W],
+// [H][W], [3][H][W]); direct and indirect are filtered in place.  std::exp and std::pow as in
+// the reference.
+OAPI int oracle_denoise(float* direct, float* indirect, const float* albedo, const float* depth,
+                        const float* normal, uint32_t width, uint32_t height, uint32_t nbands,
+                        uint32_t levels_direct, uint32_t levels_indirect, float depth_threshold,
+                        float normal_threshold, float min_normal_weight, float epsilon) {
+    if (!direct || !indirect || !albedo || !depth || !normal || width == 0 || width != height || nbands == 0 ||
+        nbands > VGB_MAX_BANDS)
+        return 1;
+    static constexpr float K1[5] = {1.0f / 16.0f, 4.0f / 16.0f, 6.0f / 16.0f, 4.0f / 16.0f, 1.0f / 16.0f};
+    const int W = (int)width, H = (int)height;
+    const size_t P = (size_t)W * H;
+    const uint32_t B = nbands;
+    auto at = [&](int i, int j) { return (size_t)i + (size_t)j * (size_t)W; };
+    std::vector<float> dil(B * P), iil(B * P);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t q = at(y, x);
+            for (uint32_t c = 0; c < B; ++c) {
+                dil[c * P + q] = direct[c * P + q] / std::max(albedo[c * P + q], epsilon);
+                iil[c * P + q] = indirect[c * P + q] / std::max(albedo[c * P + q], epsilon);
+            }
+        }
+    auto filter_pixel = [&](const std::vector<float>& input, int cx, int cy, int step, bool horizontal,
+                            std::vector<float>& output) {
+        float sum[VGB_MAX_BANDS] = {0};
+        float weight_sum = 0.0f;
+        const float center_depth = depth[at(cy, cx)];
+        const size_t cq = at(cy, cx);
+        const float cnx = normal[cq], cny = normal[P + cq], cnz = normal[2 * P + cq];
+        for (int k = -2; k <= 2; ++k) {
+            int sx = horizontal ? cx + k * step : cx;
+            int sy = horizontal ? cy : cy + k * step;
+            sx = std::clamp(sx, 0, W - 1);
+            sy = std::clamp(sy, 0, H - 1);
+            const float kernel_weight = K1[k + 2];
+            const size_t sq = at(sy, sx);
+            const float sample_depth = depth[sq];
+            const float depth_ratio = std::max(center_depth, sample_depth) / (std::min(center_depth, sample_depth) + epsilon);
+            const float depth_weight = depth_ratio < (1.0f + depth_threshold) ? 1.0f : std::exp(-(depth_ratio - 1.0f) / depth_threshold);
+            const float normal_dot = cnx * normal[sq] + cny * normal[P + sq] + cnz * normal[2 * P + sq];
+            const float normal_similarity = std::max(0.0f, normal_dot);
+            const float normal_weight = std::max(min_normal_weight,
+                                                 std::exp(-std::pow(1.0f - normal_similarity, 2.0f) / normal_threshold));
+            const float total_weight = kernel_weight * depth_weight * normal_weight;
+            for (uint32_t c = 0; c < B; ++c) sum[c] += input[c * P + sq] * total_weight;
+            weight_sum += total_weight;
+        }
+        if (weight_sum > epsilon) {
+            for (uint32_t c = 0; c < B; ++c) output[c * P + cq] = sum[c] / weight_sum;
+        } else {
+            for (uint32_t c = 0; c < B; ++c) output[c * P + cq] = input[c * P + cq];
+        }
+    };
+    auto denoise = [&](std::vector<float>& illum, uint32_t max_levels) {
+        std::vector<float> temp(B * P);
+        std::vector<float>* current = &illum;
+        std::vector<float>* next = &temp;
+        for (uint32_t level = 0; level < max_levels; ++level) {
+            const int step = 1 << level;
+            for (int y = 0; y < H; ++y)
+                for (int x = 0; x < W; ++x) filter_pixel(*current, x, y, step, true, *next);
+            std::swap(current, next);
+            for (int y = 0; y < H; ++y)
+                for (int x = 0; x < W; ++x) filter_pixel(*current, x, y, step, false, *next);
+            std::swap(current, next);
+        }
+        if (current != &illum) illum = *current;
+    };
+    denoise(dil, levels_direct);
+    denoise(iil, levels_indirect);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t q = at(y, x);
+            for (uint32_t c = 0; c < B; ++c) {
+                direct[c * P + q] = dil[c * P + q] * albedo[c * P + q];
+                indirect[c * P + q] = iil[c * P + q] * albedo[c * P + q];
+            }
+        }
+    return 0;
+}

@@ -389,3 +389,23 @@ def test_oracle_adaptive_sampling_rule():
     opt.adaptive_sampling = False
     full, _ = oracle_render(scene, cam_id)
     assert np.array_equal(ada0["total_radiance"][:, lit], full["total_radiance"][:, lit])
+
+
+def test_oracle_denoiser_properties():
+    """EATWT restated: a constant illumination (direct = albedo * c) passes through unchanged,
+    and per-pixel noise on a smooth surface loses most of its variance."""
+    rng = np.random.default_rng(2)
+    B, N = 4, 32
+    alb = rng.uniform(0.05, 0.3, (B, N, N)).astype(np.float32)
+    depth = np.full((N, N), 1000.0, np.float32) + rng.uniform(0, 1, (N, N)).astype(np.float32)
+    normal = np.zeros((3, N, N), np.float32)
+    normal[2] = 1.0
+    d0 = (alb * 0.7).astype(np.float32)
+    i0 = (alb * 0.1).astype(np.float32)
+    d, i = oracle.denoise(d0, i0, alb, depth, normal)
+    assert np.allclose(d, d0, rtol=1e-5) and np.allclose(i, i0, rtol=1e-5)
+    noisy = (alb * (0.7 + 0.2 * rng.standard_normal((B, N, N)))).astype(np.float32)
+    d, _ = oracle.denoise(noisy, i0, alb, depth, normal)
+    assert np.std(d / alb) < 0.3 * np.std(noisy / alb)
+    with pytest.raises(ValueError):
+        oracle.denoise(noisy[:, :, :16], i0[:, :, :16], alb[:, :, :16], depth[:, :16], normal[:, :, :16])

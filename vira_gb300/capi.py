@@ -42,6 +42,11 @@ class Light(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("radius", C.c_float), ("radiance", C.c_float * MAX_BANDS)]
 
 
+class DenoiseOptions(C.Structure):
+    _fields_ = [("levels_direct", C.c_uint32), ("levels_indirect", C.c_uint32), ("depth_threshold", C.c_float),
+                ("normal_threshold", C.c_float), ("min_normal_weight", C.c_float), ("epsilon", C.c_float)]
+
+
 class PtOptions(C.Structure):
     _fields_ = [
         ("samples", C.c_uint32), ("bounces", C.c_uint32), ("show_background", C.c_uint32),
@@ -50,7 +55,7 @@ class PtOptions(C.Structure):
         ("seed", C.c_uint64), ("frame", C.c_uint32), ("nbands", C.c_uint32),
         ("ambient", C.c_float * MAX_BANDS), ("background", C.c_float * MAX_BANDS),
         ("adaptive_sampling", C.c_uint32), ("samples_per_batch", C.c_uint32), ("sampling_tolerance", C.c_float),
-        ("samples_to_detect_miss", C.c_uint32),
+        ("samples_to_detect_miss", C.c_uint32), ("denoise", C.c_uint32), ("denoiser", DenoiseOptions),
     ]
 
 
@@ -118,6 +123,7 @@ SIGNATURES = {
     "vgb_render_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), C.POINTER(BatchOptions)]),
     "vgb_batch_tuning": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
     "vgb_adjoint": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_denoise": (C.c_int, [_P, _P, _P, _P, _P, _P, _U32, _U32, _U32, _P, C.c_int]),
     "vgb_adjoint_positions": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
     "vgb_render_adjoint_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), _P, _P, C.POINTER(C.c_double)]),
     "vgb_texture_update": (C.c_int, [_P, _P, _U32, _U32]),

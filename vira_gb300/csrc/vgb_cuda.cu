@@ -909,6 +909,9 @@ struct vgb_context {
     void* d_views = nullptr;                 // DevView table of vgb_render_adjoint_batch
     size_t cap_views = 0;
     double* d_loss = nullptr;
+    // denoiser scratch: ping-pong illumination planes and the render's internal passes
+    float* d_dn = nullptr;
+    size_t cap_dn = 0;
 };
 
 namespace {
@@ -1096,6 +1099,167 @@ void dispatch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& fil
 }  // namespace
 
 // ====================================================================== C ABI
+// ====================================================================== EATWT denoiser
+// denoiseSpectralRadianceEATWT (rendering/cpu_denoise.ipp:9-214): the direct and indirect
+// radiance are divided by the albedo (clamped below by epsilon), filtered level by level with
+// the 5-tap binomial kernel at a stride of 2^level, each tap weighted by a depth-ratio and a
+// normal-similarity term, and multiplied back by the albedo.  The reference indexes its images
+// (y, x), i.e. transposed: its first ("horizontal") pass of a level runs along image columns and
+// its second along rows, which is the order used here (exactly the reference's on square images).
+namespace {
+
+__constant__ float kEatwtTaps[5] = {1.0f / 16.0f, 4.0f / 16.0f, 6.0f / 16.0f, 4.0f / 16.0f, 1.0f / 16.0f};
+
+struct DnOpts {
+    uint32_t levels_direct, levels_indirect;
+    float depth_threshold, normal_threshold, min_normal_weight, eps;
+};
+
+DnOpts dn_opts(const vgb_denoise_options* o) {
+    DnOpts d{5u, 5u, 0.2f, 0.5f, 0.3f, 1e-6f};  // EATWTOptions defaults (cpu_denoise.hpp:10-19)
+    if (!o) return d;
+    if (o->levels_direct) d.levels_direct = o->levels_direct;
+    if (o->levels_indirect) d.levels_indirect = o->levels_indirect;
+    if (o->depth_threshold != 0.f) d.depth_threshold = o->depth_threshold;
+    if (o->normal_threshold != 0.f) d.normal_threshold = o->normal_threshold;
+    if (o->min_normal_weight != 0.f) d.min_normal_weight = o->min_normal_weight;
+    if (o->epsilon != 0.f) d.eps = o->epsilon;
+    return d;
+}
+
+template <int NB>
+__global__ void k_dn_split(const float* __restrict__ direct, const float* __restrict__ indirect,
+                           const float* __restrict__ albedo, float* __restrict__ D, float* __restrict__ I, size_t P,
+                           uint32_t nb, float eps) {
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k >= (int)nb) break;
+            const float a = smax(albedo[k * P + p], eps);
+            D[k * P + p] = direct[k * P + p] / a;
+            I[k * P + p] = indirect[k * P + p] / a;
+        }
+    }
+}
+
+// One pass of one level over both illumination images (either may be null: its level count is
+// exhausted).  The tap weights depend only on depth and normal, so they are formed once.
+template <int NB>
+__global__ void k_dn_pass(const float* __restrict__ Din, float* __restrict__ Dout, const float* __restrict__ Iin,
+                          float* __restrict__ Iout, const float* __restrict__ depth, const float* __restrict__ normal,
+                          uint32_t W, uint32_t H, uint32_t nb, int step, int along_columns, const DnOpts o) {
+    const size_t P = (size_t)W * H;
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(p % W), y = (int)(p / W);
+        const float cd = depth[p];
+        const float cnx = normal[p], cny = normal[P + p], cnz = normal[2 * P + p];
+        float w[5];
+        size_t q[5];
+        float wsum = 0.f;
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            const int k = t - 2;
+            int sx = along_columns ? x : x + k * step;
+            int sy = along_columns ? y + k * step : y;
+            sx = min(max(sx, 0), (int)W - 1);
+            sy = min(max(sy, 0), (int)H - 1);
+            q[t] = (size_t)sy * W + sx;
+            const float sd = depth[q[t]];
+            const float ratio = smax(cd, sd) / (smin(cd, sd) + o.eps);
+            const float dw = ratio < (1.0f + o.depth_threshold) ? 1.0f : expf(-(ratio - 1.0f) / o.depth_threshold);
+            const float nd = (cnx * normal[q[t]] + cny * normal[P + q[t]]) + cnz * normal[2 * P + q[t]];
+            const float sim = smax(0.0f, nd);
+            const float om = 1.0f - sim;
+            const float nw = smax(o.min_normal_weight, expf(-(om * om) / o.normal_threshold));
+            w[t] = (kEatwtTaps[t] * dw) * nw;
+            wsum += w[t];
+        }
+        const bool norm = wsum > o.eps;
+#pragma unroll
+        for (int img = 0; img < 2; ++img) {
+            const float* in = img ? Iin : Din;
+            float* out = img ? Iout : Dout;
+            if (!in) continue;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k >= (int)nb) break;
+                float sum = 0.f;
+#pragma unroll
+                for (int t = 0; t < 5; ++t) sum += in[k * P + q[t]] * w[t];
+                out[k * P + p] = norm ? sum / wsum : in[k * P + p];
+            }
+        }
+    }
+}
+
+struct PowerScale { float v[VGB_MAX_BANDS]; };
+
+template <int NB>
+__global__ void k_dn_merge(const float* __restrict__ D, const float* __restrict__ I, const float* __restrict__ albedo,
+                           float* direct, float* indirect, float* __restrict__ total, float* __restrict__ power,
+                           const float* __restrict__ omega, const PowerScale ps, size_t P, uint32_t nb) {
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            if (k >= (int)nb) break;
+            const float a = albedo[k * P + p];
+            const float d = D[k * P + p] * a, i = I[k * P + p] * a;
+            if (direct) direct[k * P + p] = d;
+            if (indirect) indirect[k * P + p] = i;
+            const float t = d + i;  // renderPasses.total_radiance = direct + indirect
+            if (total) total[k * P + p] = t;
+            if (power) power[k * P + p] = (ps.v[k] * omega[p]) * t;
+        }
+    }
+}
+
+vgb_status ensure_dn_scratch(vgb_context* ctx, size_t floats) {
+    const size_t need = floats * sizeof(float);
+    if (need <= ctx->cap_dn) return VGB_OK;
+    dfree(ctx->d_dn);
+    ctx->d_dn = nullptr;
+    ctx->cap_dn = 0;
+    vgb_status s = dalloc(ctx, &ctx->d_dn, need);
+    if (s != VGB_OK) return s;
+    ctx->cap_dn = need;
+    return VGB_OK;
+}
+
+template <int NB>
+void launch_denoise_t(vgb_context* ctx, const float* in_d, const float* in_i, const float* albedo, const float* depth,
+                      const float* normal, uint32_t W, uint32_t H, uint32_t nb, const DnOpts& o, float* scratch,
+                      float* out_d, float* out_i, float* total, float* power, const float* omega, const PowerScale& ps) {
+    const size_t P = (size_t)W * H;
+    const int g = grid_for(ctx, P);
+    float* Db[2] = {scratch, scratch + nb * P};
+    float* Ib[2] = {scratch + 2 * nb * P, scratch + 3 * nb * P};
+    k_dn_split<NB><<<g, 256, 0, ctx->stream>>>(in_d, in_i, albedo, Db[0], Ib[0], P, nb, o.eps);
+    int cd = 0, ci = 0;  // buffer holding the current image
+    const uint32_t levels = std::max(o.levels_direct, o.levels_indirect);
+    for (uint32_t level = 0; level < levels; ++level) {
+        const int step = 1 << std::min<uint32_t>(level, 30u);
+        const bool fd = level < o.levels_direct, fi = level < o.levels_indirect;
+        for (int pass = 0; pass < 2; ++pass) {
+            k_dn_pass<NB><<<g, 256, 0, ctx->stream>>>(fd ? Db[cd] : nullptr, fd ? Db[cd ^ 1] : nullptr,
+                                                      fi ? Ib[ci] : nullptr, fi ? Ib[ci ^ 1] : nullptr, depth, normal,
+                                                      W, H, nb, step, pass == 0 ? 1 : 0, o);
+            if (fd) cd ^= 1;
+            if (fi) ci ^= 1;
+        }
+    }
+    k_dn_merge<NB><<<g, 256, 0, ctx->stream>>>(Db[cd], Ib[ci], albedo, out_d, out_i, total, power, omega, ps, P, nb);
+}
+
+void launch_denoise(vgb_context* ctx, const float* in_d, const float* in_i, const float* albedo, const float* depth,
+                    const float* normal, uint32_t W, uint32_t H, uint32_t nb, const DnOpts& o, float* scratch,
+                    float* out_d, float* out_i, float* total, float* power, const float* omega, const PowerScale& ps) {
+    if (nb <= 1) launch_denoise_t<1>(ctx, in_d, in_i, albedo, depth, normal, W, H, nb, o, scratch, out_d, out_i, total, power, omega, ps);
+    else if (nb <= 4) launch_denoise_t<4>(ctx, in_d, in_i, albedo, depth, normal, W, H, nb, o, scratch, out_d, out_i, total, power, omega, ps);
+    else launch_denoise_t<8>(ctx, in_d, in_i, albedo, depth, normal, W, H, nb, o, scratch, out_d, out_i, total, power, omega, ps);
+}
+
+}  // namespace
+
 extern "C" {
 
 VGB_API const char* vgb_version(void) { return "vira_gb300 0.1 (sm_103a)"; }
@@ -1140,7 +1304,7 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     dfree(ctx->d_frames);
     if (ctx->h_frames) cudaFreeHost(ctx->h_frames);
-    dfree(ctx->d_adj); dfree(ctx->d_views); dfree(ctx->d_loss);
+    dfree(ctx->d_adj); dfree(ctx->d_views); dfree(ctx->d_loss); dfree(ctx->d_dn);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1298,6 +1462,38 @@ VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) {
     return VGB_OK;
 }
 
+VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
+                               const float* depth, const float* normal, uint32_t width, uint32_t height,
+                               uint32_t nbands, const vgb_denoise_options* o, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!direct || !indirect || !albedo || !depth || !normal || width == 0 || height == 0 || nbands == 0 ||
+        nbands > VGB_MAX_BANDS)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "denoise: null plane, empty image or bands outside 1..8");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)width * height, BP = (size_t)nbands * P;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, 4 * BP + (on_device ? 0 : 3 * BP + 4 * P))) != VGB_OK) return s;
+    float *d = direct, *i = indirect;
+    const float *a = albedo, *z = depth, *n = normal;
+    if (!on_device) {
+        float* cur = ctx->d_dn + 4 * BP;
+        CK(cudaMemcpyAsync(cur, direct, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); d = cur; cur += BP;
+        CK(cudaMemcpyAsync(cur, indirect, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); i = cur; cur += BP;
+        CK(cudaMemcpyAsync(cur, albedo, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); a = cur; cur += BP;
+        CK(cudaMemcpyAsync(cur, depth, P * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); z = cur; cur += P;
+        CK(cudaMemcpyAsync(cur, normal, 3 * P * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); n = cur;
+    }
+    launch_denoise(ctx, d, i, a, z, n, width, height, nbands, dn_opts(o), ctx->d_dn, d, i, nullptr, nullptr, nullptr,
+                   PowerScale{});
+    CK(cudaGetLastError());
+    if (!on_device) {
+        CK(cudaMemcpyAsync(direct, d, BP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(indirect, i, BP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
 VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out) {
     if (!ctx || !out) return VGB_ERR_INVALID_ARGUMENT;
     *out = ctx->stats;
@@ -1373,12 +1569,33 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     }
     f.total = df[0]; f.direct = df[1]; f.indirect = df[2]; f.power = df[3]; f.albedo = df[4];
     f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
-    fp.aux = aux_for(f) | (opts->adaptive_sampling ? AUX_DEP : 0u);  // the miss test reads the depth sum
+    FilmOut fr = f;  // the planes the render itself writes
+    float* dn_scratch = nullptr;
+    if (opts->denoise) {
+        // options.denoise (cpu_path_tracer.ipp:124-134): the render writes un-denoised direct and
+        // indirect radiance (and albedo, depth and normal where the film has none) to scratch;
+        // the denoiser then writes direct, indirect, total and received power to the film.
+        if ((s = ensure_dn_scratch(ctx, (size_t)7 * B * P + 4 * P)) != VGB_OK) return s;
+        dn_scratch = ctx->d_dn;
+        float* extra = ctx->d_dn + (size_t)4 * B * P;
+        fr.total = nullptr; fr.power = nullptr;
+        fr.direct = extra; fr.indirect = extra + (size_t)B * P;
+        if (!fr.albedo) fr.albedo = extra + (size_t)2 * B * P;
+        if (!fr.normal) fr.normal = extra + (size_t)3 * B * P;
+        if (!fr.depth) fr.depth = extra + (size_t)3 * B * P + 3 * P;
+    }
+    fp.aux = aux_for(fr) | (opts->adaptive_sampling ? AUX_DEP : 0u);  // the miss test reads the depth sum
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     uint32_t launches = 0;
     ctx->prof_used = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    dispatch_render<false>(ctx, fp, f, launches);
+    dispatch_render<false>(ctx, fp, fr, launches);
+    if (dn_scratch) {
+        PowerScale ps{};
+        for (uint32_t k = 0; k < B && k < VGB_MAX_BANDS; ++k) ps.v[k] = cam->power_scale[k];
+        launch_denoise(ctx, fr.direct, fr.indirect, fr.albedo, fr.depth, fr.normal, cam->width, cam->height, B,
+                       dn_opts(&opts->denoiser), dn_scratch, f.direct, f.indirect, f.total, f.power, f.omega, ps);
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!film->on_device) {
@@ -1571,8 +1788,8 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     if (!film->on_device)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: film planes must be device memory (on_device = 1)");
     if (opts->samples == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: options.samples must be >= 1");
-    if (opts->adaptive_sampling)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: adaptive sampling keeps per-pixel statistics the fixed array has no room for; use vgb_render");
+    if (opts->adaptive_sampling || opts->denoise)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: adaptive sampling and denoising keep per-pixel planes the fixed array has no room for; use vgb_render");
     if (opts->nbands != ctx->nbands)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: nbands differs from the scene");
     if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
@@ -1998,6 +2215,10 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
             !fr.film.on_device || (fr.film.received_power && !fr.film.pixel_solid_angle))
             return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: frame " + std::to_string(f) +
                                                            ": samples/resolution/lights/film invalid (film must be device memory)");
+        if (opts->denoise && (!fr.film.direct_radiance || !fr.film.indirect_radiance || !fr.film.albedo ||
+                              !fr.film.depth || !fr.film.normal_global))
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: frame " + std::to_string(f) +
+                                                           ": denoising needs direct, indirect, albedo, depth and normal planes");
         order[f] = f;
     }
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return frames[a].samples > frames[b].samples; });
@@ -2099,6 +2320,24 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
         CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
     } else {
         CK(launch_batch_any(ctx, dfr, bp, threads, bps));
+    }
+    if (opts->denoise) {
+        // options.denoise per frame, on the frame's own planes (checked above)
+        size_t most = 0;
+        for (uint32_t f = 0; f < nframes; ++f) most = std::max(most, (size_t)frames[f].camera.width * frames[f].camera.height);
+        vgb_status ds = ensure_dn_scratch(ctx, 4 * (size_t)ctx->nbands * most);
+        if (ds != VGB_OK) return ds;
+        for (uint32_t f = 0; f < nframes; ++f) {
+            const vgb_frame& fr = frames[f];
+            const vgb_film& fl = fr.film;
+            PowerScale ps{};
+            for (uint32_t k = 0; k < ctx->nbands && k < VGB_MAX_BANDS; ++k) ps.v[k] = fr.camera.power_scale[k];
+            launch_denoise(ctx, fl.direct_radiance, fl.indirect_radiance, fl.albedo, fl.depth, fl.normal_global,
+                           fr.camera.width, fr.camera.height, ctx->nbands, dn_opts(&opts->denoiser), ctx->d_dn,
+                           fl.direct_radiance, fl.indirect_radiance, fl.total_radiance, fl.received_power,
+                           fl.pixel_solid_angle, ps);
+        }
+        CK(cudaGetLastError());
     }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -2652,8 +2891,8 @@ vgb_status adjoint_common(vgb_context* ctx, const vgb_camera* cam, const vgb_lig
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, w + ": build the BVH first");
     if (opts->samples == 0 || opts->nbands != ctx->nbands || nlights > VGB_MAX_LIGHTS || (nlights && !lights))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": samples, nbands or lights invalid");
-    if (opts->adaptive_sampling)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": adaptive sampling is not differentiated (render with fixed samples)");
+    if (opts->adaptive_sampling || opts->denoise)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": adaptive sampling and denoising are not differentiated");
     if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": at most 3 bounces");
     cudaSetDevice(ctx->device);
     FrameParams fp;
@@ -2728,8 +2967,8 @@ extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const v
     if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: nbands differs from the scene");
     if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: at most 3 bounces");
-    if (opts->adaptive_sampling)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: adaptive sampling is not differentiated");
+    if (opts->adaptive_sampling || opts->denoise)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: adaptive sampling and denoising are not differentiated");
     cudaSetDevice(ctx->device);
     std::vector<DevView> hv(nviews);
     uint32_t tiles = 0;

@@ -231,6 +231,23 @@ class SphereLight:
 
 # ============================================================================ path tracer
 @dataclass
+class EATWTOptions:
+    """EATWTOptions (include/vira/rendering/cpu_denoise.hpp:10-19)."""
+
+    max_levels_direct: int = 5
+    max_levels_indirect: int = 5
+    depth_threshold: float = 0.2
+    normal_threshold: float = 0.5
+    min_normal_weight: float = 0.3
+    epsilon: float = 1e-6
+
+    def to_c(self) -> capi.DenoiseOptions:
+        return capi.DenoiseOptions(int(self.max_levels_direct), int(self.max_levels_indirect),
+                                   float(self.depth_threshold), float(self.normal_threshold),
+                                   float(self.min_normal_weight), float(self.epsilon))
+
+
+@dataclass
 class PathTracerOptions:
     """CPUPathTracerOptions (include/vira/rendering/cpu_path_tracer.hpp:30-43) plus the
     counter-based RNG key and the two additions (deterministic light sampling, Russian roulette)."""
@@ -272,6 +289,7 @@ class PathTracer:
 
     def __init__(self):
         self.options = PathTracerOptions()
+        self.denoiser_options = EATWTOptions()   # CPUPathTracer::denoiserOptions
         self.render_passes = RenderPasses()
         self.last_stats = None
 
@@ -292,6 +310,8 @@ class PathTracer:
         o.samples_per_batch = int(opt.samples_per_batch)
         o.sampling_tolerance = float(opt.sampling_tolerance)
         o.samples_to_detect_miss = int(opt.samples_to_detect_miss)
+        o.denoise = int(bool(opt.denoise))
+        o.denoiser = self.denoiser_options.to_c()
         if scene.ambient is not None:
             o.has_ambient = 1
             for k in range(scene.bands.size):
