@@ -330,6 +330,49 @@ VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* vi
 VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
                                const float* depth, const float* normal, uint32_t width, uint32_t height,
                                uint32_t nbands, const vgb_denoise_options* o, int on_device);
+/* ---- sensor chain after the film ------------------------------------------------------
+ * Camera::simulateSensor (cameras/camera.ipp:1218-1240): received power -> photon counts
+ * (getPhotonCounts, camera.ipp:1286-1330; optional filter mosaic and Poisson photon noise) ->
+ * electrons through the quantum efficiency plus the noise model's electrons (NoiseModel::simulate,
+ * noise_models/noise_model.ipp:36-74: Poisson dark current x exposure time, Gaussian readout,
+ * sinusoidal fixed pattern) -> gain, clamp to max ADU, normalised (Photosite::exposePixel,
+ * photosites/photosite.ipp:125-136).  The reference draws from std::mt19937; here every draw
+ * comes from the counter-based Philox stream keyed by (seed, frame) and the pixel, so a sensor
+ * image is reproducible.  Without noise the result is deterministic and equals the reference's
+ * arithmetic. */
+typedef struct vgb_sensor {
+    float exposure_time;              /* s (Camera default 0.01) */
+    float photon_energy[8];           /* J per band, h c / centre wavelength (TSpectral::photonEnergies) */
+    float quantum_efficiency[8];      /* PhotositeConfig::quantum_efficiency */
+    float gain;                       /* ADU per electron (PhotositeConfig::gain) */
+    float max_adu;                    /* linear_scale_factor * (2^bit_depth - 1) */
+    uint32_t simulate_photon_noise;   /* Poisson photon counts where the pixel's total count >= 1 */
+    uint32_t noise_model;             /* 1: NoiseModel::simulate per pixel */
+    float dark_current;               /* NoiseModelConfig::dark_current */
+    float readout_noise_mean;         /* NoiseModelConfig::readout_noise_mean */
+    float readout_noise_std;          /* NoiseModelConfig::readout_noise_std */
+    float horizontal_scale;           /* NoiseModelConfig::horizontal_scale */
+    float vertical_scale;             /* NoiseModelConfig::vertical_scale */
+    uint32_t horizontal_pattern_period;
+    uint32_t vertical_pattern_period;
+    uint32_t frame;                   /* RNG key word */
+    uint64_t seed;                    /* RNG key */
+    const float* filter_mosaic;       /* [B][H][W] band transmission per pixel, or NULL */
+} vgb_sensor;
+
+/* received_power [B][H][W] -> image [H][W] in 0..1.  Planes (and the mosaic) device memory if
+ * on_device else host. */
+VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_power, uint32_t width,
+                                       uint32_t height, uint32_t nbands, const vgb_sensor* sensor,
+                                       float* image, int on_device);
+/* Image::convolveSpatial (images/image.ipp:1267-1340) of received_power ([B][H][W], in place)
+ * with a per-band kernel ([B][kh][kw]): out(x, y) = sum over (kx, ky) of
+ * in(x + kx - kw/2, y + ky - kh/2) * kernel(kx, ky), zero outside the image, rows of the kernel
+ * outer.  The reference switches to an FFT for kernels of 256 or more taps (images/image.ipp:
+ * 1012-1059), which equals this sum up to rounding.  Kernel sides up to 127. */
+VGB_API vgb_status vgb_psf_convolve(vgb_context* ctx, float* received_power, uint32_t width, uint32_t height,
+                                    uint32_t nbands, const float* kernel, uint32_t kernel_w, uint32_t kernel_h,
+                                    int on_device);
 /* Replaces the albedo texture (same size) without re-uploading the mesh or rebuilding the BVH. */
 VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h);
 

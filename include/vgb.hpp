@@ -63,6 +63,28 @@ struct SpectralBands {
         return b;
     }
     uint32_t size() const { return (uint32_t)lo.size(); }
+    // TSpectral::photonEnergies: h c / centre wavelength in FP32 (spectral_data.ipp:125-128)
+    std::vector<float> photonEnergies() const {
+        std::vector<float> e;
+        for (uint32_t i = 0; i < size(); ++i) e.push_back((6.62607015e-34f * 299792458.f) / ((lo[i] + hi[i]) / 2.f));
+        return e;
+    }
+};
+
+// PhotositeConfig (photosites/photosite.hpp:19-45); an empty quantum_efficiency means defaultQE.
+struct PhotositeConfig {
+    uint32_t bit_depth = 8;
+    float gain = 0.333333f;
+    float linear_scale_factor = 1.f;
+    std::vector<float> quantum_efficiency;
+    float maxADU() const { return linear_scale_factor * (std::pow(2.f, (float)bit_depth) - 1.f); }
+};
+
+// NoiseModelConfig (noise_models/noise_model.hpp:16-25)
+struct NoiseModelConfig {
+    float dark_current = 0, readout_noise_mean = 0, readout_noise_std = 0;
+    float horizontal_scale = 0, vertical_scale = 0;
+    uint32_t horizontal_pattern_period = 0, vertical_pattern_period = 0;
 };
 
 // blackBodyRadiance (spectral_data.ipp:613-629): trapezoid of Planck's law in FP64 per band.
@@ -93,6 +115,13 @@ public:
     Vec3 position{0, 0, 0};
     Mat3 rotation{1, 0, 0, 0, 1, 0, 0, 0, 1};
     std::vector<float> optical_efficiency{1.f};
+    // the sensor chain after the film (Camera members, camera.hpp:215-268)
+    float exposure_time = 0.01f;
+    PhotositeConfig photosite;
+    bool has_noise_model = false;
+    NoiseModelConfig noise_model;
+    bool simulate_photon_noise = false;
+    uint64_t sensor_seed = 0;
 
     void setFocalLength(double f) { focal_length = (float)f; f_stop = (float)f / aperture_diameter; }
     void setFStop(double f) { f_stop = (float)f; aperture_diameter = focal_length / f_stop; }
@@ -263,16 +292,47 @@ public:
         return out;
     }
 
-    // Scene::pathtraceRender (scene.ipp:840-845) without the sensor chain: the received power.
+    // Scene::pathtraceRender (scene.ipp:840-845): renders, then Camera::simulateSensor on the
+    // received power; returns the [H][W] image in 0..1.
     const std::vector<float>& pathtraceRender(Camera& camera) {
         pathtracer.render(camera, *this);
-        return pathtracer.renderPasses.received_power;
+        const std::vector<float>& power = pathtracer.renderPasses.received_power;
+        const uint32_t B = bands.size();
+        vgb_sensor s{};
+        s.exposure_time = camera.exposure_time;
+        const std::vector<float> e = bands.photonEnergies();
+        float total_energy = 0;  // PhotositeConfig::defaultQE (photosite.ipp:64-79)
+        for (uint32_t k = 0; k < B; ++k) total_energy += e[k] / (float)B;
+        for (uint32_t k = 0; k < B; ++k) {
+            s.photon_energy[k] = e[k];
+            s.quantum_efficiency[k] = camera.photosite.quantum_efficiency.empty()
+                                          ? 0.5f * e[k] / total_energy
+                                          : camera.photosite.quantum_efficiency[k];
+        }
+        s.gain = camera.photosite.gain;
+        s.max_adu = camera.photosite.maxADU();
+        s.simulate_photon_noise = camera.simulate_photon_noise;
+        if (camera.has_noise_model) {
+            const NoiseModelConfig& n = camera.noise_model;
+            s.noise_model = 1;
+            s.dark_current = n.dark_current; s.readout_noise_mean = n.readout_noise_mean;
+            s.readout_noise_std = n.readout_noise_std; s.horizontal_scale = n.horizontal_scale;
+            s.vertical_scale = n.vertical_scale; s.horizontal_pattern_period = n.horizontal_pattern_period;
+            s.vertical_pattern_period = n.vertical_pattern_period;
+        }
+        s.seed = camera.sensor_seed;
+        s.frame = pathtracer.options.frame;
+        sensor_image_.resize((size_t)camera.width * camera.height);
+        check(vgb_sensor_simulate(ctx_, power.data(), camera.width, camera.height, B, &s, sensor_image_.data(), 0),
+              ctx_, "sensor_simulate");
+        return sensor_image_;
     }
 
     vgb_context* context() { return ctx_; }
 
 private:
     vgb_context* ctx_ = nullptr;
+    std::vector<float> sensor_image_;
     bool dirty_ = true;
 };
 

@@ -52,6 +52,8 @@ def load():
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
                                     C.POINTER(capi.Film), U32, U32, C.c_int, P]),
         "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
+        "oracle_sensor": (C.c_int, [P, P, U32, U32, U32, C.c_float, P, P, C.c_float, C.c_float, P]),
+        "oracle_psf": (C.c_int, [P, U32, U32, U32, P, U32, U32, P]),
         "oracle_denoise": (C.c_int, [P, P, P, P, P, U32, U32, U32, U32, U32, C.c_float, C.c_float, C.c_float,
                                      C.c_float]),
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
@@ -110,6 +112,31 @@ def pixel_solid_angle(cam: capi.Camera):
 
 def blackbody_band(T, lmin_m, lmax_m, steps=1000):
     return load().oracle_blackbody_band(T, lmin_m, lmax_m, steps)
+
+
+def sensor(power, exposure_time, photon_energy, qe, gain, max_adu, mosaic=None):
+    """Noise-free sensor chain restated: [B][H][W] received power -> [H][W] image."""
+    p = np.ascontiguousarray(power, np.float32)
+    B, H, W = p.shape
+    e = np.ascontiguousarray(np.asarray(photon_energy, np.float32)[:B])
+    q = np.ascontiguousarray(np.asarray(qe, np.float32)[:B])
+    m = None if mosaic is None else np.ascontiguousarray(mosaic, np.float32)
+    out = np.empty((H, W), np.float32)
+    rc = load().oracle_sensor(p.ctypes.data, None if m is None else m.ctypes.data, W, H, B, exposure_time,
+                              e.ctypes.data, q.ctypes.data, gain, max_adu, out.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle_sensor rejected its arguments")
+    return out
+
+
+def psf(image, kernel):
+    """Spatial convolution restated: [B][H][W] with a [B][kh][kw] kernel, zero padding."""
+    a = np.ascontiguousarray(image, np.float32)
+    k = np.ascontiguousarray(kernel, np.float32)
+    B, H, W = a.shape
+    out = np.empty_like(a)
+    assert load().oracle_psf(a.ctypes.data, W, H, B, k.ctypes.data, k.shape[2], k.shape[1], out.ctypes.data) == 0
+    return out
 
 
 def denoise(direct, indirect, albedo, depth, normal, levels_direct=5, levels_indirect=5, depth_threshold=0.2,

@@ -1488,3 +1488,52 @@ OAPI int oracle_denoise(float* direct, float* indirect, const float* albedo, con
         }
     return 0;
 }
+
+// ==================================================================== sensor chain (noise-free)
+// Camera::getPhotonCounts without photon noise (cameras/camera.ipp:1286-1330) and
+// Photosite::exposePixel (photosites/photosite.ipp:125-136) with zero noise electrons:
+// photons_k = (t_exp * P_k [* mosaic_k]) / E_k, electrons = sum_k QE_k photons_k,
+// out = min(gain * electrons, max_adu) / max_adu.  Planar [B][H][W] in, [H][W] out.
+OAPI int oracle_sensor(const float* power, const float* mosaic, uint32_t width, uint32_t height, uint32_t nbands,
+                       float exposure_time, const float* photon_energy, const float* qe, float gain, float max_adu,
+                       float* out) {
+    if (!power || !photon_energy || !qe || !out || nbands == 0 || nbands > VGB_MAX_BANDS || !(max_adu > 0.f)) return 1;
+    const size_t P = (size_t)width * height;
+    for (size_t p = 0; p < P; ++p) {
+        float ph[VGB_MAX_BANDS];
+        for (uint32_t k = 0; k < nbands; ++k) {
+            float e = exposure_time * power[k * P + p];
+            if (mosaic) e = e * mosaic[k * P + p];
+            ph[k] = e / photon_energy[k];
+        }
+        float electrons = 0;
+        for (uint32_t k = 0; k < nbands; ++k) electrons += qe[k] * ph[k];
+        electrons = electrons + 0.0f;
+        const float amplified = std::min(gain * electrons, max_adu);
+        out[p] = amplified / max_adu;
+    }
+    return 0;
+}
+
+// Image::convolveSpatial (images/image.ipp:1267-1340) for a planar spectral image: per band,
+// out(x, y) = sum over ky outer, kx inner of in(x + kx - kw/2, y + ky - kh/2) * kernel(kx, ky),
+// zero outside the image.  kernel is [B][kh][kw].
+OAPI int oracle_psf(const float* in, uint32_t width, uint32_t height, uint32_t nbands, const float* kernel,
+                    uint32_t kw, uint32_t kh, float* out) {
+    if (!in || !kernel || !out || nbands == 0) return 1;
+    const int W = (int)width, H = (int)height, hw = (int)kw / 2, hh = (int)kh / 2;
+    const size_t P = (size_t)W * H;
+    for (uint32_t b = 0; b < nbands; ++b)
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                float sum = 0.f;
+                for (int ky = 0; ky < (int)kh; ++ky)
+                    for (int kx = 0; kx < (int)kw; ++kx) {
+                        const int ix = x + kx - hw, iy = y + ky - hh;
+                        if (ix >= 0 && ix < W && iy >= 0 && iy < H)
+                            sum += in[b * P + (size_t)iy * W + ix] * kernel[((size_t)b * kh + ky) * kw + kx];
+                    }
+                out[b * P + (size_t)y * W + x] = sum;
+            }
+    return 0;
+}

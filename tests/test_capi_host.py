@@ -42,7 +42,8 @@ def test_struct_layouts_match_the_header(tmp_path):
         pytest.skip("no C compiler")
     pairs = {"vgb_camera": capi.Camera, "vgb_light": capi.Light, "vgb_pt_options": capi.PtOptions,
              "vgb_film": capi.Film, "vgb_frame": capi.Frame, "vgb_view": capi.View,
-             "vgb_batch_options": capi.BatchOptions, "vgb_bvh_options": capi.BvhOptions, "vgb_stats": capi.Stats}
+             "vgb_batch_options": capi.BatchOptions, "vgb_bvh_options": capi.BvhOptions, "vgb_stats": capi.Stats, "vgb_sensor": capi.Sensor,
+             "vgb_denoise_options": capi.DenoiseOptions}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vgb.h"', "int main(void) {"]
     for cname, py in pairs.items():
         lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from vira_gb300 import capi, spectral, synthetic, workloads
+from vira_gb300 import FOUR_BAND, capi, spectral, synthetic, workloads
 from helpers import primary_rays
 
 F = np.float32
@@ -409,3 +409,27 @@ def test_oracle_denoiser_properties():
     assert np.std(d / alb) < 0.3 * np.std(noisy / alb)
     with pytest.raises(ValueError):
         oracle.denoise(noisy[:, :, :16], i0[:, :, :16], alb[:, :, :16], depth[:, :16], normal[:, :, :16])
+
+
+def test_oracle_sensor_chain_and_psf():
+    """Noise-free sensor chain: electrons are linear in the received power until the ADU clamp;
+    the spatial PSF with a delta kernel is the identity and a box kernel sums neighbours."""
+    from vira_gb300 import sensor
+
+    e = sensor.photon_energies(FOUR_BAND)
+    qe = sensor.default_qe(FOUR_BAND)
+    p = np.zeros((4, 2, 3), np.float32)
+    p[:, 0, 0] = 1e-16
+    p[:, 0, 1] = 2e-16
+    p[:, 1, 2] = 1.0  # saturates
+    out = oracle.sensor(p, 0.01, e, qe, 0.333333, 255.0)
+    assert out[0, 1] == pytest.approx(2 * out[0, 0], rel=1e-6) and 0 < out[0, 0] < 1
+    assert out[1, 2] == 1.0 and out[1, 0] == 0.0
+    img = np.random.default_rng(0).uniform(0, 1, (2, 7, 9)).astype(np.float32)
+    delta = np.zeros((2, 3, 3), np.float32)
+    delta[:, 1, 1] = 1.0
+    assert np.array_equal(oracle.psf(img, delta), img)
+    box = np.ones((2, 3, 3), np.float32)
+    s = oracle.psf(img, box)
+    assert s[0, 3, 4] == pytest.approx(img[0, 2:5, 3:6].sum(), rel=1e-6)
+    assert s[1, 0, 0] == pytest.approx(img[1, 0:2, 0:2].sum(), rel=1e-6)

@@ -78,6 +78,15 @@ class View(C.Structure):
                 ("frame", C.c_uint32), ("pad", C.c_uint32), ("target", C.c_void_p), ("radiance", C.c_void_p)]
 
 
+class Sensor(C.Structure):
+    _fields_ = [("exposure_time", C.c_float), ("photon_energy", C.c_float * 8), ("quantum_efficiency", C.c_float * 8),
+                ("gain", C.c_float), ("max_adu", C.c_float), ("simulate_photon_noise", C.c_uint32),
+                ("noise_model", C.c_uint32), ("dark_current", C.c_float), ("readout_noise_mean", C.c_float),
+                ("readout_noise_std", C.c_float), ("horizontal_scale", C.c_float), ("vertical_scale", C.c_float),
+                ("horizontal_pattern_period", C.c_uint32), ("vertical_pattern_period", C.c_uint32),
+                ("frame", C.c_uint32), ("seed", C.c_uint64), ("filter_mosaic", C.c_void_p)]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("autotune", C.c_uint32), ("use_graph", C.c_uint32), ("block_threads", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("tiles_per_grab", C.c_uint32)]
@@ -123,6 +132,8 @@ SIGNATURES = {
     "vgb_render_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), C.POINTER(BatchOptions)]),
     "vgb_batch_tuning": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
     "vgb_adjoint": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_sensor_simulate": (C.c_int, [_P, _P, _U32, _U32, _U32, C.POINTER(Sensor), _P, C.c_int]),
+    "vgb_psf_convolve": (C.c_int, [_P, _P, _U32, _U32, _U32, _P, _U32, _U32, C.c_int]),
     "vgb_denoise": (C.c_int, [_P, _P, _P, _P, _P, _P, _U32, _U32, _U32, _P, C.c_int]),
     "vgb_adjoint_positions": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
     "vgb_render_adjoint_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), _P, _P, C.POINTER(C.c_double)]),

@@ -37,10 +37,10 @@ using namespace vgbd;
 #ifndef VGB_SHADE_MINB
 #define VGB_SHADE_MINB 4
 #endif
-// k_batch without bounces: 3 blocks of 256 threads cap it at 80 registers (spills outside the
-// traversal loop), measured faster on the trajectory workload than 124 registers.
+// k_batch without bounces: 2 blocks of 256 threads cap it at 128 registers; with the traversal
+// out of line this measured fastest on the trajectory workload (64 and 80 registers spill).
 #ifndef VGB_BATCH_DIRECT_MINB
-#define VGB_BATCH_DIRECT_MINB 3
+#define VGB_BATCH_DIRECT_MINB 2
 #endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene 
 }
 
 // ------------------------------------------------------------------ k_end_sample
-template <int NB>
+template <int NB, bool ADAPTIVE>
 __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_constant__ FrameParams fp, uint32_t smp,
                                                     uint32_t last, FilmOut f) {
     const size_t P = st.P;                       // plane stride of the scratch state
@@ -697,7 +697,7 @@ __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_co
     const uint32_t npix = fp.cam.width * fp.cam.height;
     const size_t FP = npix;                      // plane stride of the caller's film
     const float sf_all = (float)fp.opt.samples;
-    const bool adaptive = fp.opt.adaptive_sampling != 0;
+    const bool adaptive = ADAPTIVE;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
         const bool want_dir = (fp.aux & AUX_DIR) != 0;
         uint32_t stopped = adaptive ? st.anum[p] : 0u;
@@ -1077,7 +1077,9 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
         }
         {
             Prof p(ctx, 2);
-            k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+            const uint32_t last = smp + 1 == fp.opt.samples ? 1u : 0u;
+            if (fp.opt.adaptive_sampling) k_end_sample<NB, true><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, last, film);
+            else k_end_sample<NB, false><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, last, film);
         }
         launches++;
     }
@@ -1462,6 +1464,73 @@ VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) {
     return VGB_OK;
 }
 
+VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_power, uint32_t width,
+                                       uint32_t height, uint32_t nbands, const vgb_sensor* sensor, float* image,
+                                       int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!received_power || !sensor || !image || width == 0 || height == 0 || nbands == 0 || nbands > VGB_MAX_BANDS)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate: null plane or sensor, empty image or bands outside 1..8");
+    if (!(sensor->max_adu > 0.f)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate: max_adu must be > 0");
+    for (uint32_t k = 0; k < nbands; ++k)
+        if (!(sensor->photon_energy[k] > 0.f))
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate: photon energies must be > 0");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)width * height, BP = (size_t)nbands * P;
+    vgb::SensorParams sp{};
+    sp.exposure_time = sensor->exposure_time;
+    for (int k = 0; k < 8; ++k) { sp.photon_energy[k] = sensor->photon_energy[k]; sp.quantum_efficiency[k] = sensor->quantum_efficiency[k]; }
+    sp.gain = sensor->gain; sp.max_adu = sensor->max_adu;
+    sp.photon_noise = sensor->simulate_photon_noise; sp.noise_model = sensor->noise_model;
+    sp.dark_current = sensor->dark_current; sp.readout_mean = sensor->readout_noise_mean; sp.readout_std = sensor->readout_noise_std;
+    sp.hscale = sensor->horizontal_scale; sp.vscale = sensor->vertical_scale;
+    sp.hperiod = sensor->horizontal_pattern_period; sp.vperiod = sensor->vertical_pattern_period;
+    sp.frame = sensor->frame; sp.seed = sensor->seed; sp.mosaic = sensor->filter_mosaic;
+    const float* pw = received_power;
+    float* img = image;
+    vgb_status s;
+    if (!on_device) {
+        if ((s = ensure_staging(ctx, (BP * (sensor->filter_mosaic ? 2 : 1) + P) * sizeof(float))) != VGB_OK) return s;
+        float* cur = (float*)ctx->staging_base;
+        CK(cudaMemcpyAsync(cur, received_power, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); pw = cur; cur += BP;
+        if (sensor->filter_mosaic) {
+            CK(cudaMemcpyAsync(cur, sensor->filter_mosaic, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+            sp.mosaic = cur; cur += BP;
+        }
+        img = cur;
+    }
+    CK((cudaError_t)vgb::launch_sensor(ctx->stream, pw, width, height, nbands, sp, img, ctx->num_sms));
+    if (!on_device) CK(cudaMemcpyAsync(image, img, P * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_psf_convolve(vgb_context* ctx, float* received_power, uint32_t width, uint32_t height,
+                                    uint32_t nbands, const float* kernel, uint32_t kernel_w, uint32_t kernel_h,
+                                    int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!received_power || !kernel || width == 0 || height == 0 || nbands == 0 || nbands > VGB_MAX_BANDS)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "psf_convolve: null plane or kernel, empty image or bands outside 1..8");
+    if (kernel_w == 0 || kernel_h == 0 || kernel_w > 127 || kernel_h > 127)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "psf_convolve: kernel sides must be 1..127");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)width * height, BP = (size_t)nbands * P, KN = (size_t)nbands * kernel_w * kernel_h;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, BP + (on_device ? 0 : BP + KN))) != VGB_OK) return s;
+    float* out = ctx->d_dn;
+    float* io = received_power;
+    const float* kr = kernel;
+    if (!on_device) {
+        float* cur = ctx->d_dn + BP;
+        CK(cudaMemcpyAsync(cur, received_power, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); io = cur; cur += BP;
+        CK(cudaMemcpyAsync(cur, kernel, KN * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); kr = cur;
+    }
+    CK((cudaError_t)vgb::launch_psf(ctx->stream, io, out, width, height, nbands, kr, kernel_w, kernel_h));
+    CK(cudaMemcpyAsync(on_device ? received_power : io, out, BP * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (!on_device) CK(cudaMemcpyAsync(received_power, io, BP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
 VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
                                const float* depth, const float* normal, uint32_t width, uint32_t height,
                                uint32_t nbands, const vgb_denoise_options* o, int on_device) {
@@ -1773,7 +1842,7 @@ void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film
             }
             q ^= 1u;
         }
-        k_end_sample<NB><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
+        k_end_sample<NB, false><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
         launches++;
     }
 }

@@ -38,4 +38,20 @@ struct BvhHost {
 bool build_bvh(const float* positions, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
                uint32_t max_leaf, uint32_t threads, uint32_t layout, BvhHost& out, const char** err);
 
+// Sensor chain and PSF kernels (vgb_sensor.cu); the C ABI in vgb_cuda.cu validates and stages
+// the planes and calls these on the context's stream.  All pointers are device memory.
+struct SensorParams {
+    float exposure_time, photon_energy[8], quantum_efficiency[8], gain, max_adu;
+    uint32_t photon_noise, noise_model;
+    float dark_current, readout_mean, readout_std, hscale, vscale;
+    uint32_t hperiod, vperiod, frame;
+    uint64_t seed;
+    const float* mosaic;
+};
+int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t height, uint32_t nbands,
+                  const SensorParams& sp, float* image, int num_sms);
+// out = correlation of in ([B][H][W]) with kernel ([B][kh][kw], zero padding); out != in.
+int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32_t height, uint32_t nbands,
+               const float* kernel, uint32_t kw, uint32_t kh);
+
 }  // namespace vgb

@@ -1,0 +1,180 @@
+// vgb_sensor.cu -- the sensor chain after the film and the PSF convolution.
+//
+// k_sensor restates Camera::simulateSensor (cameras/camera.ipp:1218-1240) per pixel:
+// getPhotonCounts (camera.ipp:1286-1330), NoiseModel::simulate with its fixed pattern
+// (noise_models/noise_model.ipp:36-74) and Photosite::exposePixel (photosites/photosite.ipp:
+// 125-136), in the reference's FP32 operation order.  Random draws come from Philox-4x32-10
+// keyed by (seed, frame) with the counter (pixel, purpose, frame, 0xE0): exact Poisson samples by
+// inversion below a mean of 10 and by Hormann's transformed rejection (PTRS, 1993) above,
+// Gaussian samples by Box-Muller.
+//
+// k_psf restates Image::convolveSpatial (images/image.ipp:1267-1340): a correlation with a
+// centred kernel and zero padding, kernel rows outer, each output summed in the reference's
+// order; an output tile and its halo are staged in shared memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "vgb_device.cuh"
+#include "vgb_internal.h"
+
+using namespace vgbd;
+
+namespace {
+
+constexpr uint32_t kSlotSensor = 0xE0u;
+
+__device__ __forceinline__ float u01_open(uint32_t x) {  // (0, 1]
+    return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f);
+}
+
+// Poisson(lambda) for lambda >= 0: inversion (sequential search) below 10, PTRS above.  Both
+// loops are bounded; the rejection loop accepts with probability ~0.9 per round, and after 64
+// rounds (never expected) returns the rounded mean.
+__device__ float poisson(float lambda, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1) {
+    if (!(lambda > 0.f)) return 0.f;
+    if (lambda < 10.f) {
+        const U4 r = philox(U4{c0, c1, c2, kSlotSensor}, k0, k1);
+        const float u = u01(r.x);
+        float p = expf(-lambda), F = p;
+        int k = 0;
+        while (u > F && k < 1000) {
+            ++k;
+            p *= lambda / (float)k;
+            F += p;
+        }
+        return (float)k;
+    }
+    const float slam = sqrtf(lambda), loglam = logf(lambda);
+    const float b = 0.931f + 2.53f * slam;
+    const float a = -0.059f + 0.02483f * b;
+    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float vr = 0.9277f - 3.6224f / (b - 2.f);
+    for (uint32_t round = 0; round < 64; ++round) {
+        const U4 r = philox(U4{c0, c1 + (round << 16), c2, kSlotSensor | 1u}, k0, k1);
+        const float U = u01(r.x) - 0.5f, V = u01_open(r.y);
+        const float us = 0.5f - fabsf(U);
+        const float kf = floorf((2.f * a / us + b) * U + lambda + 0.43f);
+        if (us >= 0.07f && V <= vr) return kf;
+        if (kf < 0.f || (us < 0.013f && V > us)) continue;
+        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= -lambda + kf * loglam - lgammaf(kf + 1.f)) return kf;
+    }
+    return rintf(lambda);
+}
+
+__device__ __forceinline__ float gaussian(float mean, float std, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0,
+                                          uint32_t k1) {
+    const U4 r = philox(U4{c0, c1, c2, kSlotSensor | 2u}, k0, k1);
+    const float u1 = u01_open(r.x), u2 = u01(r.y);
+    return mean + std * (sqrtf(-2.f * logf(u1)) * cosf(6.2831853f * u2));
+}
+
+template <int NB>
+__global__ void k_sensor(const float* __restrict__ power, uint32_t W, uint32_t H, uint32_t nb,
+                         const vgb::SensorParams sp, float* __restrict__ image) {
+    const size_t P = (size_t)W * H;
+    const uint32_t k0 = (uint32_t)sp.seed, k1 = (uint32_t)(sp.seed >> 32);
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(p % W), j = (uint32_t)(p / W);
+        float ph[NB];
+        float total = 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            ph[k] = 0.f;
+            if (k >= (int)nb) continue;
+            float e = sp.exposure_time * power[k * P + p];
+            if (sp.mosaic) e = e * sp.mosaic[k * P + p];
+            ph[k] = e / sp.photon_energy[k];
+            total += ph[k];
+        }
+        if (sp.photon_noise && total >= 1.f) {
+#pragma unroll
+            for (int k = 0; k < NB; ++k)
+                if (k < (int)nb) ph[k] = poisson(ph[k], (uint32_t)p, (uint32_t)k, sp.frame, k0, k1);
+        }
+        float noise = 0.f;
+        if (sp.noise_model) {
+            const float dark = poisson(sp.dark_current, (uint32_t)p, 0x100u, sp.frame, k0, k1) * sp.exposure_time;
+            const float readout = gaussian(sp.readout_mean, sp.readout_std, (uint32_t)p, 0x101u, sp.frame, k0, k1);
+            float scale = 1.f;
+            if (sp.hperiod != 0)
+                scale *= (1.f - sp.hscale) +
+                         (sp.hscale * (1.f + sinf(2.f * kPi * (float)i / (2.f * (float)sp.hperiod))));
+            if (sp.vperiod != 0)
+                scale *= (1.f - sp.vscale) +
+                         (sp.vscale * (1.f + sinf(2.f * kPi * (float)j / (2.f * (float)sp.vperiod))));
+            noise = scale * (dark + readout);
+        }
+        float electrons = 0.f;
+#pragma unroll
+        for (int k = 0; k < NB; ++k)
+            if (k < (int)nb) electrons += sp.quantum_efficiency[k] * ph[k];
+        electrons = electrons + noise;
+        const float amplified = smin(sp.gain * electrons, sp.max_adu);
+        image[p] = amplified / sp.max_adu;
+    }
+}
+
+constexpr int kTileW = 32, kTileH = 8;
+constexpr int kMaxKernel = 127;
+
+// One block: a 32x8 output tile of one band; the input tile with its halo and the band's
+// kernel in dynamic shared memory.
+__global__ void k_psf(const float* __restrict__ in, float* __restrict__ out, uint32_t W, uint32_t H,
+                      const float* __restrict__ kernel, int kw, int kh) {
+    extern __shared__ float sm[];
+    const int band = blockIdx.z;
+    const size_t P = (size_t)W * H;
+    const float* src = in + band * P;
+    const float* ker = kernel + (size_t)band * kw * kh;
+    const int hw = kw / 2, hh = kh / 2;
+    const int tw = kTileW + kw - 1, th = kTileH + kh - 1;
+    float* tile = sm;
+    float* ks = sm + tw * th;
+    const int x0 = blockIdx.x * kTileW - hw, y0 = blockIdx.y * kTileH - hh;
+    const int tid = threadIdx.y * kTileW + threadIdx.x, nthr = kTileW * kTileH;
+    for (int q = tid; q < tw * th; q += nthr) {
+        const int ix = x0 + q % tw, iy = y0 + q / tw;
+        tile[q] = (ix >= 0 && ix < (int)W && iy >= 0 && iy < (int)H) ? src[(size_t)iy * W + ix] : 0.f;
+    }
+    for (int q = tid; q < kw * kh; q += nthr) ks[q] = ker[q];
+    __syncthreads();
+    const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+    if (x >= (int)W || y >= (int)H) return;
+    float sum = 0.f;
+    for (int ky = 0; ky < kh; ++ky) {
+        const float* row = tile + (threadIdx.y + ky) * tw + threadIdx.x;
+        const float* krow = ks + ky * kw;
+        for (int kx = 0; kx < kw; ++kx) sum += row[kx] * krow[kx];
+    }
+    out[band * P + (size_t)y * W + x] = sum;
+}
+
+}  // namespace
+
+namespace vgb {
+
+int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t height, uint32_t nbands,
+                  const SensorParams& sp, float* image, int num_sms) {
+    const size_t P = (size_t)width * height;
+    const int g = (int)std::max<size_t>(1, std::min<size_t>((P + 255) / 256, (size_t)num_sms * 8));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nbands <= 1) k_sensor<1><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
+    else if (nbands <= 4) k_sensor<4><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
+    else k_sensor<8><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
+    return (int)cudaGetLastError();
+}
+
+int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32_t height, uint32_t nbands,
+               const float* kernel, uint32_t kw, uint32_t kh) {
+    if (kw > (uint32_t)kMaxKernel || kh > (uint32_t)kMaxKernel) return (int)cudaErrorInvalidValue;
+    const size_t smem = ((size_t)(kTileW + kw - 1) * (kTileH + kh - 1) + (size_t)kw * kh) * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_psf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    const dim3 grid((width + kTileW - 1) / kTileW, (height + kTileH - 1) / kTileH, nbands);
+    k_psf<<<grid, dim3(kTileW, kTileH), smem, (cudaStream_t)stream>>>(in, out, width, height, kernel, (int)kw, (int)kh);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace vgb

@@ -24,7 +24,7 @@ PI_F = np.float32(3.14159265358979323846)
 
 # ============================================================================ camera
 class Camera:
-    """Pinhole camera: Camera (include/vira/cameras/camera.hpp) without the sensor chain.
+    """Pinhole camera: Camera (include/vira/cameras/camera.hpp); `sensor` holds the sensor chain.
 
     Defaults follow camera.hpp:220-235: focal length 50 mm, sensor 36 x 20.25 mm,
     resolution 1920 x 1080, f-stop 2.8, optical efficiency 1, principal point at the centre.
@@ -44,6 +44,18 @@ class Camera:
         self.position = np.zeros(3, np.float64)          # FP64, scene (global) frame
         self.rotation = np.eye(3, dtype=np.float64)       # FP64, columns = camera axes
         self._kinv = None
+        # the sensor chain after the film (exposure, photosite, noise model, PSF, filter mosaic)
+        from .sensor import SensorModel
+
+        self.sensor = SensorModel()
+        self._psf_kernel = None
+
+    def psf_kernel(self, bands):
+        """The PSF kernel the render convolves with (built once per PSF, size and bands)."""
+        key = (id(self.sensor.psf), self.sensor.psf_kernel_size, bands.size)
+        if self._psf_kernel is None or self._psf_kernel[0] != key:
+            self._psf_kernel = (key, self.sensor.psf.make_kernel(bands, self.sensor.psf_kernel_size, 20))
+        return self._psf_kernel[1]
 
     # --- setters (camera.ipp:235-470)
     def set_focal_length(self, f: float):
@@ -357,6 +369,12 @@ class PathTracer:
         st = capi.Stats()
         lib.vgb_get_stats(ctx, C.byref(st))
         self.last_stats = st
+        if rp.received_power is not None and camera.sensor.psf is not None:
+            # CPUPathTracer::render convolves the received power with the camera's PSF
+            # (cpu_path_tracer.ipp:150-158)
+            from .sensor import psf_convolve
+
+            psf_convolve(scene, rp.received_power, camera.psf_kernel(scene.bands))
         return rp
 
 
@@ -632,9 +650,15 @@ class Scene:
 
     # --- renders (scene.ipp:840-915)
     def pathtrace_render(self, camera_id):
-        """Renders and returns the received-power pass (the sensor chain is not part of this path)."""
-        rp = self.pathtracer.render(self[camera_id], self)
-        return rp.received_power
+        """Scene::pathtraceRender (scene.ipp:840-845): renders, then simulates the camera's sensor
+        on the received power; returns the [H][W] image in 0..1 (torch CUDA tensor)."""
+        from .sensor import simulate_sensor
+
+        cam = self[camera_id]
+        rp = self.pathtracer.render(cam, self)
+        if rp.received_power is None:
+            raise ValueError("pathtrace_render needs render_passes.simulate_lighting")
+        return simulate_sensor(self, rp.received_power, cam.sensor, frame=self.pathtracer.options.frame)
 
     def intersect(self, origins: np.ndarray, directions: np.ndarray, any_hit: bool = False, tmax=None):
         """Scene::intersect / TLAS::intersect (scene.hpp:230) for a batch of rays (host arrays)."""
