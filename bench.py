@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-trajectory line item")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint line item")
     ap.add_argument("--no-asteroid", action="store_true", help="skip the fused batched-adjoint asteroid line item")
+    ap.add_argument("--no-after-film", action="store_true", help="skip the denoiser / PSF / sensor line item")
     return ap.parse_args()
 
 
@@ -387,6 +388,9 @@ def run_ours(args, p, rank, world, local_rank):
     # workload (profiles/traffic_path_traced_dem4097_2048px.md), or None for other workloads.
     traffic = MEASURED_TRAFFIC.get((config_name(p), args.layout), {}).get(dominant)
 
+    after_film = None
+    if not args.no_after_film and p["kind"] == "path_traced" and rank == 0:
+        after_film = after_film_item(torch, dev, scene, cam_id, peak)
     direct = None
     if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
         direct = plain_direct_item(torch, dev, args.layout)
@@ -452,6 +456,8 @@ def run_ours(args, p, rank, world, local_rank):
             line["adjoint"] = adjoint
         if asteroid is not None:
             line["batched_adjoint"] = asteroid
+        if after_film is not None:
+            line["after_film"] = after_film
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -590,6 +596,80 @@ def adjoint_item(torch, dev, layout=2, reps=2):
            "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
     scene.close()
     return out
+
+
+def after_film_item(torch, dev, scene, cam_id, hbm_peak, reps=5):
+    """The steps after the film on the path-traced frame (2048^2, 8 bands): the EATWT denoiser
+    (vgb_denoise, 5 levels on direct and indirect), the 81x81 Gaussian PSF convolution of the
+    received power and the sensor chain with photon, dark and readout noise.  CUDA events on the
+    context's stream, best of `reps`."""
+    from vira_gb300 import capi, sensor
+
+    rp = scene.pathtracer.render(scene[cam_id], scene)
+    lib = capi.load()
+    ctx = scene.context()
+    B, H, W = rp.direct_radiance.shape
+    P = H * W
+    stream = torch.cuda.Stream(device=dev)
+    capi.check(lib.vgb_set_stream(ctx, C.c_void_p(stream.cuda_stream)), ctx, "set_stream")
+    d0, i0 = rp.direct_radiance.clone(), rp.indirect_radiance.clone()
+    d, i = torch.empty_like(d0), torch.empty_like(i0)
+
+    def timed(fn):
+        best = float("inf")
+        for _ in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    def den():
+        with torch.cuda.stream(stream):
+            d.copy_(d0)
+            i.copy_(i0)
+        capi.check(lib.vgb_denoise(ctx, d.data_ptr(), i.data_ptr(), rp.albedo.data_ptr(), rp.depth.data_ptr(),
+                                   rp.normal_global.data_ptr(), W, H, B, None, 1), ctx, "denoise")
+
+    t_den = timed(den)
+    kern = sensor.GaussianPSF(1.5).make_kernel(scene.bands, 81, 20)
+    kt = torch.tensor(kern, device=dev)
+    pw = rp.received_power.clone()
+
+    def psf():
+        capi.check(lib.vgb_psf_convolve(ctx, pw.data_ptr(), W, H, B, kt.data_ptr(), 81, 81, 1), ctx, "psf")
+
+    t_psf = timed(psf)
+    sm = sensor.SensorModel(simulate_photon_noise=True,
+                            noise_model=sensor.NoiseModelConfig(dark_current=20.0, readout_noise_mean=1.0,
+                                                                readout_noise_std=3.0))
+    sc = sm.to_c(scene.bands)
+    img = torch.empty((H, W), device=dev)
+
+    def sen():
+        capi.check(lib.vgb_sensor_simulate(ctx, rp.received_power.data_ptr(), W, H, B, C.byref(sc), img.data_ptr(), 1),
+                   ctx, "sensor")
+
+    t_sen = timed(sen)
+    capi.check(lib.vgb_set_stream(ctx, None), ctx, "set_stream")
+    # unique bytes: split reads 3 and writes 2 planes of B; each of 20 passes (5 levels x 2
+    # directions x direct+indirect share one launch, so 10 launches) reads 2B + 4 and writes 2B
+    # floats per pixel; merge reads 3B, writes 2B
+    den_bytes = 4 * P * ((3 * B + 2 * B) + 10 * (2 * B + 4 + 2 * B) + (3 * B + 2 * B))
+    psf_flops = 2.0 * 81 * 81 * B * P
+    sen_bytes = 4 * P * (B + 1)
+    return {"image": [W, H], "bands": B,
+            "denoise": {"ms": t_den, "levels": 5, "unique_gb_s": den_bytes / (t_den / 1e3) / 1e9,
+                        "frac_of_hbm": den_bytes / (t_den / 1e3) / 1e9 / hbm_peak},
+            "psf_81x81": {"ms": t_psf, "tflop_s": psf_flops / (t_psf / 1e3) / 1e12,
+                          "note": "FP32 multiply + add per tap (no FMA contraction, reference rounding); CUDA cores"},
+            "sensor_with_noise": {"ms": t_sen, "unique_gb_s": sen_bytes / (t_sen / 1e3) / 1e9,
+                                  "frac_of_hbm": sen_bytes / (t_sen / 1e3) / 1e9 / hbm_peak},
+            "timing": "CUDA events on the context stream, best of %d" % reps}
 
 
 def asteroid_item(torch, dev, layout=2, reps=2):

@@ -3,6 +3,7 @@
     python -m vira_gb300.profile_cases path [scale]   # k_trace / k_shade / k_shadow / k_end_sample
     python -m vira_gb300.profile_cases batch          # k_batch: 24 trajectory frames, 256^2-1024^2
     python -m vira_gb300.profile_cases adjoint        # k_adjoint: 2 views of a 513^2 crater DEM
+    python -m vira_gb300.profile_cases after_film     # k_dn_*, k_psf, k_sensor on a 1024^2 frame
 
 ``path`` renders the path-traced workload shrunk by ``scale`` (posts, texture and pixels; 4 spp)
 twice; the captures skip the launches of the first render.
@@ -42,8 +43,19 @@ def main(argv=None):
         gt, gz = adjoint_views(scene, views, [torch.ones_like(i) for i in imgs], dev)
         torch.cuda.synchronize()
         print("adjoint", float(gt.abs().sum()))
+    elif kind == "after_film":
+        from . import sensor
+
+        scene, cam = workloads.path_traced(posts=1025, tex=1024, resolution=1024, spp=2)
+        scene.pathtracer.options.denoise = True
+        rp = scene.pathtracer.render(scene[cam], scene)
+        sensor.psf_convolve(scene, rp.received_power, sensor.GaussianPSF(1.5).make_kernel(scene.bands, 81, 20))
+        sm = sensor.SensorModel(simulate_photon_noise=True, noise_model=sensor.NoiseModelConfig(dark_current=20.0))
+        img = sensor.simulate_sensor(scene, rp.received_power, sm)
+        torch.cuda.synchronize()
+        print("after_film", float(img.mean()))
     else:
-        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint")
+        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint | after_film")
 
 
 if __name__ == "__main__":
