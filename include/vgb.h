@@ -330,6 +330,18 @@ VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* vi
 VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
                                const float* depth, const float* normal, uint32_t width, uint32_t height,
                                uint32_t nbands, const vgb_denoise_options* o, int on_device);
+/* ---- DEM triangulation and vertex normals on the GPU ------------------------------------
+ * The same outputs as vgb_dem_triangulate and vgb_compute_vertex_normals (bit for bit): posts
+ * in FP64 then FP32, the index buffer in the reference's quad order with infinite posts skipped
+ * (an exclusive scan places each quad's triangles), and per-vertex sums of unit face normals in
+ * face order (each vertex gathers its faces, sorted).  idx must hold 2 (W-1)(H-1) triangles;
+ * *nt_out receives the count.  Arrays device memory if on_device else host. */
+VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* heights, uint32_t W, uint32_t H, double sx,
+                                           double sy, float* pos, uint32_t* idx, uint32_t* nt_out, int on_device);
+VGB_API vgb_status vgb_compute_vertex_normals_gpu(vgb_context* ctx, const float* pos, uint32_t nverts,
+                                                  const uint32_t* idx, uint32_t ntris, float* normals,
+                                                  int on_device);
+
 /* ---- sensor chain after the film ------------------------------------------------------
  * Camera::simulateSensor (cameras/camera.ipp:1218-1240): received power -> photon counts
  * (getPhotonCounts, camera.ipp:1286-1330; optional filter mosaic and Poisson photon noise) ->

@@ -132,6 +132,8 @@ SIGNATURES = {
     "vgb_render_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), C.POINTER(BatchOptions)]),
     "vgb_batch_tuning": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
     "vgb_adjoint": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
+    "vgb_dem_triangulate_gpu": (C.c_int, [_P, _P, _U32, _U32, C.c_double, C.c_double, _P, _P, C.POINTER(_U32), C.c_int]),
+    "vgb_compute_vertex_normals_gpu": (C.c_int, [_P, _P, _U32, _P, _U32, _P, C.c_int]),
     "vgb_sensor_simulate": (C.c_int, [_P, _P, _U32, _U32, _U32, C.POINTER(Sensor), _P, C.c_int]),
     "vgb_psf_convolve": (C.c_int, [_P, _P, _U32, _U32, _U32, _P, _U32, _U32, C.c_int]),
     "vgb_denoise": (C.c_int, [_P, _P, _P, _P, _P, _P, _U32, _U32, _U32, _P, C.c_int]),

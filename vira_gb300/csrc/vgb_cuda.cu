@@ -1464,6 +1464,72 @@ VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) {
     return VGB_OK;
 }
 
+VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* heights, uint32_t W, uint32_t H, double sx,
+                                           double sy, float* pos, uint32_t* idx, uint32_t* nt_out, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!heights || !pos || !idx || !nt_out || W < 2 || H < 2 || (uint64_t)W * H >= (1ull << 31))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "dem_triangulate_gpu: null array or grid outside 2..2^31 posts");
+    cudaSetDevice(ctx->device);
+    const size_t nv = (size_t)W * H, nq = (size_t)(W - 1) * (H - 1);
+    const size_t work = vgb::dem_work_words(W, H);
+    const size_t stage = on_device ? 0 : nv + 3 * nv + 6 * nq;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, work + stage)) != VGB_OK) return s;
+    uint32_t* w = reinterpret_cast<uint32_t*>(ctx->d_dn);
+    const float* h = heights;
+    float* p = pos;
+    uint32_t* ix = idx;
+    if (!on_device) {
+        float* cur = ctx->d_dn + work;
+        CK(cudaMemcpyAsync(cur, heights, nv * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        h = cur; cur += nv;
+        p = cur; cur += 3 * nv;
+        ix = reinterpret_cast<uint32_t*>(cur);
+    }
+    uint32_t nt = 0;
+    CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, h, W, H, sx, sy, p, ix, w, &nt));
+    if (!on_device) {
+        CK(cudaMemcpyAsync(pos, p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(idx, ix, 3 * (size_t)nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    *nt_out = nt;
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_compute_vertex_normals_gpu(vgb_context* ctx, const float* pos, uint32_t nverts,
+                                                  const uint32_t* idx, uint32_t ntris, float* normals,
+                                                  int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!pos || !idx || !normals || nverts == 0)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "compute_vertex_normals_gpu: null array or no vertices");
+    cudaSetDevice(ctx->device);
+    const size_t work = vgb::normals_work_words(nverts, ntris);
+    const size_t stage = on_device ? 0 : 6 * (size_t)nverts + 3 * (size_t)ntris;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, work + stage)) != VGB_OK) return s;
+    uint32_t* w = reinterpret_cast<uint32_t*>(ctx->d_dn);
+    const float* p = pos;
+    const uint32_t* ix = idx;
+    float* out = normals;
+    if (!on_device) {
+        float* cur = ctx->d_dn + work;
+        CK(cudaMemcpyAsync(cur, pos, 3 * (size_t)nverts * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        p = cur; cur += 3 * (size_t)nverts;
+        out = cur; cur += 3 * (size_t)nverts;
+        CK(cudaMemcpyAsync(cur, idx, 3 * (size_t)ntris * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+        ix = reinterpret_cast<const uint32_t*>(cur);
+    }
+    const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, nverts, ix, ntris, out, w);
+    if (rc == -1) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "compute_vertex_normals_gpu: an index is >= nverts");
+    CK((cudaError_t)rc);
+    if (!on_device) {
+        CK(cudaMemcpyAsync(normals, out, 3 * (size_t)nverts * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return VGB_OK;
+}
+
 VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_power, uint32_t width,
                                        uint32_t height, uint32_t nbands, const vgb_sensor* sensor, float* image,
                                        int on_device) {

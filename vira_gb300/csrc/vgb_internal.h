@@ -54,4 +54,13 @@ int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t hei
 int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32_t height, uint32_t nbands,
                const float* kernel, uint32_t kw, uint32_t kh);
 
+// DEM triangulation and vertex normals (vgb_mesh.cu), equal to the host functions; all pointers
+// device memory; `work` is scratch of dem_work_words / normals_work_words 32-bit words.
+size_t dem_work_words(uint32_t W, uint32_t H);
+size_t normals_work_words(uint32_t nv, uint32_t nt);
+int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, double sx, double sy,
+                           float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out);
+int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                          float* out, uint32_t* work);
+
 }  // namespace vgb

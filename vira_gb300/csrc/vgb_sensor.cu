@@ -29,10 +29,27 @@ __device__ __forceinline__ float u01_open(uint32_t x) {  // (0, 1]
     return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f);
 }
 
+// -lambda + k ln(lambda) - ln(k!), the log of the Poisson pmf up to its normalisation, formed
+// without the cancellation of its large terms: for k >= 10 with Stirling's series for ln(k!)
+// (z = k + 1: (z - 1/2) ln z - z + ln(2 pi)/2 + 1/(12 z) - 1/(360 z^3)), rearranged as
+// k ln(lambda / z) + (z - lambda) - ln(z)/2 - ln(2 pi)/2 - 1/(12 z) + 1/(360 z^3); below 10 with
+// exact ln(k!).
+__device__ __forceinline__ float log_pmf_ratio(float lambda, float loglam, float kf) {
+    if (kf < 10.f) {
+        const float lnfact[10] = {0.f, 0.f, 0.6931472f, 1.7917595f, 3.1780539f,
+                                  4.7874917f, 6.5792512f, 8.5251614f, 10.6046029f, 12.8018275f};
+        return -lambda + kf * loglam - lnfact[(int)kf];
+    }
+    const float z = kf + 1.f;
+    const float iz = 1.f / z;
+    return kf * log1pf((lambda - z) * iz) + (z - lambda) - 0.5f * logf(z) - 0.91893853f - iz * (1.f / 12.f) +
+           iz * iz * iz * (1.f / 360.f);
+}
+
 // Poisson(lambda) for lambda >= 0: inversion (sequential search) below 10, PTRS above.  Both
 // loops are bounded; the rejection loop accepts with probability ~0.9 per round, and after 64
-// rounds (never expected) returns the rounded mean.
-__device__ float poisson(float lambda, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1) {
+// rounds (never expected) returns the rounded mean.  Out of line: one copy serves every band.
+__device__ __noinline__ float poisson(float lambda, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1) {
     if (!(lambda > 0.f)) return 0.f;
     if (lambda < 10.f) {
         const U4 r = philox(U4{c0, c1, c2, kSlotSensor}, k0, k1);
@@ -58,7 +75,7 @@ __device__ float poisson(float lambda, uint32_t c0, uint32_t c1, uint32_t c2, ui
         const float kf = floorf((2.f * a / us + b) * U + lambda + 0.43f);
         if (us >= 0.07f && V <= vr) return kf;
         if (kf < 0.f || (us < 0.013f && V > us)) continue;
-        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= -lambda + kf * loglam - lgammaf(kf + 1.f)) return kf;
+        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= log_pmf_ratio(lambda, loglam, kf)) return kf;
     }
     return rintf(lambda);
 }
@@ -116,39 +133,68 @@ __global__ void k_sensor(const float* __restrict__ power, uint32_t W, uint32_t H
     }
 }
 
-constexpr int kTileW = 32, kTileH = 8;
+constexpr int kTileW = 128, kTileH = 8;  // outputs per block: 32 threads x 4 columns, 8 rows
 constexpr int kMaxKernel = 127;
 
-// One block: a 32x8 output tile of one band; the input tile with its halo and the band's
-// kernel in dynamic shared memory.
-__global__ void k_psf(const float* __restrict__ in, float* __restrict__ out, uint32_t W, uint32_t H,
-                      const float* __restrict__ kernel, int kw, int kh) {
-    extern __shared__ float sm[];
+__host__ __device__ constexpr int round4(int v) { return (v + 3) & ~3; }
+
+// One block: a 128x8 output tile of one band.  Each thread owns 4 adjacent outputs of a row;
+// the input tile (with its halo) and the band's kernel (rows padded to a multiple of 4 with
+// zeros, never summed) sit in dynamic shared memory, read as float4: per 4 kernel taps a
+// thread loads one float4 of input and one of kernel for 16 multiply-adds.  Every output is
+// summed over ky outer, kx inner, as the reference's loop.
+__global__ void __launch_bounds__(256) k_psf(const float* __restrict__ in, float* __restrict__ out, uint32_t W,
+                                             uint32_t H, const float* __restrict__ kernel, int kw, int kh) {
+    extern __shared__ float4 sm4[];
+    float* sm = reinterpret_cast<float*>(sm4);
     const int band = blockIdx.z;
     const size_t P = (size_t)W * H;
     const float* src = in + band * P;
     const float* ker = kernel + (size_t)band * kw * kh;
     const int hw = kw / 2, hh = kh / 2;
-    const int tw = kTileW + kw - 1, th = kTileH + kh - 1;
+    const int kwp = round4(kw);
+    const int tw = round4(kTileW + kwp + 3), th = kTileH + kh - 1;
     float* tile = sm;
-    float* ks = sm + tw * th;
+    float* ks = sm + (size_t)tw * th;
     const int x0 = blockIdx.x * kTileW - hw, y0 = blockIdx.y * kTileH - hh;
-    const int tid = threadIdx.y * kTileW + threadIdx.x, nthr = kTileW * kTileH;
+    const int tid = threadIdx.y * 32 + threadIdx.x, nthr = 32 * kTileH;
     for (int q = tid; q < tw * th; q += nthr) {
         const int ix = x0 + q % tw, iy = y0 + q / tw;
         tile[q] = (ix >= 0 && ix < (int)W && iy >= 0 && iy < (int)H) ? src[(size_t)iy * W + ix] : 0.f;
     }
-    for (int q = tid; q < kw * kh; q += nthr) ks[q] = ker[q];
-    __syncthreads();
-    const int x = blockIdx.x * kTileW + threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
-    if (x >= (int)W || y >= (int)H) return;
-    float sum = 0.f;
-    for (int ky = 0; ky < kh; ++ky) {
-        const float* row = tile + (threadIdx.y + ky) * tw + threadIdx.x;
-        const float* krow = ks + ky * kw;
-        for (int kx = 0; kx < kw; ++kx) sum += row[kx] * krow[kx];
+    for (int q = tid; q < kwp * kh; q += nthr) {
+        const int kx = q % kwp, ky = q / kwp;
+        ks[q] = kx < kw ? ker[ky * kw + kx] : 0.f;
     }
-    out[band * P + (size_t)y * W + x] = sum;
+    __syncthreads();
+    const int xo = blockIdx.x * kTileW + 4 * threadIdx.x, y = blockIdx.y * kTileH + threadIdx.y;
+    if (y >= (int)H || xo >= (int)W) return;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    for (int ky = 0; ky < kh; ++ky) {
+        const float4* row = reinterpret_cast<const float4*>(tile + (threadIdx.y + ky) * tw + 4 * threadIdx.x);
+        const float4* krow = reinterpret_cast<const float4*>(ks + ky * kwp);
+        float4 a = row[0];
+        for (int c = 0; c < kwp / 4; ++c) {
+            const float4 b = row[c + 1];
+            const float4 k = krow[c];
+            const float in[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            const float kk[4] = {k.x, k.y, k.z, k.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                if (4 * c + t >= kw) break;  // padded taps are not summed
+                s0 += in[t] * kk[t];
+                s1 += in[t + 1] * kk[t];
+                s2 += in[t + 2] * kk[t];
+                s3 += in[t + 3] * kk[t];
+            }
+            a = b;
+        }
+    }
+    float* o = out + band * P + (size_t)y * W + xo;
+    o[0] = s0;
+    if (xo + 1 < (int)W) o[1] = s1;
+    if (xo + 2 < (int)W) o[2] = s2;
+    if (xo + 3 < (int)W) o[3] = s3;
 }
 
 }  // namespace
@@ -169,11 +215,13 @@ int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t hei
 int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32_t height, uint32_t nbands,
                const float* kernel, uint32_t kw, uint32_t kh) {
     if (kw > (uint32_t)kMaxKernel || kh > (uint32_t)kMaxKernel) return (int)cudaErrorInvalidValue;
-    const size_t smem = ((size_t)(kTileW + kw - 1) * (kTileH + kh - 1) + (size_t)kw * kh) * sizeof(float);
+    const int kwp = round4((int)kw);
+    const size_t tw = round4(kTileW + kwp + 3), th = kTileH + kh - 1;
+    const size_t smem = (tw * th + (size_t)kwp * kh) * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(k_psf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     const dim3 grid((width + kTileW - 1) / kTileW, (height + kTileH - 1) / kTileH, nbands);
-    k_psf<<<grid, dim3(kTileW, kTileH), smem, (cudaStream_t)stream>>>(in, out, width, height, kernel, (int)kw, (int)kh);
+    k_psf<<<grid, dim3(32, kTileH), smem, (cudaStream_t)stream>>>(in, out, width, height, kernel, (int)kw, (int)kh);
     return (int)cudaGetLastError();
 }
 
