@@ -1129,18 +1129,53 @@ DnOpts dn_opts(const vgb_denoise_options* o) {
     return d;
 }
 
+// Working layout of the filter: each illumination image interleaved per pixel ([P][NB], so a
+// tap is one or two float4 loads) and the guide packed as one float4 per pixel (depth, normal).
 template <int NB>
 __global__ void k_dn_split(const float* __restrict__ direct, const float* __restrict__ indirect,
-                           const float* __restrict__ albedo, float* __restrict__ D, float* __restrict__ I, size_t P,
-                           uint32_t nb, float eps) {
+                           const float* __restrict__ albedo, const float* __restrict__ depth,
+                           const float* __restrict__ normal, float* __restrict__ D, float* __restrict__ I,
+                           float4* __restrict__ guide, size_t P, uint32_t nb, float eps) {
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
-            if (k >= (int)nb) break;
-            const float a = smax(albedo[k * P + p], eps);
-            D[k * P + p] = direct[k * P + p] / a;
-            I[k * P + p] = indirect[k * P + p] / a;
+            float d = 0.f, i = 0.f;
+            if (k < (int)nb) {
+                const float a = smax(albedo[k * P + p], eps);
+                d = direct[k * P + p] / a;
+                i = indirect[k * P + p] / a;
+            }
+            D[p * NB + k] = d;
+            I[p * NB + k] = i;
         }
+        guide[p] = make_float4(depth[p], normal[p], normal[P + p], normal[2 * P + p]);
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ void dn_load(const float* __restrict__ src, size_t q, float* v) {
+    if (NB % 4 == 0) {
+        const float4* s4 = reinterpret_cast<const float4*>(src + q * NB);
+#pragma unroll
+        for (int j = 0; j < NB / 4; ++j) {
+            const float4 t = s4[j];
+            v[4 * j] = t.x; v[4 * j + 1] = t.y; v[4 * j + 2] = t.z; v[4 * j + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < NB; ++k) v[k] = src[q * NB + k];
+    }
+}
+
+template <int NB>
+__device__ __forceinline__ void dn_store(float* __restrict__ dst, size_t q, const float* v) {
+    if (NB % 4 == 0) {
+        float4* d4 = reinterpret_cast<float4*>(dst + q * NB);
+#pragma unroll
+        for (int j = 0; j < NB / 4; ++j) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < NB; ++k) dst[q * NB + k] = v[k];
     }
 }
 
@@ -1148,13 +1183,13 @@ __global__ void k_dn_split(const float* __restrict__ direct, const float* __rest
 // exhausted).  The tap weights depend only on depth and normal, so they are formed once.
 template <int NB>
 __global__ void k_dn_pass(const float* __restrict__ Din, float* __restrict__ Dout, const float* __restrict__ Iin,
-                          float* __restrict__ Iout, const float* __restrict__ depth, const float* __restrict__ normal,
-                          uint32_t W, uint32_t H, uint32_t nb, int step, int along_columns, const DnOpts o) {
+                          float* __restrict__ Iout, const float4* __restrict__ guide, uint32_t W, uint32_t H,
+                          uint32_t nb, int step, int along_columns, const DnOpts o) {
     const size_t P = (size_t)W * H;
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(p % W), y = (int)(p / W);
-        const float cd = depth[p];
-        const float cnx = normal[p], cny = normal[P + p], cnz = normal[2 * P + p];
+        const float4 cg = guide[p];
+        const float cd = cg.x;
         float w[5];
         size_t q[5];
         float wsum = 0.f;
@@ -1166,10 +1201,11 @@ __global__ void k_dn_pass(const float* __restrict__ Din, float* __restrict__ Dou
             sx = min(max(sx, 0), (int)W - 1);
             sy = min(max(sy, 0), (int)H - 1);
             q[t] = (size_t)sy * W + sx;
-            const float sd = depth[q[t]];
+            const float4 sg = guide[q[t]];
+            const float sd = sg.x;
             const float ratio = smax(cd, sd) / (smin(cd, sd) + o.eps);
             const float dw = ratio < (1.0f + o.depth_threshold) ? 1.0f : expf(-(ratio - 1.0f) / o.depth_threshold);
-            const float nd = (cnx * normal[q[t]] + cny * normal[P + q[t]]) + cnz * normal[2 * P + q[t]];
+            const float nd = (cg.y * sg.y + cg.z * sg.z) + cg.w * sg.w;
             const float sim = smax(0.0f, nd);
             const float om = 1.0f - sim;
             const float nw = smax(o.min_normal_weight, expf(-(om * om) / o.normal_threshold));
@@ -1182,14 +1218,22 @@ __global__ void k_dn_pass(const float* __restrict__ Din, float* __restrict__ Dou
             const float* in = img ? Iin : Din;
             float* out = img ? Iout : Dout;
             if (!in) continue;
+            float sum[NB], v[NB];
 #pragma unroll
-            for (int k = 0; k < NB; ++k) {
-                if (k >= (int)nb) break;
-                float sum = 0.f;
+            for (int k = 0; k < NB; ++k) sum[k] = 0.f;
 #pragma unroll
-                for (int t = 0; t < 5; ++t) sum += in[k * P + q[t]] * w[t];
-                out[k * P + p] = norm ? sum / wsum : in[k * P + p];
+            for (int t = 0; t < 5; ++t) {
+                dn_load<NB>(in, q[t], v);
+#pragma unroll
+                for (int k = 0; k < NB; ++k) sum[k] += v[k] * w[t];
             }
+            if (norm) {
+#pragma unroll
+                for (int k = 0; k < NB; ++k) sum[k] = sum[k] / wsum;
+            } else {
+                dn_load<NB>(in, p, sum);
+            }
+            dn_store<NB>(out, p, sum);
         }
     }
 }
@@ -1201,11 +1245,14 @@ __global__ void k_dn_merge(const float* __restrict__ D, const float* __restrict_
                            float* direct, float* indirect, float* __restrict__ total, float* __restrict__ power,
                            const float* __restrict__ omega, const PowerScale ps, size_t P, uint32_t nb) {
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+        float dv[NB], iv[NB];
+        dn_load<NB>(D, p, dv);
+        dn_load<NB>(I, p, iv);
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
             if (k >= (int)nb) break;
             const float a = albedo[k * P + p];
-            const float d = D[k * P + p] * a, i = I[k * P + p] * a;
+            const float d = dv[k] * a, i = iv[k] * a;
             if (direct) direct[k * P + p] = d;
             if (indirect) indirect[k * P + p] = i;
             const float t = d + i;  // renderPasses.total_radiance = direct + indirect
@@ -1213,6 +1260,13 @@ __global__ void k_dn_merge(const float* __restrict__ D, const float* __restrict_
             if (power) power[k * P + p] = (ps.v[k] * omega[p]) * t;
         }
     }
+}
+
+// Floats of the filter's working buffers: two ping-pong pairs of interleaved images (bands
+// rounded up to the kernel instance, 1, 4 or 8) and the packed guide.
+size_t dn_work_floats(uint32_t nb, size_t P) {
+    const size_t nbs = nb <= 1 ? 1 : (nb <= 4 ? 4 : 8);
+    return 4 * nbs * P + 4 * P;
 }
 
 vgb_status ensure_dn_scratch(vgb_context* ctx, size_t floats) {
@@ -1233,9 +1287,10 @@ void launch_denoise_t(vgb_context* ctx, const float* in_d, const float* in_i, co
                       float* out_d, float* out_i, float* total, float* power, const float* omega, const PowerScale& ps) {
     const size_t P = (size_t)W * H;
     const int g = grid_for(ctx, P);
-    float* Db[2] = {scratch, scratch + nb * P};
-    float* Ib[2] = {scratch + 2 * nb * P, scratch + 3 * nb * P};
-    k_dn_split<NB><<<g, 256, 0, ctx->stream>>>(in_d, in_i, albedo, Db[0], Ib[0], P, nb, o.eps);
+    float* Db[2] = {scratch, scratch + NB * P};
+    float* Ib[2] = {scratch + 2 * NB * P, scratch + 3 * NB * P};
+    float4* guide = reinterpret_cast<float4*>(scratch + 4 * NB * P);
+    k_dn_split<NB><<<g, 256, 0, ctx->stream>>>(in_d, in_i, albedo, depth, normal, Db[0], Ib[0], guide, P, nb, o.eps);
     int cd = 0, ci = 0;  // buffer holding the current image
     const uint32_t levels = std::max(o.levels_direct, o.levels_indirect);
     for (uint32_t level = 0; level < levels; ++level) {
@@ -1243,8 +1298,8 @@ void launch_denoise_t(vgb_context* ctx, const float* in_d, const float* in_i, co
         const bool fd = level < o.levels_direct, fi = level < o.levels_indirect;
         for (int pass = 0; pass < 2; ++pass) {
             k_dn_pass<NB><<<g, 256, 0, ctx->stream>>>(fd ? Db[cd] : nullptr, fd ? Db[cd ^ 1] : nullptr,
-                                                      fi ? Ib[ci] : nullptr, fi ? Ib[ci ^ 1] : nullptr, depth, normal,
-                                                      W, H, nb, step, pass == 0 ? 1 : 0, o);
+                                                      fi ? Ib[ci] : nullptr, fi ? Ib[ci ^ 1] : nullptr, guide, W, H,
+                                                      nb, step, pass == 0 ? 1 : 0, o);
             if (fd) cd ^= 1;
             if (fi) ci ^= 1;
         }
@@ -1607,11 +1662,12 @@ VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect,
     cudaSetDevice(ctx->device);
     const size_t P = (size_t)width * height, BP = (size_t)nbands * P;
     vgb_status s;
-    if ((s = ensure_dn_scratch(ctx, 4 * BP + (on_device ? 0 : 3 * BP + 4 * P))) != VGB_OK) return s;
+    const size_t work = dn_work_floats(nbands, P);
+    if ((s = ensure_dn_scratch(ctx, work + (on_device ? 0 : 3 * BP + 4 * P))) != VGB_OK) return s;
     float *d = direct, *i = indirect;
     const float *a = albedo, *z = depth, *n = normal;
     if (!on_device) {
-        float* cur = ctx->d_dn + 4 * BP;
+        float* cur = ctx->d_dn + work;
         CK(cudaMemcpyAsync(cur, direct, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); d = cur; cur += BP;
         CK(cudaMemcpyAsync(cur, indirect, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); i = cur; cur += BP;
         CK(cudaMemcpyAsync(cur, albedo, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); a = cur; cur += BP;
@@ -1710,9 +1766,10 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
         // options.denoise (cpu_path_tracer.ipp:124-134): the render writes un-denoised direct and
         // indirect radiance (and albedo, depth and normal where the film has none) to scratch;
         // the denoiser then writes direct, indirect, total and received power to the film.
-        if ((s = ensure_dn_scratch(ctx, (size_t)7 * B * P + 4 * P)) != VGB_OK) return s;
+        const size_t work = dn_work_floats(B, P);
+        if ((s = ensure_dn_scratch(ctx, work + (size_t)3 * B * P + 4 * P)) != VGB_OK) return s;
         dn_scratch = ctx->d_dn;
-        float* extra = ctx->d_dn + (size_t)4 * B * P;
+        float* extra = ctx->d_dn + work;
         fr.total = nullptr; fr.power = nullptr;
         fr.direct = extra; fr.indirect = extra + (size_t)B * P;
         if (!fr.albedo) fr.albedo = extra + (size_t)2 * B * P;
@@ -2460,7 +2517,7 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
         // options.denoise per frame, on the frame's own planes (checked above)
         size_t most = 0;
         for (uint32_t f = 0; f < nframes; ++f) most = std::max(most, (size_t)frames[f].camera.width * frames[f].camera.height);
-        vgb_status ds = ensure_dn_scratch(ctx, 4 * (size_t)ctx->nbands * most);
+        vgb_status ds = ensure_dn_scratch(ctx, dn_work_floats(ctx->nbands, most));
         if (ds != VGB_OK) return ds;
         for (uint32_t f = 0; f < nframes; ++f) {
             const vgb_frame& fr = frames[f];
