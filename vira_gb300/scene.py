@@ -182,28 +182,41 @@ class Mesh:
     def set_smooth_shading(self, on: bool):
         self.smooth_shading = bool(on)
 
-    def compute_normals(self) -> np.ndarray:
+    def compute_normals(self, gpu: int | None = None) -> np.ndarray:
+        """Mesh::calculateNormals (mesh.ipp:199-233); with `gpu` by vgb_compute_vertex_normals_gpu,
+        which gives the same normals."""
         if self.normals is None:
             lib = capi.load()
             p = np.ascontiguousarray(self.positions, np.float32)
             i = np.ascontiguousarray(self.indices, np.uint32)
             n = np.empty_like(p)
-            capi.check(lib.vgb_compute_vertex_normals(capi.ptr(p), p.shape[0], capi.ptr(i), i.shape[0], capi.ptr(n)),
-                       what="compute_vertex_normals")
+            if gpu is None:
+                capi.check(lib.vgb_compute_vertex_normals(capi.ptr(p), p.shape[0], capi.ptr(i), i.shape[0], capi.ptr(n)),
+                           what="compute_vertex_normals")
+            else:
+                ctx = _mesh_context(gpu)
+                capi.check(lib.vgb_compute_vertex_normals_gpu(ctx, capi.ptr(p), p.shape[0], capi.ptr(i), i.shape[0],
+                                                              capi.ptr(n), 0), ctx, "compute_vertex_normals_gpu")
             self.normals = n
         return self.normals
 
     @staticmethod
-    def from_dem(heights: np.ndarray, posting: float, albedo=None, nbands: int = 1) -> "Mesh":
-        """DEM::makeMesh with the non-OGR projection (dem.ipp:138-211)."""
+    def from_dem(heights: np.ndarray, posting: float, albedo=None, nbands: int = 1, gpu: int | None = None) -> "Mesh":
+        """DEM::makeMesh with the non-OGR projection (dem.ipp:138-211).  With `gpu` (a device index)
+        the grid is triangulated by vgb_dem_triangulate_gpu, which gives the same arrays."""
         lib = capi.load()
         h = np.ascontiguousarray(heights, np.float32)
         H, W = h.shape
         pos = np.empty((H * W, 3), np.float32)
         idx = np.empty((2 * (W - 1) * (H - 1), 3), np.uint32)
         nt = C.c_uint32(0)
-        capi.check(lib.vgb_dem_triangulate(capi.ptr(h), W, H, float(posting), float(posting), capi.ptr(pos),
-                                           capi.ptr(idx), C.byref(nt)), what="dem_triangulate")
+        if gpu is None:
+            capi.check(lib.vgb_dem_triangulate(capi.ptr(h), W, H, float(posting), float(posting), capi.ptr(pos),
+                                               capi.ptr(idx), C.byref(nt)), what="dem_triangulate")
+        else:
+            ctx = _mesh_context(gpu)
+            capi.check(lib.vgb_dem_triangulate_gpu(ctx, capi.ptr(h), W, H, float(posting), float(posting), capi.ptr(pos),
+                                                   capi.ptr(idx), C.byref(nt), 0), ctx, "dem_triangulate_gpu")
         alb = None
         if albedo is not None:
             a = np.asarray(albedo, np.float32)
@@ -212,6 +225,19 @@ class Mesh:
             else:
                 alb = a.reshape(H * W, -1).astype(np.float32)
         return Mesh(pos, idx[: nt.value].copy(), albedo=alb)
+
+
+_MESH_CONTEXTS: dict = {}
+
+
+def _mesh_context(device: int):
+    """A context per device for the mesh helpers (triangulation, normals)."""
+    if device not in _MESH_CONTEXTS:
+        lib = capi.load()
+        h = C.c_void_p()
+        capi.check(lib.vgb_context_create(C.byref(h), int(device)), what="context_create (is a GPU present?)")
+        _MESH_CONTEXTS[device] = h
+    return _MESH_CONTEXTS[device]
 
 
 @dataclass
