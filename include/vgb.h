@@ -215,6 +215,14 @@ VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* positions, ui
 /* Replaces Mesh::buildBVH -> EmbreeBLAS (include/implementation/geometry/mesh.ipp:396-408,
  * include/implementation/rendering/acceleration/embree_blas.ipp:14-71). */
 VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts);
+/* Moves the uploaded vertices (same triangles), in place of re-uploading the mesh and rebuilding
+ * the BVH that Scene::buildTLAS does when geometry changed (include/implementation/scene.ipp:711-805).
+ * positions: 3 floats per vertex; normals: 3 floats per vertex or NULL (recomputed on the device,
+ * the same normals vgb_compute_vertex_normals gives); both device memory if on_device else host.
+ * A binary BVH is refitted on the device (every box recomputed bottom up, topology kept: the
+ * boxes equal a rebuild's for unchanged positions); an 8-wide BVH is rebuilt. */
+VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* positions, const float* normals,
+                                              int on_device);
 
 /* ========================= rendering =========================================== */
 /* Camera::initializePixelSolidAngle (include/implementation/cameras/camera.ipp:1622-1666):
@@ -405,6 +413,111 @@ VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
 /* Per-launch CUDA events around every kernel of vgb_render, summed per kernel family into
  * vgb_stats.ms_trace / ms_shade / ms_shadow / ms_film. */
 VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
+
+/* ========================= DEM Quipu files (.qld) ==============================
+ * Vira's on-disk DEM pyramid (include/implementation/quipu/dem_quipu.ipp,
+ * include/implementation/quipu/quipu_io.ipp): the identifier "QUIPU", class id 2002, the
+ * transformation (position, rotation, scale, FP64), the LoD count, an albedo flag, the
+ * normal cone, a table of (GSD, byte offset) per LoD, then per LoD its DEMProjection,
+ * heights stored as uint8 / uint16 fixed point or FP32 (LZ4 block or raw), and optional
+ * albedo (constant, one uint8 plane or one uint8 plane per band).
+ * Reading: the file is parsed and LZ4-decoded on the host (own decoder of the LZ4 block
+ * format, bounds-checked); the quantised heights and albedo travel to the device, where the
+ * fixed-point decode, DEMProjection::transformToWorld, the triangulation and the vertex
+ * normals run.  Errors of the functions without a context are read with
+ * vgb_quipu_last_error(). */
+typedef struct vgb_quipu_dem vgb_quipu_dem;
+
+#define VGB_QUIPU_MAX_LODS 64
+#define VGB_QUIPU_NO_ALBEDO 0xFFFFFFFFu
+
+typedef struct vgb_quipu_header {
+    uint16_t class_id;          /* 2002 (VIRA_DEM_PYRAMID) */
+    uint16_t num_lods;
+    uint32_t has_albedos;
+    double position[3];         /* transformation: translation */
+    double rotation[9];         /* column-major 3x3 rotation */
+    double scale[3];
+    float normal[3];            /* normal cone of the coarsest LoD: mean direction ... */
+    float cone_angle;           /* ... and half angle, radians */
+} vgb_quipu_header;
+
+typedef struct vgb_quipu_projection {   /* DEMProjection (include/vira/dems/dem_projection.hpp) */
+    uint32_t width, height;             /* resolution */
+    double pixel_scale[2];
+    uint32_t tile_definitions[2];
+    uint32_t tile_row, tile_col;
+    double xoff, yoff, dx, dy;
+    uint32_t is_ogr;                    /* map-projected (GDAL); vertices are not built for these */
+    uint32_t pad;
+    double row_col_rotation[2];
+    double model_tie_point[2];
+} vgb_quipu_projection;
+
+typedef struct vgb_quipu_lod_info {
+    double gsd;                 /* table-of-contents GSD (x) */
+    uint64_t offset;            /* byte offset of the LoD block */
+    uint32_t width, height;     /* resolution of the stored heights: the vertex grid */
+    vgb_quipu_projection projection;   /* as stored (its resolution sets the grid's extent) */
+    float height_min, height_max;
+    uint32_t precision;         /* class id of the stored heights: 3 uint8, 4 uint16, 1 float */
+    uint32_t compressed;        /* heights are an LZ4 block */
+    uint32_t albedo_type;       /* 0 constant, 1 grey uint8 plane, 2 one uint8 plane per band;
+                                   VGB_QUIPU_NO_ALBEDO when the file stores none */
+    uint32_t albedo_channels;   /* planes of a type-2 albedo */
+} vgb_quipu_lod_info;
+
+typedef struct vgb_quipu_read_options {   /* DEMQuipuReaderOptions (quipu/dem_quipu.hpp) */
+    uint32_t nbands;            /* TSpectral::size() of the reading program */
+    uint32_t read_albedos;      /* 0: every vertex gets default_albedo */
+    float default_albedo;       /* reference default 0.06 */
+    float albedo_profile[VGB_MAX_BANDS];   /* multiplies a grey albedo plane per band (1.0 = none) */
+} vgb_quipu_read_options;
+
+/* DEMQuipu::DEMQuipu (dem_quipu.ipp:29-60) + an index of every LoD block. */
+VGB_API vgb_status vgb_quipu_open(const char* path, vgb_quipu_dem** out);
+VGB_API void vgb_quipu_close(vgb_quipu_dem* q);
+VGB_API const char* vgb_quipu_last_error(void);
+VGB_API vgb_status vgb_quipu_get_header(const vgb_quipu_dem* q, vgb_quipu_header* out);
+VGB_API vgb_status vgb_quipu_get_lod(const vgb_quipu_dem* q, uint32_t lod, vgb_quipu_lod_info* out);
+/* The LoD DEMQuipu::readBuffers picks for a required GSD (dem_quipu.ipp:136-152): the last of
+ * the leading LoDs whose GSD is <= required, LoD 0 if none. */
+VGB_API uint32_t vgb_quipu_select_lod(const vgb_quipu_dem* q, double required_gsd);
+/* readDEMHeights + fixedToFloat (quipu_io.ipp:601-626, image_utils.ipp:509-527) on the host:
+ * [H][W] floats, +inf where the stored code is 0. */
+VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float* heights);
+/* DEMQuipu::readBuffers (dem_quipu.ipp:124-221) -> DEM::makeVertexBuffer / makeIndexBuffer
+ * (dem.ipp:152-211) on the device: positions [H*W][3], per-vertex albedo [H*W][nbands] (NULL to
+ * skip), vertex normals [H*W][3] (NULL to skip; Mesh::calculateNormals), indices [2(W-1)(H-1)][3]
+ * of which *ntris are written.  Arrays device memory if on_device else host.  Non-OGR
+ * projections only. */
+VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint32_t lod,
+                                       const vgb_quipu_read_options* opts, float* positions,
+                                       float* vert_albedo, float* normals, uint32_t* indices,
+                                       uint32_t* ntris, int on_device);
+
+typedef struct vgb_quipu_lod_data {       /* one DEM of the pyramid to write */
+    vgb_quipu_projection projection;      /* width/height give the heights' resolution */
+    const float* heights;                 /* [H][W]; +inf / NaN = no data */
+    uint32_t albedo_type;                 /* 0 constant, 1 grey plane, 2 plane per band */
+    uint32_t nbands;                      /* bands of a constant or per-band albedo */
+    const float* albedo;                  /* constant: nbands; grey: [H][W]; per band: [H][W][nbands] */
+} vgb_quipu_lod_data;
+
+/* DEMQuipu::write (dem_quipu.ipp:224-332): the pyramid finest first; heights quantised to
+ * uint8 / uint16 when the height range over 255 / 65535 is below GSD / 50, else FP32; LZ4
+ * block format when compress (own encoder).  The rotation is written as given (column-major). */
+VGB_API vgb_status vgb_quipu_write(const char* path, const vgb_quipu_lod_data* lods, uint32_t nlods,
+                                   const double position[3], const double rotation[9],
+                                   const double scale[3], int write_albedos, int compress);
+
+/* The LZ4 block format (no frame) as the reference uses it through LZ4_compress_default /
+ * LZ4_decompress_safe (quipu_io.ipp:181-231): decompress returns the bytes written or -1 for
+ * a malformed or overrunning block; compress returns the block size or 0 when dst_cap <
+ * vgb_lz4_bound(n). */
+VGB_API int64_t vgb_lz4_decompress(const void* src, uint64_t src_size, void* dst, uint64_t dst_cap);
+VGB_API uint64_t vgb_lz4_bound(uint64_t n);
+VGB_API uint64_t vgb_lz4_compress(const void* src, uint64_t n, void* dst, uint64_t dst_cap);
 
 #ifdef __cplusplus
 }

@@ -38,20 +38,16 @@ class View:
 
 def _apply_parameters(scene: Scene, texture, heights):
     """Puts the parameters into the scene: the texture through vgb_texture_update, the heights
-    by moving the mesh's vertices (re-upload and BVH rebuild when they changed)."""
+    by moving the mesh's vertices (device update and BVH refit when they changed)."""
     mesh = scene.meshes[0]
     tex = None if texture is None else texture.detach().float().contiguous().cpu().numpy()
     z = heights.detach().float().contiguous().cpu().numpy()
+    scene.build_tlas()
     if not np.array_equal(mesh.positions[:, 2], z):
         p = mesh.positions.copy()
         p[:, 2] = z
-        mesh.positions = p
-        mesh.normals = None
-        if tex is not None:
-            mesh.albedo_map = tex
-        scene.mark_dirty()
-        scene.build_tlas()
-    elif tex is not None and not np.array_equal(mesh.albedo_map, tex):
+        scene.update_positions(0, p)
+    if tex is not None and not np.array_equal(mesh.albedo_map, tex):
         mesh.albedo_map = tex
         scene.build_tlas()
         lib = capi.load()
@@ -61,14 +57,13 @@ def _apply_parameters(scene: Scene, texture, heights):
 
 
 def _apply_positions(scene: Scene, texture, positions):
-    """Puts texture and vertex positions ([nverts][3]) into the scene (re-upload and BVH
-    rebuild when the positions changed)."""
+    """Puts texture and vertex positions ([nverts][3]) into the scene (device update and BVH
+    refit when the positions changed)."""
     mesh = scene.meshes[0]
     p = positions.detach().float().contiguous().cpu().numpy()
+    scene.build_tlas()
     if not np.array_equal(mesh.positions, p):
-        mesh.positions = p.copy()
-        mesh.normals = None
-        scene.mark_dirty()
+        scene.update_positions(0, p)
     _apply_parameters(scene, texture, positions.detach()[:, 2])
 
 

@@ -109,6 +109,41 @@ class Stats(C.Structure):
     ]
 
 
+QUIPU_MAX_LODS = 64
+QUIPU_NO_ALBEDO = 0xFFFFFFFF
+
+
+class QuipuHeader(C.Structure):
+    _fields_ = [("class_id", C.c_uint16), ("num_lods", C.c_uint16), ("has_albedos", C.c_uint32),
+                ("position", C.c_double * 3), ("rotation", C.c_double * 9), ("scale", C.c_double * 3),
+                ("normal", C.c_float * 3), ("cone_angle", C.c_float)]
+
+
+class QuipuProjection(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("pixel_scale", C.c_double * 2),
+                ("tile_definitions", C.c_uint32 * 2), ("tile_row", C.c_uint32), ("tile_col", C.c_uint32),
+                ("xoff", C.c_double), ("yoff", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+                ("is_ogr", C.c_uint32), ("pad", C.c_uint32), ("row_col_rotation", C.c_double * 2),
+                ("model_tie_point", C.c_double * 2)]
+
+
+class QuipuLodInfo(C.Structure):
+    _fields_ = [("gsd", C.c_double), ("offset", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("projection", QuipuProjection), ("height_min", C.c_float), ("height_max", C.c_float),
+                ("precision", C.c_uint32), ("compressed", C.c_uint32), ("albedo_type", C.c_uint32),
+                ("albedo_channels", C.c_uint32)]
+
+
+class QuipuReadOptions(C.Structure):
+    _fields_ = [("nbands", C.c_uint32), ("read_albedos", C.c_uint32), ("default_albedo", C.c_float),
+                ("albedo_profile", C.c_float * MAX_BANDS)]
+
+
+class QuipuLodData(C.Structure):
+    _fields_ = [("projection", QuipuProjection), ("heights", C.c_void_p), ("albedo_type", C.c_uint32),
+                ("nbands", C.c_uint32), ("albedo", C.c_void_p)]
+
+
 # exported symbol -> (restype, argtypes); the symbol list is the one include/vgb.h declares
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -125,6 +160,7 @@ SIGNATURES = {
                                         C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]),
     "vgb_scene_upload": (C.c_int, [_P, _P, _U32, _P, _U32, _U32, _P, _P, _P, _P, _U32, _U32]),
     "vgb_bvh_build": (C.c_int, [_P, C.POINTER(BvhOptions)]),
+    "vgb_scene_update_positions": (C.c_int, [_P, _P, _P, C.c_int]),
     "vgb_pixel_solid_angle": (C.c_int, [_P, C.POINTER(Camera), _P, C.c_int]),
     "vgb_render": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
     "vgb_render_noalloc": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), C.POINTER(Film)]),
@@ -143,6 +179,20 @@ SIGNATURES = {
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
+    "vgb_quipu_open": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "vgb_quipu_close": (None, [_P]),
+    "vgb_quipu_last_error": (C.c_char_p, []),
+    "vgb_quipu_get_header": (C.c_int, [_P, C.POINTER(QuipuHeader)]),
+    "vgb_quipu_get_lod": (C.c_int, [_P, _U32, C.POINTER(QuipuLodInfo)]),
+    "vgb_quipu_select_lod": (_U32, [_P, C.c_double]),
+    "vgb_quipu_read_heights": (C.c_int, [_P, _U32, _P]),
+    "vgb_quipu_read_mesh": (C.c_int, [_P, _P, _U32, C.POINTER(QuipuReadOptions), _P, _P, _P, _P, C.POINTER(_U32),
+                                      C.c_int]),
+    "vgb_quipu_write": (C.c_int, [C.c_char_p, _P, _U32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.c_int, C.c_int]),
+    "vgb_lz4_decompress": (C.c_int64, [_P, C.c_uint64, _P, C.c_uint64]),
+    "vgb_lz4_bound": (C.c_uint64, [C.c_uint64]),
+    "vgb_lz4_compress": (C.c_uint64, [_P, C.c_uint64, _P, C.c_uint64]),
 }
 
 _LIB = None

@@ -877,6 +877,10 @@ struct vgb_context {
     uint32_t nnodes = 0;
     uint32_t bvh_layout = 2;
     bool bvh_ready = false;
+    uint32_t* d_parent = nullptr;   // binary layout: (parent << 1 | side) per node, for refits
+    uint32_t* d_refit = nullptr;    // nnodes + 1 words: arrival counters and the walk-bound flag
+    uint32_t bvh_leaf = 0, bvh_threads = 0;
+    bool h_pos_stale = false;       // device positions moved by a device-side update
     // render scratch
     size_t cap_P = 0;
     uint32_t cap_B = 0, cap_L = 0;
@@ -912,6 +916,9 @@ struct vgb_context {
     // denoiser scratch: ping-pong illumination planes and the render's internal passes
     float* d_dn = nullptr;
     size_t cap_dn = 0;
+    // pinned host staging of file payloads (Quipu LoDs)
+    void* h_pin = nullptr;
+    size_t cap_pin = 0;
 };
 
 namespace {
@@ -946,8 +953,9 @@ void free_scene(vgb_context* ctx) {
     ctx->d_vpos = nullptr; ctx->d_vnrm = nullptr; ctx->d_vuv = nullptr; ctx->d_valb = nullptr; ctx->d_idx = nullptr; ctx->d_tex = nullptr;
 }
 void free_bvh(vgb_context* ctx) {
-    dfree(ctx->d_nodes); dfree(ctx->d_tris);
-    ctx->d_nodes = nullptr; ctx->d_tris = nullptr; ctx->bvh_ready = false; ctx->nnodes = 0;
+    dfree(ctx->d_nodes); dfree(ctx->d_tris); dfree(ctx->d_parent); dfree(ctx->d_refit);
+    ctx->d_nodes = nullptr; ctx->d_tris = nullptr; ctx->d_parent = nullptr; ctx->d_refit = nullptr;
+    ctx->bvh_ready = false; ctx->nnodes = 0;
 }
 void free_scratch(vgb_context* ctx) {
     for (void* p : ctx->scratch) dfree(p);
@@ -1362,6 +1370,7 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     dfree(ctx->d_frames);
     if (ctx->h_frames) cudaFreeHost(ctx->h_frames);
     dfree(ctx->d_adj); dfree(ctx->d_views); dfree(ctx->d_loss); dfree(ctx->d_dn);
+    if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1457,6 +1466,7 @@ VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t
     ctx->tw = tw; ctx->th = th;
     ctx->h_pos.assign(pos, pos + 3 * (size_t)nverts);
     ctx->h_idx.assign(idx, idx + 3 * (size_t)ntris);
+    ctx->h_pos_stale = false;
     return VGB_OK;
 }
 
@@ -1469,19 +1479,36 @@ VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) 
     if (layout != 2 && layout != 8) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: layout must be 2 or 8");
     if (leaf > (layout == 8 ? vgb::kMaxLeaf8 : vgb::kMaxLeaf))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8 (binary) or <= 3 (8-wide)");
+    cudaSetDevice(ctx->device);
+    if (ctx->h_pos_stale) {
+        // positions were last updated on the device: bring them back for the host builder
+        std::vector<float4> p4(ctx->nverts);
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(p4.data(), ctx->d_vpos, sizeof(float4) * ctx->nverts, cudaMemcpyDeviceToHost));
+        for (uint32_t v = 0; v < ctx->nverts; ++v) {
+            ctx->h_pos[3 * (size_t)v] = p4[v].x; ctx->h_pos[3 * (size_t)v + 1] = p4[v].y; ctx->h_pos[3 * (size_t)v + 2] = p4[v].z;
+        }
+        ctx->h_pos_stale = false;
+    }
     vgb::BvhHost bvh;
     const char* why = "";
     if (!vgb::build_bvh(ctx->h_pos.data(), ctx->nverts, ctx->h_idx.data(), ctx->ntris, leaf, threads, layout, bvh, &why))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("bvh_build: ") + why);
-    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
     free_bvh(ctx);
     vgb_status s;
     if ((s = dalloc(ctx, &ctx->d_nodes, bvh.nodes.size() * sizeof(uint32_t))) != VGB_OK) return s;
     if ((s = dalloc(ctx, &ctx->d_tris, bvh.tris.size() * sizeof(float))) != VGB_OK) return s;
     CK(cudaMemcpy(ctx->d_nodes, bvh.nodes.data(), bvh.nodes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_tris, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (layout == 2) {
+        if ((s = dalloc(ctx, &ctx->d_parent, bvh.parent.size() * sizeof(uint32_t))) != VGB_OK) return s;
+        if ((s = dalloc(ctx, &ctx->d_refit, (bvh.parent.size() + 1) * sizeof(uint32_t))) != VGB_OK) return s;
+        CK(cudaMemcpy(ctx->d_parent, bvh.parent.data(), bvh.parent.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
     ctx->nnodes = bvh.num_nodes;
     ctx->bvh_layout = layout;
+    ctx->bvh_leaf = leaf; ctx->bvh_threads = threads;
     ctx->bvh_ready = true;
     ctx->stats.bvh_nodes = bvh.num_nodes;
     ctx->stats.bvh_node_bytes = layout == 8 ? 80 : 64;
@@ -1542,7 +1569,8 @@ VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* height
         ix = reinterpret_cast<uint32_t*>(cur);
     }
     uint32_t nt = 0;
-    CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, h, W, H, sx, sy, p, ix, w, &nt));
+    CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, h, W, H,
+                                                vgb::dem_pose_of(1.0 * sx, 1.0 * sy, 0.0, 0.0, W, H), p, ix, w, &nt));
     if (!on_device) {
         CK(cudaMemcpyAsync(pos, p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaMemcpyAsync(idx, ix, 3 * (size_t)nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1582,6 +1610,170 @@ VGB_API vgb_status vgb_compute_vertex_normals_gpu(vgb_context* ctx, const float*
         CK(cudaMemcpyAsync(normals, out, 3 * (size_t)nverts * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
     }
+    return VGB_OK;
+}
+
+namespace {
+__global__ void k_pack_vertices(const float* __restrict__ p3, const float* __restrict__ n3, uint32_t nv,
+                                float4* __restrict__ p4, float4* __restrict__ n4) {
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (size_t)gridDim.x * blockDim.x) {
+        p4[v] = make_float4(p3[3 * v], p3[3 * v + 1], p3[3 * v + 2], 0.f);
+        n4[v] = make_float4(n3[3 * v], n3[3 * v + 1], n3[3 * v + 2], 0.f);
+    }
+}
+}  // namespace
+
+VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos, const float* normals, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (ctx->nverts == 0) return fail(ctx, VGB_ERR_NOT_READY, "scene_update_positions: no scene uploaded");
+    if (!pos) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_update_positions: null positions");
+    cudaSetDevice(ctx->device);
+    const size_t nv = ctx->nverts, nt = ctx->ntris;
+    const size_t work = normals ? 0 : vgb::normals_work_words((uint32_t)nv, (uint32_t)nt);
+    const size_t stage = (on_device ? 0 : 3 * nv) + (normals && on_device ? 0 : 3 * nv);
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, work + stage)) != VGB_OK) return s;
+    float* cur = ctx->d_dn + work;
+    const float* p = pos;
+    if (!on_device) {
+        CK(cudaMemcpyAsync(cur, pos, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        p = cur; cur += 3 * nv;
+    }
+    const float* n = normals;
+    if (normals && !on_device) {
+        CK(cudaMemcpyAsync(cur, normals, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+        n = cur;
+    } else if (!normals) {
+        const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ctx->d_idx, (uint32_t)nt, cur,
+                                                  reinterpret_cast<uint32_t*>(ctx->d_dn));
+        CK((cudaError_t)rc);
+        n = cur;
+    }
+    k_pack_vertices<<<grid_for(ctx, nv, 8), 256, 0, ctx->stream>>>(p, n, (uint32_t)nv, ctx->d_vpos, ctx->d_vnrm);
+    CK(cudaGetLastError());
+    if (on_device) {
+        ctx->h_pos_stale = true;
+    } else {
+        ctx->h_pos.assign(pos, pos + 3 * nv);
+        ctx->h_pos_stale = false;
+    }
+    if (ctx->bvh_ready) {
+        if (ctx->bvh_layout == 2) {
+            const int rc = vgb::launch_refit(ctx->stream, ctx->num_sms, ctx->d_vpos, ctx->d_idx, (uint32_t)nt, ctx->d_tris,
+                                             reinterpret_cast<uint32_t*>(ctx->d_nodes), ctx->nnodes, ctx->d_parent,
+                                             ctx->d_refit);
+            if (rc == -2) return fail(ctx, VGB_ERR_CUDA, "scene_update_positions: refit walk exceeded the tree depth");
+            CK((cudaError_t)rc);
+        } else {
+            vgb_bvh_options o{};
+            o.max_leaf_size = ctx->bvh_leaf; o.threads = ctx->bvh_threads; o.layout = ctx->bvh_layout;
+            if ((s = vgb_bvh_build(ctx, &o)) != VGB_OK) return s;
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+}
+
+// DEMQuipu::readBuffers (dem_quipu.ipp:124-221): the file's stored codes are read and LZ4-decoded
+// on the host into pinned memory, copied to the device as stored (1-4 bytes per post), and
+// decoded, posed (DEM::makeVertexBuffer), triangulated (imageToIndexBuffer) and given vertex
+// normals (Mesh::calculateNormals) there.
+VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint32_t lod,
+                                       const vgb_quipu_read_options* opts, float* positions, float* vert_albedo,
+                                       float* normals, uint32_t* indices, uint32_t* ntris, int on_device) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!q || !opts || !positions || !indices || !ntris)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: null argument");
+    if (vert_albedo && (opts->nbands == 0 || opts->nbands > VGB_MAX_BANDS))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: nbands must be 1..8");
+    vgb::QuipuPayload pl;
+    if (vgb::quipu_lod_payload(q, lod, &pl) != VGB_OK)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
+    if (pl.proj.is_ogr)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: map-projected (OGR) LoDs need GDAL, which is absent");
+    const uint32_t W = pl.heights.w, H = pl.heights.h;
+    if (W < 2 || H < 2) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: fewer than 2x2 posts");
+    const size_t nv = (size_t)W * H, nq = (size_t)(W - 1) * (H - 1);
+    const uint32_t nb = vert_albedo ? opts->nbands : 0;
+    const bool use_albedo = vert_albedo && opts->read_albedos && pl.albedo_type != VGB_QUIPU_NO_ALBEDO;
+    if (use_albedo && pl.albedo_type == 2 && pl.planes.size() != nb)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: the file's albedo has " +
+                    std::to_string(pl.planes.size()) + " channels, the reader " + std::to_string(nb) + " bands");
+    // host: stored codes and albedo planes into pinned staging
+    const size_t code_bytes = (pl.heights.raw_bytes + 15) & ~(size_t)15;
+    const size_t plane_bytes = use_albedo && pl.albedo_type != 0 ? pl.planes.size() * nv : 0;
+    const size_t pin_need = code_bytes + ((plane_bytes + 15) & ~(size_t)15);
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (pin_need > ctx->cap_pin) {
+        if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
+        ctx->h_pin = nullptr;
+        ctx->cap_pin = 0;
+        CK(cudaMallocHost(&ctx->h_pin, pin_need));
+        ctx->cap_pin = pin_need;
+    }
+    uint8_t* hp = (uint8_t*)ctx->h_pin;
+    if (vgb::quipu_read_pixels(pl.path, pl.heights, hp) != VGB_OK)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
+    for (size_t c = 0; c < (plane_bytes ? pl.planes.size() : 0); ++c)
+        if (vgb::quipu_read_pixels(pl.path, pl.planes[c].img, hp + code_bytes + c * nv) != VGB_OK)
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
+    vgb::QuipuDecode d{};
+    d.W = W; d.H = H; d.precision = pl.precision; d.nbands = nb;
+    d.hmin = pl.hmin; d.hmax = pl.hmax;
+    d.albedo_type = use_albedo ? pl.albedo_type : VGB_QUIPU_NO_ALBEDO;
+    d.nplanes = (uint32_t)(plane_bytes ? pl.planes.size() : 0);
+    for (uint32_t b = 0; b < VGB_MAX_BANDS; ++b) {
+        d.constant[b] = opts->default_albedo;
+        d.profile[b] = opts->albedo_profile[b];
+    }
+    for (uint32_t c = 0; c < d.nplanes && c < VGB_MAX_BANDS; ++c) { d.pmin[c] = pl.planes[c].mn; d.pmax[c] = pl.planes[c].mx; }
+    if (use_albedo && pl.albedo_type == 0 && nb) {
+        float cst[VGB_MAX_BANDS];
+        if (vgb::quipu_read_constant(pl.path, pl.constant_pos, nb, cst) != VGB_OK)
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
+        for (uint32_t b = 0; b < nb; ++b) d.constant[b] = cst[b];
+    }
+    // device scratch (floats): codes | planes | heights | triangulation work | normals work |
+    // output staging when the caller's arrays are on the host
+    const size_t f_codes = code_bytes / 4, f_planes = ((plane_bytes + 15) & ~(size_t)15) / 4;
+    const size_t f_work = std::max(vgb::dem_work_words(W, H), normals ? vgb::normals_work_words((uint32_t)nv, (uint32_t)(2 * nq)) : 0);
+    const size_t f_out = on_device ? 0 : 3 * nv + (size_t)nb * nv + (normals ? 3 * nv : 0) + 6 * nq;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, f_codes + f_planes + nv + f_work + f_out)) != VGB_OK) return s;
+    float* cur = ctx->d_dn;
+    void* d_codes = cur; cur += f_codes;
+    uint8_t* d_planes = (uint8_t*)cur; cur += f_planes;
+    float* d_h = cur; cur += nv;
+    uint32_t* d_work = (uint32_t*)cur; cur += f_work;
+    float* p = positions;
+    float* a = vert_albedo;
+    float* nr = normals;
+    uint32_t* ix = indices;
+    if (!on_device) {
+        p = cur; cur += 3 * nv;
+        if (nb) { a = cur; cur += (size_t)nb * nv; }
+        if (normals) { nr = cur; cur += 3 * nv; }
+        ix = (uint32_t*)cur;
+    }
+    CK(cudaMemcpyAsync(d_codes, hp, pl.heights.raw_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (plane_bytes) CK(cudaMemcpyAsync(d_planes, hp + code_bytes, plane_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK((cudaError_t)vgb::launch_quipu_decode(ctx->stream, ctx->num_sms, d, d_codes, d_planes, d_h, nb ? a : nullptr));
+    uint32_t nt = 0;
+    CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, d_h, W, H, vgb::dem_pose(pl.proj), p, ix,
+                                                d_work, &nt));
+    if (normals) {
+        const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ix, nt, nr, d_work);
+        CK((cudaError_t)rc);
+    }
+    if (!on_device) {
+        CK(cudaMemcpyAsync(positions, p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (nb) CK(cudaMemcpyAsync(vert_albedo, a, (size_t)nb * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (normals) CK(cudaMemcpyAsync(normals, nr, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(indices, ix, 3 * (size_t)nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    *ntris = nt;
     return VGB_OK;
 }
 

@@ -54,14 +54,8 @@ extern "C" VGB_API vgb_status vgb_compute_vertex_normals(const float* p, uint32_
 }
 
 // DEM::makeVertexBuffer (dem.ipp:165-211) with DEMProjection's non-OGR mapping
-// (dem_projection.ipp:131-141, initToWorld :54-61) and imageToIndexBuffer
-// (image_utils.ipp:364-409): quad (i, j) gives {(i,j+1),(i+1,j),(i,j)} and
-// {(i+1,j),(i,j+1),(i+1,j+1)}, i outer, j inner, skipping infinite heights.
-extern "C" VGB_API vgb_status vgb_dem_triangulate(const float* h, uint32_t W, uint32_t H, double sx,
-                                                  double sy, float* pos, uint32_t* idx, uint32_t* nt_out) {
-    if (!h || !pos || !idx || !nt_out || W < 2 || H < 2) return VGB_ERR_INVALID_ARGUMENT;
-    const double half_x = ((double)W - 1.) / 2., half_y = ((double)H - 1.) / 2.;
-    const double scale_x = (half_x + 0.5) / (double)W, scale_y = (half_y + 0.5) / (double)H;
+// (dem_projection.ipp:66-71, 131-141); Pixel{i, j} holds floats, exact for i, j < 2^24.
+void vgb::dem_vertices_host(const float* h, uint32_t W, uint32_t H, const DemPose& pose, float* pos) {
     for (uint32_t j = 0; j < H; ++j) {
         for (uint32_t i = 0; i < W; ++i) {
             const size_t v = (size_t)j * W + i;
@@ -70,12 +64,17 @@ extern "C" VGB_API vgb_status vgb_dem_triangulate(const float* h, uint32_t W, ui
                 pos[3 * v] = pos[3 * v + 1] = pos[3 * v + 2] = std::numeric_limits<float>::infinity();
                 continue;
             }
-            const double xs = (double)i * scale_x, ys = -(double)j * scale_y;
-            pos[3 * v] = (float)((1.0 * sx) * (-half_x + 2. * xs));
-            pos[3 * v + 1] = (float)((1.0 * sy) * (half_y + 2. * ys));
+            const double xs = ((double)i + pose.xo) * pose.scale_x, ys = -((double)j + pose.yo) * pose.scale_y;
+            pos[3 * v] = (float)(pose.ax * (-pose.half_x + 2. * xs));
+            pos[3 * v + 1] = (float)(pose.ay * (pose.half_y + 2. * ys));
             pos[3 * v + 2] = z;
         }
     }
+}
+
+// imageToIndexBuffer (image_utils.ipp:364-409): quad (i, j) gives {(i,j+1),(i+1,j),(i,j)} and
+// {(i+1,j),(i,j+1),(i+1,j+1)}, i outer, j inner, skipping infinite heights.
+void vgb::dem_faces_host(const float* h, uint32_t W, uint32_t H, uint32_t* idx, uint32_t* nt_out) {
     size_t k = 0;
     for (uint32_t i = 0; i + 1 < W; ++i) {
         for (uint32_t j = 0; j + 1 < H; ++j) {
@@ -89,6 +88,14 @@ extern "C" VGB_API vgb_status vgb_dem_triangulate(const float* h, uint32_t W, ui
         }
     }
     *nt_out = (uint32_t)(k / 3);
+}
+
+// A DEM of posts `sx` x `sy` metres, no tile offset, dx = dy = 1.
+extern "C" VGB_API vgb_status vgb_dem_triangulate(const float* h, uint32_t W, uint32_t H, double sx,
+                                                  double sy, float* pos, uint32_t* idx, uint32_t* nt_out) {
+    if (!h || !pos || !idx || !nt_out || W < 2 || H < 2) return VGB_ERR_INVALID_ARGUMENT;
+    vgb::dem_vertices_host(h, W, H, vgb::dem_pose_of(1.0 * sx, 1.0 * sy, 0.0, 0.0, W, H), pos);
+    vgb::dem_faces_host(h, W, H, idx, nt_out);
     return VGB_OK;
 }
 
@@ -368,7 +375,7 @@ bool build_bvh(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t 
         max_depth += md + 1;
     }
 
-    out.nodes.clear(); out.tris.clear();
+    out.nodes.clear(); out.tris.clear(); out.parent.clear();
     out.tris.reserve(12 * (size_t)ntris);
     out.layout = layout;
     out.max_depth = max_depth;
@@ -395,7 +402,12 @@ bool build_bvh(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t 
         };
         struct Item { int64_t ref; uint32_t slot; };
         std::vector<Item> stack;
-        auto alloc = [&]() { uint32_t sl = (uint32_t)(words.size() / 16); words.resize(words.size() + 16, 0u); return sl; };
+        auto alloc = [&]() {
+            uint32_t sl = (uint32_t)(words.size() / 16);
+            words.resize(words.size() + 16, 0u);
+            out.parent.push_back(kNoParent);
+            return sl;
+        };
         auto fbits = [](float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; };
         auto put_child = [&](uint32_t slot, int side, const Box& b, int32_t link) {
             uint32_t* n = &words[16 * (size_t)slot];
@@ -426,6 +438,7 @@ bool build_bvh(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t 
                         put_child(it.slot, side, ch.box, emit_leaf(ch));
                     } else {
                         uint32_t sl = alloc();
+                        out.parent[sl] = (it.slot << 1) | (uint32_t)side;
                         put_child(it.slot, side, ch.box, (int32_t)sl);
                         stack.push_back(Item{cr, sl});
                     }

@@ -15,7 +15,17 @@
 // id is the triangle's index in the caller's index buffer.
 #pragma once
 #include <cstdint>
+#include <limits>
+#include <string>
 #include <vector>
+
+#include "../../include/vgb.h"
+
+#if defined(__CUDACC__)
+#define VGB_HD __host__ __device__
+#else
+#define VGB_HD
+#endif
 
 namespace vgb {
 
@@ -30,7 +40,10 @@ struct BvhHost {
     uint32_t num_nodes = 0;
     uint32_t max_depth = 0;
     float root_lo[3] = {0, 0, 0}, root_hi[3] = {0, 0, 0};
+    // binary layout: per node (parent << 1 | side), kNoParent for the root (bottom-up refits)
+    std::vector<uint32_t> parent;
 };
+constexpr uint32_t kNoParent = 0xFFFFFFFFu;
 
 // Binned-SAH build over the triangles of (positions, indices), emitted in the binary layout or
 // collapsed into the compressed 8-wide layout.  Deterministic for a given input, leaf size and
@@ -58,9 +71,84 @@ int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32
 // device memory; `work` is scratch of dem_work_words / normals_work_words 32-bit words.
 size_t dem_work_words(uint32_t W, uint32_t H);
 size_t normals_work_words(uint32_t nv, uint32_t nt);
-int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, double sx, double sy,
+// DEMProjection's non-OGR mapping (dem_projection.ipp:66-71, 131-141) as FP64 constants:
+//   x = ax * (-half_x + 2 * ((i + xo) * scale_x)),  y = ay * (half_y + 2 * (-(j + yo) * scale_y))
+// with ax = dx * pixelScale[0], xo = xoff / dx, half_x = (Wp - 1) / 2, scale_x = (half_x + 0.5) / Wp
+// for the projection's resolution Wp (and the same in y).
+struct DemPose {
+    double ax, ay, xo, yo, half_x, half_y, scale_x, scale_y;
+};
+inline DemPose dem_pose_of(double ax, double ay, double xo, double yo, uint32_t pw, uint32_t ph) {
+    DemPose p;
+    p.ax = ax; p.ay = ay; p.xo = xo; p.yo = yo;
+    p.half_x = ((double)pw - 1.) / 2.;
+    p.half_y = ((double)ph - 1.) / 2.;
+    p.scale_x = (p.half_x + 0.5) / (double)pw;
+    p.scale_y = (p.half_y + 0.5) / (double)ph;
+    return p;
+}
+inline DemPose dem_pose(const vgb_quipu_projection& pr) {
+    return dem_pose_of(pr.dx * pr.pixel_scale[0], pr.dy * pr.pixel_scale[1], pr.xoff / pr.dx, pr.yoff / pr.dy,
+                       pr.width, pr.height);
+}
+// DEM::makeVertexBuffer positions and imageToIndexBuffer faces on the host (vgb_host.cpp).
+void dem_vertices_host(const float* h, uint32_t W, uint32_t H, const DemPose& pose, float* pos);
+void dem_faces_host(const float* h, uint32_t W, uint32_t H, uint32_t* idx, uint32_t* nt_out);
+int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, const DemPose& pose,
                            float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out);
 int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
                           float* out, uint32_t* work);
+// Refit of the binary BVH after the vertices moved (same triangles): triangle records rewritten
+// from vpos, then every child box recomputed bottom up.  counts: nnodes words of scratch.
+// Returns nonzero on a CUDA error, -2 when an upward walk exceeded its bound.
+int launch_refit(void* stream, int sms, const void* vpos /* float4 */, const uint32_t* idx, uint32_t ntris,
+                 void* tris /* float4 */, uint32_t* nodes, uint32_t nnodes, const uint32_t* parent, uint32_t* counts);
+
+
+// ---- DEM Quipu (vgb_quipu.cpp host side, vgb_mesh.cu device decode)
+// fixedToFloat (image_utils.ipp:509-527): code 0 is +inf, else (max - min) * (code / (m - 1)) + min
+VGB_HD inline float quipu_dequantize(uint32_t code, float m, float mn, float mx) {
+    if (code == 0) {
+#if defined(__CUDA_ARCH__)
+        return __int_as_float(0x7f800000);
+#else
+        return std::numeric_limits<float>::infinity();
+#endif
+    }
+    const float f = (float)code / (m - 1.f);
+    return ((mx - mn) * f) + mn;
+}
+struct ImageRefView {          // an image's pixels in the file
+    uint64_t pos, stored, raw_bytes;
+    uint32_t w, h, elem;
+    bool compressed;
+};
+struct QuipuPlane { float mn, mx; ImageRefView img; };
+struct QuipuPayload {
+    std::string path;
+    ImageRefView heights;
+    uint32_t precision;        // 3 uint8, 4 uint16, 1 float
+    float hmin, hmax;
+    uint32_t albedo_type;      // 0 constant, 1 grey, 2 per band, VGB_QUIPU_NO_ALBEDO
+    uint64_t constant_pos;
+    std::vector<QuipuPlane> planes;
+    vgb_quipu_projection proj;
+};
+vgb_status quipu_lod_payload(const vgb_quipu_dem* q, uint32_t lod, QuipuPayload* out);
+// Row-major pixels of an image (LZ4-decoded, or transposed from the stored column order).
+vgb_status quipu_read_pixels(const std::string& path, const ImageRefView& v, void* out);
+vgb_status quipu_read_constant(const std::string& path, uint64_t pos, uint32_t nbands, float* out);
+void quipu_set_error(const std::string& m);
+// Device decode of one LoD: float heights [H][W] from the stored codes, and per-vertex albedo
+// [H*W][nbands] (alb may be null).  planes: the uint8 albedo planes, one after the other.
+struct QuipuDecode {
+    uint32_t W, H, precision, albedo_type, nplanes, nbands;
+    float hmin, hmax;
+    float pmin[VGB_MAX_BANDS], pmax[VGB_MAX_BANDS];   // per-plane fixed-point range
+    float constant[VGB_MAX_BANDS];                     // constant / default albedo
+    float profile[VGB_MAX_BANDS];                      // grey-plane profile
+};
+int launch_quipu_decode(void* stream, int sms, const QuipuDecode& d, const void* codes, const uint8_t* planes,
+                        float* heights, float* alb);
 
 }  // namespace vgb

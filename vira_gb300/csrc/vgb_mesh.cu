@@ -20,13 +20,14 @@
 #include "vgb_internal.h"
 
 using namespace vgbd;
+using vgb::DemPose;
+using vgb::QuipuDecode;
+using vgb::quipu_dequantize;
 
 namespace {
 
-__global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t H, double sx, double sy,
+__global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t H, DemPose pose,
                                float* __restrict__ pos) {
-    const double half_x = ((double)W - 1.) / 2., half_y = ((double)H - 1.) / 2.;
-    const double scale_x = (half_x + 0.5) / (double)W, scale_y = (half_y + 0.5) / (double)H;
     const size_t n = (size_t)W * H;
     for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)(v % W), j = (uint32_t)(v / W);
@@ -35,10 +36,38 @@ __global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t
             pos[3 * v] = pos[3 * v + 1] = pos[3 * v + 2] = __int_as_float(0x7f800000);
             continue;
         }
-        const double xs = (double)i * scale_x, ys = -(double)j * scale_y;
-        pos[3 * v] = (float)((1.0 * sx) * (-half_x + 2. * xs));
-        pos[3 * v + 1] = (float)((1.0 * sy) * (half_y + 2. * ys));
+        const double xs = ((double)i + pose.xo) * pose.scale_x, ys = -((double)j + pose.yo) * pose.scale_y;
+        pos[3 * v] = (float)(pose.ax * (-pose.half_x + 2. * xs));
+        pos[3 * v + 1] = (float)(pose.ay * (pose.half_y + 2. * ys));
         pos[3 * v + 2] = z;
+    }
+}
+
+// Quipu LoD decode: heights from their stored codes (fixedToFloat, or FP32 as stored) and the
+// per-vertex albedo DEM::makeVertexBuffer assigns (dem.ipp:191-200; Vertex's default 1 where
+// the height is not finite), with readBuffers' grey-plane profile (dem_quipu.ipp:184-194).
+template <typename T>
+__global__ void k_quipu_decode(QuipuDecode d, const T* __restrict__ codes, const uint8_t* __restrict__ planes,
+                               float* __restrict__ h, float* __restrict__ alb) {
+    const size_t n = (size_t)d.W * d.H;
+    const float m = sizeof(T) == 1 ? 255.f : 65535.f;
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+        float z;
+        if constexpr (sizeof(T) == 4) z = codes[v];
+        else z = quipu_dequantize((uint32_t)codes[v], m, d.hmin, d.hmax);
+        h[v] = z;
+        if (!alb) continue;
+        float* a = alb + v * d.nbands;
+        const bool valid = !(isinf(z) || isnan(z));
+        if (!valid || d.albedo_type == 0 || d.albedo_type == VGB_QUIPU_NO_ALBEDO) {
+            for (uint32_t b = 0; b < d.nbands; ++b) a[b] = valid ? d.constant[b] : 1.f;
+        } else if (d.albedo_type == 1) {
+            const float g = quipu_dequantize(planes[v], 255.f, d.pmin[0], d.pmax[0]);
+            for (uint32_t b = 0; b < d.nbands; ++b) a[b] = d.profile[b] * g;
+        } else {
+            for (uint32_t b = 0; b < d.nbands; ++b)
+                a[b] = quipu_dequantize(planes[b * n + v], 255.f, d.pmin[b], d.pmax[b]);
+        }
     }
 }
 
@@ -187,14 +216,24 @@ size_t scan_temp_words(size_t n) {
     return words + 64;
 }
 
-int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, double sx, double sy,
+int launch_quipu_decode(void* stream, int sms, const QuipuDecode& d, const void* codes, const uint8_t* planes,
+                        float* heights, float* alb) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const int g = grid((size_t)d.W * d.H, sms);
+    if (d.precision == 3) k_quipu_decode<uint8_t><<<g, 256, 0, s>>>(d, (const uint8_t*)codes, planes, heights, alb);
+    else if (d.precision == 4) k_quipu_decode<uint16_t><<<g, 256, 0, s>>>(d, (const uint16_t*)codes, planes, heights, alb);
+    else k_quipu_decode<float><<<g, 256, 0, s>>>(d, (const float*)codes, planes, heights, alb);
+    return (int)cudaGetLastError();
+}
+
+int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, const DemPose& pose,
                            float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out) {
     cudaStream_t s = (cudaStream_t)stream;
     const size_t nq = (size_t)(W - 1) * (H - 1);
     uint32_t* cnt = work;
     uint32_t* off = work + nq + 1;
     uint32_t* tmp = off + nq + 1;
-    k_dem_vertices<<<grid((size_t)W * H, sms), 256, 0, s>>>(h, W, H, sx, sy, pos);
+    k_dem_vertices<<<grid((size_t)W * H, sms), 256, 0, s>>>(h, W, H, pose, pos);
     k_dem_quad_counts<<<grid(nq, sms), 256, 0, s>>>(h, W, H, cnt);
     cudaMemsetAsync(cnt + nq, 0, sizeof(uint32_t), s);
     scan(s, cnt, off, nq + 1, tmp);  // off[nq] = total triangles
@@ -241,6 +280,99 @@ int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, 
     k_vertex_normals<<<grid(nv, sms), 256, 0, s>>>(fn, off, cnt, list, nv, out);
     cudaError_t e = cudaStreamSynchronize(s);
     return e != cudaSuccess ? (int)e : (int)cudaGetLastError();
+}
+
+}  // namespace vgb
+
+// ---------------------------------------------------------------- BVH refit
+namespace {
+
+__global__ void k_refit_tris(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t ntris,
+                             float4* __restrict__ tris) {
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < ntris; r += (size_t)gridDim.x * blockDim.x) {
+        const float idbits = tris[3 * r].w;
+        const uint32_t t = __float_as_uint(idbits);
+        const float4 a = vpos[idx[3 * (size_t)t]], b = vpos[idx[3 * (size_t)t + 1]], c = vpos[idx[3 * (size_t)t + 2]];
+        tris[3 * r] = make_float4(a.x, a.y, a.z, idbits);
+        tris[3 * r + 1] = make_float4(b.x, b.y, b.z, 0.f);
+        tris[3 * r + 2] = make_float4(c.x, c.y, c.z, 0.f);
+    }
+}
+
+struct RBox { float lx, hx, ly, hy, lz, hz; };
+
+__device__ __forceinline__ void put_box(uint32_t* nodes, uint32_t node, int side, const RBox& b) {
+    uint32_t* n = nodes + 16 * (size_t)node;
+    const int o = side ? 4 : 0;
+    n[o + 0] = __float_as_uint(b.lx); n[o + 1] = __float_as_uint(b.hx);
+    n[o + 2] = __float_as_uint(b.ly); n[o + 3] = __float_as_uint(b.hy);
+    n[8 + 2 * side] = __float_as_uint(b.lz); n[9 + 2 * side] = __float_as_uint(b.hz);
+}
+
+__device__ __forceinline__ RBox get_box(const uint32_t* nodes, uint32_t node, int side) {
+    const uint32_t* n = nodes + 16 * (size_t)node;
+    const int o = side ? 4 : 0;
+    // the other side was written by another thread: read through L2
+    return RBox{__uint_as_float(__ldcg(n + o)), __uint_as_float(__ldcg(n + o + 1)), __uint_as_float(__ldcg(n + o + 2)),
+                __uint_as_float(__ldcg(n + o + 3)), __uint_as_float(__ldcg(n + 8 + 2 * side)),
+                __uint_as_float(__ldcg(n + 9 + 2 * side))};
+}
+
+// One thread per (node, side) whose child is a leaf: the leaf's box from its triangle records,
+// then up the tree: the second of a node's two sides to finish writes that node's box into its
+// parent.  Walks are bounded by `cap` steps (the tree depth); a walk that would exceed it flags.
+__global__ void k_refit_nodes(const float4* __restrict__ tris, uint32_t* nodes, uint32_t nnodes,
+                              const uint32_t* __restrict__ parent, uint32_t* counts, uint32_t cap, uint32_t* flag) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < 2 * (size_t)nnodes;
+         q += (size_t)gridDim.x * blockDim.x) {
+        uint32_t node = (uint32_t)(q >> 1);
+        const int side = (int)(q & 1);
+        const int32_t link = (int32_t)nodes[16 * (size_t)node + 12 + side];
+        if (link >= 0) continue;
+        const uint32_t x = ~(uint32_t)link;
+        const uint32_t start = x >> 3, cnt = (x & 7u) + 1u;
+        RBox b{INFINITY, -INFINITY, INFINITY, -INFINITY, INFINITY, -INFINITY};
+        for (uint32_t k = 0; k < cnt; ++k)
+            for (int v = 0; v < 3; ++v) {
+                const float4 p = tris[3 * (size_t)(start + k) + v];
+                b.lx = fminf(b.lx, p.x); b.hx = fmaxf(b.hx, p.x);
+                b.ly = fminf(b.ly, p.y); b.hy = fmaxf(b.hy, p.y);
+                b.lz = fminf(b.lz, p.z); b.hz = fmaxf(b.hz, p.z);
+            }
+        put_box(nodes, node, side, b);
+        for (uint32_t step = 0;; ++step) {
+            __threadfence();
+            if (atomicAdd(&counts[node], 1u) == 0u) break;  // the other side is not done yet
+            __threadfence();
+            if (step >= cap) { atomicOr(flag, 1u); break; }
+            const RBox a = get_box(nodes, node, 0), c = get_box(nodes, node, 1);
+            const RBox u{fminf(a.lx, c.lx), fmaxf(a.hx, c.hx), fminf(a.ly, c.ly),
+                         fmaxf(a.hy, c.hy), fminf(a.lz, c.lz), fmaxf(a.hz, c.hz)};
+            const uint32_t pr = parent[node];
+            if (pr == vgb::kNoParent) break;
+            node = pr >> 1;
+            put_box(nodes, node, (int)(pr & 1u), u);
+        }
+    }
+}
+
+}  // namespace
+
+namespace vgb {
+
+int launch_refit(void* stream, int sms, const void* vpos, const uint32_t* idx, uint32_t ntris, void* tris,
+                 uint32_t* nodes, uint32_t nnodes, const uint32_t* parent, uint32_t* counts) {
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* flag = counts + nnodes;
+    cudaMemsetAsync(counts, 0, ((size_t)nnodes + 1) * sizeof(uint32_t), s);
+    k_refit_tris<<<grid(ntris, sms), 256, 0, s>>>((const float4*)vpos, idx, ntris, (float4*)tris);
+    k_refit_nodes<<<grid(2 * (size_t)nnodes, sms), 256, 0, s>>>((const float4*)tris, nodes, nnodes, parent, counts,
+                                                                 4096u, flag);
+    uint32_t bad = 0;
+    cudaMemcpyAsync(&bad, flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int)e;
+    return bad ? -2 : (int)cudaGetLastError();
 }
 
 }  // namespace vgb

@@ -573,6 +573,43 @@ class Scene:
         capi.check(lib.vgb_bvh_build(ctx, C.byref(self.bvh_options)), ctx, "bvh_build")
         self._dirty = False
 
+    def update_positions(self, mesh_index: int, positions) -> None:
+        """Moves the vertices of mesh `mesh_index` (same triangles).  When the uploaded scene is
+        that mesh alone, untransformed, the device vertices are replaced and the BVH refitted
+        (vgb_scene_update_positions); otherwise the scene is flattened and rebuilt."""
+        mesh = self.meshes[mesh_index]
+        p = np.ascontiguousarray(positions, np.float32)
+        if p.shape != mesh.positions.shape:
+            raise ValueError("update_positions: shape differs from the mesh's vertices")
+        mesh.positions = p.copy()
+        mesh.normals = None
+        vis = [inst for inst in self.instances if inst.visible]
+        in_place = (not self._dirty and self._ctx is not None and len(vis) == 1 and vis[0].mesh == mesh_index
+                    and np.array_equal(vis[0].rotation, np.eye(3)) and vis[0].scale == 1.0
+                    and not vis[0].position.any() and not self.origin.any())
+        if not in_place:
+            self._dirty = True
+            self.build_tlas()
+            return
+        ctx = self._ctx
+        capi.check(capi.load().vgb_scene_update_positions(ctx, capi.ptr(mesh.positions), None, 0), ctx,
+                   "scene_update_positions")
+        self._flat_stale = True
+
+    @property
+    def flat(self):
+        """The flattened scene arrays of the last upload (None before the first); recomputed on
+        access after vertices were moved in place."""
+        if self._flat is not None and self._flat_stale:
+            self._flat_stale = False
+            self.flatten()
+        return self._flat
+
+    @flat.setter
+    def flat(self, value):
+        self._flat = value
+        self._flat_stale = False
+
     def c_lights(self):
         arr = (capi.Light * max(1, len(self.lights)))()
         for k, L in enumerate(self.lights):
