@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint line item")
     ap.add_argument("--no-asteroid", action="store_true", help="skip the fused batched-adjoint asteroid line item")
     ap.add_argument("--no-after-film", action="store_true", help="skip the denoiser / PSF / sensor line item")
+    ap.add_argument("--no-quipu", action="store_true", help="skip the DEM Quipu ingestion line item")
     return ap.parse_args()
 
 
@@ -391,6 +392,9 @@ def run_ours(args, p, rank, world, local_rank):
     after_film = None
     if not args.no_after_film and p["kind"] == "path_traced" and rank == 0:
         after_film = after_film_item(torch, dev, scene, cam_id, peak)
+    quipu = None
+    if not args.no_quipu and p["kind"] == "path_traced" and rank == 0:
+        quipu = quipu_item(torch, dev, peak, cpu=not args.no_cpu_baseline)
     direct = None
     if not args.no_direct and p["kind"] == "path_traced" and rank == 0:
         direct = plain_direct_item(torch, dev, args.layout, 0.0 if args.no_cpu_baseline else 5.0)
@@ -458,6 +462,8 @@ def run_ours(args, p, rank, world, local_rank):
             line["batched_adjoint"] = asteroid
         if after_film is not None:
             line["after_film"] = after_film
+        if quipu is not None:
+            line["quipu_ingest"] = quipu
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -596,6 +602,84 @@ def adjoint_item(torch, dev, layout=2, reps=2):
            "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
     scene.close()
     return out
+
+
+def quipu_item(torch, dev, hbm_peak, reps=3, cpu=True):
+    """DEM ingestion from a Quipu file: a 4097^2 crater DEM at 1 m posts (uint16 heights, grey
+    uint8 albedo, LZ4 blocks) with a 1025^2 LoD, read into a device mesh (positions, indices,
+    8-band vertex albedo, vertex normals) by vgb_quipu_read_mesh -- DEMQuipu::readBuffers and
+    Mesh::init -- against the oracle's CPU restatement of the same steps on the same file."""
+    import shutil
+    import tempfile
+
+    from vira_gb300 import capi, synthetic
+    from vira_gb300 import quipu as VQ
+    from vira_gb300.scene import _mesh_context
+
+    n, nb = 4097, 8
+    z = synthetic.fbm_heights(n, 0.8, seed=21, lo=-200.0, hi=200.0)
+    z = np.ascontiguousarray(synthetic.add_crater_field(z, 1.0, seed=22, dmin=20, dmax=2000), np.float32)
+    alb = synthetic.lognormal_albedo(n, 0.12, 0.3, seed=23)
+    dem = VQ.DEM(z, VQ.DEMProjection(n, n, (1.0, 1.0)), alb, VQ.FLOAT_IMAGE_ALBEDO)
+    tmp = Path(tempfile.mkdtemp())
+    try:
+        t0 = time.perf_counter()
+        VQ.DEMQuipu.write(tmp / "dem", [dem, dem.downsample(4)], options=VQ.DEMQuipuWriterOptions(compress=True))
+        write_s = time.perf_counter() - t0
+        path = tmp / "dem.qld"
+        fbytes = path.stat().st_size
+        q = VQ.DEMQuipu(path, nbands=nb)
+        q.read_lod_mesh(0, gpu=dev.index, nbands=nb, device_arrays=True)      # warm-up, pinned staging
+        lib = capi.load()
+        ctx = _mesh_context(dev.index)
+        e2e, dev_ms = [], []
+        for _ in range(reps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            out = q.read_lod_mesh(0, gpu=dev.index, nbands=nb, device_arrays=True)
+            torch.cuda.synchronize(dev)
+            e2e.append(time.perf_counter() - t0)
+            st = capi.Stats()
+            capi.check(lib.vgb_get_stats(ctx, C.byref(st)), ctx, "stats")
+            dev_ms.append(st.ms_last)
+            del out
+        t0 = time.perf_counter()
+        q.read_heights(0)
+        host_decode_s = time.perf_counter() - t0
+        info = q.lods[0]
+        posts, quads = n * n, (n - 1) * (n - 1)
+        # unique bytes of the device phase: codes 2 + albedo code 1 in; heights 4 (written, read
+        # back), positions 12, albedo 4 nb, normals 12 per post and 2 x 12 index bytes per quad out
+        uniq = posts * (2 + 1 + 4 + 12 + 4 * nb + 12) + quads * 24
+        best_dev = min(dev_ms)
+        line = {"workload": f"quipu_dem{n}_u16_lz4_grey_albedo_{nb}band_2lods",
+                "file_mb": fbytes / 1e6, "precision": VQ.PRECISION[info.precision], "write_s": write_s,
+                "e2e_ms": 1e3 * min(e2e), "device_ms": best_dev, "host_read_decode_ms": 1e3 * host_decode_s,
+                "mposts_per_s_e2e": posts / min(e2e) / 1e6,
+                "device_unique_gb_s": uniq / (best_dev / 1e3) / 1e9,
+                "device_frac_of_hbm": uniq / (best_dev / 1e3) / 1e9 / hbm_peak,
+                "timing": "wall clock around the blocking call (file in page cache) / CUDA events around the "
+                          "device phase, best of %d" % reps}
+        if cpu:
+            from oracle import oracle
+            from oracle import quipu as Q
+
+            t0 = time.perf_counter()
+            o = Q.read(path)
+            L = o.lods[0]
+            h = Q.heights(L)
+            pos = Q.vertex_positions(h, L.projection)
+            Q.vertex_albedo(L, h, nb)
+            idx = Q.index_buffer(h)
+            oracle.compute_normals(pos, idx)
+            cs = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": posts / cs / 1e6, "unit": "Mposts/s", "cores": 1, "kind": "port",
+                                    "sample": f"the whole file ({cs:.1f} s): oracle LZ4 decode, fixed point, "
+                                              "makeVertexBuffer, imageToIndexBuffer, calculateNormals"}
+        q.close()
+        return line
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def after_film_item(torch, dev, scene, cam_id, hbm_peak, reps=5):

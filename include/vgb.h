@@ -163,7 +163,7 @@ typedef struct vgb_stats {
     uint32_t tri_record_bytes; /* bytes per triangle record */
     uint32_t kernel_launches;  /* kernels launched by the last render */
     uint32_t device_error;     /* last device error word (0 = none) */
-    float ms_last;             /* device time of the last render (CUDA events) */
+    float ms_last;             /* device time of the last render, or of the device phase of the last vgb_quipu_read_mesh (CUDA events) */
     /* profiling mode only (vgb_set_profiling): device time and launches per kernel family:
      * closest-hit traversal, shading, shadow traversal, film */
     float ms_trace, ms_shade, ms_shadow, ms_film;
@@ -486,6 +486,10 @@ VGB_API uint32_t vgb_quipu_select_lod(const vgb_quipu_dem* q, double required_gs
 /* readDEMHeights + fixedToFloat (quipu_io.ipp:601-626, image_utils.ipp:509-527) on the host:
  * [H][W] floats, +inf where the stored code is 0. */
 VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float* heights);
+/* The LoD's albedo as the DEM holds it (readAlbedos_f / readAlbedos, quipu_io.ipp:643-702), on
+ * the host: constant: nbands floats; grey: [H][W]; per band: [H][W][nbands] (nbands must equal
+ * the stored channels).  VGB_ERR_NOT_READY when the file stores none. */
+VGB_API vgb_status vgb_quipu_read_albedo(vgb_quipu_dem* q, uint32_t lod, uint32_t nbands, float* albedo);
 /* DEMQuipu::readBuffers (dem_quipu.ipp:124-221) -> DEM::makeVertexBuffer / makeIndexBuffer
  * (dem.ipp:152-211) on the device: positions [H*W][3], per-vertex albedo [H*W][nbands] (NULL to
  * skip), vertex normals [H*W][3] (NULL to skip; Mesh::calculateNormals), indices [2(W-1)(H-1)][3]

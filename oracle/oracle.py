@@ -58,6 +58,8 @@ def load():
                                      C.c_float]),
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
                                                C.c_int]),
+        "oracle_lz4_decompress": (C.c_int64, [P, C.c_uint64, P, C.c_uint64]),
+        "oracle_normal_cone": (C.c_int, [P, C.c_uint64, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -26,6 +26,9 @@
 //   blackBodyRadiance        include/implementation/spectral_data.ipp:613-629, math.ipp:34-59
 //   ViraBLAS build/traverse  include/implementation/rendering/acceleration/vira_blas.ipp:43-254
 //   Triangle::intersect      include/implementation/geometry/triangle.ipp:35-87
+//   LZ4 block decoding and the DEM Quipu normal cone (quipu_io.ipp:216-231,
+//                            dem_quipu.ipp:256-270); the Quipu format itself is restated in
+//                            oracle/quipu.py
 //
 // Two things cannot be restated and are replaced, identically in oracle and product:
 //   * Embree's rtcIntersect1 arithmetic (third party, not vendored).  The oracle uses the
@@ -1535,5 +1538,72 @@ OAPI int oracle_psf(const float* in, uint32_t width, uint32_t height, uint32_t n
                     }
                 out[b * P + (size_t)y * W + x] = sum;
             }
+    return 0;
+}
+
+// ---------------------------------------------------------------- DEM Quipu helpers
+// LZ4 block decompression as LZ4_decompress_safe (lz4 1.9.4, the version the reference pins in
+// dependencies/vcpkg.json) performs it for quipu::decompressData (quipu_io.ipp:216-231),
+// restated from the published LZ4 block format: token, literal-length run, literals, 2-byte
+// little-endian offset, match-length run; the last sequence carries literals only.  Copies
+// byte by byte.  Returns the decoded size or -1.
+OAPI int64_t oracle_lz4_decompress(const uint8_t* in, uint64_t n, uint8_t* out, uint64_t cap) {
+    uint64_t i = 0, o = 0;
+    if (n == 0) return -1;
+    while (i < n) {
+        const uint8_t token = in[i++];
+        uint64_t run = token >> 4;
+        if (run == 15) {
+            for (;;) {
+                if (i >= n) return -1;
+                const uint8_t b = in[i++];
+                run += b;
+                if (b != 255) break;
+            }
+        }
+        for (uint64_t k = 0; k < run; ++k) {
+            if (i >= n || o >= cap) return -1;
+            out[o++] = in[i++];
+        }
+        if (i == n) return (int64_t)o;
+        if (i + 2 > n) return -1;
+        const uint64_t back = (uint64_t)in[i] + 256u * (uint64_t)in[i + 1];
+        i += 2;
+        if (back == 0 || back > o) return -1;
+        uint64_t len = token & 15;
+        if (len == 15) {
+            for (;;) {
+                if (i >= n) return -1;
+                const uint8_t b = in[i++];
+                len += b;
+                if (b != 255) break;
+            }
+        }
+        len += 4;
+        for (uint64_t k = 0; k < len; ++k) {
+            if (o >= cap) return -1;
+            out[o] = out[o - back];
+            ++o;
+        }
+    }
+    return -1;  // ended right after a match
+}
+
+// The normal cone DEMQuipu::write stores (dem_quipu.ipp:256-270): the glm-normalised sum of the
+// coarsest LoD's vertex normals, and the largest std::acos(dot(n, mean)) in FP32 (std::max,
+// so NaN angles drop out).  out = {mean.x, mean.y, mean.z, angle}.
+OAPI int oracle_normal_cone(const float* normals, uint64_t nv, float* out) {
+    float s[3] = {0.f, 0.f, 0.f};
+    for (uint64_t v = 0; v < nv; ++v)
+        for (int k = 0; k < 3; ++k) s[k] += normals[3 * v + k];
+    const float dd = (s[0] * s[0] + s[1] * s[1]) + s[2] * s[2];
+    const float inv = 1.0f / std::sqrt(dd);
+    const float m[3] = {s[0] * inv, s[1] * inv, s[2] * inv};
+    float cone = 0.f;
+    for (uint64_t v = 0; v < nv; ++v) {
+        const float d = (normals[3 * v] * m[0] + normals[3 * v + 1] * m[1]) + normals[3 * v + 2] * m[2];
+        cone = std::max(cone, std::acos(d));
+    }
+    out[0] = m[0]; out[1] = m[1]; out[2] = m[2]; out[3] = cone;
     return 0;
 }

@@ -186,6 +186,7 @@ SIGNATURES = {
     "vgb_quipu_get_lod": (C.c_int, [_P, _U32, C.POINTER(QuipuLodInfo)]),
     "vgb_quipu_select_lod": (_U32, [_P, C.c_double]),
     "vgb_quipu_read_heights": (C.c_int, [_P, _U32, _P]),
+    "vgb_quipu_read_albedo": (C.c_int, [_P, _U32, _U32, _P]),
     "vgb_quipu_read_mesh": (C.c_int, [_P, _P, _U32, C.POINTER(QuipuReadOptions), _P, _P, _P, _P, C.POINTER(_U32),
                                       C.c_int]),
     "vgb_quipu_write": (C.c_int, [C.c_char_p, _P, _U32, C.POINTER(C.c_double), C.POINTER(C.c_double),

@@ -1758,6 +1758,7 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
     }
     CK(cudaMemcpyAsync(d_codes, hp, pl.heights.raw_bytes, cudaMemcpyHostToDevice, ctx->stream));
     if (plane_bytes) CK(cudaMemcpyAsync(d_planes, hp + code_bytes, plane_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
     CK((cudaError_t)vgb::launch_quipu_decode(ctx->stream, ctx->num_sms, d, d_codes, d_planes, d_h, nb ? a : nullptr));
     uint32_t nt = 0;
     CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, d_h, W, H, vgb::dem_pose(pl.proj), p, ix,
@@ -1766,6 +1767,7 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
         const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ix, nt, nr, d_work);
         CK((cudaError_t)rc);
     }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!on_device) {
         CK(cudaMemcpyAsync(positions, p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
         if (nb) CK(cudaMemcpyAsync(vert_albedo, a, (size_t)nb * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1773,6 +1775,9 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
         CK(cudaMemcpyAsync(indices, ix, 3 * (size_t)nt * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.ms_last = ms;   // device decode + triangulation + normals
     *ntris = nt;
     return VGB_OK;
 }

@@ -168,6 +168,13 @@ struct File {
     bool read(void* p, size_t n) { ok = ok && std::fread(p, 1, n, f) == n; return ok; }
     template <typename T> T get() { T v{}; read(&v, sizeof(T)); return v; }
     bool skip(uint64_t n) { ok = ok && fseeko(f, (off_t)n, SEEK_CUR) == 0; return ok; }
+    uint64_t size() {
+        const off_t here = ftello(f);
+        fseeko(f, 0, SEEK_END);
+        const uint64_t n = (uint64_t)ftello(f);
+        fseeko(f, here, SEEK_SET);
+        return n;
+    }
 };
 
 enum : uint16_t { kFloat = 1, kDouble = 2, kU8 = 3, kU16 = 4, kDemPyramid = 2002 };
@@ -214,7 +221,8 @@ bool read_image_ref(File& f, ImageRef& r) {
         r.stored = r.raw_bytes;
         r.pos = f.tell();
     }
-    return f.ok && f.skip(r.stored);
+    // the pixels must lie inside the file
+    return f.ok && r.stored <= f.size() && r.pos <= f.size() - r.stored && f.skip(r.stored);
 }
 
 }  // namespace
@@ -458,6 +466,29 @@ VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float*
     } else {
         const uint16_t* r = (const uint16_t*)raw.data();
         for (size_t k = 0; k < n; ++k) heights[k] = vgb::quipu_dequantize(r[k], 65535.f, mn, mx);
+    }
+    return VGB_OK;
+}
+
+VGB_API vgb_status vgb_quipu_read_albedo(vgb_quipu_dem* q, uint32_t lod, uint32_t nbands, float* albedo) {
+    if (!q || !albedo) return qfail("quipu_read_albedo: null argument");
+    vgb::QuipuPayload pl;
+    vgb_status s = vgb::quipu_lod_payload(q, lod, &pl);
+    if (s != VGB_OK) return s;
+    if (pl.albedo_type == VGB_QUIPU_NO_ALBEDO) return qfail("quipu_read_albedo: the file stores no albedo", VGB_ERR_NOT_READY);
+    if (pl.albedo_type == 0) {
+        if (nbands == 0 || nbands > VGB_MAX_BANDS) return qfail("quipu_read_albedo: nbands must be 1..8");
+        return vgb::quipu_read_constant(pl.path, pl.constant_pos, nbands, albedo);
+    }
+    if (pl.albedo_type == 2 && pl.planes.size() != nbands)
+        return qfail("Quipu file uses a Spectral albedo with " + std::to_string(pl.planes.size()) +
+                     " channels, while the reader has " + std::to_string(nbands) + " bands");
+    const size_t n = (size_t)pl.heights.w * pl.heights.h, nc = pl.planes.size();
+    std::vector<uint8_t> codes(n);
+    for (size_t c = 0; c < nc; ++c) {
+        if ((s = vgb::quipu_read_pixels(pl.path, pl.planes[c].img, codes.data())) != VGB_OK) return s;
+        for (size_t k = 0; k < n; ++k)
+            albedo[k * nc + c] = vgb::quipu_dequantize(codes[k], 255.f, pl.planes[c].mn, pl.planes[c].mx);
     }
     return VGB_OK;
 }
