@@ -1736,24 +1736,26 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
     }
     // device scratch (floats): codes | planes | heights | triangulation work | normals work |
     // output staging when the caller's arrays are on the host
+    // every section starts on a 16-byte boundary (4 floats)
+    auto al4 = [](size_t f) { return (f + 3) & ~(size_t)3; };
     const size_t f_codes = code_bytes / 4, f_planes = ((plane_bytes + 15) & ~(size_t)15) / 4;
-    const size_t f_work = std::max(vgb::dem_work_words(W, H), normals ? vgb::normals_work_words((uint32_t)nv, (uint32_t)(2 * nq)) : 0);
-    const size_t f_out = on_device ? 0 : 3 * nv + (size_t)nb * nv + (normals ? 3 * nv : 0) + 6 * nq;
+    const size_t f_work = al4(vgb::dem_work_words(W, H));
+    const size_t f_out = on_device ? 0 : al4(3 * nv) + al4((size_t)nb * nv) + (normals ? al4(3 * nv) : 0) + 6 * nq;
     vgb_status s;
-    if ((s = ensure_dn_scratch(ctx, f_codes + f_planes + nv + f_work + f_out)) != VGB_OK) return s;
+    if ((s = ensure_dn_scratch(ctx, f_codes + f_planes + al4(nv) + f_work + f_out)) != VGB_OK) return s;
     float* cur = ctx->d_dn;
     void* d_codes = cur; cur += f_codes;
     uint8_t* d_planes = (uint8_t*)cur; cur += f_planes;
-    float* d_h = cur; cur += nv;
+    float* d_h = cur; cur += al4(nv);
     uint32_t* d_work = (uint32_t*)cur; cur += f_work;
     float* p = positions;
     float* a = vert_albedo;
     float* nr = normals;
     uint32_t* ix = indices;
     if (!on_device) {
-        p = cur; cur += 3 * nv;
-        if (nb) { a = cur; cur += (size_t)nb * nv; }
-        if (normals) { nr = cur; cur += 3 * nv; }
+        p = cur; cur += al4(3 * nv);
+        if (nb) { a = cur; cur += al4((size_t)nb * nv); }
+        if (normals) { nr = cur; cur += al4(3 * nv); }
         ix = (uint32_t*)cur;
     }
     CK(cudaMemcpyAsync(d_codes, hp, pl.heights.raw_bytes, cudaMemcpyHostToDevice, ctx->stream));
@@ -1761,12 +1763,9 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     CK((cudaError_t)vgb::launch_quipu_decode(ctx->stream, ctx->num_sms, d, d_codes, d_planes, d_h, nb ? a : nullptr));
     uint32_t nt = 0;
+    // normals from the grid's structure (the same sums launch_vertex_normals forms on these arrays)
     CK((cudaError_t)vgb::launch_dem_triangulate(ctx->stream, ctx->num_sms, d_h, W, H, vgb::dem_pose(pl.proj), p, ix,
-                                                d_work, &nt));
-    if (normals) {
-        const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ix, nt, nr, d_work);
-        CK((cudaError_t)rc);
-    }
+                                                d_work, &nt, normals ? nr : nullptr));
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!on_device) {
         CK(cudaMemcpyAsync(positions, p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));

@@ -94,8 +94,9 @@ inline DemPose dem_pose(const vgb_quipu_projection& pr) {
 // DEM::makeVertexBuffer positions and imageToIndexBuffer faces on the host (vgb_host.cpp).
 void dem_vertices_host(const float* h, uint32_t W, uint32_t H, const DemPose& pose, float* pos);
 void dem_faces_host(const float* h, uint32_t W, uint32_t H, uint32_t* idx, uint32_t* nt_out);
+// nrm (optional): vertex normals of the grid's mesh, equal to launch_vertex_normals on its arrays.
 int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, const DemPose& pose,
-                           float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out);
+                           float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out, float* nrm = nullptr);
 int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
                           float* out, uint32_t* work);
 // Refit of the binary BVH after the vertices moved (same triangles): triangle records rewritten

@@ -26,20 +26,69 @@ using vgb::quipu_dequantize;
 
 namespace {
 
-__global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t H, DemPose pose,
-                               float* __restrict__ pos) {
+// The grid's x per column and y per row (FP64, then FP32): a vertex's position is
+// (xs[i], ys[j], h) -- each coordinate of DEMProjection::transformToWorld depends on one index.
+__global__ void k_dem_axes(uint32_t W, uint32_t H, DemPose pose, float* __restrict__ xs, float* __restrict__ ys) {
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < (size_t)W + H; k += (size_t)gridDim.x * blockDim.x) {
+        if (k < W) {
+            const double s = ((double)k + pose.xo) * pose.scale_x;
+            xs[k] = (float)(pose.ax * (-pose.half_x + 2. * s));
+        } else {
+            const double s = -((double)(k - W) + pose.yo) * pose.scale_y;
+            ys[k - W] = (float)(pose.ay * (pose.half_y + 2. * s));
+        }
+    }
+}
+
+__device__ __forceinline__ F3 dem_point(const float* __restrict__ h, const float* __restrict__ xs,
+                                        const float* __restrict__ ys, uint32_t W, uint32_t i, uint32_t j) {
+    const float z = h[(size_t)j * W + i];
+    if (isinf(z) || isnan(z)) {
+        const float inf = __int_as_float(0x7f800000);
+        return F3{inf, inf, inf};
+    }
+    return F3{xs[i], ys[j], z};
+}
+
+// Positions, and with NORMALS the vertex normals Mesh::calculateNormals gives on this grid's
+// index buffer: the faces around vertex (i, j) in index-buffer order are
+//   quad (i-1, j-1) t1, quad (i-1, j) t0 and t1, quad (i, j-1) t0 and t1, quad (i, j) t0
+// (quads ordered i outer, j inner; t0 = {a, b, c}, t1 = {b, a, d}); a face exists when none of
+// its heights is infinite, contributes when no corner's x is infinite and its normal is not
+// NaN, and the contributions are summed in that order -- the general path's sum, bit for bit.
+template <bool NORMALS>
+__global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t H, const float* __restrict__ xs,
+                               const float* __restrict__ ys, float* __restrict__ pos, float* __restrict__ nrm) {
     const size_t n = (size_t)W * H;
     for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)(v % W), j = (uint32_t)(v / W);
-        const float z = h[v];
-        if (isinf(z) || isnan(z)) {
-            pos[3 * v] = pos[3 * v + 1] = pos[3 * v + 2] = __int_as_float(0x7f800000);
-            continue;
+        const F3 p = dem_point(h, xs, ys, W, i, j);
+        pos[3 * v] = p.x; pos[3 * v + 1] = p.y; pos[3 * v + 2] = p.z;
+        if constexpr (NORMALS) {
+            F3 acc{0.f, 0.f, 0.f};
+            auto face = [&](uint32_t i0, uint32_t j0, uint32_t i1, uint32_t j1, uint32_t i2, uint32_t j2) {
+                if (isinf(h[(size_t)j0 * W + i0]) || isinf(h[(size_t)j1 * W + i1]) || isinf(h[(size_t)j2 * W + i2]))
+                    return;  // not in the index buffer
+                const F3 p0 = dem_point(h, xs, ys, W, i0, j0), p1 = dem_point(h, xs, ys, W, i1, j1),
+                         p2 = dem_point(h, xs, ys, W, i2, j2);
+                if (isinf(p0.x) || isinf(p1.x) || isinf(p2.x)) return;
+                const F3 f = normalize(cross(p1 - p0, p2 - p0));
+                if (isnan(f.x) || isnan(f.y) || isnan(f.z)) return;
+                acc = acc + f;
+            };
+            if (i >= 1 && j >= 1) face(i, j - 1, i - 1, j, i, j);                       // quad (i-1, j-1) t1
+            if (i >= 1 && j + 1 < H) {
+                face(i - 1, j + 1, i, j, i - 1, j);                                     // quad (i-1, j) t0
+                face(i, j, i - 1, j + 1, i, j + 1);                                     //               t1
+            }
+            if (i + 1 < W && j >= 1) {
+                face(i, j, i + 1, j - 1, i, j - 1);                                     // quad (i, j-1) t0
+                face(i + 1, j - 1, i, j, i + 1, j);                                     //               t1
+            }
+            if (i + 1 < W && j + 1 < H) face(i, j + 1, i + 1, j, i, j);                 // quad (i, j) t0
+            if (sqrtf(dot(acc, acc)) != 0.f) acc = normalize(acc);
+            nrm[3 * v] = acc.x; nrm[3 * v + 1] = acc.y; nrm[3 * v + 2] = acc.z;
         }
-        const double xs = ((double)i + pose.xo) * pose.scale_x, ys = -((double)j + pose.yo) * pose.scale_y;
-        pos[3 * v] = (float)(pose.ax * (-pose.half_x + 2. * xs));
-        pos[3 * v + 1] = (float)(pose.ay * (pose.half_y + 2. * ys));
-        pos[3 * v + 2] = z;
     }
 }
 
@@ -48,7 +97,7 @@ __global__ void k_dem_vertices(const float* __restrict__ h, uint32_t W, uint32_t
 // the height is not finite), with readBuffers' grey-plane profile (dem_quipu.ipp:184-194).
 template <typename T>
 __global__ void k_quipu_decode(QuipuDecode d, const T* __restrict__ codes, const uint8_t* __restrict__ planes,
-                               float* __restrict__ h, float* __restrict__ alb) {
+                               float* __restrict__ h, float* __restrict__ alb, bool vec4) {
     const size_t n = (size_t)d.W * d.H;
     const float m = sizeof(T) == 1 ? 255.f : 65535.f;
     for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
@@ -57,16 +106,31 @@ __global__ void k_quipu_decode(QuipuDecode d, const T* __restrict__ codes, const
         else z = quipu_dequantize((uint32_t)codes[v], m, d.hmin, d.hmax);
         h[v] = z;
         if (!alb) continue;
-        float* a = alb + v * d.nbands;
         const bool valid = !(isinf(z) || isnan(z));
+        float av[VGB_MAX_BANDS];
         if (!valid || d.albedo_type == 0 || d.albedo_type == VGB_QUIPU_NO_ALBEDO) {
-            for (uint32_t b = 0; b < d.nbands; ++b) a[b] = valid ? d.constant[b] : 1.f;
+#pragma unroll
+            for (uint32_t b = 0; b < VGB_MAX_BANDS; ++b) av[b] = valid ? d.constant[b] : 1.f;
         } else if (d.albedo_type == 1) {
             const float g = quipu_dequantize(planes[v], 255.f, d.pmin[0], d.pmax[0]);
-            for (uint32_t b = 0; b < d.nbands; ++b) a[b] = d.profile[b] * g;
+#pragma unroll
+            for (uint32_t b = 0; b < VGB_MAX_BANDS; ++b) av[b] = d.profile[b] * g;
         } else {
-            for (uint32_t b = 0; b < d.nbands; ++b)
-                a[b] = quipu_dequantize(planes[b * n + v], 255.f, d.pmin[b], d.pmax[b]);
+#pragma unroll
+            for (uint32_t b = 0; b < VGB_MAX_BANDS; ++b)
+                av[b] = b < d.nbands ? quipu_dequantize(planes[b * n + v], 255.f, d.pmin[b], d.pmax[b]) : 0.f;
+        }
+        // 16-byte stores when the rows allow them (4 or 8 bands on an aligned array)
+        float* a = alb + v * d.nbands;
+        if (vec4 && d.nbands == 8) {
+            reinterpret_cast<float4*>(a)[0] = make_float4(av[0], av[1], av[2], av[3]);
+            reinterpret_cast<float4*>(a)[1] = make_float4(av[4], av[5], av[6], av[7]);
+        } else if (vec4 && d.nbands == 4) {
+            reinterpret_cast<float4*>(a)[0] = make_float4(av[0], av[1], av[2], av[3]);
+        } else {
+#pragma unroll
+            for (uint32_t b = 0; b < VGB_MAX_BANDS; ++b)
+                if (b < d.nbands) a[b] = av[b];
         }
     }
 }
@@ -220,20 +284,25 @@ int launch_quipu_decode(void* stream, int sms, const QuipuDecode& d, const void*
                         float* heights, float* alb) {
     cudaStream_t s = (cudaStream_t)stream;
     const int g = grid((size_t)d.W * d.H, sms);
-    if (d.precision == 3) k_quipu_decode<uint8_t><<<g, 256, 0, s>>>(d, (const uint8_t*)codes, planes, heights, alb);
-    else if (d.precision == 4) k_quipu_decode<uint16_t><<<g, 256, 0, s>>>(d, (const uint16_t*)codes, planes, heights, alb);
-    else k_quipu_decode<float><<<g, 256, 0, s>>>(d, (const float*)codes, planes, heights, alb);
+    const bool vec4 = ((uintptr_t)alb & 15u) == 0 && (d.nbands == 4 || d.nbands == 8);
+    if (d.precision == 3) k_quipu_decode<uint8_t><<<g, 256, 0, s>>>(d, (const uint8_t*)codes, planes, heights, alb, vec4);
+    else if (d.precision == 4) k_quipu_decode<uint16_t><<<g, 256, 0, s>>>(d, (const uint16_t*)codes, planes, heights, alb, vec4);
+    else k_quipu_decode<float><<<g, 256, 0, s>>>(d, (const float*)codes, planes, heights, alb, vec4);
     return (int)cudaGetLastError();
 }
 
 int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, uint32_t H, const DemPose& pose,
-                           float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out) {
+                           float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out, float* nrm) {
     cudaStream_t s = (cudaStream_t)stream;
     const size_t nq = (size_t)(W - 1) * (H - 1);
     uint32_t* cnt = work;
     uint32_t* off = work + nq + 1;
-    uint32_t* tmp = off + nq + 1;
-    k_dem_vertices<<<grid((size_t)W * H, sms), 256, 0, s>>>(h, W, H, pose, pos);
+    float* xs = reinterpret_cast<float*>(off + nq + 1);
+    float* ys = xs + W;
+    uint32_t* tmp = reinterpret_cast<uint32_t*>(ys + H);
+    k_dem_axes<<<grid((size_t)W + H, sms), 256, 0, s>>>(W, H, pose, xs, ys);
+    if (nrm) k_dem_vertices<true><<<grid((size_t)W * H, sms), 256, 0, s>>>(h, W, H, xs, ys, pos, nrm);
+    else k_dem_vertices<false><<<grid((size_t)W * H, sms), 256, 0, s>>>(h, W, H, xs, ys, pos, nullptr);
     k_dem_quad_counts<<<grid(nq, sms), 256, 0, s>>>(h, W, H, cnt);
     cudaMemsetAsync(cnt + nq, 0, sizeof(uint32_t), s);
     scan(s, cnt, off, nq + 1, tmp);  // off[nq] = total triangles
@@ -245,7 +314,7 @@ int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, ui
 
 size_t dem_work_words(uint32_t W, uint32_t H) {
     const size_t nq = (size_t)(W - 1) * (H - 1);
-    return 2 * (nq + 1) + scan_temp_words(nq + 1);
+    return 2 * (nq + 1) + (size_t)W + H + scan_temp_words(nq + 1);
 }
 
 size_t normals_work_words(uint32_t nv, uint32_t nt) {

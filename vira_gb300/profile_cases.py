@@ -4,6 +4,7 @@
     python -m vira_gb300.profile_cases batch          # k_batch: 24 trajectory frames, 256^2-1024^2
     python -m vira_gb300.profile_cases adjoint        # k_adjoint: 2 views of a 513^2 crater DEM
     python -m vira_gb300.profile_cases after_film     # k_dn_*, k_psf, k_sensor on a 1024^2 frame
+    python -m vira_gb300.profile_cases quipu          # k_quipu_decode, k_dem_*, normals: a 2049^2 LoD, twice
 
 ``path`` renders the path-traced workload shrunk by ``scale`` (posts, texture and pixels; 4 spp)
 twice; the captures skip the launches of the first render.
@@ -54,8 +55,28 @@ def main(argv=None):
         img = sensor.simulate_sensor(scene, rp.received_power, sm)
         torch.cuda.synchronize()
         print("after_film", float(img.mean()))
+    elif kind == "quipu":
+        import tempfile
+        from pathlib import Path
+
+        import numpy as np
+
+        from . import quipu, synthetic
+
+        n = 2049
+        z = np.ascontiguousarray(synthetic.fbm_heights(n, 0.8, seed=21, lo=-200.0, hi=200.0), np.float32)
+        dem = quipu.DEM(z, quipu.DEMProjection(n, n, (1.0, 1.0)), synthetic.lognormal_albedo(n, 0.12, 0.3, seed=23),
+                        quipu.FLOAT_IMAGE_ALBEDO)
+        with tempfile.TemporaryDirectory() as tmp:
+            quipu.DEMQuipu.write(Path(tmp) / "dem", [dem], options=quipu.DEMQuipuWriterOptions(compress=True))
+            q = quipu.DEMQuipu(Path(tmp) / "dem.qld", nbands=8)
+            for _ in range(2):
+                out = q.read_lod_mesh(0, nbands=8, device_arrays=True)
+            torch.cuda.synchronize()
+            print("quipu", int(out[1].shape[0]), "triangles")
+            q.close()
     else:
-        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint | after_film")
+        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint | after_film | quipu")
 
 
 if __name__ == "__main__":
