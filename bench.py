@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--no-asteroid", action="store_true", help="skip the fused batched-adjoint asteroid line item")
     ap.add_argument("--no-after-film", action="store_true", help="skip the denoiser / PSF / sensor line item")
     ap.add_argument("--no-quipu", action="store_true", help="skip the DEM Quipu ingestion line item")
+    ap.add_argument("--no-raster", action="store_true", help="skip the rasterizer line item")
     return ap.parse_args()
 
 
@@ -392,6 +393,9 @@ def run_ours(args, p, rank, world, local_rank):
     after_film = None
     if not args.no_after_film and p["kind"] == "path_traced" and rank == 0:
         after_film = after_film_item(torch, dev, scene, cam_id, peak)
+    raster = None
+    if not args.no_raster and p["kind"] == "path_traced" and rank == 0:
+        raster = raster_item(torch, dev, scene, cam_id, cpu=not args.no_cpu_baseline)
     quipu = None
     if not args.no_quipu and p["kind"] == "path_traced" and rank == 0:
         quipu = quipu_item(torch, dev, peak, cpu=not args.no_cpu_baseline)
@@ -464,6 +468,8 @@ def run_ours(args, p, rank, world, local_rank):
             line["after_film"] = after_film
         if quipu is not None:
             line["quipu_ingest"] = quipu
+        if raster is not None:
+            line["raster"] = raster
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -601,6 +607,57 @@ def adjoint_item(torch, dev, layout=2, reps=2):
            "grad_norm": {"texture": float(gt.double().norm()), "heights": float(gz.double().norm())},
            "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
     scene.close()
+    return out
+
+
+def raster_item(torch, dev, scene, cam_id, reps=5, cpu=True):
+    """The rasterizer (vgb_rasterize, CPURasterizer::render) with lighting on the path-traced
+    frame's scene (33.5M triangles, 2048^2, 8 bands) and on the direct-lighting scene (0.52M
+    triangles, 1024^2, 4 bands); the oracle's sequential restatement times the latter on one
+    host core."""
+    from vira_gb300 import workloads
+
+    def timed(sc, cid):
+        rz = sc.rasterizer
+        rz.render_passes.simulate_lighting = True
+        rz.render(sc[cid], sc)        # warm-up (scratch, solid angles)
+        ms = []
+        for _ in range(reps):
+            rz.render(sc[cid], sc)
+            ms.append(rz.last_stats.ms_last)
+        return min(ms), rz.render_passes
+
+    out = {}
+    ms, rp = timed(scene, cam_id)
+    W, H = scene[cam_id].resolution
+    ntri = int(scene.flat["indices"].shape[0])
+    out["path_traced_scene"] = {"triangles": ntri, "image": [W, H], "bands": scene.bands.size, "ms": ms,
+                                "mtris_per_s": ntri / ms / 1e3,
+                                "covered_pixels": int(torch.isfinite(rp.depth).sum().item())}
+    small, cid = workloads.plain_direct(device=dev.index)
+    ms2, rp2 = timed(small, cid)
+    ntri2 = int(small.flat["indices"].shape[0])
+    W2, H2 = small[cid].resolution
+    item = {"triangles": ntri2, "image": [W2, H2], "bands": small.bands.size, "ms": ms2,
+            "mtris_per_s": ntri2 / ms2 / 1e3}
+    if cpu:
+        from oracle import oracle
+
+        B = small.bands.size
+        c = small[cid].to_c(small.origin, B)
+        lights, nl = small.c_lights()
+        omega = small.pixel_solid_angle(small[cid], c).cpu().numpy()
+        osc = oracle.OracleScene.from_flat(small.flat, B)
+        t0 = time.perf_counter()
+        osc.rasterize(c, small[cid].intrinsic_matrix(), lights, nl, True, small.smooth_shading(), omega)
+        cs = time.perf_counter() - t0
+        osc.close()
+        item["cpu_baseline"] = {"value": ntri2 / cs / 1e6, "unit": "Mtris/s", "cores": 1, "kind": "port",
+                                "sample": f"the whole frame ({cs:.2f} s): the oracle's sequential CPURasterizer"}
+        item["speedup_over_cpu"] = cs * 1e3 / ms2
+    out["plain_direct_scene"] = item
+    out["timing"] = "CUDA events around the three raster kernels on the context stream, best of %d" % reps
+    small.close()
     return out
 
 

@@ -414,6 +414,31 @@ VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
  * vgb_stats.ms_trace / ms_shade / ms_shadow / ms_film. */
 VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
 
+/* ========================= rasterizer =========================================
+ * CPURasterizer::render (include/implementation/rendering/cpu_rasterizer.ipp:29-270) on the
+ * device, for the uploaded scene (no BVH needed): every triangle is moved to the camera frame,
+ * culled when a corner is behind the camera, projected, and its bounding box of integer pixel
+ * coordinates (X, Y) -- pixel corners, as the reference samples -- tested with edge functions;
+ * the closest fragment by interpolated distance wins, ties going to the earlier triangle, as the
+ * reference's strict `<` over triangles in order gives.  The winner's passes: depth, alpha
+ * (count / sample = 1/0 = +inf, the reference's value), albedo (vertex albedo x texture), the
+ * face or smooth normal, triangle_id = triangle index + 1 (the reference counts from 1), and with
+ * simulate_lighting the unshadowed direct radiance of the RNG-free light samples (total_radiance;
+ * direct and indirect stay 0, as in the reference) and the received power.
+ * Camera frame: p_cam = R^T (p - origin) in FP32 from the vgb_camera (the reference multiplies by
+ * glm's FP32 inverse of the camera transform: equal up to rounding); projection
+ * (x, y) = K (p_cam.x / p_cam.z, p_cam.y / p_cam.z, 1), mirrored in x when z_dir < 0 (Blender). */
+typedef struct vgb_raster_options {
+    float intrinsic[6];        /* rows of K with z_dir folded in: fx, kxy, px, kyx, fy, py (camera.ipp:1540-1556) */
+    uint32_t simulate_lighting;
+    uint32_t smooth_shading;
+    uint32_t nbands;
+    uint32_t pad;
+} vgb_raster_options;
+
+VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                                 const vgb_raster_options* opts, vgb_film* film);
+
 /* ========================= DEM Quipu files (.qld) ==============================
  * Vira's on-disk DEM pyramid (include/implementation/quipu/dem_quipu.ipp,
  * include/implementation/quipu/quipu_io.ipp): the identifier "QUIPU", class id 2002, the

@@ -59,6 +59,7 @@ def load():
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
                                                C.c_int]),
         "oracle_lz4_decompress": (C.c_int64, [P, C.c_uint64, P, C.c_uint64]),
+        "oracle_rasterize": (C.c_int, [P, C.POINTER(capi.Camera), P, P, U32, C.c_int, C.c_int, P, P, P, P, P, P, P, P]),
         "oracle_normal_cone": (C.c_int, [P, C.c_uint64, P]),
     }
     for name, (res, args) in sig.items():
@@ -193,6 +194,25 @@ class OracleScene:
             self.close()
         except Exception:
             pass
+
+    def rasterize(self, cam: capi.Camera, K, lights, nlights: int, lighting: bool, smooth: bool, omega=None):
+        """The CPURasterizer restatement: planes depth, alpha, albedo, normal_global, triangle_id
+        (index + 1), total_radiance and received_power (with lighting)."""
+        W, H, B = cam.width, cam.height, self.nbands
+        k = np.ascontiguousarray(K, np.float32)
+        out = dict(depth=np.empty((H, W), np.float32), alpha=np.empty((H, W), np.float32),
+                   albedo=np.empty((B, H, W), np.float32), normal_global=np.empty((3, H, W), np.float32),
+                   triangle_id=np.empty((H, W), np.uint32))
+        if lighting:
+            out["total_radiance"] = np.empty((B, H, W), np.float32)
+            out["received_power"] = np.empty((B, H, W), np.float32)
+        om = None if omega is None else np.ascontiguousarray(omega, np.float32)
+        p = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+        assert load().oracle_rasterize(self.h, C.byref(cam), k.ctypes.data, lights, nlights, int(lighting), int(smooth),
+                                       p(out["depth"]), p(out["alpha"]), p(out["albedo"]), p(out["normal_global"]),
+                                       p(out["triangle_id"]), p(out.get("total_radiance")), p(out.get("received_power")),
+                                       p(om)) == 0
+        return out
 
     def trace(self, origins, dirs, any_hit=False, tmax=None, mode=0, threads=None):
         o = np.ascontiguousarray(origins, np.float32)

@@ -1607,3 +1607,114 @@ OAPI int oracle_normal_cone(const float* normals, uint64_t nv, float* out) {
     out[0] = m[0]; out[1] = m[1]; out[2] = m[2]; out[3] = cone;
     return 0;
 }
+
+// ---------------------------------------------------------------- rasterizer
+// CPURasterizer::render (include/implementation/rendering/cpu_rasterizer.ipp:29-270), literally:
+// triangles in buffer order, pixel boxes walked X outer / Y inner at integer corners, the depth
+// test `current < previous` against +inf, and the passes overwritten by every fragment that
+// passes it (passes.ipp:80-128).  The camera frame is R^T (p - origin) from the vgb_camera and
+// the fragment's scene position R p_cam + origin (FP32), as vgb_rasterize defines them.
+// static_cast<int>(float) is taken as x86-64 performs it: out-of-range values and NaN give INT_MIN.
+static inline int x86_int(float x) { return (x >= -2147483648.f && x < 2147483648.f) ? (int)x : INT32_MIN; }
+static inline float edge_fn(float ax, float ay, float bx, float by, float cx, float cy) {
+    return (cx - ax) * (by - ay) - (cy - ay) * (bx - ax);
+}
+
+OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const vgb_light* lights, uint32_t nlights,
+                          int lighting, int smooth, float* depth_o, float* alpha_o, float* albedo_o, float* normal_o,
+                          uint32_t* tri_o, float* total_o, float* power_o, const float* omega) {
+    const Scene& s = *static_cast<Scene*>(h);
+    const uint32_t W = cam->width, H = cam->height, B = s.nbands;
+    const size_t P = (size_t)W * H;
+    for (size_t v = 0; v < P; ++v) {
+        depth_o[v] = INFINITY; alpha_o[v] = 0.f; tri_o[v] = 0xFFFFFFFFu;
+        for (int k = 0; k < 3; ++k) normal_o[k * P + v] = 0.f;
+        for (uint32_t b = 0; b < B; ++b) { albedo_o[b * P + v] = 0.f; if (total_o) total_o[b * P + v] = 0.f; }
+    }
+    const V3 O{cam->origin[0], cam->origin[1], cam->origin[2]};
+    const V3 ax{cam->rotation[0], cam->rotation[1], cam->rotation[2]};
+    const V3 ay{cam->rotation[3], cam->rotation[4], cam->rotation[5]};
+    const V3 az{cam->rotation[6], cam->rotation[7], cam->rotation[8]};
+    for (uint32_t t = 0; t < s.ntris; ++t) {
+        const uint32_t vi[3] = {s.idx[3 * t], s.idx[3 * t + 1], s.idx[3 * t + 2]};
+        if (std::isinf(s.pos[vi[0]].x) || std::isinf(s.pos[vi[1]].x) || std::isinf(s.pos[vi[2]].x)) continue;
+        V3 vc[3];
+        for (int k = 0; k < 3; ++k) {
+            const V3 d = s.pos[vi[k]] - O;
+            vc[k] = V3{dot(ax, d), dot(ay, d), dot(az, d)};
+        }
+        bool behind = false;
+        for (int k = 0; k < 3; ++k) behind = behind || ((-cam->z_dir * vc[k].z) >= 0);
+        if (behind) continue;
+        float px[3], py[3];
+        for (int k = 0; k < 3; ++k) {
+            const float hx = vc[k].x / vc[k].z, hy = vc[k].y / vc[k].z;
+            float X = (K[0] * hx + K[1] * hy) + K[2];
+            const float Y = (K[3] * hx + K[4] * hy) + K[5];
+            if (cam->z_dir < 0) X = (float)(W - 1) - X;
+            px[k] = X; py[k] = Y;
+        }
+        const int sx = x86_int(std::floor(std::min(px[0], std::min(px[1], px[2]))));
+        const int sy = x86_int(std::floor(std::min(py[0], std::min(py[1], py[2]))));
+        const int ex = x86_int(std::ceil(std::max(px[0], std::max(px[1], px[2]))));
+        const int ey = x86_int(std::ceil(std::max(py[0], std::max(py[1], py[2]))));
+        if (ex < 0 || sx > (int)W || ey < 0 || sy > (int)H) continue;
+        const int x0 = std::clamp(sx, 0, (int)W), y0 = std::clamp(sy, 0, (int)H);
+        const int x1 = std::clamp(ex, 0, (int)W), y1 = std::clamp(ey, 0, (int)H);
+        const float d0 = length(vc[0]), d1 = length(vc[1]), d2 = length(vc[2]);
+        const float area = edge_fn(px[0], py[0], px[1], py[1], px[2], py[2]);
+        for (int X = x0; X < x1; ++X) {
+            for (int Y = y0; Y < y1; ++Y) {
+                const float fx = (float)X, fy = (float)Y;
+                const float w0 = edge_fn(px[1], py[1], px[2], py[2], fx, fy) / area;
+                const float w1 = edge_fn(px[2], py[2], px[0], py[0], fx, fy) / area;
+                const float w2 = edge_fn(px[0], py[0], px[1], py[1], fx, fy) / area;
+                if (!(w0 >= 0 && w1 >= 0 && w2 >= 0)) continue;
+                const size_t v = (size_t)Y * W + X;
+                const float cur = ((w0 * d0) + (w1 * d1)) + (w2 * d2);
+                if (!(cur < depth_o[v])) continue;
+                depth_o[v] = cur;
+                const float uvx = (w0 * s.uv[2 * vi[0]] + w1 * s.uv[2 * vi[1]]) + w2 * s.uv[2 * vi[2]];
+                const float uvy = (w0 * s.uv[2 * vi[0] + 1] + w1 * s.uv[2 * vi[1] + 1]) + w2 * s.uv[2 * vi[2] + 1];
+                float texv[VGB_MAX_BANDS], alb[VGB_MAX_BANDS];
+                sample_uvs(s, uvx, uvy, texv);
+                for (uint32_t b = 0; b < B; ++b) {
+                    const float va = (w0 * s.albedo[(size_t)vi[0] * B + b] + w1 * s.albedo[(size_t)vi[1] * B + b]) +
+                                     w2 * s.albedo[(size_t)vi[2] * B + b];
+                    alb[b] = va * texv[b];
+                }
+                const V3 fn = normalize(cross(s.pos[vi[0]] - s.pos[vi[1]], s.pos[vi[2]] - s.pos[vi[0]]));
+                V3 N{-fn.x, -fn.y, -fn.z};
+                if (smooth) N = normalize((w0 * s.nrm[vi[0]] + w1 * s.nrm[vi[1]]) + w2 * s.nrm[vi[2]]);
+                float rad[VGB_MAX_BANDS] = {0};
+                if (lighting) {
+                    const V3 fc = (w0 * vc[0] + w1 * vc[1]) + w2 * vc[2];
+                    const float* R = cam->rotation;
+                    const V3 fg{((R[0] * fc.x + R[3] * fc.y) + R[6] * fc.z) + cam->origin[0],
+                                ((R[1] * fc.x + R[4] * fc.y) + R[7] * fc.z) + cam->origin[1],
+                                ((R[2] * fc.x + R[5] * fc.y) + R[8] * fc.z) + cam->origin[2]};
+                    for (uint32_t l = 0; l < nlights; ++l) {
+                        V3 L; float dist, pdf;
+                        light_sample(lights[l], fg, true, 0.f, 0.f, L, dist, pdf);
+                        const float nl = std::max(dot(N, L), 0.f);
+                        for (uint32_t b = 0; b < B; ++b) {
+                            const float bsdf = ((alb[b] * INV_PI_F) * nl) / pdf;
+                            rad[b] = rad[b] + lights[l].radiance[b] * bsdf;
+                        }
+                    }
+                }
+                alpha_o[v] = INFINITY;
+                tri_o[v] = t + 1;
+                normal_o[v] = N.x; normal_o[P + v] = N.y; normal_o[2 * P + v] = N.z;
+                for (uint32_t b = 0; b < B; ++b) {
+                    albedo_o[b * P + v] = alb[b];
+                    if (total_o) total_o[b * P + v] = rad[b];
+                }
+            }
+        }
+    }
+    if (lighting && power_o && omega)
+        for (size_t v = 0; v < P; ++v)
+            for (uint32_t b = 0; b < B; ++b) power_o[b * P + v] = (cam->power_scale[b] * omega[v]) * total_o[b * P + v];
+    return 0;
+}

@@ -45,7 +45,8 @@ def test_struct_layouts_match_the_header(tmp_path):
              "vgb_batch_options": capi.BatchOptions, "vgb_bvh_options": capi.BvhOptions, "vgb_stats": capi.Stats, "vgb_sensor": capi.Sensor,
              "vgb_denoise_options": capi.DenoiseOptions, "vgb_quipu_header": capi.QuipuHeader,
              "vgb_quipu_projection": capi.QuipuProjection, "vgb_quipu_lod_info": capi.QuipuLodInfo,
-             "vgb_quipu_read_options": capi.QuipuReadOptions, "vgb_quipu_lod_data": capi.QuipuLodData}
+             "vgb_quipu_read_options": capi.QuipuReadOptions, "vgb_quipu_lod_data": capi.QuipuLodData,
+             "vgb_raster_options": capi.RasterOptions}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vgb.h"', "int main(void) {"]
     for cname, py in pairs.items():
         lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')

@@ -115,3 +115,41 @@ def test_large_pyramid_round_trip(gpu, tmp_path):
     fin = np.isfinite(h.ravel())
     assert np.all(alb[fin] == np.float32(0.12)) and np.all(alb[~fin] == 1.0)
     q.close()
+
+
+def test_level_of_detail_manager_swaps_quipu_lods(gpu):
+    import torch
+
+    from vira_gb300 import FOUR_BAND, Mesh, Scene
+
+    path = GOLDEN / "quipu_u16_lz4_color.qld"
+    s = Scene(FOUR_BAND)
+    m = Mesh.from_quipu(path, nbands=4)
+    assert m.gsd() == 40.0 and m.positions.shape[0] == 17 * 13      # the default: the coarsest LoD
+    s.add_mesh(m)
+    s.new_instance(("mesh", 0))
+    sun = s.new_sun(5778.0)
+    s.set_sun_direction(sun, 20.0, 40.0)
+    cid = s.new_camera()
+    c = s[cid]
+    c.set_resolution(256, 256)
+    c.set_sensor_size(0.036)
+    c.set_field_of_view(30.0)
+    c.set_local_position(100.0, -150.0, 1500.0)
+    c.look_at((0.0, 0.0, 0.0))
+    s.pathtracer.options.samples = 2
+    s.pathtracer.render_passes.simulate_lighting = True
+    s.pathtracer.render(c, s)
+    assert s.update_level_of_detail(cid) == 1
+    assert m.gsd() == 10.0 and m.positions.shape[0] == 65 * 49
+    q = VQ.DEMQuipu(path, nbands=4)
+    pos, idx, alb, nrm = q.read_lod_mesh(0)
+    q.close()
+    assert _eq(m.positions, pos) and _eq(m.indices, idx) and _eq(m.normals, nrm)
+    rp = s.pathtracer.render(c, s)
+    torch.cuda.synchronize()
+    tid = rp.triangle_id.cpu().numpy()
+    assert (tid >= 0).mean() > 0.3 and tid.max() < idx.shape[0]   # the fine LoD's triangles
+    c.set_local_position(100.0, -150.0, 40000.0)
+    assert s.update_level_of_detail(cid) == 1 and m.gsd() == 40.0
+    s.close()

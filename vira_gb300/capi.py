@@ -109,6 +109,11 @@ class Stats(C.Structure):
     ]
 
 
+class RasterOptions(C.Structure):
+    _fields_ = [("intrinsic", C.c_float * 6), ("simulate_lighting", C.c_uint32), ("smooth_shading", C.c_uint32),
+                ("nbands", C.c_uint32), ("pad", C.c_uint32)]
+
+
 QUIPU_MAX_LODS = 64
 QUIPU_NO_ALBEDO = 0xFFFFFFFF
 
@@ -179,6 +184,7 @@ SIGNATURES = {
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
+    "vgb_rasterize": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(RasterOptions), C.POINTER(Film)]),
     "vgb_quipu_open": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "vgb_quipu_close": (None, [_P]),
     "vgb_quipu_last_error": (C.c_char_p, []),

@@ -1674,6 +1674,305 @@ VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos
     return VGB_OK;
 }
 
+// ---------------------------------------------------------------- rasterizer
+namespace {
+
+// static_cast<int>(float) as x86-64 performs it (cvttss2si): values outside int's range and NaN
+// become INT_MIN.  The reference's bounding boxes go through this cast.
+__device__ __forceinline__ int x86_int(float x) {
+    return (x >= -2147483648.f && x < 2147483648.f) ? (int)x : (int)0x80000000;
+}
+
+struct RasterParams {
+    vgb_camera cam;
+    float K[6];
+    vgb_light lights[VGB_MAX_LIGHTS];
+    uint32_t nlights, nb, smooth, lighting;
+};
+
+struct RTri {
+    F3 vc[3];            // corners in the camera frame
+    float px[3], py[3];  // projected corners
+    float d[3];          // distances to the camera
+    float area;
+    int x0, x1, y0, y1;  // clamped pixel box [x0, x1) x [y0, y1)
+};
+
+// Camera frame, behind test, projection and pixel box of triangle t (cpu_rasterizer.ipp:73-120).
+__device__ __forceinline__ bool raster_setup(const DevScene& s, const RasterParams& rp, uint32_t t, RTri& r) {
+    const vgb_camera& c = rp.cam;
+    F3 p[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p[k] = ld3(__ldg(&s.vpos[__ldg(&s.idx[3 * (size_t)t + k])]));
+    if (isinf(p[0].x) || isinf(p[1].x) || isinf(p[2].x)) return false;
+    const F3 O{c.origin[0], c.origin[1], c.origin[2]};
+    const F3 ax{c.rotation[0], c.rotation[1], c.rotation[2]}, ay{c.rotation[3], c.rotation[4], c.rotation[5]},
+             az{c.rotation[6], c.rotation[7], c.rotation[8]};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const F3 d = p[k] - O;
+        r.vc[k] = F3{dot(ax, d), dot(ay, d), dot(az, d)};
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if ((-c.z_dir * r.vc[k].z) >= 0) return false;   // Camera::behind (camera.ipp:1394-1397)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float hx = r.vc[k].x / r.vc[k].z, hy = r.vc[k].y / r.vc[k].z;
+        float X = (rp.K[0] * hx + rp.K[1] * hy) + rp.K[2];
+        const float Y = (rp.K[3] * hx + rp.K[4] * hy) + rp.K[5];
+        if (c.z_dir < 0) X = (float)(c.width - 1) - X;   // Blender frame (camera.ipp:1062-1080)
+        r.px[k] = X;
+        r.py[k] = Y;
+    }
+    const int sx = x86_int(floorf(smin(r.px[0], smin(r.px[1], r.px[2]))));
+    const int sy = x86_int(floorf(smin(r.py[0], smin(r.py[1], r.py[2]))));
+    const int ex = x86_int(ceilf(smax(r.px[0], smax(r.px[1], r.px[2]))));
+    const int ey = x86_int(ceilf(smax(r.py[0], smax(r.py[1], r.py[2]))));
+    const int W = (int)c.width, H = (int)c.height;
+    if (ex < 0 || sx > W || ey < 0 || sy > H) return false;
+    r.x0 = min(max(sx, 0), W); r.y0 = min(max(sy, 0), H);
+    r.x1 = min(max(ex, 0), W); r.y1 = min(max(ey, 0), H);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r.d[k] = length(r.vc[k]);
+    // edgeFunction(p0, p1, p2) (triangle.ipp:90-93)
+    r.area = (r.px[2] - r.px[0]) * (r.py[1] - r.py[0]) - (r.py[2] - r.py[0]) * (r.px[1] - r.px[0]);
+    return true;
+}
+
+// Barycentric weights at the pixel corner (X, Y), the inside test and the interpolated distance
+// (cpu_rasterizer.ipp:132-146).
+__device__ __forceinline__ bool raster_w(const RTri& r, int X, int Y, float* w, float& depth) {
+    const float fx = (float)X, fy = (float)Y;
+    w[0] = ((fx - r.px[1]) * (r.py[2] - r.py[1]) - (fy - r.py[1]) * (r.px[2] - r.px[1])) / r.area;
+    w[1] = ((fx - r.px[2]) * (r.py[0] - r.py[2]) - (fy - r.py[2]) * (r.px[0] - r.px[2])) / r.area;
+    w[2] = ((fx - r.px[0]) * (r.py[1] - r.py[0]) - (fy - r.py[0]) * (r.px[1] - r.px[0])) / r.area;
+    if (!(w[0] >= 0 && w[1] >= 0 && w[2] >= 0)) return false;
+    depth = ((w[0] * r.d[0]) + (w[1] * r.d[1])) + (w[2] * r.d[2]);
+    return true;
+}
+
+// Closest fragment per pixel: the smallest (distance, triangle) pair, which is what the
+// reference's in-order `current < previous` leaves (only finite distances ever pass it).
+__device__ __forceinline__ void raster_fragment(unsigned long long* keys, uint32_t W, int X, int Y, float depth,
+                                                uint32_t t) {
+    if (!(depth < __int_as_float(0x7f800000))) return;
+    const uint32_t bits = depth == 0.f ? 0u : __float_as_uint(depth);
+    atomicMin(&keys[(size_t)Y * W + X], ((unsigned long long)bits << 32) | t);
+}
+
+constexpr uint32_t kRasterSmall = 256;   // box pixels a thread walks by itself
+
+__global__ void k_raster_cover(DevScene s, RasterParams rp, uint32_t ntris, unsigned long long* __restrict__ keys,
+                               uint32_t* __restrict__ bigq, uint32_t* __restrict__ nbig) {
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ntris; t += (size_t)gridDim.x * blockDim.x) {
+        RTri r;
+        if (!raster_setup(s, rp, (uint32_t)t, r)) continue;
+        const uint64_t npix = (uint64_t)(r.x1 - r.x0) * (uint64_t)(r.y1 - r.y0);
+        if (npix == 0) continue;
+        if (npix > kRasterSmall) { bigq[atomicAdd(nbig, 1u)] = (uint32_t)t; continue; }
+        for (int X = r.x0; X < r.x1; ++X)
+            for (int Y = r.y0; Y < r.y1; ++Y) {
+                float w[3], depth;
+                if (raster_w(r, X, Y, w, depth)) raster_fragment(keys, rp.cam.width, X, Y, depth, (uint32_t)t);
+            }
+    }
+}
+
+// Triangles with large boxes: one block per triangle, the box's pixels spread over its threads.
+__global__ void k_raster_big(DevScene s, RasterParams rp, const uint32_t* __restrict__ bigq,
+                             const uint32_t* __restrict__ nbig, unsigned long long* __restrict__ keys) {
+    const uint32_t n = *nbig;
+    for (uint32_t q = blockIdx.x; q < n; q += gridDim.x) {
+        const uint32_t t = bigq[q];
+        RTri r;
+        if (!raster_setup(s, rp, t, r)) continue;
+        const uint64_t ww = (uint64_t)(r.x1 - r.x0), npix = ww * (uint64_t)(r.y1 - r.y0);
+        for (uint64_t k = threadIdx.x; k < npix; k += blockDim.x) {
+            const int X = r.x0 + (int)(k % ww), Y = r.y0 + (int)(k / ww);
+            float w[3], depth;
+            if (raster_w(r, X, Y, w, depth)) raster_fragment(keys, rp.cam.width, X, Y, depth, t);
+        }
+    }
+}
+
+struct RasterOut {
+    float *depth, *alpha, *albedo, *normal, *total, *direct, *indirect, *power;
+    uint32_t* tri;
+    const float* omega;
+};
+
+// The winner's passes (cpu_rasterizer.ipp:148-250, passes.ipp:80-128): the fragment is
+// recomputed from its triangle with the same arithmetic as the coverage pass.
+__global__ void k_raster_resolve(DevScene s, RasterParams rp, const unsigned long long* __restrict__ keys,
+                                 RasterOut o) {
+    const uint32_t W = rp.cam.width, H = rp.cam.height, nb = rp.nb;
+    const size_t P = (size_t)W * H;
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < P; v += (size_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = keys[v];
+        float depth = __int_as_float(0x7f800000), alpha = 0.f;
+        float alb[VGB_MAX_BANDS], rad[VGB_MAX_BANDS];
+#pragma unroll
+        for (int k = 0; k < VGB_MAX_BANDS; ++k) { alb[k] = 0.f; rad[k] = 0.f; }
+        F3 N{0.f, 0.f, 0.f};
+        uint32_t tri = VGB_NO_HIT;
+        RTri r;
+        float w[3];
+        const uint32_t t = (uint32_t)(key & 0xFFFFFFFFull);
+        if (key != ~0ull && raster_setup(s, rp, t, r) && raster_w(r, (int)(v % W), (int)(v / W), w, depth)) {
+            const uint32_t vi[3] = {__ldg(&s.idx[3 * (size_t)t]), __ldg(&s.idx[3 * (size_t)t + 1]),
+                                    __ldg(&s.idx[3 * (size_t)t + 2])};
+            F3 vp[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) vp[k] = ld3(__ldg(&s.vpos[vi[k]]));
+            const float2 u0 = __ldg(&s.vuv[vi[0]]), u1 = __ldg(&s.vuv[vi[1]]), u2 = __ldg(&s.vuv[vi[2]]);
+            const float uvx = (w[0] * u0.x + w[1] * u1.x) + w[2] * u2.x;
+            const float uvy = (w[0] * u0.y + w[1] * u1.y) + w[2] * u2.y;
+            float texv[VGB_MAX_BANDS];
+            sample_uvs<VGB_MAX_BANDS>(s, nb, uvx, uvy, texv);
+#pragma unroll
+            for (int k = 0; k < VGB_MAX_BANDS; ++k) {
+                if (k >= (int)nb) break;
+                float va;
+                if (s.albedo_uniform) {
+                    const float cst = s.albedo_value[k];
+                    va = (w[0] * cst + w[1] * cst) + w[2] * cst;
+                } else {
+                    va = (w[0] * __ldg(&s.valb[(size_t)vi[0] * nb + k]) + w[1] * __ldg(&s.valb[(size_t)vi[1] * nb + k])) +
+                         w[2] * __ldg(&s.valb[(size_t)vi[2] * nb + k]);
+                }
+                alb[k] = va * texv[k];
+            }
+            // Triangle::init's face normal -normalize((v0 - v1) x (v2 - v0)), or the smooth normal
+            const F3 fn = normalize(cross(vp[0] - vp[1], vp[2] - vp[0]));
+            N = F3{-fn.x, -fn.y, -fn.z};
+            if (rp.smooth) {
+                F3 vn[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) vn[k] = ld3(__ldg(&s.vnrm[vi[k]]));
+                N = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
+            }
+            if (rp.lighting) {
+                const F3 fc = (w[0] * r.vc[0] + w[1] * r.vc[1]) + w[2] * r.vc[2];
+                const vgb_camera& c = rp.cam;
+                const F3 fg{((c.rotation[0] * fc.x + c.rotation[3] * fc.y) + c.rotation[6] * fc.z) + c.origin[0],
+                            ((c.rotation[1] * fc.x + c.rotation[4] * fc.y) + c.rotation[7] * fc.z) + c.origin[1],
+                            ((c.rotation[2] * fc.x + c.rotation[5] * fc.y) + c.rotation[8] * fc.z) + c.origin[2]};
+                for (uint32_t l = 0; l < rp.nlights; ++l) {
+                    F3 L;
+                    float dist, pdf;
+                    light_sample(rp.lights[l], fg, true, 0.f, 0.f, L, dist, pdf);
+                    const float nl = smax(dot(N, L), 0.f);
+#pragma unroll
+                    for (int k = 0; k < VGB_MAX_BANDS; ++k) {
+                        if (k >= (int)nb) break;
+                        const float bsdf = ((alb[k] * kInvPi) * nl) / pdf;   // Lambertian::evaluateBSDF / pdf
+                        rad[k] = rad[k] + rp.lights[l].radiance[k] * bsdf;
+                    }
+                }
+            }
+            alpha = __int_as_float(0x7f800000);   // count / sample with sample = 0: 1/0
+            tri = t + 1u;
+        } else {
+            depth = __int_as_float(0x7f800000);
+        }
+        if (o.depth) o.depth[v] = depth;
+        if (o.alpha) o.alpha[v] = alpha;
+        if (o.tri) o.tri[v] = tri;
+        if (o.normal) { o.normal[v] = N.x; o.normal[P + v] = N.y; o.normal[2 * P + v] = N.z; }
+        for (uint32_t k = 0; k < nb; ++k) {
+            if (o.albedo) o.albedo[k * P + v] = alb[k];
+            if (o.total) o.total[k * P + v] = rad[k];
+            if (o.direct) o.direct[k * P + v] = 0.f;
+            if (o.indirect) o.indirect[k * P + v] = 0.f;
+            if (o.power) o.power[k * P + v] = (rp.cam.power_scale[k] * o.omega[v]) * rad[k];
+        }
+    }
+}
+
+}  // namespace
+
+VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
+                                 const vgb_raster_options* opts, vgb_film* film) {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: null argument");
+    if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "rasterize: no scene uploaded");
+    if (cam->width == 0 || cam->height == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: empty image");
+    if ((uint64_t)cam->width * cam->height >= (1ull << 32))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: image larger than 2^32 pixels");
+    if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: nbands differs from the scene's");
+    if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: 0..8 lights");
+    if (film->received_power && !film->pixel_solid_angle)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: received_power needs pixel_solid_angle");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)cam->width * cam->height, B = ctx->nbands;
+    RasterParams rp{};
+    rp.cam = *cam;
+    for (int k = 0; k < 6; ++k) rp.K[k] = opts->intrinsic[k];
+    for (uint32_t l = 0; l < nlights; ++l) rp.lights[l] = lights[l];
+    rp.nlights = opts->simulate_lighting ? nlights : 0;
+    rp.nb = (uint32_t)B;
+    rp.smooth = opts->smooth_shading ? 1u : 0u;
+    rp.lighting = opts->simulate_lighting ? 1u : 0u;
+    // scratch: keys (P x 8 B), big-triangle queue and its count
+    const size_t key_floats = 2 * P, q_floats = (size_t)ctx->ntris + 4;
+    const size_t host_planes = film->on_device ? 0 : (size_t)(5 * B + 6) * P + 4 * 8;
+    vgb_status s;
+    if ((s = ensure_dn_scratch(ctx, key_floats + q_floats + host_planes)) != VGB_OK) return s;
+    unsigned long long* keys = reinterpret_cast<unsigned long long*>(ctx->d_dn);
+    uint32_t* bigq = reinterpret_cast<uint32_t*>(ctx->d_dn + key_floats);
+    uint32_t* nbig = bigq + ctx->ntris;
+    RasterOut o{film->depth, film->alpha, film->albedo, film->normal_global, film->total_radiance,
+                film->direct_radiance, film->indirect_radiance, film->received_power, film->triangle_id,
+                film->pixel_solid_angle};
+    if (!rp.lighting) o.total = o.direct = o.indirect = o.power = nullptr;
+    float* stage = ctx->d_dn + key_floats + q_floats;
+    if (!film->on_device) {
+        // host film: device planes in scratch, copied back below
+        auto take = [&](float* hp, size_t n) -> float* { if (!hp) return nullptr; float* d = stage; stage += (n + 3) & ~(size_t)3; return d; };
+        o.depth = take(film->depth, P); o.alpha = take(film->alpha, P); o.albedo = take(film->albedo, B * P);
+        o.normal = take(film->normal_global, 3 * P);
+        o.tri = reinterpret_cast<uint32_t*>(take(reinterpret_cast<float*>(film->triangle_id), P));
+        if (rp.lighting) {
+            o.total = take(film->total_radiance, B * P); o.direct = take(film->direct_radiance, B * P);
+            o.indirect = take(film->indirect_radiance, B * P); o.power = take(film->received_power, B * P);
+            float* om = take(const_cast<float*>(film->pixel_solid_angle), P);
+            if (om) {
+                CK(cudaMemcpyAsync(om, film->pixel_solid_angle, P * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+                o.omega = om;
+            }
+        }
+    }
+    const DevScene sc = dev_scene(ctx);
+    CK(cudaMemsetAsync(keys, 0xFF, P * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(nbig, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    k_raster_cover<<<grid_for(ctx, ctx->ntris, 8), 256, 0, ctx->stream>>>(sc, rp, ctx->ntris, keys, bigq, nbig);
+    k_raster_big<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(sc, rp, bigq, nbig, keys);
+    k_raster_resolve<<<grid_for(ctx, P, 8), 256, 0, ctx->stream>>>(sc, rp, keys, o);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (!film->on_device) {
+        auto back = [&](void* hp, const void* dp, size_t bytes) -> cudaError_t {
+            return (hp && dp) ? cudaMemcpyAsync(hp, dp, bytes, cudaMemcpyDeviceToHost, ctx->stream) : cudaSuccess;
+        };
+        CK(back(film->depth, o.depth, P * 4)); CK(back(film->alpha, o.alpha, P * 4));
+        CK(back(film->albedo, o.albedo, B * P * 4)); CK(back(film->normal_global, o.normal, 3 * P * 4));
+        CK(back(film->triangle_id, o.tri, P * 4));
+        if (rp.lighting) {
+            CK(back(film->total_radiance, o.total, B * P * 4)); CK(back(film->direct_radiance, o.direct, B * P * 4));
+            CK(back(film->indirect_radiance, o.indirect, B * P * 4)); CK(back(film->received_power, o.power, B * P * 4));
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->stats.ms_last = ms;
+    ctx->stats.kernel_launches = 3;
+    return VGB_OK;
+}
+
 // DEMQuipu::readBuffers (dem_quipu.ipp:124-221): the file's stored codes are read and LZ4-decoded
 // on the host into pinned memory, copied to the device as stored (1-4 bytes per post), and
 // decoded, posed (DEM::makeVertexBuffer), triangulated (imageToIndexBuffer) and given vertex

@@ -129,6 +129,13 @@ class Camera:
     def z_dir(self) -> np.float32:
         return np.float32(-1.0 if self.blender_frame else 1.0)
 
+    @property
+    def intrinsics_z_dir(self) -> np.float32:
+        """The z_dir the intrinsic matrices are built with: Camera::initialize computes them before
+        it switches z_dir to -1 for the Blender frame (camera.ipp:131-138), so a camera initialized
+        once carries +1 in K and K^-1 and -1 only in its ray directions, behind test and mirror."""
+        return np.float32(1.0)
+
     def kinv(self) -> np.ndarray:
         """Inverse intrinsic matrix, FP32, through the C ABI (camera.ipp:1526-1568)."""
         lib = capi.load()
@@ -136,8 +143,23 @@ class Camera:
         W, H = self.resolution
         capi.check(lib.vgb_camera_intrinsics(self.focal_length, self.sensor_size[0], self.sensor_size[1], W, H,
                                              self.principal_point[0], self.principal_point[1], self.skew[0],
-                                             self.skew[1], self.z_dir, out), what="camera_intrinsics")
+                                             self.skew[1], self.intrinsics_z_dir, out), what="camera_intrinsics")
         return np.array(out[:], np.float32)
+
+    def intrinsic_matrix(self) -> np.ndarray:
+        """The rows of K, FP32 (camera.ipp:1526-1556): fx, kxy, px, kyx, fy, py with z_dir folded in."""
+        f32 = np.float32
+        W, H = self.resolution
+        kx = f32(f32(W) / f32(self.sensor_size[0]))
+        ky0 = f32(f32(H) / f32(self.sensor_size[1]))
+        px = f32(f32(W) / f32(2)) if np.isinf(self.principal_point[0]) else f32(self.principal_point[0])
+        py = f32(f32(H) / f32(2)) if np.isinf(self.principal_point[1]) else f32(self.principal_point[1])
+        zd = self.intrinsics_z_dir
+        ky = f32(zd * ky0)
+        fx = f32(f32(self.focal_length) * kx)
+        fy = f32(f32(self.focal_length) * ky)
+        return np.array([fx, f32(zd * f32(self.skew[0])), f32(zd * px), f32(zd * f32(self.skew[1])), fy,
+                         f32(zd * py)], np.float32)
 
     def aperture_area(self) -> np.float32:
         """CircularAperture::getArea after Camera::initialize (aperture.ipp:25-31)."""
@@ -178,6 +200,55 @@ class Mesh:
     normals: np.ndarray | None = None      # (n, 3) float32; computed by Mesh::init when absent
     albedo_map: np.ndarray | None = None   # (h, w, B) float32 material albedo texture
     smooth_shading: bool = False
+    quipu: object = None                   # DEMQuipu the mesh's LoDs come from (Mesh::hasQuipu_)
+    target_gsd: float = math.inf           # set by the level-of-detail manager
+
+    # --- level of detail (mesh.ipp:86-113 and the queries lod_manager.ipp reads)
+    @staticmethod
+    def from_quipu(path, nbands: int = 1, options=None, required_gsd: float | None = None,
+                   gpu: int = 0) -> "Mesh":
+        """A mesh whose vertices come from a DEM Quipu file: the LoD for `required_gsd` (the
+        reader's default GSD when None), read into a mesh on GPU `gpu`."""
+        from .quipu import DEMQuipu
+
+        q = DEMQuipu(path, options, nbands=nbands)
+        m = q.read_buffers(required_gsd, gpu=gpu, nbands=nbands)
+        m.quipu = q
+        return m
+
+    def gsd(self) -> float:
+        """Mesh::getGSD: the GSD of the loaded LoD (0 without a Quipu)."""
+        return float(self.quipu.current_gsd) if self.quipu is not None else 0.0
+
+    def normal(self) -> np.ndarray:
+        """Mesh::getNormal: the Quipu's normal cone axis (+z without one)."""
+        if self.quipu is not None:
+            return np.asarray(self.quipu.normal, np.float64)
+        return np.array([0.0, 0.0, 1.0])
+
+    def cone_angle(self) -> float:
+        return float(self.quipu.cone_angle) if self.quipu is not None else math.pi
+
+    def aabb(self):
+        """Mesh::getAABB over the finite vertices."""
+        p = self.positions[np.isfinite(self.positions).all(axis=1)]
+        return p.min(axis=0).astype(np.float64), p.max(axis=0).astype(np.float64)
+
+    def update_gsd(self, target_gsd: float, gpu: int = 0) -> bool:
+        """Mesh::updateGSD: reloads the vertices from the Quipu LoD for the target GSD (the default
+        GSD for +inf).  Returns whether the mesh changed."""
+        q = self.quipu
+        if q is None:
+            return False
+        t = q.default_gsd if math.isinf(target_gsd) else target_gsd
+        if t == q.current_gsd:
+            return False
+        m = q.read_buffers(t, gpu=gpu, nbands=q.nbands)
+        if m is None:
+            return False
+        self.positions, self.indices, self.albedo, self.normals = m.positions, m.indices, m.albedo, m.normals
+        self.uv = None
+        return True
 
     def set_smooth_shading(self, on: bool):
         self.smooth_shading = bool(on)
@@ -404,6 +475,71 @@ class PathTracer:
         return rp
 
 
+class Rasterizer:
+    """GPU replacement of CPURasterizer (cpu_rasterizer.hpp:18-36): ``render(camera, scene)`` fills
+    ``render_passes`` (torch CUDA planes) through vgb_rasterize.  triangle_id counts from 1 within
+    each instance, as the reference's loop does; alpha is +inf where a triangle was drawn (the
+    reference's count / sample with sample 0)."""
+
+    def __init__(self):
+        self.render_passes = RenderPasses()
+        self.last_stats = None
+
+    def render(self, camera: Camera, scene: "Scene"):
+        import torch
+
+        scene.build_tlas()
+        ctx = scene.context()
+        lib = capi.load()
+        W, H = camera.resolution
+        B = scene.bands.size
+        dev = torch.device("cuda", scene.device)
+        cam = camera.to_c(scene.origin, B)
+        lights, nl = scene.c_lights()
+        o = capi.RasterOptions()
+        o.intrinsic[:] = [float(x) for x in camera.intrinsic_matrix()]
+        rp = self.render_passes
+        o.simulate_lighting = 1 if rp.simulate_lighting else 0
+        o.smooth_shading = 1 if scene.smooth_shading() else 0
+        o.nbands = B
+        rp.depth = torch.empty((H, W), dtype=torch.float32, device=dev)
+        rp.alpha = torch.empty((H, W), dtype=torch.float32, device=dev)
+        rp.albedo = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+        rp.normal_global = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+        rp.triangle_id = torch.empty((H, W), dtype=torch.int32, device=dev)
+        omega = None
+        if rp.simulate_lighting:
+            omega = scene.pixel_solid_angle(camera, cam)
+            for name in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power"):
+                setattr(rp, name, torch.empty((B, H, W), dtype=torch.float32, device=dev))
+        else:
+            rp.total_radiance = rp.direct_radiance = rp.indirect_radiance = rp.received_power = None
+        f = capi.Film()
+        for name in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo",
+                     "normal_global", "depth", "alpha", "triangle_id"):
+            setattr(f, name, capi.ptr(getattr(rp, name)))
+        f.pixel_solid_angle = capi.ptr(omega)
+        f.on_device = 1
+        torch.cuda.current_stream(dev).synchronize()
+        capi.check(lib.vgb_rasterize(ctx, C.byref(cam), lights, nl, C.byref(o), C.byref(f)), ctx, "rasterize")
+        st = capi.Stats()
+        lib.vgb_get_stats(ctx, C.byref(st))
+        self.last_stats = st
+        # triangle ids restart at 1 for every instance (cpu_rasterizer.ipp:70-72)
+        counts = [n for (_, _, n) in scene.flat["tri_offsets"]]
+        if len(counts) > 1:
+            starts = torch.tensor(np.cumsum([0] + counts[:-1]), dtype=torch.int64, device=dev)
+            tid = rp.triangle_id.to(torch.int64)
+            hit = tid != -1
+            k = torch.searchsorted(starts, (tid - 1).clamp(min=0), right=True) - 1
+            rp.triangle_id = torch.where(hit, tid - starts[k], tid).to(torch.int32)
+        if rp.received_power is not None and camera.sensor.psf is not None:
+            from .sensor import psf_convolve
+
+            psf_convolve(scene, rp.received_power, camera.psf_kernel(scene.bands))   # cpu_rasterizer.ipp:264-270
+        return rp
+
+
 @dataclass
 class BatchFrame:
     """One frame of a batched render: its camera, samples per pixel, RNG frame key and, optionally,
@@ -434,6 +570,10 @@ class Scene:
         self.ambient = None
         self.background = np.zeros(bands.size, np.float32)
         self.pathtracer = PathTracer()
+        self.rasterizer = Rasterizer()
+        from .lod import LevelOfDetailManager
+
+        self.lod_manager = LevelOfDetailManager()
         self.bvh_options = capi.BvhOptions(0, 0, 0, 0)
         self._ctx = None
         self._dirty = True
@@ -712,6 +852,21 @@ class Scene:
         return om
 
     # --- renders (scene.ipp:840-915)
+    def update_level_of_detail(self, camera_id) -> int:
+        """Scene::updateLevelOfDetail: the LoD manager's update for this camera (lod_manager.ipp:24-30)."""
+        return self.lod_manager.update(self[camera_id], self)
+
+    def rasterize_render(self, camera_id):
+        """Scene::rasterizeRender (scene.ipp:857-862): rasterizes, then simulates the camera's
+        sensor on the received power."""
+        from .sensor import simulate_sensor
+
+        cam = self[camera_id]
+        rp = self.rasterizer.render(cam, self)
+        if rp.received_power is None:
+            raise ValueError("rasterize_render needs rasterizer.render_passes.simulate_lighting")
+        return simulate_sensor(self, rp.received_power, cam.sensor)
+
     def pathtrace_render(self, camera_id):
         """Scene::pathtraceRender (scene.ipp:840-845): renders, then simulates the camera's sensor
         on the received power; returns the [H][W] image in 0..1 (torch CUDA tensor)."""
