@@ -73,6 +73,7 @@ def parse():
     ap.add_argument("--no-after-film", action="store_true", help="skip the denoiser / PSF / sensor line item")
     ap.add_argument("--no-quipu", action="store_true", help="skip the DEM Quipu ingestion line item")
     ap.add_argument("--no-raster", action="store_true", help="skip the rasterizer line item")
+    ap.add_argument("--no-bvh", action="store_true", help="skip the BVH build line item")
     return ap.parse_args()
 
 
@@ -396,6 +397,9 @@ def run_ours(args, p, rank, world, local_rank):
     raster = None
     if not args.no_raster and p["kind"] == "path_traced" and rank == 0:
         raster = raster_item(torch, dev, scene, cam_id, cpu=not args.no_cpu_baseline)
+    bvh = None
+    if not args.no_bvh and p["kind"] == "path_traced" and rank == 0 and args.layout == 2:
+        bvh = bvh_item(torch, dev, scene, cam_id)
     quipu = None
     if not args.no_quipu and p["kind"] == "path_traced" and rank == 0:
         quipu = quipu_item(torch, dev, peak, cpu=not args.no_cpu_baseline)
@@ -470,6 +474,8 @@ def run_ours(args, p, rank, world, local_rank):
             line["quipu_ingest"] = quipu
         if raster is not None:
             line["raster"] = raster
+        if bvh is not None:
+            line["bvh_build"] = bvh
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))
@@ -607,6 +613,32 @@ def adjoint_item(torch, dev, layout=2, reps=2):
            "grad_norm": {"texture": float(gt.double().norm()), "heights": float(gz.double().norm())},
            "timing": "wall clock over all views (blocking C-ABI calls), best of %d" % reps}
     scene.close()
+    return out
+
+
+def bvh_item(torch, dev, scene, cam_id):
+    """BVH build of the path-traced frame's 33.5M triangles: the host binned-SAH builder (all host
+    threads) against the GPU linear BVH (builder 1), and one render of the frame with each tree
+    (the closest hits are the same; the traversal work differs)."""
+    from vira_gb300 import capi
+
+    lib = capi.load()
+    ctx = scene.context()
+    out = {}
+    for name, builder in (("host_sah", 0), ("gpu_lbvh", 1)):
+        o = capi.BvhOptions(0, builder, 0, 2)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        capi.check(lib.vgb_bvh_build(ctx, C.byref(o)), ctx, "bvh_build")
+        torch.cuda.synchronize(dev)
+        build_s = time.perf_counter() - t0
+        scene.pathtracer.render(scene[cam_id], scene)
+        st = scene.pathtracer.last_stats
+        out[name] = {"build_s": build_s, "nodes": int(st.bvh_nodes), "render_ms": float(st.ms_last),
+                     "mrays_s": (st.rays_closest + st.rays_shadow) / (st.ms_last / 1e3) / 1e6}
+    out["build_speedup"] = out["host_sah"]["build_s"] / out["gpu_lbvh"]["build_s"]
+    out["timing"] = "wall clock around the blocking build call; render: CUDA events of one render"
+    capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 0, 0, 2))), ctx, "bvh_build")
     return out
 
 

@@ -144,7 +144,10 @@ typedef struct vgb_film {
 /* ---- BVH build options -------------------------------------------------------- */
 typedef struct vgb_bvh_options {
     uint32_t max_leaf_size;    /* triangles per leaf: 1..8 (binary), 1..3 (8-wide); 0 = default */
-    uint32_t builder;          /* 0 = binned SAH (host, threaded) */
+    uint32_t builder;          /* 0 = binned SAH (host, threaded); 1 = linear BVH on the GPU (30-bit Morton
+                                  order, Karras's hierarchy, ranges of <= max_leaf_size triangles as leaves;
+                                  binary layout only; seconds -> milliseconds at tens of millions of
+                                  triangles, at some traversal speed) */
     uint32_t threads;          /* host threads for the build; 0 = all */
     uint32_t layout;           /* device node layout: 2 = binary (default, 0), 8 = compressed 8-wide */
 } vgb_bvh_options;

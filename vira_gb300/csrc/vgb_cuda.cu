@@ -1475,8 +1475,46 @@ VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) 
     if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "bvh_build: no scene uploaded");
     uint32_t leaf = opts ? opts->max_leaf_size : 0, threads = opts ? opts->threads : 0;
     uint32_t layout = (opts && opts->layout) ? opts->layout : 2;
-    if (opts && opts->builder != 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: unknown builder");
+    if (opts && opts->builder > 1) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: unknown builder");
     if (layout != 2 && layout != 8) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: layout must be 2 or 8");
+    if (opts && opts->builder == 1 && layout != 2)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: the GPU builder writes the binary layout");
+    if (leaf > (layout == 8 ? vgb::kMaxLeaf8 : vgb::kMaxLeaf))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8 (binary) or <= 3 (8-wide)");
+    if (opts && opts->builder == 1 && ctx->ntris > (leaf ? leaf : 4u)) {
+        // GPU linear BVH (binary layout), from the device vertices; a scene that fits one leaf
+        // takes the host path below
+        if (leaf == 0) leaf = 4;
+        const uint32_t n = ctx->ntris;
+        if ((uint64_t)n >= (1ull << (31 - vgb::kLeafShift)))
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: too many triangles for the leaf encoding");
+        cudaSetDevice(ctx->device);
+        CK(cudaStreamSynchronize(ctx->stream));
+        free_bvh(ctx);
+        vgb_status s;
+        uint32_t nn = 0;
+        if ((s = ensure_dn_scratch(ctx, vgb::lbvh_work_words(n))) != VGB_OK) return s;
+        CK((cudaError_t)vgb::launch_lbvh_sort_and_link(ctx->stream, ctx->num_sms, ctx->d_vpos, ctx->d_idx, n, leaf,
+                                                       reinterpret_cast<uint32_t*>(ctx->d_dn), &nn));
+        if ((s = dalloc(ctx, &ctx->d_nodes, (size_t)nn * 64)) != VGB_OK) return s;
+        if ((s = dalloc(ctx, &ctx->d_tris, (size_t)n * 48)) != VGB_OK) return s;
+        if ((s = dalloc(ctx, &ctx->d_parent, (size_t)nn * 4)) != VGB_OK) return s;
+        if ((s = dalloc(ctx, &ctx->d_refit, ((size_t)nn + 1) * 4)) != VGB_OK) return s;
+        const int rc = vgb::launch_lbvh_emit(ctx->stream, ctx->num_sms, ctx->d_vpos, ctx->d_idx, n, leaf,
+                                             reinterpret_cast<const uint32_t*>(ctx->d_dn),
+                                             reinterpret_cast<uint32_t*>(ctx->d_nodes), nn, ctx->d_tris, ctx->d_parent,
+                                             ctx->d_refit);
+        if (rc == -2) return fail(ctx, VGB_ERR_INTERNAL, "bvh_build: GPU build walk exceeded the tree depth");
+        CK((cudaError_t)rc);
+        ctx->nnodes = nn;
+        ctx->bvh_layout = 2;
+        ctx->bvh_leaf = leaf; ctx->bvh_threads = 0;
+        ctx->bvh_ready = true;
+        ctx->stats.bvh_nodes = nn;
+        ctx->stats.bvh_node_bytes = 64;
+        ctx->stats.tri_record_bytes = 48;
+        return VGB_OK;
+    }
     if (leaf > (layout == 8 ? vgb::kMaxLeaf8 : vgb::kMaxLeaf))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "bvh_build: max_leaf_size must be <= 8 (binary) or <= 3 (8-wide)");
     cudaSetDevice(ctx->device);

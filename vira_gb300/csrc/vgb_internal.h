@@ -99,6 +99,15 @@ int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, ui
                            float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out, float* nrm = nullptr);
 int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
                           float* out, uint32_t* work);
+// GPU build of the binary BVH (linear BVH, Morton order): sort and link into `work`
+// (lbvh_work_words), returning the number of nodes kept; then emit nodes, triangle records and
+// parents into arrays of that size and compute the boxes.  counts: nnodes + 1 words of scratch.
+size_t lbvh_work_words(uint32_t ntris);
+int launch_lbvh_sort_and_link(void* stream, int sms, const void* vpos, const uint32_t* idx, uint32_t ntris,
+                              uint32_t max_leaf, uint32_t* work, uint32_t* nkept_out);
+int launch_lbvh_emit(void* stream, int sms, const void* vpos, const uint32_t* idx, uint32_t ntris, uint32_t max_leaf,
+                     const uint32_t* work, uint32_t* nodes, uint32_t nnodes, void* tris, uint32_t* parent,
+                     uint32_t* counts);
 // Refit of the binary BVH after the vertices moved (same triangles): triangle records rewritten
 // from vpos, then every child box recomputed bottom up.  counts: nnodes words of scratch.
 // Returns nonzero on a CUDA error, -2 when an upward walk exceeded its bound.

@@ -445,3 +445,310 @@ int launch_refit(void* stream, int sms, const void* vpos, const uint32_t* idx, u
 }
 
 }  // namespace vgb
+
+// ---------------------------------------------------------------- GPU BVH build (binary layout)
+// Linear BVH after Karras (HPG 2012): triangles sorted by the 30-bit Morton code of their
+// centroid (ties by triangle index), internal nodes from the longest common prefixes of
+// neighbouring keys, every node a contiguous range of the sorted triangles.  Nodes whose range
+// holds at most `max_leaf` triangles become leaves of that range; the kept nodes are compacted
+// in Karras order (the root stays node 0), the triangle records are written in sorted order, and
+// the boxes come from the bottom-up refit.
+namespace {
+
+constexpr int kSortThreads = 256, kSortItems = 8, kSortTile = kSortThreads * kSortItems;
+
+__device__ __forceinline__ uint32_t ordered(float f) {   // float -> uint32 preserving order
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float unordered(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+__device__ __forceinline__ F3 centroid_of(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, size_t t) {
+    const F3 a = ld3(vpos[idx[3 * t]]), b = ld3(vpos[idx[3 * t + 1]]), c = ld3(vpos[idx[3 * t + 2]]);
+    return F3{(a.x + b.x + c.x) * (1.f / 3.f), (a.y + b.y + c.y) * (1.f / 3.f), (a.z + b.z + c.z) * (1.f / 3.f)};
+}
+
+// bounds of the finite centroids: lo[3], hi[3] as ordered uint32 (lo initialised to ~0, hi to 0)
+__global__ void k_centroid_bounds(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t n,
+                                  uint32_t* __restrict__ bounds) {
+    uint32_t lo[3] = {~0u, ~0u, ~0u}, hi[3] = {0u, 0u, 0u};
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const F3 c = centroid_of(vpos, idx, t);
+        const float v[3] = {c.x, c.y, c.z};
+        if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) continue;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { lo[k] = min(lo[k], ordered(v[k])); hi[k] = max(hi[k], ordered(v[k])); }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[k] = min(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+            hi[k] = max(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { atomicMin(&bounds[k], lo[k]); atomicMax(&bounds[3 + k], hi[k]); }
+    }
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {   // 10 bits -> every third bit
+    x &= 0x3FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void k_morton(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t n,
+                         const uint32_t* __restrict__ bounds, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    float lo[3], ext[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = bounds[k] == ~0u ? 0.f : unordered(bounds[k]);
+        const float h = bounds[k] == ~0u ? 0.f : unordered(bounds[3 + k]);
+        ext[k] = h - lo[k];
+    }
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const F3 c = centroid_of(vpos, idx, t);
+        const float v[3] = {c.x, c.y, c.z};
+        uint32_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float u = ext[k] > 0.f ? (v[k] - lo[k]) / ext[k] : 0.f;
+            const float s = u * 1024.f;
+            q[k] = (s >= 1023.f) ? 1023u : (s > 0.f ? (uint32_t)s : 0u);   // NaN -> 0
+        }
+        keys[t] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        vals[t] = (uint32_t)t;
+    }
+}
+
+// LSD radix sort, 8-bit digits: per-tile digit counts (digit-major over tiles) ...
+__global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t ntiles,
+                            uint32_t* __restrict__ counts) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const size_t base = (size_t)blockIdx.x * kSortTile;
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        const size_t i = base + (size_t)j * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFFu], 1u);
+    }
+    __syncthreads();
+    counts[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// ... then a stable scatter: within a tile each warp owns 256 consecutive keys (8 rounds of 32),
+// ranks come from __match_any_sync and per-warp running digit counts, warps are ordered by an
+// exclusive prefix over the warps, tiles by the scanned counts.
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keys,
+                                                               const uint32_t* __restrict__ vals, uint32_t n, int shift,
+                                                               uint32_t ntiles, const uint32_t* __restrict__ offsets,
+                                                               uint32_t* __restrict__ okeys, uint32_t* __restrict__ ovals) {
+    __shared__ uint32_t wcnt[kSortThreads / 32][256];
+    __shared__ uint32_t toff[256];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int d = lane; d < 256; d += 32) wcnt[w][d] = 0;
+    toff[threadIdx.x] = offsets[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    __syncwarp();
+    const size_t base = (size_t)blockIdx.x * kSortTile + (size_t)w * 32 * kSortItems;
+    const uint32_t lt = (1u << lane) - 1u;
+    uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
+    int dg[kSortItems];
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        const size_t i = base + (size_t)j * 32 + lane;
+        const bool ok = i < n;
+        k[j] = ok ? keys[i] : 0u;
+        v[j] = ok ? vals[i] : 0u;
+        dg[j] = ok ? (int)((k[j] >> shift) & 0xFFu) : 256 + lane;   // invalid lanes match only themselves
+        const uint32_t m = __match_any_sync(0xffffffffu, dg[j]);
+        const uint32_t lower = __popc(m & lt);
+        uint32_t b = 0;
+        if (ok) b = wcnt[w][dg[j]];
+        __syncwarp();
+        if (ok && lower == 0) wcnt[w][dg[j]] = b + (uint32_t)__popc(m);
+        __syncwarp();
+        rank[j] = b + lower;
+    }
+    __syncthreads();
+    {   // exclusive prefix over the warps, per digit
+        uint32_t run = 0;
+#pragma unroll
+        for (int ww = 0; ww < kSortThreads / 32; ++ww) {
+            const uint32_t c = wcnt[ww][threadIdx.x];
+            wcnt[ww][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSortItems; ++j) {
+        if (dg[j] >= 256) continue;
+        const uint32_t pos = toff[dg[j]] + wcnt[w][dg[j]] + rank[j];
+        okeys[pos] = k[j];
+        ovals[pos] = v[j];
+    }
+}
+
+__device__ __forceinline__ int lcp(const uint32_t* __restrict__ keys, uint32_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= (int64_t)n) return -1;
+    const uint32_t a = keys[i], b = keys[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+// Karras internal node i: its range [first, last] and split g (left child covers [first, g]).
+__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ first,
+                         uint32_t* __restrict__ last, uint32_t* __restrict__ split) {
+    for (size_t ii = (size_t)blockIdx.x * blockDim.x + threadIdx.x; ii + 1 < n; ii += (size_t)gridDim.x * blockDim.x) {
+        const int64_t i = (int64_t)ii;
+        const int d = (lcp(keys, n, i, i + 1) - lcp(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = lcp(keys, n, i, i - d);
+        int64_t lmax = 2;
+        while (lcp(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+        int64_t l = 0;
+        for (int64_t t = lmax / 2; t >= 1; t /= 2)
+            if (lcp(keys, n, i, i + (l + t) * d) > dmin) l += t;
+        const int64_t j = i + l * d;
+        const int dnode = lcp(keys, n, i, j);
+        int64_t s = 0;
+        for (int64_t div = 2;; div *= 2) {
+            const int64_t t = (l + div - 1) / div;
+            if (lcp(keys, n, i, i + (s + t) * d) > dnode) s += t;
+            if (t == 1) break;
+        }
+        const int64_t g = i + s * d + (d < 0 ? -1 : 0);
+        first[i] = (uint32_t)(i < j ? i : j);
+        last[i] = (uint32_t)(i < j ? j : i);
+        split[i] = (uint32_t)g;
+    }
+}
+
+__global__ void k_lbvh_keep(const uint32_t* __restrict__ first, const uint32_t* __restrict__ last, uint32_t n,
+                            uint32_t max_leaf, uint32_t* __restrict__ kept) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i + 1 < n; i += (size_t)gridDim.x * blockDim.x)
+        kept[i] = (last[i] - first[i] + 1u > max_leaf) ? 1u : 0u;
+}
+
+__global__ void k_lbvh_emit(const uint32_t* __restrict__ first, const uint32_t* __restrict__ last,
+                            const uint32_t* __restrict__ split, const uint32_t* __restrict__ kept,
+                            const uint32_t* __restrict__ newidx, uint32_t n, uint32_t max_leaf,
+                            uint32_t* __restrict__ nodes, uint32_t* __restrict__ parent) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i + 1 < n; i += (size_t)gridDim.x * blockDim.x) {
+        if (!kept[i]) continue;
+        const uint32_t me = newidx[i], g = split[i];
+        const uint32_t cf[2] = {first[i], g + 1u}, cl[2] = {g, last[i]};
+        uint32_t* nd = nodes + 16 * (size_t)me;
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t cnt = cl[s] - cf[s] + 1u;
+            int32_t link;
+            if (cnt <= max_leaf) {
+                link = ~(int32_t)((cf[s] << vgb::kLeafShift) | (cnt - 1u));
+            } else {
+                const uint32_t c = newidx[g + (uint32_t)s];   // the child is internal node g (left) or g + 1 (right)
+                link = (int32_t)c;
+                parent[c] = (me << 1) | (uint32_t)s;
+            }
+            nd[12 + s] = (uint32_t)link;
+        }
+        nd[14] = nd[15] = 0u;
+        if (i == 0) parent[me] = vgb::kNoParent;
+    }
+}
+
+__global__ void k_lbvh_tris(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx,
+                            const uint32_t* __restrict__ order, uint32_t n, float4* __restrict__ tris) {
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t t = order[r];
+        const float4 a = vpos[idx[3 * (size_t)t]], b = vpos[idx[3 * (size_t)t + 1]], c = vpos[idx[3 * (size_t)t + 2]];
+        tris[3 * r] = make_float4(a.x, a.y, a.z, __uint_as_float(t));
+        tris[3 * r + 1] = make_float4(b.x, b.y, b.z, 0.f);
+        tris[3 * r + 2] = make_float4(c.x, c.y, c.z, 0.f);
+    }
+}
+
+}  // namespace
+
+namespace vgb {
+
+size_t lbvh_work_words(uint32_t n) {
+    const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
+    return 4 * (size_t)n /* keys, vals x2 */ + 2 * 256 * tiles /* counts, offsets */ + scan_temp_words(256 * tiles) +
+           3 * (size_t)n /* first, last, split */ + 2 * ((size_t)n + 1) /* kept, newidx */ +
+           scan_temp_words((size_t)n + 1) + 8 /* bounds */;
+}
+
+int launch_lbvh_sort_and_link(void* stream, int sms, const void* vpos_, const uint32_t* idx, uint32_t n,
+                              uint32_t max_leaf, uint32_t* work, uint32_t* nkept_out) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const float4* vpos = (const float4*)vpos_;
+    const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
+    uint32_t* keys = work;
+    uint32_t* vals = keys + n;
+    uint32_t* keys2 = vals + n;
+    uint32_t* vals2 = keys2 + n;
+    uint32_t* counts = vals2 + n;
+    uint32_t* offs = counts + 256 * tiles;
+    uint32_t* stmp = offs + 256 * tiles;
+    uint32_t* first = stmp + scan_temp_words(256 * tiles);
+    uint32_t* last = first + n;
+    uint32_t* split = last + n;
+    uint32_t* kept = split + n;
+    uint32_t* newidx = kept + n + 1;
+    uint32_t* ktmp = newidx + n + 1;
+    uint32_t* bounds = ktmp + scan_temp_words((size_t)n + 1);
+    const uint32_t init[6] = {~0u, ~0u, ~0u, 0u, 0u, 0u};
+    cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    k_centroid_bounds<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, bounds);
+    k_morton<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, bounds, keys, vals);
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 8 * pass;
+        k_sort_hist<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, n, shift, (uint32_t)tiles, counts);
+        scan(s, counts, offs, 256 * tiles, stmp);
+        k_sort_scatter<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, vals, n, shift, (uint32_t)tiles, offs, keys2, vals2);
+        std::swap(keys, keys2);
+        std::swap(vals, vals2);
+    }
+    // after four passes the sorted keys and order are back in the first two arrays
+    k_karras<<<grid(n, sms), 256, 0, s>>>(keys, n, first, last, split);
+    k_lbvh_keep<<<grid(n, sms), 256, 0, s>>>(first, last, n, max_leaf, kept);
+    cudaMemsetAsync(kept + (n - 1), 0, 2 * sizeof(uint32_t), s);
+    scan(s, kept, newidx, (size_t)n, ktmp);   // newidx[n - 1] = number kept
+    cudaMemcpyAsync(nkept_out, newidx + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    return e != cudaSuccess ? (int)e : (int)cudaGetLastError();
+}
+
+int launch_lbvh_emit(void* stream, int sms, const void* vpos, const uint32_t* idx, uint32_t n, uint32_t max_leaf,
+                     const uint32_t* work, uint32_t* nodes, uint32_t nnodes, void* tris, uint32_t* parent,
+                     uint32_t* counts) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
+    const uint32_t* vals = work + n;
+    const uint32_t* first = work + 4 * (size_t)n + 2 * 256 * tiles + scan_temp_words(256 * tiles);
+    const uint32_t* last = first + n;
+    const uint32_t* split = last + n;
+    const uint32_t* kept = split + n;
+    const uint32_t* newidx = kept + n + 1;
+    k_lbvh_tris<<<grid(n, sms), 256, 0, s>>>((const float4*)vpos, idx, vals, n, (float4*)tris);
+    k_lbvh_emit<<<grid(n, sms), 256, 0, s>>>(first, last, split, kept, newidx, n, max_leaf, nodes, parent);
+    // boxes: the refit over the new topology (triangle records are already in place)
+    uint32_t* flag = counts + nnodes;
+    cudaMemsetAsync(counts, 0, ((size_t)nnodes + 1) * sizeof(uint32_t), s);
+    k_refit_nodes<<<grid(2 * (size_t)nnodes, sms), 256, 0, s>>>((const float4*)tris, nodes, nnodes, parent, counts,
+                                                                 4096u, flag);
+    uint32_t bad = 0;
+    cudaMemcpyAsync(&bad, flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int)e;
+    return bad ? -2 : (int)cudaGetLastError();
+}
+
+}  // namespace vgb
