@@ -448,7 +448,7 @@ int launch_refit(void* stream, int sms, const void* vpos, const uint32_t* idx, u
 
 // ---------------------------------------------------------------- GPU BVH build (binary layout)
 // Linear BVH after Karras (HPG 2012): triangles sorted by the 30-bit Morton code of their
-// centroid (ties by triangle index), internal nodes from the longest common prefixes of
+// centroid in the scene's bounding cube (ties by triangle index), internal nodes from the longest common prefixes of
 // neighbouring keys, every node a contiguous range of the sorted triangles.  Nodes whose range
 // holds at most `max_leaf` triangles become leaves of that range; the kept nodes are compacted
 // in Karras order (the root stays node 0), the triangle records are written in sorted order, and
@@ -505,13 +505,17 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {   // 10 bits -> every
 
 __global__ void k_morton(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t n,
                          const uint32_t* __restrict__ bounds, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
-    float lo[3], ext[3];
+    // one scale for all three axes (the largest extent): a flat terrain's heights then take few
+    // of the code's bits instead of a third of them, so the splits stay mostly horizontal
+    float lo[3], ext[3], emax = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         lo[k] = bounds[k] == ~0u ? 0.f : unordered(bounds[k]);
         const float h = bounds[k] == ~0u ? 0.f : unordered(bounds[3 + k]);
-        ext[k] = h - lo[k];
+        emax = fmaxf(emax, h - lo[k]);
     }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ext[k] = emax;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
         const F3 c = centroid_of(vpos, idx, t);
         const float v[3] = {c.x, c.y, c.z};
