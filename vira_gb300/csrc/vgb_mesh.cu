@@ -370,6 +370,12 @@ __global__ void k_refit_tris(const float4* __restrict__ vpos, const uint32_t* __
 
 struct RBox { float lx, hx, ly, hy, lz, hz; };
 
+__device__ __forceinline__ uint32_t atomic_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ void put_box(uint32_t* nodes, uint32_t node, int side, const RBox& b) {
     uint32_t* n = nodes + 16 * (size_t)node;
     const int o = side ? 4 : 0;
@@ -410,9 +416,9 @@ __global__ void k_refit_nodes(const float4* __restrict__ tris, uint32_t* nodes, 
             }
         put_box(nodes, node, side, b);
         for (uint32_t step = 0;; ++step) {
-            __threadfence();
-            if (atomicAdd(&counts[node], 1u) == 0u) break;  // the other side is not done yet
-            __threadfence();
+            // release: this side's box is visible before the count; acquire: the other side's is
+            // visible to the second arrival
+            if (atomic_add_acq_rel(&counts[node], 1u) == 0u) break;  // the other side is not done yet
             if (step >= cap) { atomicOr(flag, 1u); break; }
             const RBox a = get_box(nodes, node, 0), c = get_box(nodes, node, 1);
             const RBox u{fminf(a.lx, c.lx), fmaxf(a.hx, c.hx), fminf(a.ly, c.ly),
@@ -447,7 +453,7 @@ int launch_refit(void* stream, int sms, const void* vpos, const uint32_t* idx, u
 }  // namespace vgb
 
 // ---------------------------------------------------------------- GPU BVH build (binary layout)
-// Linear BVH after Karras (HPG 2012): triangles sorted by the 30-bit Morton code of their
+// Linear BVH after Karras (HPG 2012): triangles sorted by the 63-bit Morton code of their
 // centroid in the scene's bounding cube (ties by triangle index), internal nodes from the longest common prefixes of
 // neighbouring keys, every node a contiguous range of the sorted triangles.  Nodes whose range
 // holds at most `max_leaf` triangles become leaves of that range; the kept nodes are compacted
@@ -494,17 +500,20 @@ __global__ void k_centroid_bounds(const float4* __restrict__ vpos, const uint32_
     }
 }
 
-__device__ __forceinline__ uint32_t spread10(uint32_t x) {   // 10 bits -> every third bit
-    x &= 0x3FFu;
-    x = (x | (x << 16)) & 0x030000FFu;
-    x = (x | (x << 8)) & 0x0300F00Fu;
-    x = (x | (x << 4)) & 0x030C30C3u;
-    x = (x | (x << 2)) & 0x09249249u;
+using MKey = unsigned long long;
+
+__device__ __forceinline__ MKey spread21(uint32_t v) {   // 21 bits -> every third bit of 63
+    MKey x = v & 0x1FFFFFull;
+    x = (x | (x << 32)) & 0x1F00000000FFFFull;
+    x = (x | (x << 16)) & 0x1F0000FF0000FFull;
+    x = (x | (x << 8)) & 0x100F00F00F00F00Full;
+    x = (x | (x << 4)) & 0x10C30C30C30C30C3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
     return x;
 }
 
 __global__ void k_morton(const float4* __restrict__ vpos, const uint32_t* __restrict__ idx, uint32_t n,
-                         const uint32_t* __restrict__ bounds, uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+                         const uint32_t* __restrict__ bounds, MKey* __restrict__ keys, uint32_t* __restrict__ vals) {
     // one scale for all three axes (the largest extent): a flat terrain's heights then take few
     // of the code's bits instead of a third of them, so the splits stay mostly horizontal
     float lo[3], ext[3], emax = 0.f;
@@ -523,16 +532,16 @@ __global__ void k_morton(const float4* __restrict__ vpos, const uint32_t* __rest
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const float u = ext[k] > 0.f ? (v[k] - lo[k]) / ext[k] : 0.f;
-            const float s = u * 1024.f;
-            q[k] = (s >= 1023.f) ? 1023u : (s > 0.f ? (uint32_t)s : 0u);   // NaN -> 0
+            const float sc = u * 2097152.f;
+            q[k] = (sc >= 2097151.f) ? 2097151u : (sc > 0.f ? (uint32_t)sc : 0u);   // NaN -> 0
         }
-        keys[t] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+        keys[t] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
         vals[t] = (uint32_t)t;
     }
 }
 
 // LSD radix sort, 8-bit digits: per-tile digit counts (digit-major over tiles) ...
-__global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t ntiles,
+__global__ void k_sort_hist(const MKey* __restrict__ keys, uint32_t n, int shift, uint32_t ntiles,
                             uint32_t* __restrict__ counts) {
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
@@ -550,10 +559,10 @@ __global__ void k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n, int s
 // ... then a stable scatter: within a tile each warp owns 256 consecutive keys (8 rounds of 32),
 // ranks come from __match_any_sync and per-warp running digit counts, warps are ordered by an
 // exclusive prefix over the warps, tiles by the scanned counts.
-__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* __restrict__ keys,
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const MKey* __restrict__ keys,
                                                                const uint32_t* __restrict__ vals, uint32_t n, int shift,
                                                                uint32_t ntiles, const uint32_t* __restrict__ offsets,
-                                                               uint32_t* __restrict__ okeys, uint32_t* __restrict__ ovals) {
+                                                               MKey* __restrict__ okeys, uint32_t* __restrict__ ovals) {
     __shared__ uint32_t wcnt[kSortThreads / 32][256];
     __shared__ uint32_t toff[256];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -562,13 +571,14 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
     __syncwarp();
     const size_t base = (size_t)blockIdx.x * kSortTile + (size_t)w * 32 * kSortItems;
     const uint32_t lt = (1u << lane) - 1u;
-    uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
+    MKey k[kSortItems];
+    uint32_t v[kSortItems], rank[kSortItems];
     int dg[kSortItems];
 #pragma unroll
     for (int j = 0; j < kSortItems; ++j) {
         const size_t i = base + (size_t)j * 32 + lane;
         const bool ok = i < n;
-        k[j] = ok ? keys[i] : 0u;
+        k[j] = ok ? keys[i] : 0ull;
         v[j] = ok ? vals[i] : 0u;
         dg[j] = ok ? (int)((k[j] >> shift) & 0xFFu) : 256 + lane;   // invalid lanes match only themselves
         const uint32_t m = __match_any_sync(0xffffffffu, dg[j]);
@@ -600,15 +610,15 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(const uint32_t* _
     }
 }
 
-__device__ __forceinline__ int lcp(const uint32_t* __restrict__ keys, uint32_t n, int64_t i, int64_t j) {
+__device__ __forceinline__ int lcp(const MKey* __restrict__ keys, uint32_t n, int64_t i, int64_t j) {
     if (j < 0 || j >= (int64_t)n) return -1;
-    const uint32_t a = keys[i], b = keys[j];
-    if (a != b) return __clz(a ^ b);
-    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    const MKey a = keys[i], b = keys[j];
+    if (a != b) return __clzll((long long)(a ^ b));
+    return 64 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
 // Karras internal node i: its range [first, last] and split g (left child covers [first, g]).
-__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ first,
+__global__ void k_karras(const MKey* __restrict__ keys, uint32_t n, uint32_t* __restrict__ first,
                          uint32_t* __restrict__ last, uint32_t* __restrict__ split) {
     for (size_t ii = (size_t)blockIdx.x * blockDim.x + threadIdx.x; ii + 1 < n; ii += (size_t)gridDim.x * blockDim.x) {
         const int64_t i = (int64_t)ii;
@@ -682,50 +692,58 @@ __global__ void k_lbvh_tris(const float4* __restrict__ vpos, const uint32_t* __r
 
 namespace vgb {
 
-size_t lbvh_work_words(uint32_t n) {
+// work: keys (64-bit) x2, triangle order x2, tile digit counts and their scan, Karras ranges and
+// splits, kept flags and their scan, centroid bounds
+struct LbvhWork {
+    MKey *keys, *keys2;
+    uint32_t *vals, *vals2, *counts, *offs, *stmp, *first, *last, *split, *kept, *newidx, *ktmp, *bounds;
+    size_t words;
+};
+
+LbvhWork lbvh_layout(uint32_t* w, uint32_t n) {
     const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
-    return 4 * (size_t)n /* keys, vals x2 */ + 2 * 256 * tiles /* counts, offsets */ + scan_temp_words(256 * tiles) +
-           3 * (size_t)n /* first, last, split */ + 2 * ((size_t)n + 1) /* kept, newidx */ +
-           scan_temp_words((size_t)n + 1) + 8 /* bounds */;
+    LbvhWork L;
+    size_t o = 0;
+    auto take = [&](size_t words) { uint32_t* p = w ? w + o : nullptr; o += (words + 1) & ~(size_t)1; return p; };
+    L.keys = reinterpret_cast<MKey*>(take(2 * (size_t)n));
+    L.keys2 = reinterpret_cast<MKey*>(take(2 * (size_t)n));
+    L.vals = take(n); L.vals2 = take(n);
+    L.counts = take(256 * tiles); L.offs = take(256 * tiles); L.stmp = take(scan_temp_words(256 * tiles));
+    L.first = take(n); L.last = take(n); L.split = take(n);
+    L.kept = take((size_t)n + 1); L.newidx = take((size_t)n + 1); L.ktmp = take(scan_temp_words((size_t)n + 1));
+    L.bounds = take(8);
+    L.words = o;
+    return L;
 }
+
+size_t lbvh_work_words(uint32_t n) { return lbvh_layout(nullptr, n).words; }
 
 int launch_lbvh_sort_and_link(void* stream, int sms, const void* vpos_, const uint32_t* idx, uint32_t n,
                               uint32_t max_leaf, uint32_t* work, uint32_t* nkept_out) {
     cudaStream_t s = (cudaStream_t)stream;
     const float4* vpos = (const float4*)vpos_;
     const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
-    uint32_t* keys = work;
-    uint32_t* vals = keys + n;
-    uint32_t* keys2 = vals + n;
-    uint32_t* vals2 = keys2 + n;
-    uint32_t* counts = vals2 + n;
-    uint32_t* offs = counts + 256 * tiles;
-    uint32_t* stmp = offs + 256 * tiles;
-    uint32_t* first = stmp + scan_temp_words(256 * tiles);
-    uint32_t* last = first + n;
-    uint32_t* split = last + n;
-    uint32_t* kept = split + n;
-    uint32_t* newidx = kept + n + 1;
-    uint32_t* ktmp = newidx + n + 1;
-    uint32_t* bounds = ktmp + scan_temp_words((size_t)n + 1);
+    LbvhWork L = lbvh_layout(work, n);
     const uint32_t init[6] = {~0u, ~0u, ~0u, 0u, 0u, 0u};
-    cudaMemcpyAsync(bounds, init, sizeof(init), cudaMemcpyHostToDevice, s);
-    k_centroid_bounds<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, bounds);
-    k_morton<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, bounds, keys, vals);
-    for (int pass = 0; pass < 4; ++pass) {
+    cudaMemcpyAsync(L.bounds, init, sizeof(init), cudaMemcpyHostToDevice, s);
+    k_centroid_bounds<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, L.bounds);
+    k_morton<<<grid(n, sms), 256, 0, s>>>(vpos, idx, n, L.bounds, L.keys, L.vals);
+    MKey *keys = L.keys, *keys2 = L.keys2;
+    uint32_t *vals = L.vals, *vals2 = L.vals2;
+    for (int pass = 0; pass < 8; ++pass) {
         const int shift = 8 * pass;
-        k_sort_hist<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, n, shift, (uint32_t)tiles, counts);
-        scan(s, counts, offs, 256 * tiles, stmp);
-        k_sort_scatter<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, vals, n, shift, (uint32_t)tiles, offs, keys2, vals2);
+        k_sort_hist<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, n, shift, (uint32_t)tiles, L.counts);
+        scan(s, L.counts, L.offs, 256 * tiles, L.stmp);
+        k_sort_scatter<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys, vals, n, shift, (uint32_t)tiles, L.offs, keys2, vals2);
         std::swap(keys, keys2);
         std::swap(vals, vals2);
     }
-    // after four passes the sorted keys and order are back in the first two arrays
-    k_karras<<<grid(n, sms), 256, 0, s>>>(keys, n, first, last, split);
-    k_lbvh_keep<<<grid(n, sms), 256, 0, s>>>(first, last, n, max_leaf, kept);
-    cudaMemsetAsync(kept + (n - 1), 0, 2 * sizeof(uint32_t), s);
-    scan(s, kept, newidx, (size_t)n, ktmp);   // newidx[n - 1] = number kept
-    cudaMemcpyAsync(nkept_out, newidx + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    // after eight passes the sorted keys and order are back in the first arrays
+    k_karras<<<grid(n, sms), 256, 0, s>>>(L.keys, n, L.first, L.last, L.split);
+    k_lbvh_keep<<<grid(n, sms), 256, 0, s>>>(L.first, L.last, n, max_leaf, L.kept);
+    cudaMemsetAsync(L.kept + (n - 1), 0, 2 * sizeof(uint32_t), s);
+    scan(s, L.kept, L.newidx, (size_t)n, L.ktmp);   // newidx[n - 1] = number kept
+    cudaMemcpyAsync(nkept_out, L.newidx + (n - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     return e != cudaSuccess ? (int)e : (int)cudaGetLastError();
 }
@@ -734,13 +752,9 @@ int launch_lbvh_emit(void* stream, int sms, const void* vpos, const uint32_t* id
                      const uint32_t* work, uint32_t* nodes, uint32_t nnodes, void* tris, uint32_t* parent,
                      uint32_t* counts) {
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t tiles = ((size_t)n + kSortTile - 1) / kSortTile;
-    const uint32_t* vals = work + n;
-    const uint32_t* first = work + 4 * (size_t)n + 2 * 256 * tiles + scan_temp_words(256 * tiles);
-    const uint32_t* last = first + n;
-    const uint32_t* split = last + n;
-    const uint32_t* kept = split + n;
-    const uint32_t* newidx = kept + n + 1;
+    const LbvhWork L = lbvh_layout(const_cast<uint32_t*>(work), n);
+    const uint32_t *vals = L.vals, *first = L.first, *last = L.last, *split = L.split, *kept = L.kept,
+                   *newidx = L.newidx;
     k_lbvh_tris<<<grid(n, sms), 256, 0, s>>>((const float4*)vpos, idx, vals, n, (float4*)tris);
     k_lbvh_emit<<<grid(n, sms), 256, 0, s>>>(first, last, split, kept, newidx, n, max_leaf, nodes, parent);
     // boxes: the refit over the new topology (triangle records are already in place)

@@ -5,6 +5,8 @@
     python -m vira_gb300.profile_cases adjoint        # k_adjoint: 2 views of a 513^2 crater DEM
     python -m vira_gb300.profile_cases after_film     # k_dn_*, k_psf, k_sensor on a 1024^2 frame
     python -m vira_gb300.profile_cases quipu          # k_quipu_decode, k_dem_*, normals: a 2049^2 LoD, twice
+    python -m vira_gb300.profile_cases raster         # k_raster_*: 8.4M triangles at 1024^2, 8 bands, twice
+    python -m vira_gb300.profile_cases lbvh           # GPU BVH build of 8.4M triangles twice, then one refit
 
 ``path`` renders the path-traced workload shrunk by ``scale`` (posts, texture and pixels; 4 spp)
 twice; the captures skip the launches of the first render.
@@ -75,8 +77,31 @@ def main(argv=None):
             torch.cuda.synchronize()
             print("quipu", int(out[1].shape[0]), "triangles")
             q.close()
+    elif kind in ("raster", "lbvh"):
+        import ctypes as C
+
+        from . import capi
+
+        scene, cam = workloads.path_traced(posts=2049, tex=2048, resolution=1024, spp=1)
+        scene.build_tlas()
+        if kind == "raster":
+            scene.rasterizer.render_passes.simulate_lighting = True
+            for _ in range(2):
+                scene.rasterizer.render(scene[cam], scene)
+            torch.cuda.synchronize()
+            print("raster", scene.rasterizer.last_stats.ms_last, "ms")
+        else:
+            lib = capi.load()
+            ctx = scene.context()
+            for _ in range(2):
+                capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 1, 0, 2))), ctx, "bvh_build")
+            p = scene.meshes[0].positions.copy()
+            p[:, 2] += 1.0
+            scene.update_positions(0, p)
+            torch.cuda.synchronize()
+            print("lbvh + refit done")
     else:
-        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint | after_film | quipu")
+        raise SystemExit(f"unknown case {kind!r}: path | batch | adjoint | after_film | quipu | raster | lbvh")
 
 
 if __name__ == "__main__":
