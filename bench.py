@@ -396,7 +396,7 @@ def run_ours(args, p, rank, world, local_rank):
         after_film = after_film_item(torch, dev, scene, cam_id, peak)
     raster = None
     if not args.no_raster and p["kind"] == "path_traced" and rank == 0:
-        raster = raster_item(torch, dev, scene, cam_id, cpu=not args.no_cpu_baseline)
+        raster = raster_item(torch, dev, scene, cam_id, peak, cpu=not args.no_cpu_baseline)
     bvh = None
     if not args.no_bvh and p["kind"] == "path_traced" and rank == 0 and args.layout == 2:
         bvh = bvh_item(torch, dev, scene, cam_id)
@@ -642,11 +642,16 @@ def bvh_item(torch, dev, scene, cam_id):
     return out
 
 
-def raster_item(torch, dev, scene, cam_id, reps=5, cpu=True):
+def raster_item(torch, dev, scene, cam_id, hbm_peak, reps=5, cpu=True):
     """The rasterizer (vgb_rasterize, CPURasterizer::render) with lighting on the path-traced
     frame's scene (33.5M triangles, 2048^2, 8 bands) and on the direct-lighting scene (0.52M
     triangles, 1024^2, 4 bands); the oracle's sequential restatement times the latter on one
-    host core."""
+    host core.  Unique bytes: per triangle its 3 indices and 3 vertex records (60 B), per pixel
+    the 8-byte fragment key, the solid angle and the written planes (depth, alpha, triangle id,
+    normal: 24 B; albedo, total, direct, indirect radiance and power: 20 B per band)."""
+
+    def unique(ntri, npix, nb):
+        return 60.0 * ntri + (8 + 4 + 24 + 20 * nb) * float(npix)
     from vira_gb300 import workloads
 
     def timed(sc, cid):
@@ -663,9 +668,11 @@ def raster_item(torch, dev, scene, cam_id, reps=5, cpu=True):
     ms, rp = timed(scene, cam_id)
     W, H = scene[cam_id].resolution
     ntri = int(scene.flat["indices"].shape[0])
+    gbs = unique(ntri, W * H, scene.bands.size) / (ms / 1e3) / 1e9
     out["path_traced_scene"] = {"triangles": ntri, "image": [W, H], "bands": scene.bands.size, "ms": ms,
                                 "mtris_per_s": ntri / ms / 1e3,
-                                "covered_pixels": int(torch.isfinite(rp.depth).sum().item())}
+                                "covered_pixels": int(torch.isfinite(rp.depth).sum().item()),
+                                "unique_gb_s": gbs, "frac_of_hbm": gbs / hbm_peak}
     small, cid = workloads.plain_direct(device=dev.index)
     ms2, rp2 = timed(small, cid)
     ntri2 = int(small.flat["indices"].shape[0])

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -881,6 +882,7 @@ struct vgb_context {
     uint32_t* d_refit = nullptr;    // nnodes + 1 words: arrival counters and the walk-bound flag
     uint32_t bvh_leaf = 0, bvh_threads = 0;
     bool h_pos_stale = false;       // device positions moved by a device-side update
+    uint32_t* d_vnl = nullptr;      // per-vertex corner lists of the uploaded mesh (vertex-normal updates)
     // render scratch
     size_t cap_P = 0;
     uint32_t cap_B = 0, cap_L = 0;
@@ -951,6 +953,8 @@ void dfree(void* p) { if (p) cudaFree(p); }
 void free_scene(vgb_context* ctx) {
     dfree(ctx->d_vpos); dfree(ctx->d_vnrm); dfree(ctx->d_vuv); dfree(ctx->d_valb); dfree(ctx->d_idx); dfree(ctx->d_tex);
     ctx->d_vpos = nullptr; ctx->d_vnrm = nullptr; ctx->d_vuv = nullptr; ctx->d_valb = nullptr; ctx->d_idx = nullptr; ctx->d_tex = nullptr;
+    dfree(ctx->d_vnl);
+    ctx->d_vnl = nullptr;
 }
 void free_bvh(vgb_context* ctx) {
     dfree(ctx->d_nodes); dfree(ctx->d_tris); dfree(ctx->d_parent); dfree(ctx->d_refit);
@@ -1667,9 +1671,19 @@ VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos
     if (!pos) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_update_positions: null positions");
     cudaSetDevice(ctx->device);
     const size_t nv = ctx->nverts, nt = ctx->ntris;
-    const size_t work = normals ? 0 : vgb::normals_work_words((uint32_t)nv, (uint32_t)nt);
-    const size_t stage = (on_device ? 0 : 3 * nv) + (normals && on_device ? 0 : 3 * nv);
     vgb_status s;
+    if (!normals && !ctx->d_vnl) {
+        // the corner lists of this topology, once per upload
+        if ((s = dalloc(ctx, &ctx->d_vnl, vgb::vertex_normal_list_words((uint32_t)nv, (uint32_t)nt) * 4)) != VGB_OK)
+            return s;
+        if ((s = ensure_dn_scratch(ctx, nv + vgb::scan_temp_words(nv + 1))) != VGB_OK) return s;
+        const int rc = vgb::launch_vertex_normal_lists(ctx->stream, ctx->num_sms, ctx->d_idx, (uint32_t)nv, (uint32_t)nt,
+                                                       ctx->d_vnl, reinterpret_cast<uint32_t*>(ctx->d_dn));
+        if (rc != 0) { dfree(ctx->d_vnl); ctx->d_vnl = nullptr; }
+        CK((cudaError_t)(rc == -1 ? (int)cudaErrorInvalidValue : rc));
+    }
+    const size_t work = normals ? 0 : (3 * nt + 3) & ~(size_t)3;   // face normals
+    const size_t stage = (on_device ? 0 : 3 * nv) + (normals && on_device ? 0 : 3 * nv);
     if ((s = ensure_dn_scratch(ctx, work + stage)) != VGB_OK) return s;
     float* cur = ctx->d_dn + work;
     const float* p = pos;
@@ -1682,9 +1696,8 @@ VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos
         CK(cudaMemcpyAsync(cur, normals, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
         n = cur;
     } else if (!normals) {
-        const int rc = vgb::launch_vertex_normals(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ctx->d_idx, (uint32_t)nt, cur,
-                                                  reinterpret_cast<uint32_t*>(ctx->d_dn));
-        CK((cudaError_t)rc);
+        CK((cudaError_t)vgb::launch_vertex_normals_listed(ctx->stream, ctx->num_sms, p, (uint32_t)nv, ctx->d_idx,
+                                                          (uint32_t)nt, ctx->d_vnl, ctx->d_dn, cur));
         n = cur;
     }
     k_pack_vertices<<<grid_for(ctx, nv, 8), 256, 0, ctx->stream>>>(p, n, (uint32_t)nv, ctx->d_vpos, ctx->d_vnrm);
@@ -2050,11 +2063,22 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
         ctx->cap_pin = pin_need;
     }
     uint8_t* hp = (uint8_t*)ctx->h_pin;
-    if (vgb::quipu_read_pixels(pl.path, pl.heights, hp) != VGB_OK)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
-    for (size_t c = 0; c < (plane_bytes ? pl.planes.size() : 0); ++c)
-        if (vgb::quipu_read_pixels(pl.path, pl.planes[c].img, hp + code_bytes + c * nv) != VGB_OK)
-            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, std::string("quipu_read_mesh: ") + vgb_quipu_last_error());
+    {
+        // every image is its own LZ4 block: the heights and the albedo planes decode in parallel
+        const size_t nimg = 1 + (plane_bytes ? pl.planes.size() : 0);
+        std::vector<std::string> errs(nimg);
+        auto read_one = [&](size_t k) {
+            const vgb::ImageRefView& img = k == 0 ? pl.heights : pl.planes[k - 1].img;
+            uint8_t* dst = k == 0 ? hp : hp + code_bytes + (k - 1) * nv;
+            if (vgb::quipu_read_pixels(pl.path, img, dst) != VGB_OK) errs[k] = vgb_quipu_last_error();
+        };
+        std::vector<std::thread> workers;
+        for (size_t k = 1; k < nimg; ++k) workers.emplace_back(read_one, k);
+        read_one(0);
+        for (std::thread& t : workers) t.join();
+        for (const std::string& e : errs)
+            if (!e.empty()) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: " + e);
+    }
     vgb::QuipuDecode d{};
     d.W = W; d.H = H; d.precision = pl.precision; d.nbands = nb;
     d.hmin = pl.hmin; d.hmax = pl.hmax;

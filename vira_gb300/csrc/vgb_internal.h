@@ -99,6 +99,16 @@ int launch_dem_triangulate(void* stream, int sms, const float* h, uint32_t W, ui
                            float* pos, uint32_t* idx, uint32_t* work, uint32_t* nt_out, float* nrm = nullptr);
 int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
                           float* out, uint32_t* work);
+// Vertex normals of a mesh whose topology stays while its vertices move: the per-vertex corner
+// lists (counts, offsets, corners: vertex_normal_list_words) are built once, `work` holding
+// nv + scan_temp_words(nv + 1) words; each evaluation then forms the face normals (fn: 3 nt
+// floats) and the ordered sums -- the same normals as launch_vertex_normals.
+size_t scan_temp_words(size_t n);   // scratch of the device exclusive scan of n words
+size_t vertex_normal_list_words(uint32_t nv, uint32_t nt);
+int launch_vertex_normal_lists(void* stream, int sms, const uint32_t* idx, uint32_t nv, uint32_t nt, uint32_t* lists,
+                               uint32_t* work);
+int launch_vertex_normals_listed(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                                 uint32_t* lists, float* fn, float* out);
 // GPU build of the binary BVH (linear BVH, Morton order): sort and link into `work`
 // (lbvh_work_words), returning the number of nodes kept; then emit nodes, triangle records and
 // parents into arrays of that size and compute the boxes.  counts: nnodes + 1 words of scratch.

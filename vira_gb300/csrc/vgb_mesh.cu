@@ -351,6 +351,46 @@ int launch_vertex_normals(void* stream, int sms, const float* pos, uint32_t nv, 
     return e != cudaSuccess ? (int)e : (int)cudaGetLastError();
 }
 
+size_t vertex_normal_list_words(uint32_t nv, uint32_t nt) { return 2 * ((size_t)nv + 1) + 3 * (size_t)nt; }
+
+int launch_vertex_normal_lists(void* stream, int sms, const uint32_t* idx, uint32_t nv, uint32_t nt, uint32_t* lists,
+                               uint32_t* work) {
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nc = 3 * (size_t)nt;
+    uint32_t* cnt = lists;
+    uint32_t* off = cnt + nv + 1;
+    uint32_t* list = off + nv + 1;
+    uint32_t* cur = work;
+    uint32_t* tmp = work + nv;
+    cudaMemsetAsync(cnt, 0, sizeof(uint32_t), s);
+    k_check_indices<<<grid(nc, sms), 256, 0, s>>>(idx, nc, nv, cnt);
+    uint32_t bad = 0;
+    cudaMemcpyAsync(&bad, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaError_t e0 = cudaStreamSynchronize(s);
+    if (e0 != cudaSuccess) return (int)e0;
+    if (bad) return -1;
+    cudaMemsetAsync(cnt, 0, ((size_t)nv + 1) * sizeof(uint32_t), s);
+    cudaMemsetAsync(cur, 0, (size_t)nv * sizeof(uint32_t), s);
+    k_corner_counts<<<grid(nc, sms), 256, 0, s>>>(idx, nc, cnt);
+    scan(s, cnt, off, (size_t)nv + 1, tmp);
+    k_corner_fill<<<grid(nc, sms), 256, 0, s>>>(idx, nc, off, cur, list);
+    cudaError_t e = cudaStreamSynchronize(s);
+    return e != cudaSuccess ? (int)e : (int)cudaGetLastError();
+}
+
+int launch_vertex_normals_listed(void* stream, int sms, const float* pos, uint32_t nv, const uint32_t* idx, uint32_t nt,
+                                 uint32_t* lists, float* fn, float* out) {
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* cnt = lists;
+    uint32_t* off = cnt + nv + 1;
+    uint32_t* list = off + nv + 1;
+    k_face_normals<<<grid(nt, sms), 256, 0, s>>>(pos, idx, nt, fn);
+    // the first call sorts each vertex's corners into face order in place; later calls find
+    // them sorted (one comparison per corner)
+    k_vertex_normals<<<grid(nv, sms), 256, 0, s>>>(fn, off, cnt, list, nv, out);
+    return (int)cudaGetLastError();
+}
+
 }  // namespace vgb
 
 // ---------------------------------------------------------------- BVH refit
