@@ -163,3 +163,36 @@ def test_rasterize_rejects_bad_arguments(gpu):
     assert b"nbands" in lib.vgb_last_error(ctx)
     s.close()
 
+
+
+def test_id_passes_and_camera_normals(gpu):
+    """Two instances side by side: instance_id / mesh_id / material_id of the first hit, triangle
+    ids local to each instance (from 0 for the path tracer, from 1 for the rasterizer), and the
+    rasterizer's normal in the camera frame (the inverse camera rotation times the normal)."""
+    import torch
+
+    s, cid = _dem_scene(posts=33, tex=16, cam_pos=(500.0, -900.0, 1400.0), target=(500.0, 0.0, 0.0))
+    inst = s.new_instance(("mesh", 0))
+    s[inst].position = np.array([1000.0, 0.0, 0.0])
+    s.pathtracer.render_passes.simulate_lighting = True
+    s.pathtracer.options.samples = 1
+    nt = s.meshes[0].indices.shape[0]
+    for renderer, first in ((s.pathtracer, 0), (s.rasterizer, 1)):
+        rp = renderer.render(s[cid], s)
+        torch.cuda.synchronize()
+        tid = rp.triangle_id.cpu().numpy()
+        iid = rp.instance_id.cpu().numpy()
+        hit = tid != -1
+        assert set(np.unique(iid[hit])) == {0, 1}                     # both instances seen
+        assert np.all(iid[~hit] == -1) and np.all(rp.mesh_id.cpu().numpy()[hit] == 0)
+        assert np.all(rp.material_id.cpu().numpy()[hit] == 0)
+        assert tid[hit].min() >= first and tid[hit].max() < nt + first
+        n = rp.normal_global.cpu().numpy()
+        nc = rp.normal_camera.cpu().numpy()
+        if renderer is s.rasterizer:
+            R = s[cid].rotation.astype(np.float32)
+            want = np.stack([(n[0] * R[0, r] + n[1] * R[1, r]) + n[2] * R[2, r] for r in range(3)])
+            assert np.array_equal(nc, want)
+        else:
+            assert np.all(nc == 0)
+    s.close()

@@ -390,6 +390,47 @@ class RenderPasses:
     total_radiance: object = None
     direct_radiance: object = None
     indirect_radiance: object = None
+    # first-hit ids (passes.ipp:96-101; -1 where nothing was hit): the instance, its mesh and the
+    # material (0: the default material, the only one this path shades with); normal_camera is
+    # the normal in the camera frame, which only the rasterizer fills (zeros from the path tracer,
+    # as the reference's)
+    instance_id: object = None
+    mesh_id: object = None
+    material_id: object = None
+    normal_camera: object = None
+
+
+def _id_passes(rp: "RenderPasses", scene: "Scene", camera: "Camera", first: int, raster: bool):
+    """Turns the device's triangle ids (index in the flattened scene, + `first`) into the reference's
+    per-instance ids and derives instance_id, mesh_id, material_id and normal_camera."""
+    import torch
+
+    dev = rp.triangle_id.device
+    tid = rp.triangle_id.to(torch.int64)
+    hit = tid != -1
+    fi = (tid - first).clamp(min=0)
+    offs = scene.flat["tri_offsets"]
+    counts = [n for (_, _, n) in offs]
+    starts = torch.tensor(np.cumsum([0] + counts[:-1]), dtype=torch.int64, device=dev)
+    k = (torch.searchsorted(starts, fi, right=True) - 1).clamp(min=0)
+    inst = torch.tensor([ii for (ii, _, _) in offs], dtype=torch.int64, device=dev)
+    mesh = torch.tensor([scene.instances[ii].mesh for (ii, _, _) in offs], dtype=torch.int64, device=dev)
+    none = torch.full_like(tid, -1)
+    rp.triangle_id = torch.where(hit, fi - starts[k] + first, none).to(torch.int32)
+    rp.instance_id = torch.where(hit, inst[k], none).to(torch.int32)
+    rp.mesh_id = torch.where(hit, mesh[k], none).to(torch.int32)
+    rp.material_id = torch.where(hit, torch.zeros_like(tid), none).to(torch.int32)
+    n = rp.normal_global
+    if raster:
+        # Camera::getViewNormalMatrix (the inverse rotation) times the normal, glm's row sums
+        R = np.asarray(camera.rotation, np.float64).astype(np.float32)
+        rows = []
+        for r in range(3):
+            a, b, c = (float(R[0, r]), float(R[1, r]), float(R[2, r]))
+            rows.append((n[0] * a + n[1] * b) + n[2] * c)
+        rp.normal_camera = torch.stack(rows)
+    else:
+        rp.normal_camera = torch.zeros_like(n)
 
 
 class PathTracer:
@@ -466,6 +507,7 @@ class PathTracer:
         st = capi.Stats()
         lib.vgb_get_stats(ctx, C.byref(st))
         self.last_stats = st
+        _id_passes(rp, scene, camera, 0, raster=False)
         if rp.received_power is not None and camera.sensor.psf is not None:
             # CPUPathTracer::render convolves the received power with the camera's PSF
             # (cpu_path_tracer.ipp:150-158)
@@ -526,13 +568,7 @@ class Rasterizer:
         lib.vgb_get_stats(ctx, C.byref(st))
         self.last_stats = st
         # triangle ids restart at 1 for every instance (cpu_rasterizer.ipp:70-72)
-        counts = [n for (_, _, n) in scene.flat["tri_offsets"]]
-        if len(counts) > 1:
-            starts = torch.tensor(np.cumsum([0] + counts[:-1]), dtype=torch.int64, device=dev)
-            tid = rp.triangle_id.to(torch.int64)
-            hit = tid != -1
-            k = torch.searchsorted(starts, (tid - 1).clamp(min=0), right=True) - 1
-            rp.triangle_id = torch.where(hit, tid - starts[k], tid).to(torch.int32)
+        _id_passes(rp, scene, camera, 1, raster=True)
         if rp.received_power is not None and camera.sensor.psf is not None:
             from .sensor import psf_convolve
 
