@@ -142,3 +142,18 @@ def test_tiny_scene_takes_one_leaf(gpu):
     p = np.array([[0, 0, 0], [100, 0, 0], [0, 100, 0], [100, 100, 5]], np.float32)
     i = np.array([[0, 1, 2], [1, 3, 2]], np.uint32)
     _same([Mesh(positions=p, indices=i)], cam_pos=(50.0, 40.0, 300.0), nrays=512, spread=60.0)
+
+
+def test_gpu_builder_arguments(gpu):
+    import ctypes as C
+
+    s, _ = _scene([_dem(posts=17)], 0)
+    s.build_tlas()
+    lib = capi.load()
+    ctx = s.context()
+    assert lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 1, 0, 8))) != 0     # binary layout only
+    assert b"binary" in lib.vgb_last_error(ctx)
+    assert lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(9, 1, 0, 2))) != 0     # leaf size <= 8
+    assert lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 2, 0, 2))) != 0     # unknown builder
+    capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(2, 1, 0, 2))), ctx, "bvh_build")
+    s.close()

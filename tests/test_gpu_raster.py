@@ -196,3 +196,61 @@ def test_id_passes_and_camera_normals(gpu):
         else:
             assert np.all(nc == 0)
     s.close()
+
+
+def test_host_film_and_no_lighting(gpu):
+    """vgb_rasterize with host planes (staged on the device and copied back) equals the device
+    planes; without simulate_lighting the geometry passes are unchanged."""
+    import ctypes as C
+
+    import torch
+
+    s, cid = _dem_scene(res=48)
+    rp = s.rasterizer.render(s[cid], s)
+    torch.cuda.synchronize()
+    B = s.bands.size
+    cam = s[cid].to_c(s.origin, B)
+    lights, nl = s.c_lights()
+    o = capi.RasterOptions()
+    o.intrinsic[:] = [float(x) for x in s[cid].intrinsic_matrix()]
+    o.simulate_lighting = 1
+    o.nbands = B
+    H = W = 48
+    host = {"depth": np.empty((H, W), np.float32), "alpha": np.empty((H, W), np.float32),
+            "albedo": np.empty((B, H, W), np.float32), "normal_global": np.empty((3, H, W), np.float32),
+            "triangle_id": np.empty((H, W), np.uint32), "total_radiance": np.empty((B, H, W), np.float32),
+            "received_power": np.empty((B, H, W), np.float32)}
+    omega = s.pixel_solid_angle(s[cid], cam).cpu().numpy().copy()
+    f = capi.Film()
+    for k, a in host.items():
+        setattr(f, k, a.ctypes.data)
+    f.pixel_solid_angle = omega.ctypes.data
+    f.on_device = 0
+    lib = capi.load()
+    ctx = s.context()
+    capi.check(lib.vgb_rasterize(ctx, C.byref(cam), lights, nl, C.byref(o), C.byref(f)), ctx, "rasterize")
+    for k in ("depth", "alpha", "albedo", "normal_global", "total_radiance", "received_power"):
+        assert np.array_equal(host[k], getattr(rp, k).cpu().numpy(), equal_nan=True), k
+    tid = host["triangle_id"].astype(np.int64)
+    tid[tid == 0xFFFFFFFF] = -1
+    assert np.array_equal(tid, rp.triangle_id.cpu().numpy().astype(np.int64))
+    s.rasterizer.render_passes.simulate_lighting = False
+    rq = s.rasterizer.render(s[cid], s)
+    torch.cuda.synchronize()
+    assert rq.total_radiance is None and rq.received_power is None
+    assert np.array_equal(rq.depth.cpu().numpy(), host["depth"], equal_nan=True)
+    assert np.array_equal(rq.albedo.cpu().numpy(), host["albedo"])
+    s.close()
+
+
+def test_render_total_power_reuses_the_render(gpu):
+    s, cid = _dem_scene(res=32)
+    s.pathtracer.render_passes.simulate_lighting = True
+    s.pathtracer.options.samples = 2
+    p1 = s.render_total_power(cid)
+    p2 = s.render_total_power(cid)
+    assert p2 is p1                              # the scene did not change: no new render
+    s.mark_dirty()
+    p3 = s.render_total_power(cid)
+    assert p3 is not p1 and bool((p3 == p1).all())
+    s.close()

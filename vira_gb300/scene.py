@@ -888,6 +888,18 @@ class Scene:
         return om
 
     # --- renders (scene.ipp:840-915)
+    def render_total_power(self, camera_id):
+        """Scene::renderTotalPower (scene.ipp:873-915): path-traces only when the scene changed since
+        the last render (so several exposures reuse one render), then returns the received power.
+        Unresolved objects (stars, unresolved bodies) are not rendered here, so the total power is
+        the path tracer's received power."""
+        rp = self.pathtracer.render_passes
+        if self._dirty or rp.received_power is None:
+            rp = self.pathtracer.render(self[camera_id], self)
+        if rp.received_power is None:
+            raise ValueError("render_total_power needs pathtracer.render_passes.simulate_lighting")
+        return rp.received_power
+
     def update_level_of_detail(self, camera_id) -> int:
         """Scene::updateLevelOfDetail: the LoD manager's update for this camera (lod_manager.ipp:24-30)."""
         return self.lod_manager.update(self[camera_id], self)
