@@ -2680,6 +2680,50 @@ __device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ fram
     return lo;
 }
 
+// Cold paths of k_batch, out of line so that the sample loop's instruction footprint stays small:
+// the bilinear weights of the background lookup of a missed ray (cpu_path_tracer.ipp:256-270) ...
+__device__ __noinline__ float4 batch_background_weights(F3 rd) {
+    float x = rd.x, y = rd.y, z = rd.z;
+    float u = atan2f(y, x) / (2 * kPi);
+    float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+    float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+    if (px < 0) px += 1.f;
+    if (py < 0) py += 1.f;
+    float ddx = px - 0.f, ddy = py - 0.f;
+    return make_float4((1.f - ddx) * (1.f - ddy), ddx * (1.f - ddy), (1.f - ddx) * ddy, ddx * ddy);
+}
+
+// ... and unidirectional's adaptive stopping rule after a sample (cpu_path_tracer.ipp:198-226).
+struct AdaptStep { float s1, s2; bool stop; };
+template <int NB>
+__device__ __noinline__ AdaptStep batch_adaptive_step(const float* acc, int lane, uint32_t nb, uint32_t sample,
+                                                      const vgb_pt_options& opt, float s1, float s2) {
+    float sq = 0.f;
+#pragma unroll
+    for (int k = 0; k < NB; ++k) {
+        const float pr = acc[(3 * NB + 4 + k) * 32 + lane];
+        if (k < (int)nb) sq += pr * pr;
+    }
+    const float illum = sqrtf(sq);
+    s1 = s1 + illum;
+    s2 = s2 + illum * illum;
+    bool stop = false;
+    if (sample != 0 && sample % opt.samples_to_detect_miss == 0 && acc[(3 * NB + 3) * 32 + lane] == 0.f) {
+        stop = true;
+    } else if (sample != 0 && sample % opt.samples_per_batch == 0) {
+        if (s1 == 0.f) {
+            stop = true;
+        } else {
+            const float n = (float)sample + 1.f;
+            const float mu = s1 / n;
+            const float variance = (1.f / (n - 1.f)) * (s2 - (s1 * s1) / n);
+            const float I = 1.96f * sqrtf(variance / n);
+            stop = I <= opt.sampling_tolerance * mu;
+        }
+    }
+    return AdaptStep{s1, s2, stop};
+}
+
 // Shared-memory planes per lane of k_batch: arad[NB] adir[NB] aalb[NB] anrm[3] adep (the
 // pixel's sums over samples) | prad[NB] brad[NB] (the current sample).
 __host__ __device__ constexpr int batch_planes(int nb, bool) { return 5 * nb + 4; }
@@ -2763,14 +2807,8 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
-                            float x = rd.x, y = rd.y, z = rd.z;
-                            float u = atan2f(y, x) / (2 * kPi);
-                            float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
-                            float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
-                            if (px < 0) px += 1.f;
-                            if (py < 0) py += 1.f;
-                            float ddx = px - 0.f, ddy = py - 0.f;
-                            float a = (1.f - ddx) * (1.f - ddy), b = ddx * (1.f - ddy), c = (1.f - ddx) * ddy, e = ddx * ddy;
+                            const float4 bw = batch_background_weights(rd);
+                            const float a = bw.x, b = bw.y, c = bw.z, e = bw.w;
 #pragma unroll
                             for (int k = 0; k < NB; ++k) {
                                 const float bgv = opt.background[k];
@@ -2846,28 +2884,10 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
 #pragma unroll
                 for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(k) = ACC(k) + PRAD(k);
                 if (opt.adaptive_sampling) {
-                    // unidirectional's stopping rule (cpu_path_tracer.ipp:198-226)
-                    float sq = 0.f;
-#pragma unroll
-                    for (int k = 0; k < NB; ++k) if (k < (int)nb) sq += PRAD(k) * PRAD(k);
-                    const float illum = sqrtf(sq);
-                    s1 = s1 + illum;
-                    s2 = s2 + illum * illum;
-                    bool stop = false;
-                    if (sample != 0 && sample % opt.samples_to_detect_miss == 0 && ACC(3 * NB + 3) == 0.f) {
-                        stop = true;
-                    } else if (sample != 0 && sample % opt.samples_per_batch == 0) {
-                        if (s1 == 0.f) {
-                            stop = true;
-                        } else {
-                            const float n = (float)sample + 1.f;
-                            const float mu = s1 / n;
-                            const float variance = (1.f / (n - 1.f)) * (s2 - (s1 * s1) / n);
-                            const float I = 1.96f * sqrtf(variance / n);
-                            stop = I <= opt.sampling_tolerance * mu;
-                        }
-                    }
-                    if (stop) { stopped = sample; break; }
+                    const AdaptStep st = batch_adaptive_step<NB>(acc, lane, nb, sample, opt, s1, s2);
+                    s1 = st.s1;
+                    s2 = st.s2;
+                    if (st.stop) { stopped = sample; break; }
                 }
 #undef PRAD
 #undef BRAD
