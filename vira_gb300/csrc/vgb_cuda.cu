@@ -463,6 +463,19 @@ __global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s,
 // ------------------------------------------------------------------ k_shade
 // processIntersection for every item of k_trace: AOVs, shading point, NEE shadow-ray enqueue,
 // BSDF-sampled continuation and live-path enqueue (warp-aggregated appends).
+// The bilinear weights of the background lookup of a missed ray (cpu_path_tracer.ipp:256-270),
+// out of line: a cold path of the shading kernels, kept out of their instruction footprint.
+__device__ __noinline__ float4 background_weights(F3 rd) {
+    float x = rd.x, y = rd.y, z = rd.z;
+    float u = atan2f(y, x) / (2 * kPi);
+    float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
+    float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
+    if (px < 0) px += 1.f;
+    if (py < 0) py += 1.f;
+    float ddx = px - 0.f, ddy = py - 0.f;
+    return make_float4((1.f - ddx) * (1.f - ddy), ddx * (1.f - ddy), (1.f - ddx) * ddy, ddx * ddy);
+}
+
 template <int NB>
 __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
                                                uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
@@ -547,14 +560,8 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         if (active && !hit) {
             if (fp.opt.simulate_lighting && fp.opt.show_background) {
                 if (bounce != 0) rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
-                float x = rd.x, y = rd.y, z = rd.z;
-                float u = atan2f(y, x) / (2 * kPi);
-                float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
-                float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
-                if (px < 0) px += 1.f;
-                if (py < 0) py += 1.f;
-                float dx = px - 0.f, dy = py - 0.f;
-                float a = (1.f - dx) * (1.f - dy), b = dx * (1.f - dy), c = (1.f - dx) * dy, e = dx * dy;
+                const float4 bw = background_weights(rd);
+                const float a = bw.x, b = bw.y, c = bw.z, e = bw.w;
 #pragma unroll
                 for (int k = 0; k < NB; ++k) {
                     if (k < (int)nb) {
@@ -2680,20 +2687,8 @@ __device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ fram
     return lo;
 }
 
-// Cold paths of k_batch, out of line so that the sample loop's instruction footprint stays small:
-// the bilinear weights of the background lookup of a missed ray (cpu_path_tracer.ipp:256-270) ...
-__device__ __noinline__ float4 batch_background_weights(F3 rd) {
-    float x = rd.x, y = rd.y, z = rd.z;
-    float u = atan2f(y, x) / (2 * kPi);
-    float v = atan2f(sqrtf(x * x + y * y), z) / kPi;
-    float px = fmodf(u * 1.f, 1.f), py = fmodf(v * 1.f, 1.f);
-    if (px < 0) px += 1.f;
-    if (py < 0) py += 1.f;
-    float ddx = px - 0.f, ddy = py - 0.f;
-    return make_float4((1.f - ddx) * (1.f - ddy), ddx * (1.f - ddy), (1.f - ddx) * ddy, ddx * ddy);
-}
-
-// ... and unidirectional's adaptive stopping rule after a sample (cpu_path_tracer.ipp:198-226).
+// Cold path of k_batch, out of line so that the sample loop's instruction footprint stays small:
+// unidirectional's adaptive stopping rule after a sample (cpu_path_tracer.ipp:198-226).
 struct AdaptStep { float s1, s2; bool stop; };
 template <int NB>
 __device__ __noinline__ AdaptStep batch_adaptive_step(const float* acc, int lane, uint32_t nb, uint32_t sample,
@@ -2807,7 +2802,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
-                            const float4 bw = batch_background_weights(rd);
+                            const float4 bw = background_weights(rd);
                             const float a = bw.x, b = bw.y, c = bw.z, e = bw.w;
 #pragma unroll
                             for (int k = 0; k < NB; ++k) {
