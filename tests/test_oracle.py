@@ -98,7 +98,7 @@ def test_flat_plane_known_answer():
         expect = 0.12 / math.pi * cos * cos * float(L.radiance[b]) * w / float(lpdf)
         got = o["total_radiance"][b]
         assert np.all(np.abs(got - expect) <= 2e-5 * expect), (b, got.min(), got.max(), expect)
-    # the FP32 solid angle differs from the exact one by the cancellation SURVEY warns about
+    # the FP32 solid angle (sphere_light.ipp:60) loses digits to cancellation for the sun's tiny cap
     exact = 2 * math.pi * (1 - math.sqrt(1 - (float(L.radius) / float(d)) ** 2))
     assert abs(float(omega) - exact) / exact < 2e-2
     assert np.allclose(o["depth"][hit], o["depth"][hit], equal_nan=True)

@@ -153,15 +153,26 @@ __global__ void k_dem_quad_counts(const float* __restrict__ h, uint32_t W, uint3
     }
 }
 
-__global__ void k_dem_faces(const float* __restrict__ h, uint32_t W, uint32_t H, const uint32_t* __restrict__ off,
-                            uint32_t* __restrict__ idx) {
+// One block per chunk of 256 quads: the chunk's faces are one contiguous run of the index buffer
+// (the scan's offsets), so they are assembled in shared memory and written out coalesced.
+__global__ void __launch_bounds__(256) k_dem_faces(const float* __restrict__ h, uint32_t W, uint32_t H,
+                                                   const uint32_t* __restrict__ off, uint32_t* __restrict__ idx) {
+    __shared__ uint32_t stage[256 * 6];
     const size_t nq = (size_t)(W - 1) * (H - 1);
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (size_t)gridDim.x * blockDim.x) {
-        uint32_t a, b, c, d;
-        quad_corners((uint32_t)q, W, H, a, b, c, d);
-        size_t k = 3 * (size_t)off[q];
-        if (!isinf(h[a]) && !isinf(h[b]) && !isinf(h[c])) { idx[k++] = a; idx[k++] = b; idx[k++] = c; }
-        if (!isinf(h[b]) && !isinf(h[a]) && !isinf(h[d])) { idx[k++] = b; idx[k++] = a; idx[k++] = d; }
+    for (size_t q0 = (size_t)blockIdx.x * 256; q0 < nq; q0 += (size_t)gridDim.x * 256) {
+        const size_t q = q0 + threadIdx.x;
+        const uint32_t base = off[q0];
+        const uint32_t total = off[min(q0 + 256, nq)] - base;
+        if (q < nq) {
+            uint32_t a, b, c, d;
+            quad_corners((uint32_t)q, W, H, a, b, c, d);
+            uint32_t k = 3 * (off[q] - base);
+            if (!isinf(h[a]) && !isinf(h[b]) && !isinf(h[c])) { stage[k++] = a; stage[k++] = b; stage[k++] = c; }
+            if (!isinf(h[b]) && !isinf(h[a]) && !isinf(h[d])) { stage[k++] = b; stage[k++] = a; stage[k++] = d; }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < 3 * total; i += 256) idx[3 * (size_t)base + i] = stage[i];
+        __syncthreads();
     }
 }
 
