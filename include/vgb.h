@@ -13,7 +13,8 @@
  *       Embree fills through rtcIntersect1
  *       (include/implementation/rendering/acceleration/embree_tlas.ipp:128-173).
  *
- * Every entry point returns a vgb_status and never throws or aborts.  Buffers are
+ * Every entry point returns a vgb_status and never throws or aborts (a failed host
+ * allocation inside a call returns VGB_ERR_OUT_OF_MEMORY).  Buffers are
  * owned by the caller unless a vgb_*_create function made them.  A context owns one
  * CUDA stream and is not thread-safe: use one host thread per context.
  *

@@ -73,3 +73,38 @@ def same_bits(a, b) -> bool:
     a = np.ascontiguousarray(a)
     b = np.ascontiguousarray(b)
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def lz4_zero_run(n: int) -> bytes:
+    """A valid LZ4 block of n >= 25 zero bytes at the format's largest expansion: one literal,
+    one match at offset 1 whose length runs on in 255-bytes, then the five closing literals."""
+    v = n - 25
+    ext = b"\xff" * (v // 255) + bytes([v % 255])
+    return bytes([0x1F, 0]) + b"\x01\x00" + ext + bytes([0x50]) + bytes(5)
+
+
+def quipu_with_claimed_lod(path, width: int, height: int, block: bytes | None = None):
+    """A one-LoD Quipu (no albedo) whose LZ4-compressed uint8 heights claim width x height posts,
+    with `block` (default: lz4_zero_run of that size) as the stored block.  Built from a 3x3
+    pyramid written by the oracle's writer, with its height image replaced."""
+    import struct
+
+    from oracle import quipu as Q
+
+    def enc(raw: bytes) -> bytes:
+        lib = capi.load()
+        cap = lib.vgb_lz4_bound(len(raw))
+        dst = np.empty(cap, np.uint8)
+        src = np.frombuffer(raw, np.uint8)
+        return dst[:lib.vgb_lz4_compress(src.ctypes.data, len(raw), dst.ctypes.data, cap)].tobytes()
+
+    h = np.array([[0.0, 0.5, 1.0], [0.2, 0.7, 0.1], [0.9, 0.3, 0.6]], np.float32)
+    small = Q.write(path, [dict(heights=h, projection=Q.projection(3, 3))], write_albedos=False,
+                    compress=True, compressor=enc)
+    data = small.read_bytes()
+    head = struct.pack("<HIIB", Q.CLS_U8, 3, 3, 1)
+    at = data.index(head)
+    assert data.count(head) == 1
+    blk = lz4_zero_run(width * height) if block is None else block
+    small.write_bytes(data[:at] + struct.pack("<HIIBQQ", Q.CLS_U8, width, height, 1, width * height, len(blk)) + blk)
+    return small

@@ -183,3 +183,27 @@ def test_options_validation():
     s.pathtracer.options.samples = 0
     with pytest.raises(ValueError):
         s.pathtracer.c_options(s)
+
+
+def test_failed_host_allocation_returns_a_status():
+    """No exception crosses the C boundary: in a child whose address space is capped at 6 GB, a
+    host entry whose buffers would need 51 GB returns VGB_ERR_OUT_OF_MEMORY instead of ending
+    the process (the caller's one-element arrays are never touched)."""
+    import subprocess
+    import sys
+    import textwrap
+
+    code = textwrap.dedent("""
+        import ctypes as C, resource, sys
+        import numpy as np
+        from vira_gb300 import capi
+        lib = capi.load()
+        resource.setrlimit(resource.RLIMIT_AS, (6 << 30, resource.RLIM_INFINITY))
+        p = np.zeros(3, np.float32); i = np.zeros(3, np.uint32); o = np.full(3, 7.0, np.float32)
+        st = lib.vgb_compute_vertex_normals(p.ctypes.data, 0xFFFFFFFF, i.ctypes.data, 0, o.ctypes.data)
+        print(st, float(o.sum()))
+    """)
+    root = Path(__file__).resolve().parents[1]
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["3", "21.0"]

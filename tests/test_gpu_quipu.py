@@ -77,6 +77,27 @@ def test_reader_options(gpu):
     q.close()
 
 
+def test_lod_beyond_32_bit_triangle_ids_is_refused(gpu, tmp_path):
+    # 50000^2 posts (9.8 MB on disk at LZ4's largest expansion): the C entry refuses it before it
+    # reads a pixel or writes the (here one-element) output arrays
+    import ctypes as C
+
+    from helpers import quipu_with_claimed_lod
+    from vira_gb300.scene import _mesh_context
+
+    q = VQ.DEMQuipu(quipu_with_claimed_lod(tmp_path / "big.qld", 50000, 50000), nbands=1)
+    lib = capi.load()
+    ctx = _mesh_context(0)
+    one = [np.zeros(4, np.float32) for _ in range(3)]
+    idx = np.zeros(4, np.uint32)
+    nt = C.c_uint32(7)
+    st = lib.vgb_quipu_read_mesh(ctx, q._h, 0, C.byref(q._read_options(1)), capi.ptr(one[0]), capi.ptr(one[1]),
+                                 capi.ptr(one[2]), capi.ptr(idx), C.byref(nt), 0)
+    assert st == 1 and b"2^31" in lib.vgb_last_error(ctx)
+    assert nt.value == 7 and not idx.any() and not any(a.any() for a in one)
+    q.close()
+
+
 def test_read_buffers_picks_the_lod_once(gpu):
     q = VQ.DEMQuipu(GOLDEN / "quipu_u16_lz4_color.qld", nbands=4)
     m = q.read_buffers(25.0)

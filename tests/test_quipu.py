@@ -11,6 +11,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from helpers import lz4_zero_run, quipu_with_claimed_lod
 from oracle import quipu as Q
 from vira_gb300 import capi
 from vira_gb300 import quipu as VQ
@@ -308,6 +309,25 @@ def test_reader_errors(tmp_path):
     out = np.empty((49, 65, 3), np.float32)
     assert capi.load().vgb_quipu_read_albedo(q._h, 0, 3, capi.ptr(out)) != 0
     assert b"channels" in capi.load().vgb_quipu_last_error()
+    q.close()
+
+
+def test_claimed_sizes_are_bounded_before_allocation(tmp_path):
+    """An LZ4 block expands at most 255-fold, so a height image claiming more is refused when the
+    file opens, before a buffer of the claimed size exists; a block at the largest expansion is a
+    valid file (all codes 0: no-data, +inf).  A LoD of 2^31 posts or more is refused before its
+    mesh arrays are allocated (triangle ids are 32-bit)."""
+    t = quipu_with_claimed_lod(tmp_path / "claim.qld", 4000, 4000, block=lz4_zero_run(1000))
+    with pytest.raises(capi.VgbError, match="bad or truncated height image"):
+        VQ.DEMQuipu(t)
+    q = VQ.DEMQuipu(quipu_with_claimed_lod(tmp_path / "run.qld", 300, 200))
+    h = q.read_heights(0)
+    assert h.shape == (200, 300) and np.isposinf(h).all()
+    q.close()
+    q = VQ.DEMQuipu(quipu_with_claimed_lod(tmp_path / "big.qld", 50000, 50000))
+    assert (q.lods[0].width, q.lods[0].height) == (50000, 50000)
+    with pytest.raises(capi.VgbError, match="2\\^31"):
+        q.read_lod_mesh(0)
     q.close()
 
 

@@ -1340,7 +1340,7 @@ extern "C" {
 
 VGB_API const char* vgb_version(void) { return "vira_gb300 0.1 (sm_103a)"; }
 
-VGB_API vgb_status vgb_context_create(vgb_context** out, int device) {
+VGB_API vgb_status vgb_context_create(vgb_context** out, int device) try {
     if (!out) return VGB_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     vgb_context* ctx = new (std::nothrow) vgb_context();
@@ -1368,9 +1368,11 @@ VGB_API vgb_status vgb_context_create(vgb_context** out, int device) {
     cudaEventCreate(&ctx->ev1);
     *out = ctx;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(nullptr);
 }
 
-VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
+VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -1387,11 +1389,13 @@ VGB_API vgb_status vgb_context_destroy(vgb_context* ctx) {
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API const char* vgb_last_error(const vgb_context* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-VGB_API vgb_status vgb_set_stream(vgb_context* ctx, void* stream) {
+VGB_API vgb_status vgb_set_stream(vgb_context* ctx, void* stream) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1399,18 +1403,22 @@ VGB_API vgb_status vgb_set_stream(vgb_context* ctx, void* stream) {
     if (stream) { ctx->stream = (cudaStream_t)stream; ctx->own_stream = false; }
     else { CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)); ctx->own_stream = true; }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_synchronize(vgb_context* ctx) {
+VGB_API vgb_status vgb_synchronize(vgb_context* ctx) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t nverts, const uint32_t* idx,
                                     uint32_t ntris, uint32_t nbands, const float* valb, const float* vnrm,
-                                    const float* vuv, const float* tex, uint32_t tw, uint32_t th) {
+                                    const float* vuv, const float* tex, uint32_t tw, uint32_t th) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!pos || !idx || nverts == 0 || ntris == 0)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_upload: empty mesh or null buffer");
@@ -1479,9 +1487,11 @@ VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t
     ctx->h_idx.assign(idx, idx + 3 * (size_t)ntris);
     ctx->h_pos_stale = false;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) {
+VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "bvh_build: no scene uploaded");
     uint32_t leaf = opts ? opts->max_leaf_size : 0, threads = opts ? opts->threads : 0;
@@ -1563,9 +1573,11 @@ VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts) 
     ctx->stats.bvh_node_bytes = layout == 8 ? 80 : 64;
     ctx->stats.tri_record_bytes = 48;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam, float* out, int on_device) {
+VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam, float* out, int on_device) try {
     if (!ctx || !cam || !out) return VGB_ERR_INVALID_ARGUMENT;
     if (cam->width == 0 || cam->height == 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "pixel_solid_angle: empty image");
     cudaSetDevice(ctx->device);
@@ -1581,22 +1593,28 @@ VGB_API vgb_status vgb_pixel_solid_angle(vgb_context* ctx, const vgb_camera* cam
     if (!on_device) CK(cudaMemcpyAsync(out, d, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable) {
+VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     ctx->count_pass = enable != 0;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) {
+VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     ctx->profiling = enable != 0;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* heights, uint32_t W, uint32_t H, double sx,
-                                           double sy, float* pos, uint32_t* idx, uint32_t* nt_out, int on_device) {
+                                           double sy, float* pos, uint32_t* idx, uint32_t* nt_out, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!heights || !pos || !idx || !nt_out || W < 2 || H < 2 || (uint64_t)W * H >= (1ull << 31))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "dem_triangulate_gpu: null array or grid outside 2..2^31 posts");
@@ -1627,11 +1645,13 @@ VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* height
     }
     *nt_out = nt;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_compute_vertex_normals_gpu(vgb_context* ctx, const float* pos, uint32_t nverts,
                                                   const uint32_t* idx, uint32_t ntris, float* normals,
-                                                  int on_device) {
+                                                  int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!pos || !idx || !normals || nverts == 0)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "compute_vertex_normals_gpu: null array or no vertices");
@@ -1660,6 +1680,8 @@ VGB_API vgb_status vgb_compute_vertex_normals_gpu(vgb_context* ctx, const float*
         CK(cudaStreamSynchronize(ctx->stream));
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 namespace {
@@ -1672,7 +1694,7 @@ __global__ void k_pack_vertices(const float* __restrict__ p3, const float* __res
 }
 }  // namespace
 
-VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos, const float* normals, int on_device) {
+VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos, const float* normals, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (ctx->nverts == 0) return fail(ctx, VGB_ERR_NOT_READY, "scene_update_positions: no scene uploaded");
     if (!pos) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_update_positions: null positions");
@@ -1730,6 +1752,8 @@ VGB_API vgb_status vgb_scene_update_positions(vgb_context* ctx, const float* pos
     }
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 // ---------------------------------------------------------------- rasterizer
@@ -1951,7 +1975,7 @@ __global__ void k_raster_resolve(DevScene s, RasterParams rp, const unsigned lon
 }  // namespace
 
 VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
-                                 const vgb_raster_options* opts, vgb_film* film) {
+                                 const vgb_raster_options* opts, vgb_film* film) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "rasterize: null argument");
     if (ctx->ntris == 0) return fail(ctx, VGB_ERR_NOT_READY, "rasterize: no scene uploaded");
@@ -2029,6 +2053,8 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
     ctx->stats.ms_last = ms;
     ctx->stats.kernel_launches = 3;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 // DEMQuipu::readBuffers (dem_quipu.ipp:124-221): the file's stored codes are read and LZ4-decoded
@@ -2037,7 +2063,7 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
 // normals (Mesh::calculateNormals) there.
 VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint32_t lod,
                                        const vgb_quipu_read_options* opts, float* positions, float* vert_albedo,
-                                       float* normals, uint32_t* indices, uint32_t* ntris, int on_device) {
+                                       float* normals, uint32_t* indices, uint32_t* ntris, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!q || !opts || !positions || !indices || !ntris)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: null argument");
@@ -2050,6 +2076,9 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: map-projected (OGR) LoDs need GDAL, which is absent");
     const uint32_t W = pl.heights.w, H = pl.heights.h;
     if (W < 2 || H < 2) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: fewer than 2x2 posts");
+    // triangle ids and vertex indices are 32-bit, and VGB_NO_HIT (2^32 - 1) marks a miss
+    if ((uint64_t)W * H >= (1ull << 31))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: LoD of 2^31 posts or more (32-bit triangle ids)");
     const size_t nv = (size_t)W * H, nq = (size_t)(W - 1) * (H - 1);
     const uint32_t nb = vert_albedo ? opts->nbands : 0;
     const bool use_albedo = vert_albedo && opts->read_albedos && pl.albedo_type != VGB_QUIPU_NO_ALBEDO;
@@ -2147,11 +2176,13 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
     ctx->stats.ms_last = ms;   // device decode + triangulation + normals
     *ntris = nt;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_power, uint32_t width,
                                        uint32_t height, uint32_t nbands, const vgb_sensor* sensor, float* image,
-                                       int on_device) {
+                                       int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!received_power || !sensor || !image || width == 0 || height == 0 || nbands == 0 || nbands > VGB_MAX_BANDS)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate: null plane or sensor, empty image or bands outside 1..8");
@@ -2187,11 +2218,13 @@ VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_p
     if (!on_device) CK(cudaMemcpyAsync(image, img, P * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_psf_convolve(vgb_context* ctx, float* received_power, uint32_t width, uint32_t height,
                                     uint32_t nbands, const float* kernel, uint32_t kernel_w, uint32_t kernel_h,
-                                    int on_device) {
+                                    int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!received_power || !kernel || width == 0 || height == 0 || nbands == 0 || nbands > VGB_MAX_BANDS)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "psf_convolve: null plane or kernel, empty image or bands outside 1..8");
@@ -2214,11 +2247,13 @@ VGB_API vgb_status vgb_psf_convolve(vgb_context* ctx, float* received_power, uin
     if (!on_device) CK(cudaMemcpyAsync(received_power, io, BP * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect, const float* albedo,
                                const float* depth, const float* normal, uint32_t width, uint32_t height,
-                               uint32_t nbands, const vgb_denoise_options* o, int on_device) {
+                               uint32_t nbands, const vgb_denoise_options* o, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!direct || !indirect || !albedo || !depth || !normal || width == 0 || height == 0 || nbands == 0 ||
         nbands > VGB_MAX_BANDS)
@@ -2247,12 +2282,16 @@ VGB_API vgb_status vgb_denoise(vgb_context* ctx, float* direct, float* indirect,
     }
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
-VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out) {
+VGB_API vgb_status vgb_get_stats(vgb_context* ctx, vgb_stats* out) try {
     if (!ctx || !out) return VGB_ERR_INVALID_ARGUMENT;
     *out = ctx->stats;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 static vgb_status check_device_error(vgb_context* ctx) {
@@ -2269,7 +2308,7 @@ static vgb_status check_device_error(vgb_context* ctx) {
 }
 
 VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
-                              const vgb_pt_options* opts, vgb_film* film) {
+                              const vgb_pt_options* opts, vgb_film* film) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: null camera/options/film");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render: build the BVH first");
@@ -2409,10 +2448,12 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
         if ((s = check_device_error(ctx)) != VGB_OK) return s;
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const float* dir, const float* tmax,
-                                  uint32_t n, int any_hit, uint32_t* tri, float* tout, float* bary, int on_device) {
+                                  uint32_t n, int any_hit, uint32_t* tri, float* tout, float* bary, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!org || !dir || !tri) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "trace_rays: null buffer");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "trace_rays: build the BVH first");
@@ -2474,6 +2515,8 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
     if (any_hit) { ctx->stats.rays_shadow = n; ctx->stats.rays_closest = 0; }
     else { ctx->stats.rays_closest = n; ctx->stats.rays_shadow = 0; }
     return check_device_error(ctx);
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 }  // extern "C"
@@ -2537,7 +2580,7 @@ void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film
 }  // namespace
 
 extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
-                                                 uint32_t nlights, const vgb_pt_options* opts, vgb_film* film) {
+                                                 uint32_t nlights, const vgb_pt_options* opts, vgb_film* film) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!cam || !opts || !film) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: null camera/options/film");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_noalloc: build the BVH first");
@@ -2648,6 +2691,8 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
                     std::string("render_noalloc: device traversal limit hit:") + ((err_word & kErrStack) ? " stack" : "") +
                         ((err_word & kErrIter) ? " iterations" : ""));
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 
@@ -2955,16 +3000,18 @@ cudaError_t launch_batch_any(vgb_context* ctx, const DevFrame* d_frames, const B
 
 }  // namespace
 
-extern "C" VGB_API vgb_status vgb_batch_tuning(vgb_context* ctx, uint32_t* threads, uint32_t* bps, uint32_t* grab) {
+extern "C" VGB_API vgb_status vgb_batch_tuning(vgb_context* ctx, uint32_t* threads, uint32_t* bps, uint32_t* grab) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (threads) *threads = ctx->tuned_threads;
     if (bps) *bps = ctx->tuned_bps;
     if (grab) *grab = ctx->tuned_grab;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame* frames, uint32_t nframes,
-                                               const vgb_pt_options* opts, const vgb_batch_options* bo) {
+                                               const vgb_pt_options* opts, const vgb_batch_options* bo) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!frames || nframes == 0 || !opts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: no frames or options");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_batch: build the BVH first");
@@ -3114,6 +3161,8 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
     ctx->stats.kernel_launches = 1;
     ctx->stats.ms_last = ms;
     return check_device_error(ctx);
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 
@@ -3710,21 +3759,25 @@ vgb_status adjoint_common(vgb_context* ctx, const vgb_camera* cam, const vgb_lig
 
 extern "C" VGB_API vgb_status vgb_adjoint(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                                           uint32_t nlights, const vgb_pt_options* opts, const float* dL_dradiance,
-                                          float* d_texture, float* d_height, int on_device) {
+                                          float* d_texture, float* d_height, int on_device) try {
     return adjoint_common(ctx, cam, lights, nlights, opts, dL_dradiance, d_texture, d_height, false, on_device, "adjoint");
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 extern "C" VGB_API vgb_status vgb_adjoint_positions(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                                                     uint32_t nlights, const vgb_pt_options* opts,
                                                     const float* dL_dradiance, float* d_texture, float* d_position,
-                                                    int on_device) {
+                                                    int on_device) try {
     return adjoint_common(ctx, cam, lights, nlights, opts, dL_dradiance, d_texture, d_position, true, on_device,
                           "adjoint_positions");
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const vgb_view* views, uint32_t nviews,
                                                        const vgb_pt_options* opts, float* d_texture, float* d_position,
-                                                       double* loss) {
+                                                       double* loss) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!views || nviews == 0 || !opts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: no views or options");
     if (!ctx->bvh_ready) return fail(ctx, VGB_ERR_NOT_READY, "render_adjoint_batch: build the BVH first");
@@ -3795,10 +3848,12 @@ extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const v
     ctx->stats.kernel_launches = 1;
     ctx->stats.ms_last = ms;
     return check_device_error(ctx);
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
 // Albedo texture update without re-uploading the mesh or rebuilding the BVH.
-extern "C" VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h) {
+extern "C" VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* texture, uint32_t tex_w, uint32_t tex_h) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
     if (!texture || tex_w != ctx->tw || tex_h != ctx->th)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "texture_update: size differs from the uploaded texture");
@@ -3826,4 +3881,6 @@ extern "C" VGB_API vgb_status vgb_texture_update(vgb_context* ctx, const float* 
         CK(cudaMemcpy(ctx->d_tex, texture, ntex * B * sizeof(float), cudaMemcpyHostToDevice));
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }

@@ -28,7 +28,7 @@ inline F3 normalize3(F3 a) { return scale3(a, 1.0f / std::sqrt(dot3(a, a))); }
 
 // Mesh::calculateNormals, include/implementation/geometry/mesh.ipp:199-233.
 extern "C" VGB_API vgb_status vgb_compute_vertex_normals(const float* p, uint32_t nv, const uint32_t* idx,
-                                                         uint32_t nt, float* out) {
+                                                         uint32_t nt, float* out) try {
     if (!p || !idx || !out) return VGB_ERR_INVALID_ARGUMENT;
     for (size_t k = 0; k < (size_t)3 * nt; ++k)
         if (idx[k] >= nv) return VGB_ERR_INVALID_ARGUMENT;
@@ -51,6 +51,8 @@ extern "C" VGB_API vgb_status vgb_compute_vertex_normals(const float* p, uint32_
         out[3 * v] = a.x; out[3 * v + 1] = a.y; out[3 * v + 2] = a.z;
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(nullptr);
 }
 
 // DEM::makeVertexBuffer (dem.ipp:165-211) with DEMProjection's non-OGR mapping
@@ -92,17 +94,19 @@ void vgb::dem_faces_host(const float* h, uint32_t W, uint32_t H, uint32_t* idx, 
 
 // A DEM of posts `sx` x `sy` metres, no tile offset, dx = dy = 1.
 extern "C" VGB_API vgb_status vgb_dem_triangulate(const float* h, uint32_t W, uint32_t H, double sx,
-                                                  double sy, float* pos, uint32_t* idx, uint32_t* nt_out) {
+                                                  double sy, float* pos, uint32_t* idx, uint32_t* nt_out) try {
     if (!h || !pos || !idx || !nt_out || W < 2 || H < 2) return VGB_ERR_INVALID_ARGUMENT;
     vgb::dem_vertices_host(h, W, H, vgb::dem_pose_of(1.0 * sx, 1.0 * sy, 0.0, 0.0, W, H), pos);
     vgb::dem_faces_host(h, W, H, idx, nt_out);
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(nullptr);
 }
 
 // Camera::initializeIntrinsicMatrix, camera.ipp:1526-1568, in FP32.
 extern "C" VGB_API vgb_status vgb_camera_intrinsics(float focal, float sensor_x, float sensor_y, uint32_t W,
                                                     uint32_t H, float px, float py, float kxy, float kyx,
-                                                    float z_dir, float kinv[6]) {
+                                                    float z_dir, float kinv[6]) try {
     if (!kinv || W == 0 || H == 0 || !(focal > 0) || !(sensor_x > 0) || !(sensor_y > 0))
         return VGB_ERR_INVALID_ARGUMENT;
     const float kx0 = (float)W / sensor_x, ky0 = (float)H / sensor_y;
@@ -120,6 +124,8 @@ extern "C" VGB_API vgb_status vgb_camera_intrinsics(float focal, float sensor_x,
     kinv[4] = ((sxy * ppy) - (fy * ppx)) / det;
     kinv[5] = ((syx * ppx) - (fx * ppy)) / det;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(nullptr);
 }
 
 // ====================================================================== BVH builder

@@ -15,7 +15,9 @@
 // id is the triangle's index in the caller's index buffer.
 #pragma once
 #include <cstdint>
+#include <exception>
 #include <limits>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -28,6 +30,31 @@
 #endif
 
 namespace vgb {
+
+// Entry points return statuses and let no exception cross the C boundary: each exported
+// function's body is a function-try-block whose handler calls this inside the catch, for the
+// status of the exception in flight (VGB_ERR_OUT_OF_MEMORY for a failed host allocation) and
+// its message in *err (when err is not null).
+inline vgb_status status_of_exception(std::string* err) noexcept {
+    vgb_status s = VGB_ERR_INTERNAL;
+    const char* msg = "unknown exception";
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        s = VGB_ERR_OUT_OF_MEMORY;
+        msg = "host allocation failed";
+    } catch (const std::exception& e) {
+        msg = e.what();
+    } catch (...) {
+    }
+    if (err) {
+        try {
+            *err = msg;
+        } catch (...) {
+        }
+    }
+    return s;
+}
 
 constexpr int kLeafShift = 3;
 constexpr uint32_t kMaxLeaf = 8;

@@ -222,7 +222,11 @@ bool read_image_ref(File& f, ImageRef& r) {
         r.pos = f.tell();
     }
     // the pixels must lie inside the file
-    return f.ok && r.stored <= f.size() && r.pos <= f.size() - r.stored && f.skip(r.stored);
+    if (!f.ok || r.stored > f.size() || r.pos > f.size() - r.stored) return false;
+    // an LZ4 block expands at most 255-fold (a match costs at least one byte per 255 output
+    // bytes), so a larger claimed size is malformed -- and is never allocated
+    if (r.compressed && r.raw_bytes > 255 * r.stored + 255) return false;
+    return f.skip(r.stored);
 }
 
 }  // namespace
@@ -300,15 +304,18 @@ VGB_API int64_t vgb_lz4_decompress(const void* src, uint64_t src_size, void* dst
 
 VGB_API uint64_t vgb_lz4_bound(uint64_t n) { return lz4_bound(n); }
 
-VGB_API uint64_t vgb_lz4_compress(const void* src, uint64_t n, void* dst, uint64_t dst_cap) {
+VGB_API uint64_t vgb_lz4_compress(const void* src, uint64_t n, void* dst, uint64_t dst_cap) try {
     if ((!src && n) || !dst) return 0;
     return lz4_encode((const uint8_t*)src, (size_t)n, (uint8_t*)dst, dst_cap);
+} catch (...) {
+    vgb::status_of_exception(&g_quipu_err);
+    return 0;  // the encoder's hash table could not be allocated
 }
 
 // DEMQuipu::DEMQuipu (dem_quipu.ipp:29-60), quipu::open (quipu_io.ipp:24-54), and an index of
 // the LoD blocks (readDEMProjection :573-590, readDEMHeights :601-626, readAlbedos_f :643-653,
 // readAlbedos :672-702, readImage :717-752).
-VGB_API vgb_status vgb_quipu_open(const char* path, vgb_quipu_dem** out) {
+VGB_API vgb_status vgb_quipu_open(const char* path, vgb_quipu_dem** out) try {
     if (!path || !out) return qfail("quipu_open: null argument");
     *out = nullptr;
     File f;
@@ -410,17 +417,21 @@ VGB_API vgb_status vgb_quipu_open(const char* path, vgb_quipu_dem** out) {
     }
     *out = q.release();
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }
 
 VGB_API void vgb_quipu_close(vgb_quipu_dem* q) { delete q; }
 
-VGB_API vgb_status vgb_quipu_get_header(const vgb_quipu_dem* q, vgb_quipu_header* out) {
+VGB_API vgb_status vgb_quipu_get_header(const vgb_quipu_dem* q, vgb_quipu_header* out) try {
     if (!q || !out) return qfail("quipu_get_header: null argument");
     *out = q->header;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }
 
-VGB_API vgb_status vgb_quipu_get_lod(const vgb_quipu_dem* q, uint32_t lod, vgb_quipu_lod_info* out) {
+VGB_API vgb_status vgb_quipu_get_lod(const vgb_quipu_dem* q, uint32_t lod, vgb_quipu_lod_info* out) try {
     if (!q || !out) return qfail("quipu_get_lod: null argument");
     if (lod >= q->lods.size()) return qfail("quipu_get_lod: LoD index out of range");
     const Lod& L = q->lods[lod];
@@ -438,6 +449,8 @@ VGB_API vgb_status vgb_quipu_get_lod(const vgb_quipu_dem* q, uint32_t lod, vgb_q
     i.albedo_channels = L.albedo_type == 2 ? (uint32_t)L.planes.size() : (L.albedo_type == 1 ? 1u : 0u);
     *out = i;
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }
 
 VGB_API uint32_t vgb_quipu_select_lod(const vgb_quipu_dem* q, double required_gsd) {
@@ -450,7 +463,7 @@ VGB_API uint32_t vgb_quipu_select_lod(const vgb_quipu_dem* q, double required_gs
     return sel;
 }
 
-VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float* heights) {
+VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float* heights) try {
     if (!q || !heights) return qfail("quipu_read_heights: null argument");
     vgb::QuipuPayload pl;
     vgb_status s = vgb::quipu_lod_payload(q, lod, &pl);
@@ -468,9 +481,11 @@ VGB_API vgb_status vgb_quipu_read_heights(vgb_quipu_dem* q, uint32_t lod, float*
         for (size_t k = 0; k < n; ++k) heights[k] = vgb::quipu_dequantize(r[k], 65535.f, mn, mx);
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }
 
-VGB_API vgb_status vgb_quipu_read_albedo(vgb_quipu_dem* q, uint32_t lod, uint32_t nbands, float* albedo) {
+VGB_API vgb_status vgb_quipu_read_albedo(vgb_quipu_dem* q, uint32_t lod, uint32_t nbands, float* albedo) try {
     if (!q || !albedo) return qfail("quipu_read_albedo: null argument");
     vgb::QuipuPayload pl;
     vgb_status s = vgb::quipu_lod_payload(q, lod, &pl);
@@ -491,6 +506,8 @@ VGB_API vgb_status vgb_quipu_read_albedo(vgb_quipu_dem* q, uint32_t lod, uint32_
             albedo[k * nc + c] = vgb::quipu_dequantize(codes[k], 255.f, pl.planes[c].mn, pl.planes[c].mx);
     }
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }
 
 }  // extern "C"
@@ -582,7 +599,7 @@ void put_projection(Writer& w, const vgb_quipu_projection& p) {
 
 extern "C" VGB_API vgb_status vgb_quipu_write(const char* path, const vgb_quipu_lod_data* lods, uint32_t nlods,
                                              const double position[3], const double rotation[9],
-                                             const double scale[3], int write_albedos, int compress) {
+                                             const double scale[3], int write_albedos, int compress) try {
     if (!path || !lods || !position || !rotation || !scale) return qfail("quipu_write: null argument");
     if (nlods == 0 || nlods > VGB_QUIPU_MAX_LODS)
         return qfail("quipu_write: LoD count outside 1.." + std::to_string(VGB_QUIPU_MAX_LODS));
@@ -706,4 +723,6 @@ extern "C" VGB_API vgb_status vgb_quipu_write(const char* path, const vgb_quipu_
     const bool good = std::fwrite(w.buf.data(), 1, w.buf.size(), f) == w.buf.size();
     if (std::fclose(f) != 0 || !good) return qfail("quipu_write: write failed for " + fp.string());
     return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(&g_quipu_err);
 }

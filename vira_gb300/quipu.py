@@ -219,6 +219,9 @@ class DEMQuipu:
         nb = nbands or self.nbands
         nv = L.width * L.height
         nq = (L.width - 1) * (L.height - 1)
+        if L.width < 2 or L.height < 2 or nv >= 1 << 31:   # checked again by vgb_quipu_read_mesh
+            raise capi.VgbError(1, f"quipu_read_mesh: LoD {lod} has {L.width} x {L.height} posts, "
+                                   "outside 2 x 2 .. 2^31 (32-bit triangle ids)")
         ctx = _mesh_context(gpu)
         lib = capi.load()
         nt = C.c_uint32(0)
