@@ -2103,15 +2103,11 @@ VGB_API vgb_status vgb_quipu_read_mesh(vgb_context* ctx, vgb_quipu_dem* q, uint3
         // every image is its own LZ4 block: the heights and the albedo planes decode in parallel
         const size_t nimg = 1 + (plane_bytes ? pl.planes.size() : 0);
         std::vector<std::string> errs(nimg);
-        auto read_one = [&](size_t k) {
+        vgb::parallel_for_each((uint32_t)nimg, [&](uint32_t k) {
             const vgb::ImageRefView& img = k == 0 ? pl.heights : pl.planes[k - 1].img;
             uint8_t* dst = k == 0 ? hp : hp + code_bytes + (k - 1) * nv;
             if (vgb::quipu_read_pixels(pl.path, img, dst) != VGB_OK) errs[k] = vgb_quipu_last_error();
-        };
-        std::vector<std::thread> workers;
-        for (size_t k = 1; k < nimg; ++k) workers.emplace_back(read_one, k);
-        read_one(0);
-        for (std::thread& t : workers) t.join();
+        });
         for (const std::string& e : errs)
             if (!e.empty()) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "quipu_read_mesh: " + e);
     }

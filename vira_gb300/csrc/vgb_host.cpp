@@ -207,13 +207,10 @@ Split find_split(const Ctx& c, uint32_t first, uint32_t count, const Box& nb, ui
         bin_range(0, count, *total);
     } else {
         std::vector<std::unique_ptr<Bins>> part(nt);
-        std::vector<std::thread> th;
-        for (uint32_t k = 0; k < nt; ++k) {
-            part[k].reset(new Bins());
-            th.emplace_back(bin_range, (uint32_t)((uint64_t)count * k / nt),
-                            (uint32_t)((uint64_t)count * (k + 1) / nt), std::ref(*part[k]));
-        }
-        for (auto& x : th) x.join();
+        for (uint32_t k = 0; k < nt; ++k) part[k].reset(new Bins());
+        vgb::parallel_for_each(nt, [&](uint32_t k) {
+            bin_range((uint32_t)((uint64_t)count * k / nt), (uint32_t)((uint64_t)count * (k + 1) / nt), *part[k]);
+        });
         for (int a = 0; a < 3; ++a) for (int b = 0; b < kBins; ++b) {
             total->b[a][b] = Box(); total->n[a][b] = 0;
             for (uint32_t k = 0; k < nt; ++k) { total->b[a][b].grow(part[k]->b[a][b]); total->n[a][b] += part[k]->n[a][b]; }
@@ -362,20 +359,16 @@ bool build_bvh(const float* pos, uint32_t nverts, const uint32_t* idx, uint32_t 
     if (!tasks.empty()) {
         std::atomic<size_t> next{0};
         std::vector<uint32_t> depths(threads, 0);
-        std::vector<std::thread> th;
-        for (uint32_t k = 0; k < threads; ++k) {
-            th.emplace_back([&, k] {
-                while (true) {
-                    size_t ti = next.fetch_add(1);
-                    if (ti >= tasks.size()) break;
-                    const Task& t = tasks[ti];
-                    uint32_t md = 0;
-                    build_rec(c, arenas[t.arena], t.arena, t.first, t.count, 1, 0, md);
-                    depths[k] = std::max(depths[k], md);
-                }
-            });
-        }
-        for (auto& x : th) x.join();
+        vgb::parallel_for_each(threads, [&](uint32_t k) {
+            while (true) {
+                size_t ti = next.fetch_add(1);
+                if (ti >= tasks.size()) break;
+                const Task& t = tasks[ti];
+                uint32_t md = 0;
+                build_rec(c, arenas[t.arena], t.arena, t.first, t.count, 1, 0, md);
+                depths[k] = std::max(depths[k], md);
+            }
+        });
         uint32_t md = 0;
         for (uint32_t d : depths) md = std::max(md, d);
         max_depth += md + 1;

@@ -19,6 +19,7 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/vgb.h"
@@ -54,6 +55,35 @@ inline vgb_status status_of_exception(std::string* err) noexcept {
         }
     }
     return s;
+}
+
+// Runs body(k) for k = 0..n-1, each on its own thread (k = 0 on the calling thread).  A thread
+// that cannot start leaves its k to the calling thread; an exception thrown by any body is
+// rethrown here after every thread has joined, so none escapes a thread and no thread is left
+// running when the caller unwinds.
+template <class F>
+void parallel_for_each(uint32_t n, F&& body) {
+    if (n == 0) return;
+    std::vector<std::exception_ptr> errs(n);
+    auto run = [&](uint32_t k) noexcept {
+        try {
+            body(k);
+        } catch (...) {
+            errs[k] = std::current_exception();
+        }
+    };
+    std::vector<std::thread> th;
+    th.reserve(n);
+    uint32_t handed = 1;
+    try {
+        for (; handed < n; ++handed) th.emplace_back(run, handed);
+    } catch (...) {
+    }
+    for (uint32_t k = handed; k < n; ++k) run(k);
+    run(0);
+    for (std::thread& t : th) t.join();
+    for (const std::exception_ptr& e : errs)
+        if (e) std::rethrow_exception(e);
 }
 
 constexpr int kLeafShift = 3;
