@@ -46,6 +46,19 @@ using namespace vgbd;
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
 #endif
+// Grids of the wavefront kernels (grid-stride loops over the bounce's items), in blocks per SM;
+// 0 launches one 256-thread block per 256 items.  Many waves of short blocks let the block
+// scheduler even out rays of uneven cost: on the path-traced frame (2048^2 items) the closest-hit
+// launch fell from 380 us at 8 blocks per SM to 332 us at 60, and the frame from 249 to 224 ms.
+#ifndef VGB_TRACE_GRID
+#define VGB_TRACE_GRID 60
+#endif
+#ifndef VGB_SHADE_GRID
+#define VGB_SHADE_GRID 48
+#endif
+#ifndef VGB_SHADOW_GRID
+#define VGB_SHADOW_GRID 60
+#endif
 
 namespace {
 
@@ -1037,7 +1050,7 @@ DevScene dev_scene(const vgb_context* ctx) {
 
 int grid_for(const vgb_context* ctx, size_t n, int per_sm = 8) {
     size_t blocks = (n + 255) / 256;
-    size_t cap = (size_t)ctx->num_sms * per_sm;
+    size_t cap = per_sm > 0 ? (size_t)ctx->num_sms * per_sm : blocks;
     return (int)std::max<size_t>(1, std::min(blocks, cap));
 }
 
@@ -1070,7 +1083,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
     const DevScene s = dev_scene(ctx);
     DevState st = ctx->st;
     const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
-    const int g0 = grid_for(ctx, n0);
+    const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
+    const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
     const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
     for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
         uint32_t q = 0;
@@ -1080,16 +1094,16 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
             {
                 Prof p(ctx, 0);
-                k_trace<L, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                k_trace<L, COUNT><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             {
                 Prof p(ctx, 3);
-                k_shade<NB><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                k_shade<NB><<<gs, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
                 Prof p(ctx, 1);
-                k_shadow<NB, L, COUNT><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                k_shadow<NB, L, COUNT><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
@@ -2552,18 +2566,19 @@ template <int NB, int L>
 void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, uint32_t& launches) {
     const DevScene s = dev_scene(ctx);
     const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
-    const int g0 = grid_for(ctx, n0);
+    const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
+    const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
     const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
     for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
         uint32_t q = 0;
         for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
             cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
             cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
-            k_trace<L, false><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
-            k_shade<NB><<<g0, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            k_trace<L, false><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+            k_shade<NB><<<gs, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
-                k_shadow<NB, L, false><<<g0, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                k_shadow<NB, L, false><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
