@@ -39,7 +39,7 @@ ROOT = Path(__file__).resolve().parent
 # k_trace launches of one sample, averaged over its four bounces); see
 # profiles/traffic_path_traced_dem4097_2048px.md for the command and the per-launch figures.
 MEASURED_TRAFFIC = {
-    ("path_traced_dem4097_tex4096_2048px_64spp_3b_rr2_8band", 2): {"k_trace": 125293888.0},
+    ("path_traced_dem4097_tex4096_2048px_64spp_3b_rr2_8band", 2): {"k_trace": 103060416.0},
 }
 sys.path.insert(0, str(ROOT))
 
