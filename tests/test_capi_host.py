@@ -207,3 +207,18 @@ def test_failed_host_allocation_returns_a_status():
     r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.split() == ["3", "21.0"]
+
+
+def test_parallel_for_each_joins_and_rethrows(tmp_path):
+    """The host thread helper behind the Quipu decode and the SAH builder: every body runs once,
+    an exception thrown on a worker (or on the calling thread) reaches the caller only after every
+    other body has finished, and an entry's function-try-block turns it into a status."""
+    import subprocess
+
+    root = Path(__file__).resolve().parents[1]
+    exe = tmp_path / "pfe"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-I", str(root / "include"),
+                    str(root / "tests/cpp/parallel_for_each.cpp"), "-o", str(exe)], check=True, capture_output=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "worker exception -> status 3 after 7 bodies" in r.stdout
