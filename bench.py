@@ -35,12 +35,20 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 
-# ncu capture of the full path-traced frame (dram__bytes_read.sum + dram__bytes_write.sum of the
-# k_trace launches of one sample, averaged over its four bounces); see
-# profiles/traffic_path_traced_dem4097_2048px.md for the command and the per-launch figures.
+# ncu capture of the full path-traced frame: dram__bytes_read.sum + dram__bytes_write.sum of the
+# k_trace launches of one sample, averaged over its four bounces (one pass per launch).
 MEASURED_TRAFFIC = {
     ("path_traced_dem4097_tex4096_2048px_64spp_3b_rr2_8band", 2): {"k_trace": 103060416.0},
 }
+# ncu counters of k_trace on the path-traced workload at scale 0.25 (1025^2 DEM, 512^2, 4 spp):
+# bounce 0 (camera rays) and bounce 1 (diffuse continuation rays).
+MEASURED_TRACE_COUNTERS = {
+    "case": "path_traced scale 0.25 (1025^2 DEM + craters, 512^2, 4 spp, 3 bounces)",
+    "issue_active_pct": {"bounce0": 57.7, "bounce1": 48.65},
+    "l1_throughput_pct": {"bounce0": 49.27, "bounce1": 31.2},
+    "threads_per_warp_inst": {"bounce0": 26.0, "bounce1": 16.02},
+}
+L2_PROBE_BYTES = 64 << 20
 sys.path.insert(0, str(ROOT))
 
 TRI_BYTES = 48
@@ -89,16 +97,30 @@ def workload_params(args):
     return dict(kind="plain_direct", posts=posts, resolution=res, spp=args.spp or 1, bounces=0)
 
 
-def build_scene(p, device):
+def build_scene(p, device, mesher=None):
+    """The workload's scene; `mesher` triangulates the DEM (default: the product's host code; the
+    reference arm passes the oracle's restatement so that it never loads libvgb.so)."""
     from vira_gb300 import workloads
 
     if p["kind"] == "path_traced":
         scene, cam = workloads.path_traced(posts=p["posts"], tex=p["tex"], resolution=p["resolution"], spp=p["spp"],
-                                           bounces=p["bounces"], rr_depth=p["rr_depth"], device=device)
+                                           bounces=p["bounces"], rr_depth=p["rr_depth"], device=device, mesher=mesher)
     else:
-        scene, cam = workloads.plain_direct(posts=p["posts"], resolution=p["resolution"], device=device)
+        scene, cam = workloads.plain_direct(posts=p["posts"], resolution=p["resolution"], device=device, mesher=mesher)
         scene.pathtracer.options.samples = p["spp"]
     return scene, cam
+
+
+def bench_config(p, world):
+    """The workload as both arms report it (`config` of the JSON line)."""
+    res = p["resolution"]
+    out = {"workload": config_name(p), "triangles": 2 * (p["posts"] - 1) ** 2, "image": [res, res],
+           "spp": p["spp"], "bounces": p["bounces"], "bands": 8 if p["kind"] == "path_traced" else 4}
+    if p["kind"] == "path_traced":
+        out["rr_after_bounce"] = p["rr_depth"]
+    out["l2"] = "flushed between timed GPU renders (256 MB write); the scene working set also exceeds L2"
+    out["parallelism"] = "replicas" if world > 1 else "none (one device or one host process)"
+    return out
 
 
 def config_name(p):
@@ -163,68 +185,87 @@ def oracle_scene(scene):
     return oracle.OracleScene.from_flat(scene.flat, scene.bands.size)
 
 
-def cpu_sample(scene, cam_id, osc, seconds: float, threads: int, start_row=None):
-    """Times the oracle over bands of rows of the same frame until ~`seconds` of CPU work."""
-    cam = scene[cam_id].to_c(scene.origin, scene.bands.size)
-    lights, nl = scene.c_lights()
-    opts = scene.pathtracer.c_options(scene)
-    H = cam.height
-    rows, total_rays, total_t, spp_px = 0, 0, 0.0, 0
-    r = max(0, H // 2 - 1) if start_row is None else start_row % H
-    nrows = 1
-    while total_t < seconds and r < H:
-        t = time.perf_counter()
-        _, counts = osc.render(cam, lights, nl, opts, rows=(r, min(H, r + nrows)), threads=threads)
-        dt = time.perf_counter() - t
-        total_t += dt
-        total_rays += counts[0] + counts[1]
-        done = min(H, r + nrows) - r
-        rows += done
-        spp_px += done * cam.width * opts.samples
-        r += done
-        if dt < seconds / 8:
-            nrows = min(H, nrows * 2)
-    return {"mrays_s": total_rays / total_t / 1e6, "spp_s": spp_px / total_t, "rows": rows, "seconds": total_t,
-            "rays": total_rays}
+# The CPU sample of the frame both CPU legs time: every 64th row (rows 31, 95, 159, ...; a
+# stratified sample of 1/64 of the frame's pixels at the frame's full samples per pixel).
+ROW_STRIDE, ROW_OFFSET = 64, 31
+
+
+def sample_rows(H: int):
+    stride = max(1, min(ROW_STRIDE, H // 4))
+    return list(range(ROW_OFFSET % stride, H, stride))
+
+
+# the film planes both arms write per step
+STEP_PLANES = ("total_radiance", "received_power", "triangle_id", "depth")
+
+
+def cpu_step(cam, lights, nl, opts, osc, threads: int, omega):
+    """One pass of the oracle over the sampled rows, writing the planes the GPU arm writes;
+    returns (rays, pixel samples, seconds)."""
+    rays = 0
+    t = time.perf_counter()
+    for row in sample_rows(cam.height):
+        _, counts = osc.render(cam, lights, nl, opts, omega=omega, rows=(row, row + 1), threads=threads,
+                               outputs=STEP_PLANES, fill=False)
+        rays += counts[0] + counts[1]
+    dt = time.perf_counter() - t
+    return rays, len(sample_rows(cam.height)) * cam.width * opts.samples, dt
+
+
+def cpu_sample(cam, lights, nl, opts, osc, seconds: float, threads: int, omega):
+    """Repeats cpu_step until about `seconds` of CPU work (at least one pass)."""
+    rays, px, total = 0, 0, 0.0
+    passes = 0
+    while passes == 0 or total < seconds:
+        r, n, dt = cpu_step(cam, lights, nl, opts, osc, threads, omega)
+        rays, px, total, passes = rays + r, px + n, total + dt, passes + 1
+    return {"mrays_s": rays / total / 1e6, "spp_s": px / total, "passes": passes, "seconds": total, "rays": rays}
+
+
+def sample_text(cam, opts):
+    rows = sample_rows(cam.height)
+    stride = rows[1] - rows[0] if len(rows) > 1 else 1
+    return (f"rows {rows[0]}, {rows[0] + stride}, ... ({len(rows)} rows, 1 in {stride}) x {cam.width} px of the "
+            f"frame at {opts.samples} spp (CPU restatement of cpu_path_tracer.ipp, BVH2 of vira_blas.ipp, not Embree)")
 
 
 def run_reference(args, p, rank, world):
+    """The reference arm: the oracle's CPU path tracer on all host threads over the fixed row
+    sample of the frame.  The scene is built from numpy and the oracle's own triangulation,
+    normals and intrinsics; libvgb.so is never loaded."""
     if rank != 0:
         return
     from oracle import oracle
 
-    scene, cam_id = build_scene(p, device=0)
+    scene, cam_id = build_scene(p, device=0, mesher=oracle.dem_mesh)
     threads = oracle.nthreads()
     osc = oracle_scene(scene)  # the oracle's own BVH, built once outside the timed steps
-    per_step = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    camera = scene[cam_id]
+    cam = camera.to_c(scene.origin, scene.bands.size, kinv=oracle.camera_kinv(camera))
+    lights, nl = scene.c_lights()
+    opts = scene.pathtracer.c_options(scene)
+    omega = oracle.pixel_solid_angle(cam)   # Camera::initialize, outside the timed steps
     for _ in range(args.warmup):
-        cpu_sample(scene, cam_id, osc, min(per_step, 2.0), threads)
-    vals, spps, rows, secs = [], [], 0, 0.0
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        s = cpu_sample(scene, cam_id, osc, per_step, threads, start_row=scene[cam_id].resolution[1] // 4 + 17 * k)
-        vals.append(s["mrays_s"])
-        spps.append(s["spp_s"])
-        rows = s["rows"]
-        secs += s["seconds"]
+        cpu_step(cam, lights, nl, opts, osc, threads, omega)
+    rays, px, secs = 0, 0, 0.0
+    for _ in range(args.steps):
+        r, n, dt = cpu_step(cam, lights, nl, opts, osc, threads, omega)
+        rays, px, secs = rays + r, px + n, secs + dt
     osc.close()
-    elapsed = time.perf_counter() - t0
-    v = float(np.mean(vals))
-    W = scene[cam_id].resolution[0]
+    v = rays / secs / 1e6
     line = {
         "metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * secs / max(1, args.steps), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm + craters)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm DEM + Poisson craters, lognormal albedo); random-free poses",
         "impl": "reference",
-        "config": {"workload": config_name(p), "parallelism": "host threads"},
-        "spectral_path_samples_per_s": float(np.mean(spps)),
+        "config": bench_config(p, 1),
+        "spectral_path_samples_per_s": px / secs,
         "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: a band of ~{rows} rows x {W} px of the frame at full spp "
-                                   f"(CPU restatement of cpu_path_tracer.ipp, BVH2 of vira_blas.ipp, not Embree)"},
+                         "sample": "each step: " + sample_text(cam, opts)},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
-    scene.close()
 
 
 # ------------------------------------------------------------------------ GPU leg
@@ -291,6 +332,16 @@ def reduce_replicas(total_ms: float, rays: float, paths: float, world: int, devi
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     dist.all_reduce(w, op=dist.ReduceOp.SUM)
     return float(t[0]), float(w[0]), float(w[1])
+
+
+def l2_peak(lib, ctx):
+    """GB/s of streaming reads of an L2-resident 64 MiB buffer (vgb_measure_l2_read: 20 passes
+    per launch, best of 5 launches, CUDA events)."""
+    from vira_gb300 import capi
+
+    g = C.c_double(0.0)
+    capi.check(lib.vgb_measure_l2_read(ctx, L2_PROBE_BYTES, 20, 5, C.byref(g)), ctx, "measure_l2_read")
+    return float(g.value)
 
 
 def measured_peaks():
@@ -387,9 +438,14 @@ def run_ours(args, p, rank, world, local_rank):
     per_launch_ms = dms / max(1, dl)
     achieved = per_launch_bytes / (per_launch_ms / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
+    l2 = l2_peak(lib, r.ctx)
     # DRAM bytes (read + write) per launch of the dominant kernel from one ncu capture of this
-    # workload (profiles/traffic_path_traced_dem4097_2048px.md), or None for other workloads.
+    # workload, or None for other workloads.
     traffic = MEASURED_TRAFFIC.get((config_name(p), args.layout), {}).get(dominant)
+    # the traversal kernels read their nodes and triangles through L1/L2: their bound is the L2
+    # read bandwidth; the shading and film kernels stream HBM
+    traversal = dominant in ("k_trace", "k_shadow")
+    bound_peak = l2 if traversal else peak
 
     after_film = None
     if not args.no_after_film and p["kind"] == "path_traced" and rank == 0:
@@ -425,11 +481,11 @@ def run_ours(args, p, rank, world, local_rank):
 
         threads = oracle.nthreads()
         osc = oracle_scene(scene)
-        c = cpu_sample(scene, cam_id, osc, args.cpu_seconds, threads)
+        c = cpu_sample(r.cam, r.lights, r.nl, r.opts, osc, args.cpu_seconds, threads, r.omega.cpu().numpy())
         osc.close()
         cpu = {"value": c["mrays_s"], "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": f"rows {c['rows']} x {r.cam.width} px of the same frame at {r.opts.samples} spp "
-                         f"({c['rays']} rays in {c['seconds']:.1f} s; CPU restatement, BVH2 of vira_blas.ipp, not Embree)"}
+               "sample": f"{c['passes']} passes over " + sample_text(r.cam, r.opts) +
+                         f"; {c['rays']} rays in {c['seconds']:.1f} s"}
     if rank == 0:
         launches = int(sum(s.kernel_launches for s in st_list))
         line = {
@@ -437,24 +493,29 @@ def run_ours(args, p, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded fBm DEM + Poisson craters, lognormal albedo); random-free poses",
-            "config": {"workload": config_name(p), "triangles": int(scene.flat["indices"].shape[0]),
-                       "image": [r.cam.width, r.cam.height], "spp": int(r.opts.samples),
-                       "bounces": int(r.opts.bounces), "rr_after_bounce": int(r.opts.rr_depth), "bands": B,
-                       "l2": "flushed between timed renders (256 MB write); scene working set also exceeds L2",
-                       "bvh": {"layout": f"{args.layout}-wide" if args.layout == 8 else "binary",
-                               "nodes": int(cst.bvh_nodes), "node_bytes": int(cst.bvh_node_bytes)},
-                       "traversal_counts_per_frame": {"nodes_closest": int(cst.nodes_closest),
-                                                      "tris_closest": int(cst.tris_closest),
-                                                      "nodes_shadow": int(cst.nodes_visited - cst.nodes_closest),
-                                                      "tris_shadow": int(cst.tris_tested - cst.tris_closest)},
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(p, world),
+            "bvh": {"layout": f"{args.layout}-wide" if args.layout == 8 else "binary",
+                    "nodes": int(cst.bvh_nodes), "node_bytes": int(cst.bvh_node_bytes)},
+            "traversal_counts_per_frame": {"nodes_closest": int(cst.nodes_closest),
+                                           "tris_closest": int(cst.tris_closest),
+                                           "nodes_shadow": int(cst.nodes_visited - cst.nodes_closest),
+                                           "tris_shadow": int(cst.tris_tested - cst.tris_closest)},
             "spectral_path_samples_per_s": paths / (total_ms / 1000.0),
             "rays_per_step": rays / args.steps / max(1, world),
             "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(r.h2d_bytes),
                     "d2h_bytes_per_step": int(r.d2h_bytes)},
-            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "roofline": {"bound": "l2" if traversal else "hbm", "kernel": dominant, "achieved": achieved,
+                         "peak": bound_peak, "unit": "GB/s", "frac": achieved / bound_peak,
+                         "peak_source": ("measured L2 read bandwidth (vgb_measure_l2_read, 64 MiB L2-resident buffer, "
+                                         "same run)") if traversal else f"{peak_kind} HBM copy bandwidth (MEASURED_PEAKS.json)",
+                         "traffic": traffic,
                          "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                         "hbm": {"achieved": (traffic / (per_launch_ms / 1000.0) / 1e9) if traffic else None,
+                                 "peak": peak, "frac": (traffic / (per_launch_ms / 1000.0) / 1e9 / peak) if traffic else None,
+                                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
+                                 "note": "DRAM bytes per launch (ncu) over the live launch time"},
+                         "l2_peak_gb_s": l2,
+                         "ncu": MEASURED_TRACE_COUNTERS if traversal else None,
                          "kernel_share": {k: v[0] / max(1e-9, sum(x[0] for x in fam.values())) for k, v in fam.items()}},
             "gpu_launches": launches,
             "setup_s": {"scene": t1 - t0, "upload_and_bvh": t2 - t1},
@@ -934,9 +995,12 @@ def plain_direct_item(torch, dev, layout=2, cpu_seconds=0.0):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     for _ in range(5):
         r.render()
-    ms, rays = [], 0
+    ms, rays, trav_ms = [], 0, 0.0
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(20):
+    for it in range(40):
+        # even renders: the frame time; odd renders: per-launch events for the traversal kernels
+        prof = it % 2 == 1
+        r.lib.vgb_set_profiling(r.ctx, 1 if prof else 0)
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
             ev0.record(stream)
@@ -944,9 +1008,13 @@ def plain_direct_item(torch, dev, layout=2, cpu_seconds=0.0):
         with torch.cuda.stream(stream):
             ev1.record(stream)
         ev1.synchronize()
-        ms.append(ev0.elapsed_time(ev1))
         st = r.stats()
-        rays += st.rays_closest + st.rays_shadow
+        if prof:
+            trav_ms += st.ms_trace + st.ms_shadow
+        else:
+            ms.append(ev0.elapsed_time(ev1))
+            rays += st.rays_closest + st.rays_shadow
+    r.lib.vgb_set_profiling(r.ctx, 0)
     # algorithmic bytes of the same frame (counting pass: nodes x 64 B + triangles x 48 B)
     lib = r.lib
     capi.check(lib.vgb_set_count_pass(r.ctx, 1), r.ctx, "count_pass")
@@ -955,21 +1023,27 @@ def plain_direct_item(torch, dev, layout=2, cpu_seconds=0.0):
     capi.check(lib.vgb_set_count_pass(r.ctx, 0), r.ctx, "count_pass")
     alg = int(cst.nodes_visited) * int(cst.bvh_node_bytes) + int(cst.tris_tested) * int(cst.tri_record_bytes)
     tot = sum(ms)
+    l2 = l2_peak(lib, r.ctx)
+    trav_gbs = alg / (trav_ms / len(ms) / 1000.0) / 1e9
     out = {"workload": "plain_direct_dem513_1024px_1spp_4band", "mrays_s": rays / (tot / 1000.0) / 1e6,
            "ms_per_frame": tot / len(ms), "rays_per_frame": rays / len(ms),
-           "traversal_gb_s": alg / (tot / len(ms) / 1000.0) / 1e9,
-           "traversal_note": "node + triangle bytes per frame over the frame time; the 0.52M-triangle BVH "
-                             "(17 MB nodes, 25 MB triangles) is L2-resident, and no L2 peak is in the measured "
-                             "peaks, so no fraction is reported"}
+           "roofline": {"bound": "l2", "kernels": "k_trace + k_shadow", "achieved": trav_gbs, "peak": l2, "unit": "GB/s",
+                        "frac": trav_gbs / l2, "traversal_ms_per_frame": trav_ms / len(ms),
+                        "algorithmic_bytes_per_frame": alg,
+                        "peak_source": "measured L2 read bandwidth (vgb_measure_l2_read, 64 MiB, same run)",
+                        "note": "node + triangle bytes of the counting pass over the traversal kernels' time "
+                                "(CUDA events per launch); the 0.52M-triangle BVH (17 MB nodes, 25 MB triangles) "
+                                "is L2-resident"}}
     if cpu_seconds > 0:
         from oracle import oracle
 
         threads = oracle.nthreads()
         osc = oracle_scene(scene)
-        c = cpu_sample(scene, cam_id, osc, cpu_seconds, threads, start_row=0)
+        c = cpu_sample(r.cam, r.lights, r.nl, r.opts, osc, cpu_seconds, threads, r.omega.cpu().numpy())
         osc.close()
         out["cpu_baseline"] = {"value": c["mrays_s"], "unit": "Mrays/s", "cores": threads, "kind": "port",
-                               "sample": f"rows 0-{c['rows']} of the frame ({c['rays']} rays in {c['seconds']:.1f} s)"}
+                               "sample": f"{c['passes']} passes over " + sample_text(r.cam, r.opts) +
+                                         f"; {c['rays']} rays in {c['seconds']:.1f} s"}
     scene.close()
     return out
 

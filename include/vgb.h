@@ -59,12 +59,26 @@ typedef struct vgb_context vgb_context;
 
 /* ---- camera: FP32 constants derived on the host in FP64 -------------------------
  * Replaces Camera::pixelToRay (include/implementation/cameras/camera.ipp:1126-1131,
- * 1143-1163), pixelToDirectionHelper (:1738-1749) and
+ * 1143-1163), pixelToDirection / pixelToDirectionHelper (:1105-1117, 1738-1749) and
  * ReferenceFrame::localDirectionToGlobal (include/implementation/reference_frame.ipp:361-364).
  * The ray of pixel coordinate (x, y) is
- *     d_cam = { kinv·(x, y, 1) [row 0],  z_dir * kinv·(x, y, 1) [row 1],  z_dir }
+ *     h     = kinv·(x, y, 1), then h = undistort(h) when a distortion model is set
+ *     d_cam = { h[0],  z_dir * h[1],  z_dir }
  *     dir   = normalize(rotation · d_cam),   origin = origin.
- */
+ * With a distortion and interpolate_directions (the reference's default), d_cam is instead the
+ * bilinear interpolation (Image::interpolatePixel) of normalize(d_cam) at the four surrounding
+ * integer pixels, as Camera::precomputePixelDirections (:1676-1700) tabulates it.
+ * Depth of field (samples >= 1 only, as the reference's sample 0 goes through the pinhole
+ * overload): a point a of the circular aperture (radius * UniformDiskSample) moves the origin by
+ * rotation · (a.x, a.y, focal_length), and with a finite focus distance the camera direction
+ * becomes focus_distance * normalize(d_cam) - (a.x, a.y, focal_length). */
+typedef enum vgb_distortion_model {
+    VGB_DISTORTION_NONE = 0,
+    VGB_DISTORTION_BROWN = 1,   /* coeffs: k1 k2 k3 p1 p2 (brown_distortion.ipp) */
+    VGB_DISTORTION_OPENCV = 2,  /* coeffs: k1 k2 k3 k4 k5 k6 p1 p2 s1 s2 s3 s4 (opencv_distortion.ipp) */
+    VGB_DISTORTION_OWEN = 3     /* coeffs: e1 e2 e3 e4 e5 e6 (owen_distortion.ipp) */
+} vgb_distortion_model;
+
 typedef struct vgb_camera {
     uint32_t width;            /* resolution x (columns, index i) */
     uint32_t height;           /* resolution y (rows, index j) */
@@ -73,6 +87,26 @@ typedef struct vgb_camera {
     float kinv[6];             /* inverse intrinsic matrix, column-major 3 columns x 2 rows */
     float z_dir;               /* +1, or -1 for the Blender frame */
     float power_scale[VGB_MAX_BANDS]; /* optical efficiency[b] * aperture area (received power) */
+    /* lens distortion (Camera::setBrownDistortion / setOpenCVDistortion / setOwenDistortion):
+     * undistorted by 20 fixed-point iterations in FP32 for rays and the pixel solid angle,
+     * distorted in the rasterizer's projection (Camera::projectCameraPoint, camera.ipp:1060-1080) */
+    uint32_t distortion;       /* vgb_distortion_model */
+    float distortion_coeffs[12];
+    uint32_t interpolate_directions; /* Camera::interpolate_distortion_directions_ (default 1) */
+    /* depth of field (Camera::enableDepthOfField, setFocusDistance, CircularAperture) */
+    uint32_t depth_of_field;   /* 0: pinhole for every sample (reference default) */
+    float aperture_radius;     /* focal_length / f_stop / 2 (metres) */
+    float focal_length;        /* metres */
+    float focus_distance;      /* metres; +inf keeps the pinhole direction (reference default) */
+    /* first-hit passes (cpu_path_tracer.ipp:356-372): Camera::calculateGSD's sensor size and the
+     * camera's motion.  The reference evaluates the camera's point velocity at the hit point's
+     * global coordinates taken as if they were camera-local (localPointToGlobalVelocity on
+     * intersection_global), i.e. at rotation * p_global; rot_origin = rotation * (scene origin),
+     * FP64 then FP32, restores that term in the rebased frame: rotation * p + rot_origin. */
+    float sensor_size[2];      /* metres */
+    float velocity[3];         /* global frame, m/s */
+    float angular_rate[3];     /* global frame, rad/s */
+    float rot_origin[3];
 } vgb_camera;
 
 /* ---- sphere light (Vira's SphereLight; the Sun is one) --------------------------
@@ -140,6 +174,11 @@ typedef struct vgb_film {
     uint32_t* triangle_id;     /* [H][W]; VGB_NO_HIT where nothing was hit */
     const float* pixel_solid_angle; /* [H][W] input, from vgb_pixel_solid_angle */
     int32_t on_device;         /* 1: every pointer is device memory; 0: host memory */
+    /* renderPasses.save_velocity / save_triangle_size (passes.hpp:79-85), set at a pixel's first
+     * hit (cpu_path_tracer.ipp:356-372); pixels that never hit keep 0 / +inf */
+    float* velocity_global;    /* [3][H][W] the hit point's velocity (instance motion) */
+    float* velocity_camera;    /* [3][H][W] relative to the camera, in the camera frame */
+    float* triangle_size;      /* [H][W] longest edge of the hit triangle / GSD at the hit distance */
 } vgb_film;
 
 /* ---- BVH build options -------------------------------------------------------- */
@@ -216,6 +255,29 @@ VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* positions, ui
                                     const float* vert_albedo, const float* vert_normal,
                                     const float* vert_uv, const float* texture,
                                     uint32_t tex_w, uint32_t tex_h);
+/* Instance motion for the first-hit velocity pass (ReferenceFrame::localPointToGlobalVelocity,
+ * reference_frame.ipp:367-373): velocity = v + angular_rate x (p - position) for the triangles
+ * [first_triangle, next instance's first_triangle) of the uploaded (flattened) mesh. */
+typedef struct vgb_instance_motion {
+    uint32_t first_triangle;   /* ascending over the table, the first entry 0 */
+    float velocity[3];         /* global frame, m/s */
+    float angular_rate[3];     /* global frame, rad/s */
+    float position[3];         /* the instance's origin in the scene frame (rebased FP64, then FP32) */
+} vgb_instance_motion;
+
+/* Replaces the motion table of the uploaded scene (host pointer; n = 0 or NULL: every instance at
+ * rest).  Set it after vgb_scene_upload, which clears it. */
+VGB_API vgb_status vgb_scene_motion(vgb_context* ctx, const vgb_instance_motion* motion, uint32_t n);
+
+/* Material::setNormalMap / getNormal (include/implementation/materials/material.ipp:120-143,
+ * cpu_path_tracer.ipp:316-329): a tangent-space normal map [h][w][3] (host pointer) for the
+ * uploaded scene, sampled like the albedo texture (wrap + bilinear at uv * resolution); at a hit
+ * the shading normal becomes normalize([tangent | bitangent | N] * sample), used by next-event
+ * estimation, MIS, the film's normal and the rasterizer, while the continuation direction is
+ * still sampled in the frame built before the map (the reference's order).  NULL (or w or h 0)
+ * removes the map.  Set it after vgb_scene_upload, which clears it.  The adjoint entry points
+ * reject a scene with a normal map (its derivative is not formed). */
+VGB_API vgb_status vgb_scene_normal_map(vgb_context* ctx, const float* normal_map, uint32_t w, uint32_t h);
 /* Replaces Mesh::buildBVH -> EmbreeBLAS (include/implementation/geometry/mesh.ipp:396-408,
  * include/implementation/rendering/acceleration/embree_blas.ipp:14-71). */
 VGB_API vgb_status vgb_bvh_build(vgb_context* ctx, const vgb_bvh_options* opts);
@@ -241,16 +303,24 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
  * device memory to manage.  For callers that cannot allocate device memory once their scene is
  * set up -- a frame loop held to a fixed memory budget, or a host application whose own
  * allocator owns the device -- because a cudaMalloc inside a render call can synchronize the
- * device or fail.  Same kernels and results as vgb_render, with every byte of scratch taken
- * from one fixed 8 MiB array compiled into the library, which every GPU that loads the library
- * holds until the process exits.  Limits: the film must be device memory, and a frame of
- * P = width*height pixels, B bands and L lights needs about P * 4 * (19 + 6*B + L*(8 + B))
- * bytes of the 8 MiB (about 25,000 pixels at 8 bands and 1 light, 38,000 at 4 bands); larger
- * frames are rejected with VGB_ERR_INVALID_ARGUMENT and a message naming the sizes.  The
- * first call on a device looks up the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  All calls on a device share the array and it
- * keeps the last call's contents (each call clears its counters itself): calls that overlap on
- * the GPU -- two contexts or two streams rendering at once on one device -- race. */
+ * device or fail.  Same launch sequence, kernels and results as vgb_render (bit for bit), with
+ * every byte of scratch taken from one fixed 8 MiB array compiled into the library, which every
+ * GPU that loads the library holds until the process exits.  Limits: the film must be device
+ * memory; a frame of P = width*height pixels (T = its pixels rounded up to whole 8x4 tiles),
+ * B bands and L lights needs about 4 * (P * (15 + 6*B + L*(8 + B)) + 4*T) bytes of the 8 MiB
+ * (about 25,000 pixels at 8 bands and 1 light, 38,000 at 4 bands); larger frames are rejected
+ * with VGB_ERR_INVALID_ARGUMENT and a message naming the sizes, as are frames past vgb_render's
+ * limits; adaptive sampling and denoising are refused.  The first call on a context looks up
+ * the array's device address (cudaGetSymbolAddress) with the context's device current: make
+ * that first call before any stream capture.  The first call for a band count (1, 2-4, 5-8)
+ * and BVH layout may load those kernels' code onto the device under CUDA's lazy module loading
+ * (CUDA_MODULE_LOADING=EAGER loads them all at start-up).  Each call waits for ctx's stream
+ * and copies the device error word and ray counts to the host before it returns, as vgb_render
+ * does; vgb_get_stats then reports the rays, launches and device time of this call and zeros
+ * for the counting-pass and profiling fields, which this entry point does not fill.  All calls
+ * on a device share the array and it keeps the last call's contents (each call clears its
+ * counters itself): calls that overlap on the GPU -- two contexts or two streams rendering at
+ * once on one device -- race. */
 VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_camera* cam, const vgb_light* lights,
                                       uint32_t nlights, const vgb_pt_options* opts, vgb_film* film);
 /* ---- batched trajectory rendering -------------------------------------------------
@@ -417,6 +487,20 @@ VGB_API vgb_status vgb_set_count_pass(vgb_context* ctx, int enable);
 /* Per-launch CUDA events around every kernel of vgb_render, summed per kernel family into
  * vgb_stats.ms_trace / ms_shade / ms_shadow / ms_film. */
 VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
+/* Read bandwidth of the GPU's L2 (a measurement utility; no counterpart in the reference): a
+ * `bytes` buffer (1 MiB..16 GiB, a multiple of 16) is allocated on the context's device, read
+ * once to warm the cache, then read `passes` times per launch with L2-only loads in `repeats`
+ * timed launches (CUDA events on the context's stream); *gbps = the best launch's bytes read
+ * per second / 1e9.  A buffer within the L2 (e.g. 64 MiB of GB300's 126 MB) measures L2, a
+ * larger one HBM.  The buffer is freed before return. */
+VGB_API vgb_status vgb_measure_l2_read(vgb_context* ctx, uint64_t bytes, uint32_t passes, uint32_t repeats,
+                                       double* gbps);
+/* Traversal steps (node visits) one ray may take before it gives up; 0 restores the default
+ * of 2^22.  A ray past the limit stops, the call returns VGB_ERR_DEVICE_LIMIT with a message
+ * and the context stays usable.  The limit exists so that no kernel can run unbounded on a
+ * corrupt tree; a small value exercises that path on a healthy scene.  No counterpart in the
+ * reference (Embree has no such limit). */
+VGB_API vgb_status vgb_set_traversal_limit(vgb_context* ctx, uint32_t max_steps);
 
 /* ========================= rasterizer =========================================
  * CPURasterizer::render (include/implementation/rendering/cpu_rasterizer.ipp:29-270) on the

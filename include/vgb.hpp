@@ -11,6 +11,7 @@
 #include <array>
 #include <cmath>
 #include <cstdint>
+#include <initializer_list>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -122,6 +123,29 @@ public:
     NoiseModelConfig noise_model;
     bool simulate_photon_noise = false;
     uint64_t sensor_seed = 0;
+    // lens distortion (Camera::set*DistortionCoefficients) and depth of field
+    vgb_distortion_model distortion = VGB_DISTORTION_NONE;
+    float distortion_coeffs[12] = {0};
+    bool interpolate_distortion_directions = true;
+    bool depth_of_field = false;
+    float focus_distance = INFINITY;
+
+    void setBrownDistortionCoefficients(float k1, float k2, float k3, float p1, float p2) {
+        setDistortion(VGB_DISTORTION_BROWN, {k1, k2, k3, p1, p2});
+    }
+    void setOpenCVDistortionCoefficients(float k1, float k2, float k3, float k4, float k5, float k6, float p1, float p2,
+                                         float s1, float s2, float s3, float s4) {
+        setDistortion(VGB_DISTORTION_OPENCV, {k1, k2, k3, k4, k5, k6, p1, p2, s1, s2, s3, s4});
+    }
+    void setOwenDistortionCoefficients(float e1, float e2, float e3, float e4, float e5, float e6) {
+        setDistortion(VGB_DISTORTION_OWEN, {e1, e2, e3, e4, e5, e6});
+    }
+    void enableDistortionInterpolation(bool on) { interpolate_distortion_directions = on; }
+    void enableDepthOfField(bool on) { depth_of_field = on; }
+    void setFocusDistance(double d) {
+        if (std::isnan(d)) throw Error(VGB_ERR_INVALID_ARGUMENT, "Focus Distance must not be NaN");
+        focus_distance = (float)d;
+    }
 
     void setFocalLength(double f) { focal_length = (float)f; f_stop = (float)f / aperture_diameter; }
     void setFStop(double f) { f_stop = (float)f; aperture_diameter = focal_length / f_stop; }
@@ -165,7 +189,22 @@ public:
         const float d = focal_length / f_stop, r = d / 2.f, area = 3.14159265358979323846f * r * r;
         for (uint32_t k = 0; k < nbands; ++k)
             c.power_scale[k] = optical_efficiency[optical_efficiency.size() == 1 ? 0 : k] * area;
+        c.distortion = (uint32_t)distortion;
+        for (int k = 0; k < 12; ++k) c.distortion_coeffs[k] = distortion_coeffs[k];
+        c.interpolate_directions = interpolate_distortion_directions ? 1u : 0u;
+        c.depth_of_field = depth_of_field ? 1u : 0u;
+        c.aperture_radius = d / 2.f;
+        c.focal_length = focal_length;
+        c.focus_distance = focus_distance;
         return c;
+    }
+
+private:
+    void setDistortion(vgb_distortion_model m, std::initializer_list<float> k) {
+        distortion = m;
+        int i = 0;
+        for (float v : k) distortion_coeffs[i++] = v;
+        for (; i < 12; ++i) distortion_coeffs[i] = 0.f;
     }
 };
 

@@ -44,9 +44,12 @@ def load():
         "oracle_dem_triangulate": (C.c_int, [P, U32, U32, C.c_double, C.c_double, P, P, C.POINTER(U32)]),
         "oracle_intrinsics": (C.c_int, [C.c_float] * 3 + [U32, U32] + [C.c_float] * 5 + [P]),
         "oracle_pixel_solid_angle": (C.c_int, [C.POINTER(capi.Camera), P, C.c_int]),
+        "oracle_distortion": (C.c_int, [C.POINTER(capi.Camera), P, U32, C.c_int, P]),
         "oracle_blackbody_band": (C.c_double, [C.c_double, C.c_float, C.c_float, U32]),
         "oracle_scene_create": (P, [P, U32, P, U32, U32, P, P, P, P, U32, U32]),
         "oracle_scene_destroy": (None, [P]),
+        "oracle_scene_normal_map": (C.c_int, [P, P, U32, U32]),
+        "oracle_scene_motion": (C.c_int, [P, P, U32]),
         "oracle_scene_bvh_nodes": (U32, [P]),
         "oracle_trace": (C.c_int, [P, P, P, P, U32, C.c_int, C.c_int, P, P, P, C.c_int, P, P]),
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
@@ -107,6 +110,41 @@ def intrinsics(focal, sx, sy, W, H, px=np.inf, py=np.inf, kxy=0.0, kyx=0.0, z_di
     return np.array(out[:], np.float32)
 
 
+def dem_mesh(heights, posting, albedo=None, nbands: int = 1):
+    """A DEM mesh built entirely by the oracle (DEM::makeVertexBuffer / imageToIndexBuffer /
+    Mesh::calculateNormals restated), for workload builders that must not load the product
+    library: the same arrays as vira_gb300.Mesh.from_dem plus its vertex normals."""
+    from vira_gb300.scene import Mesh
+
+    pos, idx = dem_triangulate(heights, posting)
+    n = pos.shape[0]
+    alb = None
+    if albedo is not None:
+        a = np.asarray(albedo, np.float32)
+        if a.ndim == 0 or a.size == nbands:
+            alb = np.broadcast_to(a.reshape(1, -1) if a.ndim else a, (n, nbands)).astype(np.float32)
+        else:
+            alb = a.reshape(n, -1).astype(np.float32)
+    return Mesh(pos, idx, albedo=alb, normals=compute_normals(pos, idx))
+
+
+def camera_kinv(camera):
+    """K^-1 of a vira_gb300 Camera by the oracle's restatement of initializeIntrinsicMatrix."""
+    W, H = camera.resolution
+    return intrinsics(camera.focal_length, camera.sensor_size[0], camera.sensor_size[1], W, H,
+                      camera.principal_point[0], camera.principal_point[1], camera.skew[0], camera.skew[1],
+                      camera.intrinsics_z_dir)
+
+
+def distortion(cam: capi.Camera, xy, inverse: bool):
+    """The camera's lens distortion applied to (n, 2) normalised image points (undistort when
+    `inverse`), as the oracle's pixelToDirectionHelper / projectCameraPoint apply it."""
+    p = np.ascontiguousarray(xy, np.float32).reshape(-1, 2)
+    out = np.empty_like(p)
+    assert load().oracle_distortion(C.byref(cam), p.ctypes.data, p.shape[0], int(inverse), out.ctypes.data) == 0
+    return out
+
+
 def pixel_solid_angle(cam: capi.Camera):
     out = np.empty((cam.height, cam.width), np.float32)
     assert load().oracle_pixel_solid_angle(C.byref(cam), out.ctypes.data, nthreads()) == 0
@@ -162,7 +200,7 @@ def denoise(direct, indirect, albedo, depth, normal, levels_direct=5, levels_ind
 class OracleScene:
     """A flattened scene on the CPU with the reference's own BVH (vira_blas.ipp)."""
 
-    def __init__(self, positions, indices, nbands, albedo=None, normals=None, uv=None, texture=None):
+    def __init__(self, positions, indices, nbands, albedo=None, normals=None, uv=None, texture=None, normal_map=None):
         self.keep = [np.ascontiguousarray(positions, np.float32), np.ascontiguousarray(indices, np.uint32)]
         p, i = self.keep
         opt = []
@@ -178,11 +216,24 @@ class OracleScene:
         if not self.h:
             raise ValueError("oracle_scene_create rejected the scene")
         self.nbands = nbands
+        if normal_map is not None:
+            nm = np.ascontiguousarray(normal_map, np.float32)
+            self.keep.append(nm)
+            assert load().oracle_scene_normal_map(self.h, nm.ctypes.data, nm.shape[1], nm.shape[0]) == 0
+
+    def set_motion(self, motion):
+        """The instance motion table (a ctypes array of capi.InstanceMotion, or None)."""
+        self.keep.append(motion)
+        n = 0 if motion is None else len(motion)
+        assert load().oracle_scene_motion(self.h, C.cast(motion, C.c_void_p) if n else None, n) == 0
 
     @staticmethod
     def from_flat(flat, nbands):
-        return OracleScene(flat["positions"], flat["indices"], nbands, flat["albedo"], flat["normals"], flat["uv"],
-                           flat["texture"])
+        o = OracleScene(flat["positions"], flat["indices"], nbands, flat["albedo"], flat["normals"], flat["uv"],
+                        flat["texture"], flat.get("normal_map"))
+        if flat.get("motion") is not None:
+            o.set_motion(flat["motion"])
+        return o
 
     def close(self):
         if self.h:
@@ -256,25 +307,31 @@ class OracleScene:
             raise ValueError("oracle_adjoint_positions rejected its arguments")
         return gt, gp
 
+    PLANES = ("total_radiance", "direct_radiance", "indirect_radiance", "albedo", "normal_global", "depth", "alpha",
+              "triangle_id", "velocity_global", "velocity_camera", "triangle_size")
+
     def render(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, omega=None, rows=None,
-               threads=None):
-        """Renders rows [r0, r1) (all rows by default) into host planes; returns (planes, ray_counts)."""
+               threads=None, outputs=None, fill=True):
+        """Renders rows [r0, r1) (all rows by default) into host planes; returns (planes, ray_counts).
+        `outputs`: the planes to write (default all; received_power too when omega is given);
+        `fill=False` leaves the rows not rendered uninitialised (cheap for a band of rows)."""
         W, H, B = cam.width, cam.height, self.nbands
-        planes = {
-            "total_radiance": np.full((B, H, W), np.nan, np.float32),
-            "direct_radiance": np.full((B, H, W), np.nan, np.float32),
-            "indirect_radiance": np.full((B, H, W), np.nan, np.float32),
-            "albedo": np.full((B, H, W), np.nan, np.float32),
-            "normal_global": np.full((3, H, W), np.nan, np.float32),
-            "depth": np.full((H, W), np.nan, np.float32),
-            "alpha": np.full((H, W), np.nan, np.float32),
-            "triangle_id": np.full((H, W), 0xFFFFFFFF, np.uint32),
-        }
+        shapes = {"normal_global": (3, H, W), "velocity_global": (3, H, W), "velocity_camera": (3, H, W),
+                  "depth": (H, W), "alpha": (H, W), "triangle_id": (H, W), "triangle_size": (H, W)}
+        planes = {}
+        for k in (outputs or self.PLANES):
+            if k == "received_power":
+                continue
+            dt = np.uint32 if k == "triangle_id" else np.float32
+            shape = shapes.get(k, (B, H, W))
+            planes[k] = (np.full(shape, 0xFFFFFFFF if k == "triangle_id" else np.nan, dt) if fill
+                         else np.empty(shape, dt))
         f = capi.Film()
         for k, v in planes.items():
             setattr(f, k, v.ctypes.data)
-        if omega is not None:
-            planes["received_power"] = np.full((B, H, W), np.nan, np.float32)
+        if omega is not None and (outputs is None or "received_power" in outputs):
+            planes["received_power"] = (np.full((B, H, W), np.nan, np.float32) if fill
+                                        else np.empty((B, H, W), np.float32))
             om = np.ascontiguousarray(omega, np.float32)
             f.received_power = planes["received_power"].ctypes.data
             f.pixel_solid_angle = om.ctypes.data

@@ -138,6 +138,9 @@ struct Scene {
     std::vector<uint32_t> idx;
     std::vector<float> tex;      // [th][tw][B]
     uint32_t tw = 1, th = 1;
+    std::vector<float> nmap;     // [nh][nw][3] tangent-space normal map (Material::normalMap), or empty
+    uint32_t nw = 0, nh = 0;
+    std::vector<vgb_instance_motion> motion;   // ascending first_triangle, or empty (all at rest)
     // BVH2, vira_blas layout: leaf when count > 0
     struct Node { float lo[3], hi[3]; uint32_t left_first, count; };
     std::vector<Node> nodes;
@@ -500,6 +503,31 @@ static inline void sample_uvs(const Scene& s, float u, float v, float* out) {
     for (uint32_t k = 0; k < B; ++k) out[k] = ((a * p00[k] + b * p10[k]) + c * p01[k]) + e * p11[k];
 }
 
+// Material::getNormal (materials/material.ipp:129-143): normalMap.sampleUVs(uv) (wrap + bilinear of
+// a vec3<float> image, image.ipp:589-671), times tangentToWorld (columns tangent, bitangent, N),
+// normalised; N unchanged without a map.
+static inline V3 get_normal(const Scene& s, float u, float v, V3 N, V3 tangent, V3 bitangent) {
+    if (s.nmap.empty()) return N;
+    float rx = (float)s.nw, ry = (float)s.nh;
+    float px = std::fmod(u * rx, rx), py = std::fmod(v * ry, ry);
+    if (px < 0) px += rx;
+    if (py < 0) py += ry;
+    int x0 = (int)std::floor(px), y0 = (int)std::floor(py);
+    x0 = std::min(x0, (int)s.nw - 1);
+    y0 = std::min(y0, (int)s.nh - 1);
+    int x1 = std::min(x0 + 1, (int)s.nw - 1), y1 = std::min(y0 + 1, (int)s.nh - 1);
+    auto at = [&](int x, int y) {
+        const float* q = &s.nmap[((size_t)y * s.nw + x) * 3];
+        return V3{q[0], q[1], q[2]};
+    };
+    float dx = px - (float)x0, dy = py - (float)y0;
+    V3 t = (1.f - dx) * (1.f - dy) * at(x0, y0) + dx * (1.f - dy) * at(x1, y0) + (1.f - dx) * dy * at(x0, y1) +
+           dx * dy * at(x1, y1);
+    V3 w{(tangent.x * t.x + bitangent.x * t.y) + N.x * t.z, (tangent.y * t.x + bitangent.y * t.y) + N.y * t.z,
+         (tangent.z * t.x + bitangent.z * t.y) + N.z * t.z};
+    return normalize(w);
+}
+
 // offsetIntersection (ray.ipp:107-123), float path
 static inline float off1(float p, float n) {
     const float origin = 1.f / 32.f, float_scale = 1.f / 65536.f, int_scale = 256.f;
@@ -593,14 +621,162 @@ struct PixelOut {
     V3 normal;
     float depth, alpha;
     uint32_t tri;
+    // first-hit passes (DataPayload defaults: 0 velocities, +inf triangle size)
+    V3 vel_g{0, 0, 0}, vel_c{0, 0, 0};
+    float tsz = INF_F;
 };
+
+// renderPasses.save_triangle_size / save_velocity at the first hit (cpu_path_tracer.ipp:356-372):
+// vert = {v1, v2, v0}; edge lengths, the longest over Camera::calculateGSD (camera.ipp:1408-1414)
+// at |P - camera|; the instance's point velocity v + w x (P - position)
+// (reference_frame.ipp:367-373); the camera's point velocity at rotation * p_global (the
+// reference passes intersection_global to the camera's localPointToGlobalVelocity), the
+// difference taken to the camera frame by the transposed rotation.
+static void first_hit_passes(const Scene& s, const vgb_camera& cam, uint32_t t, V3 P, PixelOut& out) {
+    const V3 a = s.pos[s.idx[3 * t + 1]], b = s.pos[s.idx[3 * t + 2]], c = s.pos[s.idx[3 * t]];
+    float e01 = length(b - a), e02 = length(c - a), e12 = length(c - b);
+    float edge = std::max(e01, std::max(e02, e12));
+    float distance = length(P - V3{cam.origin[0], cam.origin[1], cam.origin[2]});
+    float gx = distance * cam.sensor_size[0] / (cam.focal_length * (float)cam.width);
+    float gy = distance * cam.sensor_size[1] / (cam.focal_length * (float)cam.height);
+    out.tsz = edge / std::min(gx, gy);
+    V3 v{0, 0, 0}, w{0, 0, 0}, o{0, 0, 0};
+    for (const vgb_instance_motion& m : s.motion)
+        if (m.first_triangle <= t) {
+            v = V3{m.velocity[0], m.velocity[1], m.velocity[2]};
+            w = V3{m.angular_rate[0], m.angular_rate[1], m.angular_rate[2]};
+            o = V3{m.position[0], m.position[1], m.position[2]};
+        }
+    out.vel_g = v + cross(w, P - o);
+    V3 rp = mat3_mul(cam.rotation, P) + V3{cam.rot_origin[0], cam.rot_origin[1], cam.rot_origin[2]};
+    V3 cv = V3{cam.velocity[0], cam.velocity[1], cam.velocity[2]} +
+            cross(V3{cam.angular_rate[0], cam.angular_rate[1], cam.angular_rate[2]}, rp);
+    V3 rv = out.vel_g - cv;
+    const float* R = cam.rotation;
+    out.vel_c = V3{(R[0] * rv.x + R[1] * rv.y) + R[2] * rv.z, (R[3] * rv.x + R[4] * rv.y) + R[5] * rv.z,
+                   (R[6] * rv.x + R[7] * rv.y) + R[8] * rv.z};
+}
 
 struct RenderCounters { uint64_t closest = 0, shadow = 0; };
 
+// ---------------------------------------------------------------- camera rays
+// Lens distortion (cameras/distortions/{brown,opencv,owen}_distortion.ipp), FP32, the
+// reference's operation order; Pixel is glm's vec2<float>.
+struct Pix { float x, y; };
+static Pix brown_delta(const float* k, Pix h) {                 // brown_distortion.ipp:24-44
+    float x = h.x, y = h.y;
+    float r = std::sqrt(x * x + y * y);
+    float r2 = r * r, r4 = r2 * r2, r6 = r2 * r2 * r2;
+    float s = (k[0] * r2 + k[1] * r4 + k[2] * r6);
+    Pix rad{s * x, s * y};
+    Pix tan{(2 * k[3] * x * y) + (k[4] * (r2 + 2 * x * x)), (k[3] * (r2 + 2 * y * y)) + (2 * k[4] * x * y)};
+    return Pix{rad.x + tan.x, rad.y + tan.y};
+}
+static Pix opencv_distort(const float* k, Pix h) {              // opencv_distortion.ipp:28-54
+    float x = h.x, y = h.y;
+    float r = std::sqrt(x * x + y * y);
+    float r2 = r * r, r4 = r2 * r2, r6 = r2 * r2 * r2;
+    float numerator = 1 + k[0] * r2 + k[1] * r4 + k[2] * r6;
+    float denominator = 1 + k[3] * r2 + k[4] * r4 + k[5] * r6;
+    float f = numerator / denominator;
+    Pix tp{(2 * k[6] * x * y) + (k[7] * (r2 + 2 * x * x)) + (k[8] * r2) + (k[9] * r4),
+           (k[6] * (r2 + 2 * y * y)) + (2 * k[7] * x * y) + (k[10] * r2) + (k[11] * r4)};
+    return Pix{f * x + tp.x, f * y + tp.y};
+}
+static Pix owen_delta(const float* e, Pix h) {                  // owen_distortion.ipp:24-46
+    float x = h.x, y = h.y;
+    float r = std::sqrt(x * x + y * y);
+    float r2 = r * r, r3 = r * r * r;
+    float rf = (e[1] * r2) + (e[3] * r2 * r2) + (e[4] * y) + (e[5] * x);
+    float of = (e[0] * r) + (e[2] * r3);
+    Pix rot{-y, x};
+    return Pix{rf * x + of * rot.x, rf * y + of * rot.y};
+}
+static Pix compute_delta(const vgb_camera& c, Pix h) {
+    if (c.distortion == VGB_DISTORTION_BROWN) return brown_delta(c.distortion_coeffs, h);
+    if (c.distortion == VGB_DISTORTION_OWEN) return owen_delta(c.distortion_coeffs, h);
+    Pix d = opencv_distort(c.distortion_coeffs, h);              // OpenCV: h - distort(h)
+    return Pix{h.x - d.x, h.y - d.y};
+}
+static Pix undistort(const vgb_camera& c, Pix h) {              // 20 fixed-point iterations
+    Pix u = h;
+    for (size_t i = 0; i < 20; ++i) {
+        Pix d = compute_delta(c, u);
+        u = Pix{h.x - d.x, h.y - d.y};
+    }
+    return u;
+}
+static Pix distort(const vgb_camera& c, Pix h) {
+    if (c.distortion == VGB_DISTORTION_OPENCV) return opencv_distort(c.distortion_coeffs, h);
+    Pix d = compute_delta(c, h);
+    return Pix{h.x + d.x, h.y + d.y};
+}
+// Camera::pixelToDirectionHelper (camera.ipp:1738-1749)
+static V3 direction_helper(const vgb_camera& cam, float X, float Y) {
+    const float* K = cam.kinv;
+    Pix h{(K[0] * X + K[2] * Y) + K[4] * 1.0f, (K[1] * X + K[3] * Y) + K[5] * 1.0f};
+    if (cam.distortion) h = undistort(cam, h);
+    return V3{h.x, cam.z_dir * h.y, cam.z_dir};
+}
+// Camera::pixelToRay (camera.ipp:1105-1163) for one camera: the direction table of
+// precomputePixelDirections (:1676-1700) when a distortion is interpolated, Image::interpolatePixel
+// (image.ipp:619-671) over it, and the depth-of-field overload for samples >= 1.
+struct CameraRays {
+    const vgb_camera& cam;
+    std::vector<V3> table;   // [H][W] normalize(direction_helper(i, j))
+    CameraRays(const vgb_camera& c, int nthreads) : cam(c) {
+        if (!(c.distortion && c.interpolate_directions)) return;
+        const uint32_t W = c.width, H = c.height;
+        table.resize((size_t)W * H);
+        auto work = [&](uint32_t j0, uint32_t j1) {
+            for (uint32_t j = j0; j < j1; ++j)
+                for (uint32_t i = 0; i < W; ++i) table[(size_t)j * W + i] = normalize(direction_helper(c, (float)i, (float)j));
+        };
+        int nt = std::max(1, nthreads);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t) th.emplace_back(work, H * t / nt, H * (t + 1) / nt);
+        for (auto& x : th) x.join();
+    }
+    V3 direction(float X, float Y) const {
+        if (table.empty()) return direction_helper(cam, X, Y);
+        int x0 = (int)std::floor(X), y0 = (int)std::floor(Y);
+        x0 = std::min(x0, (int)cam.width - 1);
+        y0 = std::min(y0, (int)cam.height - 1);
+        int x1 = std::min(x0 + 1, (int)cam.width - 1), y1 = std::min(y0 + 1, (int)cam.height - 1);
+        const V3 p00 = table[(size_t)y0 * cam.width + x0], p10 = table[(size_t)y0 * cam.width + x1];
+        const V3 p01 = table[(size_t)y1 * cam.width + x0], p11 = table[(size_t)y1 * cam.width + x1];
+        float dx = X - (float)x0, dy = Y - (float)y0;
+        return (1.f - dx) * (1.f - dy) * p00 + dx * (1.f - dy) * p10 + (1.f - dx) * dy * p01 + dx * dy * p11;
+    }
+    // the ray of pixel (i, j) for `sample` (cpu_path_tracer.ipp:182-192)
+    void ray(uint32_t i, uint32_t j, uint32_t sample, const Rng& rng, V3& ro, V3& dir) const {
+        float X = (float)i, Y = (float)j;
+        U4 jr{{0, 0, 0, 0}};
+        if (sample != 0) {
+            jr = rng.draw(0, SLOT_JITTER);
+            X = X + u01(jr.v[0]);
+            Y = Y + u01(jr.v[1]);
+        }
+        V3 d = direction(X, Y);
+        ro = V3{cam.origin[0], cam.origin[1], cam.origin[2]};
+        if (sample != 0 && cam.depth_of_field) {
+            float rand1 = u01(jr.v[2]), rand2 = u01(jr.v[3]);   // UniformDiskSample (sampling.ipp:43-52)
+            float r = std::sqrt(rand1);
+            float theta = 2 * PI_F * rand2;
+            float ax = cam.aperture_radius * (r * std::cos(theta)), ay = cam.aperture_radius * (r * std::sin(theta));
+            V3 offset{ax, ay, cam.focal_length};
+            ro = ro + mat3_mul(cam.rotation, offset);
+            if (!std::isinf(cam.focus_distance)) d = (cam.focus_distance * normalize(d)) - offset;
+        }
+        dir = normalize(mat3_mul(cam.rotation, d));
+    }
+};
+
 // one pixel: unidirectional() with simulatePath()/processIntersection() inlined
-static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light* lights,
+static void render_pixel(const Scene& s, const CameraRays& cr, const vgb_light* lights,
                          uint32_t nlights, const vgb_pt_options& o, uint32_t i, uint32_t j,
                          PixelOut& out, RenderCounters& rc) {
+    const vgb_camera& cam = cr.cam;
     const uint32_t B = s.nbands;
     Rng rng{(uint32_t)o.seed, (uint32_t)(o.seed >> 32), j * cam.width + i, 0, o.frame};
     float radiance[VGB_MAX_BANDS] = {0}, direct[VGB_MAX_BANDS] = {0}, albedo_acc[VGB_MAX_BANDS] = {0};
@@ -609,23 +785,11 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
     uint32_t count = 0, tri_first = VGB_NO_HIT;
     bool first_hit = true;
     float s1 = 0.f, s2 = 0.f;   // adaptive sampling sums
-    V3 org{cam.origin[0], cam.origin[1], cam.origin[2]};
     uint32_t sample;
     for (sample = 0; sample < o.samples; ++sample) {
         rng.sample = sample;
-        float X = (float)i, Y = (float)j;
-        if (sample != 0) {
-            U4 jr = rng.draw(0, SLOT_JITTER);
-            X = X + u01(jr.v[0]);
-            Y = Y + u01(jr.v[1]);
-        }
-        // pixelToRay: K^-1 (x, y, 1), then normalize(R * d)
-        const float* K = cam.kinv;
-        float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
-        float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-        V3 dcam{hx, cam.z_dir * hy, cam.z_dir};
-        V3 dir = normalize(mat3_mul(cam.rotation, dcam));
-        V3 ro = org;
+        V3 ro, dir;
+        cr.ray(i, j, sample, rng, ro, dir);
         float path[VGB_MAX_BANDS] = {0};
         float thr[VGB_MAX_BANDS];
         for (uint32_t k = 0; k < B; ++k) thr[k] = 1.f;
@@ -674,6 +838,8 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
             V3 arb = (std::fabs(N.x) < 0.9f) ? V3{1, 0, 0} : V3{0, 1, 0};
             V3 tangent = normalize(cross(arb, N));
             V3 bitangent = cross(N, tangent);
+            const V3 N_frame = N;   // tangent_to_global's third column, built before the normal map
+            N = get_normal(s, uvx, uvy, N, tangent, bitangent);
             float alb[VGB_MAX_BANDS], texv[VGB_MAX_BANDS];
             sample_uvs(s, uvx, uvy, texv);
             for (uint32_t k = 0; k < B; ++k) {
@@ -693,7 +859,11 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
                 if (dot(diff, N_local) > 0) P = sp;
             }
             if (bounce == 0) {
-                if (first_hit) { tri_first = t; first_hit = false; }
+                if (first_hit) {
+                    tri_first = t;
+                    first_hit = false;
+                    first_hit_passes(s, cam, t, P, out);
+                }
                 for (uint32_t k = 0; k < B; ++k) albedo_acc[k] += alb[k];
                 normal_acc = normal_acc + N;
                 depth += h.t;
@@ -729,10 +899,10 @@ static void render_pixel(const Scene& s, const vgb_camera& cam, const vgb_light*
                 if (bounce < o.bounces) {
                     V3 ls = cosine_sample(u01(r0.v[2]), u01(r0.v[3]));
                     float mpdf = ls.z * INV_PI_F;
-                    // tangent_to_global * ls: columns tangent, bitangent, normal
-                    V3 nd{(tangent.x * ls.x + bitangent.x * ls.y) + N.x * ls.z,
-                          (tangent.y * ls.x + bitangent.y * ls.y) + N.y * ls.z,
-                          (tangent.z * ls.x + bitangent.z * ls.y) + N.z * ls.z};
+                    // tangent_to_global * ls: columns tangent, bitangent, normal (before the map)
+                    V3 nd{(tangent.x * ls.x + bitangent.x * ls.y) + N_frame.x * ls.z,
+                          (tangent.y * ls.x + bitangent.y * ls.y) + N_frame.y * ls.z,
+                          (tangent.z * ls.x + bitangent.z * ls.y) + N_frame.z * ls.z};
                     if (mpdf > 0) {
                         float nl = dot(N, nd);
                         float cos_t = std::max(0.0f, dot(nd, N));
@@ -888,14 +1058,33 @@ double tri_solid_angle(V3d c0, V3d c1, V3d c2) {
     double a2 = std::acos(dotd(tangent_d(c2, c0), tangent_d(c2, c1)));
     return ((a0 + a1) + a2) - 3.141592653589793238462;
 }
+// pixelToDirectionHelper_d (camera.ipp:1759-1771): the distortion takes and returns glm's
+// vec2<float>, so the FP64 point is converted to FP32 around undistort.
 V3d corner_dir(const vgb_camera& c, double x, double y) {
     const float* K = c.kinv;
     double hx = ((double)K[0] * x + (double)K[2] * y) + (double)K[4] * 1.0;
     double hy = ((double)K[1] * x + (double)K[3] * y) + (double)K[5] * 1.0;
+    if (c.distortion) {
+        Pix u = undistort(c, Pix{(float)hx, (float)hy});
+        hx = u.x;
+        hy = u.y;
+    }
     double zd = (double)c.z_dir;
     return normalized(V3d{hx, zd * hy, zd});
 }
 }  // namespace
+
+// Distortion::distort (inverse = 0) or undistort (inverse = 1) of n normalised image points.
+OAPI int oracle_distortion(const vgb_camera* cam, const float* xy, uint32_t n, int inverse, float* out) {
+    if (!cam || !xy || !out) return 1;
+    for (uint32_t k = 0; k < n; ++k) {
+        Pix h{xy[2 * k], xy[2 * k + 1]};
+        Pix r = !cam->distortion ? h : (inverse ? undistort(*cam, h) : distort(*cam, h));
+        out[2 * k] = r.x;
+        out[2 * k + 1] = r.y;
+    }
+    return 0;
+}
 
 OAPI int oracle_pixel_solid_angle(const vgb_camera* cam, float* out, int nthreads) {
     if (!cam || !out) return 1;
@@ -962,6 +1151,26 @@ OAPI void* oracle_scene_create(const float* pos, uint32_t nverts, const uint32_t
 
 OAPI void oracle_scene_destroy(void* h) { delete static_cast<Scene*>(h); }
 
+OAPI int oracle_scene_motion(void* h, const vgb_instance_motion* m, uint32_t n) {
+    if (!h) return 1;
+    Scene& s = *static_cast<Scene*>(h);
+    s.motion.assign(m, m + (m ? n : 0));
+    return 0;
+}
+
+OAPI int oracle_scene_normal_map(void* h, const float* nmap, uint32_t w, uint32_t hh) {
+    if (!h) return 1;
+    Scene& s = *static_cast<Scene*>(h);
+    s.nmap.clear();
+    s.nw = s.nh = 0;
+    if (nmap && w && hh) {
+        s.nmap.assign(nmap, nmap + (size_t)w * hh * 3);
+        s.nw = w;
+        s.nh = hh;
+    }
+    return 0;
+}
+
 OAPI uint32_t oracle_scene_bvh_nodes(void* h) { return (uint32_t) static_cast<Scene*>(h)->nodes.size(); }
 
 OAPI int oracle_trace(void* h, const float* orig, const float* dirs, const float* tmax, uint32_t n,
@@ -1006,6 +1215,7 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
     row_end = std::min(row_end, H);
     const size_t plane = (size_t)W * H;
     int nt = std::max(1, nthreads);
+    const CameraRays cr(*cam, nt);
     std::atomic<uint32_t> next_row{row_begin};
     std::vector<RenderCounters> rcs(nt);
     auto work = [&](int tid) {
@@ -1014,7 +1224,7 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
             if (j >= row_end) break;
             for (uint32_t i = 0; i < W; ++i) {
                 PixelOut po;
-                render_pixel(s, *cam, lights, nlights, *opts, i, j, po, rcs[tid]);
+                render_pixel(s, cr, lights, nlights, *opts, i, j, po, rcs[tid]);
                 size_t p = (size_t)j * W + i;
                 for (uint32_t k = 0; k < B; ++k) {
                     if (film->total_radiance) film->total_radiance[k * plane + p] = po.total[k];
@@ -1033,6 +1243,17 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
                 if (film->depth) film->depth[p] = po.depth;
                 if (film->alpha) film->alpha[p] = po.alpha;
                 if (film->triangle_id) film->triangle_id[p] = po.tri;
+                if (film->triangle_size) film->triangle_size[p] = po.tsz;
+                if (film->velocity_global) {
+                    film->velocity_global[p] = po.vel_g.x;
+                    film->velocity_global[plane + p] = po.vel_g.y;
+                    film->velocity_global[2 * plane + p] = po.vel_g.z;
+                }
+                if (film->velocity_camera) {
+                    film->velocity_camera[p] = po.vel_c.x;
+                    film->velocity_camera[plane + p] = po.vel_c.y;
+                    film->velocity_camera[2 * plane + p] = po.vel_c.z;
+                }
             }
         }
     };
@@ -1074,25 +1295,16 @@ static inline V3d muld(V3d a, double k) { return V3d{a.x * k, a.y * k, a.z * k};
 // Gradients of sum(g * I) for one pixel, added into gtex ([th][tw][B]), gpos ([nverts][3]) and,
 // with smooth shading, gvn ([nverts][3], the vertex-normal gradients that
 // vnormal_backward carries to the positions).
-static void adjoint_pixel(const Scene& s, const vgb_camera& cam, const vgb_light* lights, uint32_t nlights,
+static void adjoint_pixel(const Scene& s, const CameraRays& cr, const vgb_light* lights, uint32_t nlights,
                           const vgb_pt_options& o, uint32_t i, uint32_t j, const double* g, double* gtex, double* gpos,
                           double* gvn) {
+    const vgb_camera& cam = cr.cam;
     const uint32_t B = s.nbands;
     Rng rng{(uint32_t)o.seed, (uint32_t)(o.seed >> 32), j * cam.width + i, 0, o.frame};
-    V3 org{cam.origin[0], cam.origin[1], cam.origin[2]};
     for (uint32_t sample = 0; sample < o.samples; ++sample) {
         rng.sample = sample;
-        float X = (float)i, Y = (float)j;
-        if (sample != 0) {
-            U4 jr = rng.draw(0, SLOT_JITTER);
-            X = X + u01(jr.v[0]);
-            Y = Y + u01(jr.v[1]);
-        }
-        const float* K = cam.kinv;
-        float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
-        float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-        V3 dir = normalize(mat3_mul(cam.rotation, V3{hx, cam.z_dir * hy, cam.z_dir}));
-        V3 ro = org;
+        V3 ro, dir;
+        cr.ray(i, j, sample, rng, ro, dir);
         float thr[VGB_MAX_BANDS], bgc[VGB_MAX_BANDS] = {0};
         for (uint32_t k = 0; k < B; ++k) thr[k] = 1.f;
         AVtx vx[4];
@@ -1359,6 +1571,7 @@ OAPI int oracle_adjoint_positions(void* h, const vgb_camera* cam, const vgb_ligh
     const size_t npix = (size_t)W * H, ntex = (size_t)s.tw * s.th * B, n3 = 3 * (size_t)s.nverts;
     const bool smooth = gpos && opts->smooth_shading;
     int nt = std::max(1, nthreads);
+    const CameraRays cr(*cam, nt);
     std::vector<std::vector<double>> tb(nt), pb(nt), nb(nt);
     std::atomic<uint32_t> next{0};
     auto work = [&](int tid) {
@@ -1375,7 +1588,7 @@ OAPI int oracle_adjoint_positions(void* h, const vgb_camera* cam, const vgb_ligh
                     g[k] = (double)dldi[k * npix + (size_t)j * W + i] / (double)(float)opts->samples;
                     any |= g[k] != 0.0;
                 }
-                if (any) adjoint_pixel(s, *cam, lights, nlights, *opts, i, j, g, gtex ? tb[tid].data() : nullptr,
+                if (any) adjoint_pixel(s, cr, lights, nlights, *opts, i, j, g, gtex ? tb[tid].data() : nullptr,
                                        gpos ? pb[tid].data() : nullptr, smooth ? nb[tid].data() : nullptr);
             }
         }
@@ -1648,7 +1861,9 @@ OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const 
         if (behind) continue;
         float px[3], py[3];
         for (int k = 0; k < 3; ++k) {
-            const float hx = vc[k].x / vc[k].z, hy = vc[k].y / vc[k].z;
+            Pix hm{vc[k].x / vc[k].z, vc[k].y / vc[k].z};     // Camera::projectCameraPoint (camera.ipp:1060-1080)
+            if (cam->distortion) hm = distort(*cam, hm);
+            const float hx = hm.x, hy = hm.y;
             float X = (K[0] * hx + K[1] * hy) + K[2];
             const float Y = (K[3] * hx + K[4] * hy) + K[5];
             if (cam->z_dir < 0) X = (float)(W - 1) - X;
@@ -1686,6 +1901,12 @@ OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const 
                 const V3 fn = normalize(cross(s.pos[vi[0]] - s.pos[vi[1]], s.pos[vi[2]] - s.pos[vi[0]]));
                 V3 N{-fn.x, -fn.y, -fn.z};
                 if (smooth) N = normalize((w0 * s.nrm[vi[0]] + w1 * s.nrm[vi[1]]) + w2 * s.nrm[vi[2]]);
+                {   // tangent frame and Material::getNormal (cpu_rasterizer.ipp:177-191)
+                    V3 arb = (std::fabs(N.x) < 0.9f) ? V3{1, 0, 0} : V3{0, 1, 0};
+                    V3 tangent = normalize(cross(arb, N));
+                    V3 bitangent = cross(N, tangent);
+                    N = get_normal(s, uvx, uvy, N, tangent, bitangent);
+                }
                 float rad[VGB_MAX_BANDS] = {0};
                 if (lighting) {
                     const V3 fc = (w0 * vc[0] + w1 * vc[1]) + w2 * vc[2];

@@ -75,6 +75,17 @@ def same_bits(a, b) -> bool:
     return a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32))
 
 
+def same_bits_or_nan(a, b) -> bool:
+    """Bit-identical wherever either value is a number; NaN wherever either is NaN (CUDA and the
+    host libm produce NaNs of different sign and payload, e.g. normalize(0) on sky pixels)."""
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    if a.shape != b.shape:
+        return False
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint32), b[~nb].view(np.uint32))
+
+
 def lz4_zero_run(n: int) -> bytes:
     """A valid LZ4 block of n >= 25 zero bytes at the format's largest expansion: one literal,
     one match at offset 1 whose length runs on in 255-bytes, then the five closing literals."""

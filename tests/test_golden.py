@@ -19,7 +19,13 @@ FIXTURES = sorted(GOLDEN.glob("golden_*.npz"))
 def _load(path):
     z = np.load(path)
     d = {k: z[k] for k in z.files}
-    cam = capi.Camera.from_buffer_copy(d["camera"].tobytes())
+    # fixtures written before the lens fields were appended to vgb_camera hold the shorter
+    # struct: no distortion, no depth of field (the reference's defaults)
+    raw = d["camera"].tobytes()
+    cam = capi.Camera.from_buffer_copy(raw.ljust(C.sizeof(capi.Camera), b"\0"))
+    if len(raw) < C.sizeof(capi.Camera):
+        cam.interpolate_directions = 1
+        cam.focus_distance = float("inf")
     nl = int(d["nlights"])
     lights = (capi.Light * max(1, nl)).from_buffer_copy(d["lights"].tobytes().ljust(C.sizeof(capi.Light) * max(1, nl), b"\0"))
     # fixtures written before the adaptive-sampling fields were appended hold the shorter struct;

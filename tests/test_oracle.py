@@ -433,3 +433,100 @@ def test_oracle_sensor_chain_and_psf():
     s = oracle.psf(img, box)
     assert s[0, 3, 4] == pytest.approx(img[0, 2:5, 3:6].sum(), rel=1e-6)
     assert s[1, 0, 0] == pytest.approx(img[1, 0:2, 0:2].sum(), rel=1e-6)
+
+
+# ---------------------------------------------------------------- lens distortion
+def _np_brown_delta(k, x, y):
+    """BrownDistortion::computeDelta (brown_distortion.ipp:24-44) in numpy FP32, written from the
+    .ipp's expressions left to right."""
+    f = np.float32
+    k = [f(v) for v in k]
+    r = np.sqrt(x * x + y * y)
+    r2 = r * r
+    r4 = r2 * r2
+    r6 = r2 * r2 * r2
+    s = k[0] * r2 + k[1] * r4 + k[2] * r6
+    tx = (f(2) * k[3] * x * y) + (k[4] * (r2 + f(2) * x * x))
+    ty = (k[3] * (r2 + f(2) * y * y)) + (f(2) * k[4] * x * y)
+    return s * x + tx, s * y + ty
+
+
+def _distortion_camera(model, coeffs):
+    from vira_gb300 import capi
+
+    c = capi.Camera()
+    c.distortion = model
+    for i, v in enumerate(coeffs):
+        c.distortion_coeffs[i] = v
+    return c
+
+
+def _points(n=4000, extent=0.4, seed=3):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-extent, extent, (n, 2)).astype(np.float32)
+
+
+def test_distortion_models_round_trip_and_zero_is_identity():
+    from oracle import oracle
+    from vira_gb300 import capi
+
+    p = _points()
+    cases = {
+        "brown": (capi.DISTORTION_BROWN, [-0.12, 0.03, -0.004, 2e-3, -1e-3]),
+        "opencv": (capi.DISTORTION_OPENCV, [-0.1, 0.02, 0.0, 0.01, -0.002, 0.0, 1e-3, -2e-3, 1e-3, 0.0, -1e-3, 0.0]),
+        "owen": (capi.DISTORTION_OWEN, [1e-3, -0.08, 2e-3, 0.01, 1e-3, -1e-3]),
+    }
+    for name, (model, coeffs) in cases.items():
+        cam = _distortion_camera(model, coeffs)
+        u = oracle.distortion(cam, p, inverse=True)
+        back = oracle.distortion(cam, u, inverse=False)
+        if model == capi.DISTORTION_OPENCV:
+            # OpenCVDistortion::computeDelta is h - distort(h), the opposite sign of the other
+            # models' delta, and undistort still steps u = h - delta(u): its fixed point is
+            # u - h = distort(u) - u, not distort(u) = h.  Kept as the reference has it.
+            assert float(np.abs((u - p) - (back - u)).max()) < 2e-6, name
+        else:
+            assert float(np.abs(back - p).max()) < 2e-6, name
+        assert float(np.abs(u - p).max()) > 1e-4, name   # the model does move the points
+        zero = _distortion_camera(model, [0.0] * len(coeffs))
+        assert np.array_equal(oracle.distortion(zero, p, inverse=True), p), name
+        assert np.array_equal(oracle.distortion(zero, p, inverse=False), p), name
+
+
+def test_brown_restatement_matches_its_formula_bit_for_bit():
+    """The oracle's Brown model against a numpy FP32 transcription of the reference's
+    expression order: distort = h + delta(h); undistort = 20 steps of u = h - delta(u)."""
+    from oracle import oracle
+    from vira_gb300 import capi
+
+    k = [-0.12, 0.03, -0.004, 2e-3, -1e-3]
+    cam = _distortion_camera(capi.DISTORTION_BROWN, k)
+    p = _points(500)
+    x, y = p[:, 0], p[:, 1]
+    dx, dy = _np_brown_delta(k, x, y)
+    d = np.stack([x + dx, y + dy], 1)
+    assert np.array_equal(oracle.distortion(cam, p, inverse=False), d)
+    ux, uy = x.copy(), y.copy()
+    for _ in range(20):
+        dx, dy = _np_brown_delta(k, ux, uy)
+        ux, uy = x - dx, y - dy
+    assert np.array_equal(oracle.distortion(cam, p, inverse=True), np.stack([ux, uy], 1))
+
+
+def test_distortion_changes_the_pixel_solid_angle_consistently():
+    """Barrel distortion (k1 < 0 in undistort's direction) spreads the outer pixels' rays: the
+    frame's total solid angle grows, the centre pixel's barely moves."""
+    from oracle import oracle
+    from vira_gb300 import Camera, capi
+
+    cam = Camera()
+    cam.set_resolution(64, 48)
+    cam.set_sensor_size(0.036)
+    cam.set_field_of_view(40.0)
+    c0 = cam.to_c(np.zeros(3), 4, kinv=oracle.camera_kinv(cam))
+    cam.set_brown_distortion_coefficients(k1=-0.15)
+    c1 = cam.to_c(np.zeros(3), 4, kinv=oracle.camera_kinv(cam))
+    assert c1.distortion == capi.DISTORTION_BROWN and c1.interpolate_directions == 1
+    o0, o1 = oracle.pixel_solid_angle(c0), oracle.pixel_solid_angle(c1)
+    assert o1.sum() > o0.sum() * 1.01
+    assert abs(float(o1[24, 32] / o0[24, 32]) - 1.0) < 1e-3

@@ -30,11 +30,19 @@ class VgbError(RuntimeError):
         self.status = status
 
 
+DISTORTION_NONE, DISTORTION_BROWN, DISTORTION_OPENCV, DISTORTION_OWEN = 0, 1, 2, 3
+
+
 class Camera(C.Structure):
     _fields_ = [
         ("width", C.c_uint32), ("height", C.c_uint32),
         ("origin", C.c_float * 3), ("rotation", C.c_float * 9), ("kinv", C.c_float * 6),
         ("z_dir", C.c_float), ("power_scale", C.c_float * MAX_BANDS),
+        ("distortion", C.c_uint32), ("distortion_coeffs", C.c_float * 12), ("interpolate_directions", C.c_uint32),
+        ("depth_of_field", C.c_uint32), ("aperture_radius", C.c_float), ("focal_length", C.c_float),
+        ("focus_distance", C.c_float),
+        ("sensor_size", C.c_float * 2), ("velocity", C.c_float * 3), ("angular_rate", C.c_float * 3),
+        ("rot_origin", C.c_float * 3),
     ]
 
 
@@ -65,7 +73,13 @@ class Film(C.Structure):
         ("received_power", C.c_void_p), ("albedo", C.c_void_p), ("normal_global", C.c_void_p),
         ("depth", C.c_void_p), ("alpha", C.c_void_p), ("triangle_id", C.c_void_p),
         ("pixel_solid_angle", C.c_void_p), ("on_device", C.c_int32),
+        ("velocity_global", C.c_void_p), ("velocity_camera", C.c_void_p), ("triangle_size", C.c_void_p),
     ]
+
+
+class InstanceMotion(C.Structure):
+    _fields_ = [("first_triangle", C.c_uint32), ("velocity", C.c_float * 3), ("angular_rate", C.c_float * 3),
+                ("position", C.c_float * 3)]
 
 
 class Frame(C.Structure):
@@ -181,9 +195,13 @@ SIGNATURES = {
     "vgb_adjoint_positions": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(PtOptions), _P, _P, _P, C.c_int]),
     "vgb_render_adjoint_batch": (C.c_int, [_P, _P, _U32, C.POINTER(PtOptions), _P, _P, C.POINTER(C.c_double)]),
     "vgb_texture_update": (C.c_int, [_P, _P, _U32, _U32]),
+    "vgb_scene_normal_map": (C.c_int, [_P, _P, _U32, _U32]),
+    "vgb_scene_motion": (C.c_int, [_P, _P, _U32]),
     "vgb_get_stats": (C.c_int, [_P, C.POINTER(Stats)]),
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
+    "vgb_set_traversal_limit": (C.c_int, [_P, C.c_uint32]),
+    "vgb_measure_l2_read": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]),
     "vgb_rasterize": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(RasterOptions), C.POINTER(Film)]),
     "vgb_quipu_open": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "vgb_quipu_close": (None, [_P]),

@@ -88,6 +88,11 @@ struct DevScene {
     const float* valb;     // B per vertex (unused when albedo_uniform)
     const float* tex;      // [th][tw][B], or [th][tw] when tex_mono
     uint32_t tw, th;
+    const float* nmap;     // [nh][nw][3] tangent-space normal map, or null (Material::normalMap)
+    uint32_t nw, nh;
+    const vgb_instance_motion* motion;   // per-instance motion, ascending first_triangle, or null
+    uint32_t nmotion;
+    uint32_t iter_cap;                // traversal steps per ray before it gives up (device error word)
     uint32_t albedo_uniform;          // every vertex has the albedo `albedo_value`
     uint32_t tex_mono;                // every texel has the same value in all bands
     float albedo_value[VGB_MAX_BANDS];
@@ -137,6 +142,8 @@ struct FrameParams {
     uint32_t nb;
     uint32_t tiles_x, tiles_y;
     uint32_t aux;   // AUX_* bits: the per-pixel sums the requested film planes need
+    // first-hit film planes k_shade writes directly (null when not requested)
+    float *vel_g, *vel_c, *tsz;
 };
 
 // Per-pixel sums kept over the samples only when a requested film plane reads them (the total
@@ -153,12 +160,14 @@ struct FilmOut {
     float *total, *direct, *indirect, *power, *albedo, *normal, *depth, *alpha;
     uint32_t* tri;
     const float* omega;
+    float *vel_g, *vel_c, *tsz;   // first-hit passes (velocity in the scene and camera frames, triangle size)
 };
 
 // The AUX_* sums that the planes of a film read.
 inline uint32_t aux_for(const FilmOut& f) {
+    // the first-hit passes find a pixel's first hit through its first-triangle sum
     return (f.albedo ? AUX_ALB : 0u) | (f.normal ? AUX_NRM : 0u) | ((f.direct || f.indirect) ? AUX_DIR : 0u) |
-           ((f.depth || f.alpha) ? AUX_DEP : 0u) | (f.tri ? AUX_TRI : 0u);
+           ((f.depth || f.alpha) ? AUX_DEP : 0u) | ((f.tri || f.vel_g || f.vel_c || f.tsz) ? AUX_TRI : 0u);
 }
 
 __device__ __forceinline__ void warp_reduce_add(uint64_t* dst, uint32_t v) {
@@ -285,6 +294,34 @@ __device__ __forceinline__ void sample_uvs(const DevScene& s, uint32_t nb, float
         if (k < (int)nb) out[k] = ((a * __ldg(p00 + k) + b * __ldg(p10 + k)) + c * __ldg(p01 + k)) + e * __ldg(p11 + k);
 }
 
+// Image<Normal>::sampleUVs of the normal map (wrap + bilinear, image.ipp:589-671).
+__device__ __forceinline__ F3 sample_normal_map(const DevScene& s, float u, float v) {
+    const float rx = (float)s.nw, ry = (float)s.nh;
+    float px = fmodf(u * rx, rx), py = fmodf(v * ry, ry);
+    if (px < 0) px += rx;
+    if (py < 0) py += ry;
+    int x0 = (int)floorf(px), y0 = (int)floorf(py);
+    x0 = min(x0, (int)s.nw - 1); y0 = min(y0, (int)s.nh - 1);
+    const int x1 = min(x0 + 1, (int)s.nw - 1), y1 = min(y0 + 1, (int)s.nh - 1);
+    const float dx = px - (float)x0, dy = py - (float)y0;
+    const float* p00 = &s.nmap[((size_t)y0 * s.nw + x0) * 3];
+    const float* p10 = &s.nmap[((size_t)y0 * s.nw + x1) * 3];
+    const float* p01 = &s.nmap[((size_t)y1 * s.nw + x0) * 3];
+    const float* p11 = &s.nmap[((size_t)y1 * s.nw + x1) * 3];
+    const F3 a{__ldg(p00), __ldg(p00 + 1), __ldg(p00 + 2)}, b{__ldg(p10), __ldg(p10 + 1), __ldg(p10 + 2)};
+    const F3 c{__ldg(p01), __ldg(p01 + 1), __ldg(p01 + 2)}, e{__ldg(p11), __ldg(p11 + 1), __ldg(p11 + 2)};
+    return (((1.f - dx) * (1.f - dy) * a + dx * (1.f - dy) * b) + (1.f - dx) * dy * c) + dx * dy * e;
+}
+
+// Material::getNormal (materials/material.ipp:129-143): the tangent-space normal map sample taken
+// to the scene frame by [tangent | bitangent | N] and normalised; N itself without a map.
+__device__ __forceinline__ F3 mapped_normal(const DevScene& s, float u, float v, F3 N, F3 tg, F3 bt) {
+    if (!s.nmap) return N;
+    const F3 t = sample_normal_map(s, u, v);
+    return normalize(F3{(tg.x * t.x + bt.x * t.y) + N.x * t.z, (tg.y * t.x + bt.y * t.y) + N.y * t.z,
+                        (tg.z * t.x + bt.z * t.y) + N.z * t.z});
+}
+
 // The tangent frame of the shading normal (cpu_path_tracer.ipp:318-321).
 __device__ __forceinline__ void tangent_frame(F3 N, F3& tg, F3& bt) {
     F3 arb = (fabsf(N.x) < 0.9f) ? F3{1, 0, 0} : F3{0, 1, 0};
@@ -293,11 +330,13 @@ __device__ __forceinline__ void tangent_frame(F3 N, F3& tg, F3& bt) {
 }
 
 // processIntersection up to the shading point (cpu_path_tracer.ipp:295-346): uv, face and
-// shading normals, tangent frame, albedo (vertex albedo x texture), interpolated position and
-// computeShadingPoint (:494-511).  The normal matrix is the identity in the flattened frame.
+// shading normals, tangent frame, the normal map, albedo (vertex albedo x texture), interpolated
+// position and computeShadingPoint (:494-511).  The normal matrix is the identity in the
+// flattened frame.  N: the shading normal after the normal map (NEE, MIS and the film's normal);
+// (tg, bt, nf): the tangent frame built before the map, which the continuation samples in.
 template <int NB>
 __device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool smooth, uint32_t t, float w0f,
-                                           float w1f, F3& Pp, F3& N, F3& fnrm, F3& tg, F3& bt, float* alb,
+                                           float w1f, F3& Pp, F3& N, F3& fnrm, F3& tg, F3& bt, F3& nf, float* alb,
                                            float* va_out = nullptr, float* tex_out = nullptr, float* uv_out = nullptr) {
     float w[3];
     w[0] = w0f;
@@ -316,8 +355,9 @@ __device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool 
     fnrm = F3{-fnn.x, -fnn.y, -fnn.z};
     F3 Nl = fnrm;
     if (smooth) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
-    N = Nl;
-    tangent_frame(N, tg, bt);
+    nf = Nl;
+    tangent_frame(Nl, tg, bt);
+    N = mapped_normal(s, uvx, uvy, Nl, tg, bt);
     float texv[NB];
     sample_uvs<NB>(s, nb, uvx, uvy, texv);
 #pragma unroll
@@ -374,14 +414,14 @@ __device__ __forceinline__ bool nee_light(const vgb_light& L, F3 Pp, F3 N, const
 // then keeps the incoming ray and throughput).
 template <int NB>
 __device__ __forceinline__ bool continue_path(const vgb_light* lights, uint32_t nlights, const vgb_pt_options& opt,
-                                              uint32_t nb, F3 Pp, F3 N, F3 tg, F3 bt, const float* alb, float* thr,
-                                              U4 r0, uint32_t slot, uint32_t sample, uint32_t frame, uint32_t bounce,
-                                              F3& nd, bool& new_ray) {
+                                              uint32_t nb, F3 Pp, F3 N, F3 tg, F3 bt, F3 nf, const float* alb,
+                                              float* thr, U4 r0, uint32_t slot, uint32_t sample, uint32_t frame,
+                                              uint32_t bounce, F3& nd, bool& new_ray) {
     new_ray = false;
     F3 ls = cosine_sample(u01(r0.z), u01(r0.w));
     const float mpdf = ls.z * kInvPi;
-    nd = F3{(tg.x * ls.x + bt.x * ls.y) + N.x * ls.z, (tg.y * ls.x + bt.y * ls.y) + N.y * ls.z,
-            (tg.z * ls.x + bt.z * ls.y) + N.z * ls.z};
+    nd = F3{(tg.x * ls.x + bt.x * ls.y) + nf.x * ls.z, (tg.y * ls.x + bt.y * ls.y) + nf.y * ls.z,
+            (tg.z * ls.x + bt.z * ls.y) + nf.z * ls.z};
     if (!(mpdf > 0)) return true;
     const float nl = dot(N, nd);
     const float cos_t = smax(0.0f, dot(nd, N));
@@ -409,26 +449,137 @@ __device__ __forceinline__ bool continue_path(const vgb_light* lights, uint32_t 
     return true;
 }
 
-// Camera::pixelToRay for the pixel of bounce-0 item `item` (8x4-pixel warp tiles).
-// Camera::pixelToRay for pixel (pi, pj) = slot: sample 0 through the pixel corner, later
-// samples jittered (camera.ipp:1126-1163, cpu_path_tracer.ipp:182-192).
-__device__ __forceinline__ void pixel_ray(const vgb_camera& cam, uint32_t pi, uint32_t pj, uint32_t slot,
-                                          uint32_t sample, uint32_t frame, uint32_t k0, uint32_t k1, F3& ro, F3& rd) {
-    float X = (float)pi, Y = (float)pj;
-    if (sample != 0) {
-        U4 jr = philox(U4{slot, sample, frame, kSlotJitter}, k0, k1);
-        X = X + u01(jr.x);
-        Y = Y + u01(jr.y);
+// ------------------------------------------------------------------ camera rays
+// Lens distortion models, FP32 in the reference's operation order:
+// BrownDistortion::computeDelta (cameras/distortions/brown_distortion.ipp:24-44),
+// OpenCVDistortion::distort (opencv_distortion.ipp:28-54), OwenDistortion::computeDelta
+// (owen_distortion.ipp:24-46).  `h` is the normalised image point K^-1 (x, y, 1).
+__device__ __forceinline__ void brown_delta(const float* k, float x, float y, float& dx, float& dy) {
+    const float r = sqrtf(x * x + y * y);
+    const float r2 = r * r, r4 = r2 * r2, r6 = r2 * r2 * r2;
+    const float s = (k[0] * r2 + k[1] * r4) + k[2] * r6;
+    dx = s * x + ((2.f * k[3] * x * y) + (k[4] * (r2 + 2.f * x * x)));
+    dy = s * y + ((k[3] * (r2 + 2.f * y * y)) + (2.f * k[4] * x * y));
+}
+__device__ __forceinline__ void opencv_distort(const float* k, float x, float y, float& ox, float& oy) {
+    const float r = sqrtf(x * x + y * y);
+    const float r2 = r * r, r4 = r2 * r2, r6 = r2 * r2 * r2;
+    const float num = 1.f + k[0] * r2 + k[1] * r4 + k[2] * r6;
+    const float den = 1.f + k[3] * r2 + k[4] * r4 + k[5] * r6;
+    const float f = num / den;
+    const float tx = (2.f * k[6] * x * y) + (k[7] * (r2 + 2.f * x * x)) + (k[8] * r2) + (k[9] * r4);
+    const float ty = (k[6] * (r2 + 2.f * y * y)) + (2.f * k[7] * x * y) + (k[10] * r2) + (k[11] * r4);
+    ox = f * x + tx;
+    oy = f * y + ty;
+}
+__device__ __forceinline__ void owen_delta(const float* e, float x, float y, float& dx, float& dy) {
+    const float r = sqrtf(x * x + y * y);
+    const float r2 = r * r, r3 = r * r * r;
+    const float rf = (e[1] * r2) + (e[3] * r2 * r2) + (e[4] * y) + (e[5] * x);
+    const float of = (e[0] * r) + (e[2] * r3);
+    dx = rf * x + of * -y;
+    dy = rf * y + of * x;
+}
+// Distortion::undistort: u = h - delta(u), 20 times from u = h.  OpenCV's delta is u - distort(u)
+// (opencv_distortion.ipp:20-23), the opposite sign of the other models', so its iteration settles
+// where u - h = distort(u) - u rather than inverting the model; kept as the reference has it.
+__device__ __noinline__ float2 undistort(const vgb_camera& c, float hx, float hy) {
+    float ux = hx, uy = hy;
+    for (int it = 0; it < 20; ++it) {
+        float dx, dy;
+        if (c.distortion == VGB_DISTORTION_OPENCV) {
+            float ox, oy;
+            opencv_distort(c.distortion_coeffs, ux, uy, ox, oy);
+            dx = ux - ox;
+            dy = uy - oy;
+        } else if (c.distortion == VGB_DISTORTION_BROWN) {
+            brown_delta(c.distortion_coeffs, ux, uy, dx, dy);
+        } else {
+            owen_delta(c.distortion_coeffs, ux, uy, dx, dy);
+        }
+        ux = hx - dx;
+        uy = hy - dy;
     }
+    return make_float2(ux, uy);
+}
+// Distortion::distort (the rasterizer's projection): h + delta(h), OpenCV's formula directly.
+__device__ __forceinline__ void distort(const vgb_camera& c, float& hx, float& hy) {
+    float dx, dy;
+    if (c.distortion == VGB_DISTORTION_OPENCV) {
+        opencv_distort(c.distortion_coeffs, hx, hy, dx, dy);
+        hx = dx;
+        hy = dy;
+        return;
+    }
+    if (c.distortion == VGB_DISTORTION_BROWN) brown_delta(c.distortion_coeffs, hx, hy, dx, dy);
+    else owen_delta(c.distortion_coeffs, hx, hy, dx, dy);
+    hx = hx + dx;
+    hy = hy + dy;
+}
+
+// Camera::pixelToDirectionHelper (camera.ipp:1738-1749): K^-1 (x, y, 1), undistorted, in the
+// camera frame.
+__device__ __forceinline__ F3 direction_helper(const vgb_camera& cam, float X, float Y) {
     const float* K = cam.kinv;
     float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
     float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-    F3 dc{hx, cam.z_dir * hy, cam.z_dir};
+    if (cam.distortion) {
+        const float2 u = undistort(cam, hx, hy);
+        hx = u.x;
+        hy = u.y;
+    }
+    return F3{hx, cam.z_dir * hy, cam.z_dir};
+}
+
+// Camera::pixelToDirection (camera.ipp:1105-1117): with a distortion and direction interpolation,
+// Image::interpolatePixel (image.ipp:619-671) of the table precomputePixelDirections fills with
+// normalize(pixelToDirectionHelper(i, j)) -- evaluated here at the four corners on the fly.
+__device__ __noinline__ F3 interpolated_direction(const vgb_camera& cam, float X, float Y) {
+    int x0 = (int)floorf(X), y0 = (int)floorf(Y);
+    x0 = min(x0, (int)cam.width - 1);
+    y0 = min(y0, (int)cam.height - 1);
+    const int x1 = min(x0 + 1, (int)cam.width - 1), y1 = min(y0 + 1, (int)cam.height - 1);
+    const F3 p00 = normalize(direction_helper(cam, (float)x0, (float)y0));
+    const F3 p10 = normalize(direction_helper(cam, (float)x1, (float)y0));
+    const F3 p01 = normalize(direction_helper(cam, (float)x0, (float)y1));
+    const F3 p11 = normalize(direction_helper(cam, (float)x1, (float)y1));
+    const float dx = X - (float)x0, dy = Y - (float)y0;
+    return (((1.f - dx) * (1.f - dy) * p00 + dx * (1.f - dy) * p10) + (1.f - dx) * dy * p01) + dx * dy * p11;
+}
+
+__device__ __forceinline__ F3 camera_direction(const vgb_camera& cam, float X, float Y) {
+    if (cam.distortion && cam.interpolate_directions) return interpolated_direction(cam, X, Y);
+    return direction_helper(cam, X, Y);
+}
+
+// Camera::pixelToRay for pixel (pi, pj) = slot: sample 0 through the pixel corner with the
+// pinhole overload, later samples jittered and, with depth of field, through a point of the
+// aperture (camera.ipp:1126-1163, cpu_path_tracer.ipp:182-192).  Random numbers: the jitter
+// draw's first two words move the pixel coordinate, its last two sample the aperture disc
+// (UniformDiskSample, sampling.ipp:43-52).
+__device__ __forceinline__ void pixel_ray(const vgb_camera& cam, uint32_t pi, uint32_t pj, uint32_t slot,
+                                          uint32_t sample, uint32_t frame, uint32_t k0, uint32_t k1, F3& ro, F3& rd) {
+    float X = (float)pi, Y = (float)pj;
+    U4 jr{0, 0, 0, 0};
+    if (sample != 0) {
+        jr = philox(U4{slot, sample, frame, kSlotJitter}, k0, k1);
+        X = X + u01(jr.x);
+        Y = Y + u01(jr.y);
+    }
+    F3 dc = camera_direction(cam, X, Y);
     const float* R = cam.rotation;
+    ro = F3{cam.origin[0], cam.origin[1], cam.origin[2]};
+    if (sample != 0 && cam.depth_of_field) {
+        const float r = sqrtf(u01(jr.z));
+        const float theta = 2.f * kPi * u01(jr.w);
+        const F3 off{cam.aperture_radius * (r * cosf(theta)), cam.aperture_radius * (r * sinf(theta)), cam.focal_length};
+        ro = ro + F3{(R[0] * off.x + R[3] * off.y) + R[6] * off.z, (R[1] * off.x + R[4] * off.y) + R[7] * off.z,
+                     (R[2] * off.x + R[5] * off.y) + R[8] * off.z};
+        if (!isinf(cam.focus_distance)) dc = cam.focus_distance * normalize(dc) - off;
+    }
     F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
           (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
     rd = normalize(dw);
-    ro = F3{cam.origin[0], cam.origin[1], cam.origin[2]};
 }
 
 __device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item, uint32_t sample, uint32_t& slot,
@@ -440,6 +591,56 @@ __device__ __forceinline__ bool camera_ray(const FrameParams& fp, uint32_t item,
     slot = pj * fp.cam.width + pi;
     pixel_ray(fp.cam, pi, pj, slot, sample, fp.opt.frame, (uint32_t)fp.opt.seed, (uint32_t)(fp.opt.seed >> 32), ro, rd);
     return true;
+}
+
+// ------------------------------------------------------------------ first-hit passes
+// renderPasses.save_triangle_size / save_velocity at a pixel's first hit (cpu_path_tracer.ipp:
+// 356-372).  Pp: the shading point before offsetIntersection; vert = {v1, v2, v0}; the triangle
+// size is the longest edge over Camera::calculateGSD (camera.ipp:1408-1414) at the hit distance;
+// the velocity is the instance's point velocity at Pp (reference_frame.ipp:367-373) and, in the
+// camera frame, relative to the camera's point velocity evaluated at rotation * p_global.
+__device__ __noinline__ void first_hit_passes(const DevScene& s, const vgb_camera& cam, uint32_t t, F3 Pp,
+                                              float* vel_g, float* vel_c, float* tsz, size_t FP, uint32_t slot) {
+    if (tsz) {
+        const F3 a = ld3(__ldg(&s.vpos[__ldg(&s.idx[3 * (size_t)t + 1])]));
+        const F3 b = ld3(__ldg(&s.vpos[__ldg(&s.idx[3 * (size_t)t + 2])]));
+        const F3 c = ld3(__ldg(&s.vpos[__ldg(&s.idx[3 * (size_t)t])]));
+        const float e01 = length(b - a), e02 = length(c - a), e12 = length(c - b);
+        const float edge = smax(e01, smax(e02, e12));
+        const float distance = length(Pp - F3{cam.origin[0], cam.origin[1], cam.origin[2]});
+        const float gx = distance * cam.sensor_size[0] / (cam.focal_length * (float)cam.width);
+        const float gy = distance * cam.sensor_size[1] / (cam.focal_length * (float)cam.height);
+        tsz[slot] = edge / smin(gx, gy);
+    }
+    if (vel_g || vel_c) {
+        F3 v{0.f, 0.f, 0.f}, w{0.f, 0.f, 0.f}, o{0.f, 0.f, 0.f};
+        if (s.nmotion) {
+            uint32_t lo = 0, hi = s.nmotion - 1;   // the last instance whose first triangle is <= t
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (s.motion[mid].first_triangle <= t) lo = mid; else hi = mid - 1;
+            }
+            const vgb_instance_motion& m = s.motion[lo];
+            v = F3{m.velocity[0], m.velocity[1], m.velocity[2]};
+            w = F3{m.angular_rate[0], m.angular_rate[1], m.angular_rate[2]};
+            o = F3{m.position[0], m.position[1], m.position[2]};
+        }
+        const F3 vg = v + cross(w, Pp - o);
+        if (vel_g) { vel_g[slot] = vg.x; vel_g[FP + slot] = vg.y; vel_g[2 * FP + slot] = vg.z; }
+        if (vel_c) {
+            const float* R = cam.rotation;
+            const F3 rp{((R[0] * Pp.x + R[3] * Pp.y) + R[6] * Pp.z) + cam.rot_origin[0],
+                        ((R[1] * Pp.x + R[4] * Pp.y) + R[7] * Pp.z) + cam.rot_origin[1],
+                        ((R[2] * Pp.x + R[5] * Pp.y) + R[8] * Pp.z) + cam.rot_origin[2]};
+            const F3 cv = F3{cam.velocity[0], cam.velocity[1], cam.velocity[2]} +
+                          cross(F3{cam.angular_rate[0], cam.angular_rate[1], cam.angular_rate[2]}, rp);
+            const F3 rv = vg - cv;
+            // globalDirectionToLocal: the inverse (transpose) of the camera rotation
+            vel_c[slot] = (R[0] * rv.x + R[1] * rv.y) + R[2] * rv.z;
+            vel_c[FP + slot] = (R[3] * rv.x + R[4] * rv.y) + R[5] * rv.z;
+            vel_c[2 * FP + slot] = (R[6] * rv.x + R[7] * rv.y) + R[8] * rv.z;
+        }
+    }
 }
 
 // ------------------------------------------------------------------ k_trace (closest hit)
@@ -468,7 +669,7 @@ __global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s,
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
         const WRay wr = make_wray(ro, rd);
-        traverse_any_layout<L, false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt);
+        traverse_any_layout<L, false, COUNT>(s.nodes, s.tris, wr, 0.f, h, err, cnt, s.iter_cap);
         nclosest++;
         float w0 = 0.f, w1 = 0.f;
         if (h.id != VGB_NO_HIT) {
@@ -546,6 +747,10 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                         if (aux & AUX_NRM) { st.anrm[slot] = 0.f; st.anrm[P + slot] = 0.f; st.anrm[2 * P + slot] = 0.f; }
                         if (aux & AUX_DEP) { st.adep[slot] = 0.f; st.acnt[slot] = 0u; }
                         if (aux & AUX_TRI) st.atri[slot] = VGB_NO_HIT;
+                        const size_t FP = (size_t)fp.cam.width * fp.cam.height;
+                        if (fp.tsz) fp.tsz[slot] = __int_as_float(0x7f800000);
+                        if (fp.vel_g) { fp.vel_g[slot] = 0.f; fp.vel_g[FP + slot] = 0.f; fp.vel_g[2 * FP + slot] = 0.f; }
+                        if (fp.vel_c) { fp.vel_c[slot] = 0.f; fp.vel_c[FP + slot] = 0.f; fp.vel_c[2 * FP + slot] = 0.f; }
                     }
                     pendv = kPradEmpty;  // the path radiance starts at 0 without being written
                 }
@@ -603,14 +808,19 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
                 pendv = 0u;
             }
         }
-        F3 tg{1, 0, 0}, bt{0, 1, 0};
+        F3 tg{1, 0, 0}, bt{0, 1, 0}, nf{0, 0, 1};
         if (hit) {
             // ---- processIntersection (cpu_path_tracer.ipp:280-469)
             const uint32_t t = hid;
             F3 fnrm;
-            surface_at<NB>(s, nb, fp.opt.smooth_shading != 0, t, hr.z, hr.w, Pp, N, fnrm, tg, bt, alb);
+            surface_at<NB>(s, nb, fp.opt.smooth_shading != 0, t, hr.z, hr.w, Pp, N, fnrm, tg, bt, nf, alb);
             if (bounce == 0) {
-                if ((aux & AUX_TRI) && st.atri[slot] == VGB_NO_HIT) st.atri[slot] = t;
+                if ((aux & AUX_TRI) && st.atri[slot] == VGB_NO_HIT) {
+                    st.atri[slot] = t;
+                    if (fp.tsz || fp.vel_g || fp.vel_c)
+                        first_hit_passes(s, fp.cam, t, Pp, fp.vel_g, fp.vel_c, fp.tsz,
+                                         (size_t)fp.cam.width * fp.cam.height, slot);
+                }
                 if (aux & AUX_ALB) {
 #pragma unroll
                     for (int k = 0; k < NB; ++k)
@@ -667,7 +877,7 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
         bool new_ray = false;
         if (lit && bounce < fp.opt.bounces) {
             F3 nd;
-            cont = continue_path<NB>(fp.lights, fp.nlights, fp.opt, nb, Pp, N, tg, bt, alb, thr, r0, slot, sample,
+            cont = continue_path<NB>(fp.lights, fp.nlights, fp.opt, nb, Pp, N, tg, bt, nf, alb, thr, r0, slot, sample,
                                      fp.opt.frame, bounce, nd, new_ray);
             if (new_ray) { ro = Pp; rd = nd; }
             // pdf 0: the reference keeps the incoming ray and throughput
@@ -707,7 +917,7 @@ __global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene 
         const float tmax = st.sq_tmax[light][i];
         WRay wr = make_wray(o, d);
         HitOut h;
-        traverse_any_layout<L, true, COUNT>(s.nodes, s.tris, wr, tmax, h, err, cnt);
+        traverse_any_layout<L, true, COUNT>(s.nodes, s.tris, wr, tmax, h, err, cnt, s.iter_cap);
         nsh++;
         if (h.id == VGB_NO_HIT) {
             const uint32_t slot = st.sq_slot[light][i];
@@ -814,10 +1024,17 @@ __global__ void __launch_bounds__(256) k_end_sample(DevState st, const __grid_co
 }
 
 // ------------------------------------------------------------------ pixel solid angle (FP64)
+// pixelToDirectionHelper_d (camera.ipp:1759-1771): the distortion models take and return FP32
+// points, so with a distortion the FP64 point is rounded to FP32, undistorted and widened back.
 __device__ double3 corner_dir(const vgb_camera& c, double x, double y) {
     const float* K = c.kinv;
     double hx = ((double)K[0] * x + (double)K[2] * y) + (double)K[4] * 1.0;
     double hy = ((double)K[1] * x + (double)K[3] * y) + (double)K[5] * 1.0;
+    if (c.distortion) {
+        const float2 u = undistort(c, (float)hx, (float)hy);
+        hx = (double)u.x;
+        hy = (double)u.y;
+    }
     double zd = (double)c.z_dir;
     double vx = hx, vy = zd * hy, vz = zd;
     double s = 1.0 / sqrt((vx * vx + vy * vy) + vz * vz);
@@ -839,7 +1056,7 @@ __device__ double tri_omega(double3 c0, double3 c1, double3 c2) {
     double a2 = acos(ddot(dtangent(c2, c0), dtangent(c2, c1)));
     return ((a0 + a1) + a2) - 3.141592653589793238462;
 }
-__global__ void k_pixel_solid_angle(const vgb_camera cam, float* out) {
+__global__ void k_pixel_solid_angle(const __grid_constant__ vgb_camera cam, float* out) {
     const uint32_t W = cam.width, H = cam.height;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < W * H; p += gridDim.x * blockDim.x) {
         const uint32_t i = p % W, j = p / W;
@@ -862,7 +1079,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const DevScene s, const flo
         WRay wr = make_wray(o, d);
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
-        traverse_any_layout<L, ANY, COUNT>(s.nodes, s.tris, wr, tmax ? tmax[i] : __int_as_float(0x7f800000), h, err, cnt);
+        traverse_any_layout<L, ANY, COUNT>(s.nodes, s.tris, wr, tmax ? tmax[i] : __int_as_float(0x7f800000), h, err, cnt, s.iter_cap);
         tri[i] = h.id;
         if (tout) tout[i] = h.t;
         if (bary) {
@@ -903,6 +1120,10 @@ struct vgb_context {
     uint32_t* d_idx = nullptr;
     float* d_tex = nullptr;
     uint32_t tw = 1, th = 1;
+    float* d_nmap = nullptr;        // tangent-space normal map [nh][nw][3], or null
+    uint32_t nw = 0, nh = 0;
+    vgb_instance_motion* d_motion = nullptr;   // instance motion table, or null (all at rest)
+    uint32_t nmotion = 0;
     uint32_t albedo_uniform = 0, tex_mono = 0;
     float albedo_value[VGB_MAX_BANDS] = {0};
     std::vector<float> h_pos;   // kept for the BVH build
@@ -919,7 +1140,7 @@ struct vgb_context {
     bool h_pos_stale = false;       // device positions moved by a device-side update
     uint32_t* d_vnl = nullptr;      // per-vertex corner lists of the uploaded mesh (vertex-normal updates)
     // render scratch
-    size_t cap_P = 0;
+    size_t cap_P = 0, cap_items = 0;
     uint32_t cap_B = 0, cap_L = 0;
     std::vector<void*> scratch;
     DevState st{};
@@ -956,6 +1177,10 @@ struct vgb_context {
     // pinned host staging of file payloads (Quipu LoDs)
     void* h_pin = nullptr;
     size_t cap_pin = 0;
+    // device address of vgb_render_noalloc's fixed array, looked up by its first call
+    unsigned char* noalloc_base = nullptr;
+    // traversal steps per ray before the ray gives up (vgb_set_traversal_limit)
+    uint32_t iter_cap = vgbd::kIterCap;
 };
 
 namespace {
@@ -990,6 +1215,12 @@ void free_scene(vgb_context* ctx) {
     ctx->d_vpos = nullptr; ctx->d_vnrm = nullptr; ctx->d_vuv = nullptr; ctx->d_valb = nullptr; ctx->d_idx = nullptr; ctx->d_tex = nullptr;
     dfree(ctx->d_vnl);
     ctx->d_vnl = nullptr;
+    dfree(ctx->d_nmap);
+    ctx->d_nmap = nullptr;
+    ctx->nw = ctx->nh = 0;
+    dfree(ctx->d_motion);
+    ctx->d_motion = nullptr;
+    ctx->nmotion = 0;
 }
 void free_bvh(vgb_context* ctx) {
     dfree(ctx->d_nodes); dfree(ctx->d_tris); dfree(ctx->d_parent); dfree(ctx->d_refit);
@@ -999,7 +1230,7 @@ void free_bvh(vgb_context* ctx) {
 void free_scratch(vgb_context* ctx) {
     for (void* p : ctx->scratch) dfree(p);
     ctx->scratch.clear();
-    ctx->cap_P = 0; ctx->cap_B = 0; ctx->cap_L = 0;
+    ctx->cap_P = 0; ctx->cap_items = 0; ctx->cap_B = 0; ctx->cap_L = 0;
 }
 void free_staging(vgb_context* ctx) {
     dfree(ctx->staging_base);
@@ -1016,9 +1247,13 @@ vgb_status ensure_staging(vgb_context* ctx, size_t bytes) {
     return VGB_OK;
 }
 
-vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
-    if (P <= ctx->cap_P && B <= ctx->cap_B && L <= ctx->cap_L) return VGB_OK;
+// Scratch for a frame of P pixels whose bounce-0 launch covers n_items queue items (the frame
+// rounded up to whole 8x4-pixel tiles, so n_items >= P): the hit records of bounce 0 are indexed
+// by item, every other plane by pixel or by a queue position below P.
+vgb_status ensure_scratch(vgb_context* ctx, size_t P, size_t n_items, uint32_t B, uint32_t L) {
+    if (P <= ctx->cap_P && n_items <= ctx->cap_items && B <= ctx->cap_B && L <= ctx->cap_L) return VGB_OK;
     P = std::max(P, ctx->cap_P);
+    n_items = std::max(std::max(n_items, P), ctx->cap_items);
     B = std::max(B, ctx->cap_B);
     L = std::max(L, ctx->cap_L);
     free_scratch(ctx);
@@ -1036,7 +1271,7 @@ vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
     AL(st.arad, B * P * f); AL(st.adir, B * P * f); AL(st.aalb, B * P * f); AL(st.anrm, 3 * P * f);
     AL(st.adep, P * f); AL(st.acnt, P * u); AL(st.atri, P * u);
     AL(st.pq[0], P * u); AL(st.pq[1], P * u);
-    AL(st.hit, P * sizeof(float4));
+    AL(st.hit, n_items * sizeof(float4));
     AL(st.as1, P * f); AL(st.as2, P * f); AL(st.anum, P * u);
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
         if (l < L) {
@@ -1050,7 +1285,7 @@ vgb_status ensure_scratch(vgb_context* ctx, size_t P, uint32_t B, uint32_t L) {
     st.counters = ctx->d_counters;
     st.stats = ctx->d_stats;
     st.P = P;
-    ctx->cap_P = P; ctx->cap_B = B; ctx->cap_L = L;
+    ctx->cap_P = P; ctx->cap_items = n_items; ctx->cap_B = B; ctx->cap_L = L;
     return VGB_OK;
 }
 
@@ -1058,7 +1293,10 @@ DevScene dev_scene(const vgb_context* ctx) {
     DevScene s;
     s.nodes = ctx->d_nodes; s.tris = ctx->d_tris; s.idx = ctx->d_idx; s.vpos = ctx->d_vpos; s.vnrm = ctx->d_vnrm;
     s.vuv = ctx->d_vuv; s.valb = ctx->d_valb; s.tex = ctx->d_tex; s.tw = ctx->tw; s.th = ctx->th;
+    s.nmap = ctx->d_nmap; s.nw = ctx->nw; s.nh = ctx->nh;
+    s.motion = ctx->d_motion; s.nmotion = ctx->nmotion;
     s.albedo_uniform = ctx->albedo_uniform; s.tex_mono = ctx->tex_mono;
+    s.iter_cap = ctx->iter_cap;
     for (int k = 0; k < VGB_MAX_BANDS; ++k) s.albedo_value[k] = ctx->albedo_value[k];
     return s;
 }
@@ -1070,12 +1308,14 @@ int grid_for(const vgb_context* ctx, size_t n, int per_sm = 8, size_t items = 25
     return (int)std::max<size_t>(1, std::min(blocks, cap));
 }
 
+// CUDA events around one launch when `on` and the context's profiling switch are both set.
 struct Prof {
     vgb_context* ctx;
     int family;
     size_t slot;
-    Prof(vgb_context* c, int fam) : ctx(c), family(fam), slot(0) {
-        if (!ctx->profiling) return;
+    bool on;
+    Prof(vgb_context* c, int fam, bool enable) : ctx(c), family(fam), slot(0), on(enable && c->profiling) {
+        if (!on) return;
         if (ctx->prof_used + 2 > ctx->prof_events.size()) {
             for (int k = 0; k < 64; ++k) {
                 cudaEvent_t e;
@@ -1090,15 +1330,29 @@ struct Prof {
         cudaEventRecord(ctx->prof_events[slot], ctx->stream);
     }
     ~Prof() {
-        if (ctx->profiling) cudaEventRecord(ctx->prof_events[slot + 1], ctx->stream);
+        if (on) cudaEventRecord(ctx->prof_events[slot + 1], ctx->stream);
     }
 };
 
+// Queue items of a frame's bounce-0 launch: the frame rounded up to whole 8x4-pixel tiles.
+inline uint64_t tile_items(uint32_t W, uint32_t H) {
+    return (((uint64_t)W + 7u) / 8u) * (((uint64_t)H + 3u) / 4u) * 32u;
+}
+
+// A frame the kernels can index: non-empty, pixel indices and tile items within 2^31 (32-bit
+// slots and grid-stride loops that cannot wrap).
+inline bool frame_fits(uint32_t W, uint32_t H) {
+    return W != 0 && H != 0 && (uint64_t)W * H <= (1ull << 31) && tile_items(W, H) <= (1ull << 31);
+}
+
+// The render's launch sequence (per sample: per bounce k_trace, k_shade, k_shadow per light;
+// then k_end_sample) over the scratch `st`.  vgb_render passes the context's scratch,
+// vgb_render_noalloc the fixed array; `prof` allows CUDA-event profiling of the launches.
 template <int NB, int L, bool COUNT>
-void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
+void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, bool prof,
+                   uint32_t& launches) {
     const DevScene s = dev_scene(ctx);
-    DevState st = ctx->st;
-    const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
+    const uint32_t n0 = (uint32_t)tile_items(fp.cam.width, fp.cam.height);
     const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
     const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
     const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
@@ -1106,26 +1360,26 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
         uint32_t q = 0;
         for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
             // reset the output path queue and the shadow queues
-            cudaMemsetAsync(&ctx->d_counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
-            cudaMemsetAsync(&ctx->d_counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
+            cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
+            cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
             {
-                Prof p(ctx, 0);
+                Prof p(ctx, 0, prof);
                 k_trace<L, COUNT><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             {
-                Prof p(ctx, 3);
+                Prof p(ctx, 3, prof);
                 k_shade<NB><<<gs, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
-                Prof p(ctx, 1);
+                Prof p(ctx, 1, prof);
                 k_shadow<NB, L, COUNT><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
         }
         {
-            Prof p(ctx, 2);
+            Prof p(ctx, 2, prof);
             const uint32_t last = smp + 1 == fp.opt.samples ? 1u : 0u;
             if (fp.opt.adaptive_sampling) k_end_sample<NB, true><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, last, film);
             else k_end_sample<NB, false><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, last, film);
@@ -1135,16 +1389,18 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
 }
 
 template <int L, bool COUNT>
-void dispatch_render_l(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
-    if (fp.nb <= 1) launch_render<1, L, COUNT>(ctx, fp, film, launches);
-    else if (fp.nb <= 4) launch_render<4, L, COUNT>(ctx, fp, film, launches);
-    else launch_render<8, L, COUNT>(ctx, fp, film, launches);
+void dispatch_render_l(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, bool prof,
+                       uint32_t& launches) {
+    if (fp.nb <= 1) launch_render<1, L, COUNT>(ctx, fp, film, st, prof, launches);
+    else if (fp.nb <= 4) launch_render<4, L, COUNT>(ctx, fp, film, st, prof, launches);
+    else launch_render<8, L, COUNT>(ctx, fp, film, st, prof, launches);
 }
 
 template <bool COUNT>
-void dispatch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, uint32_t& launches) {
-    if (ctx->bvh_layout == 8) dispatch_render_l<8, COUNT>(ctx, fp, film, launches);
-    else dispatch_render_l<2, COUNT>(ctx, fp, film, launches);
+void dispatch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, bool prof,
+                     uint32_t& launches) {
+    if (ctx->bvh_layout == 8) dispatch_render_l<8, COUNT>(ctx, fp, film, st, prof, launches);
+    else dispatch_render_l<2, COUNT>(ctx, fp, film, st, prof, launches);
 }
 
 }  // namespace
@@ -1446,6 +1702,50 @@ VGB_API vgb_status vgb_synchronize(vgb_context* ctx) try {
     return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
+VGB_API vgb_status vgb_scene_motion(vgb_context* ctx, const vgb_instance_motion* motion, uint32_t n) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (ctx->nverts == 0) return fail(ctx, VGB_ERR_NOT_READY, "scene_motion: upload the scene first");
+    if (motion && n) {
+        if (motion[0].first_triangle != 0) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_motion: the first entry must start at triangle 0");
+        for (uint32_t k = 1; k < n; ++k)
+            if (motion[k].first_triangle <= motion[k - 1].first_triangle || motion[k].first_triangle >= ctx->ntris)
+                return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_motion: first_triangle must ascend within the mesh");
+    }
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->d_motion);
+    ctx->d_motion = nullptr;
+    ctx->nmotion = 0;
+    if (!motion || n == 0) return VGB_OK;
+    vgb_status s = dalloc(ctx, &ctx->d_motion, sizeof(vgb_instance_motion) * n);
+    if (s != VGB_OK) return s;
+    CK(cudaMemcpy(ctx->d_motion, motion, sizeof(vgb_instance_motion) * n, cudaMemcpyHostToDevice));
+    ctx->nmotion = n;
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
+VGB_API vgb_status vgb_scene_normal_map(vgb_context* ctx, const float* nmap, uint32_t w, uint32_t h) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (ctx->nverts == 0) return fail(ctx, VGB_ERR_NOT_READY, "scene_normal_map: upload the scene first");
+    if (nmap && (uint64_t)w * h > (1ull << 31)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "scene_normal_map: map too large");
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx->d_nmap);
+    ctx->d_nmap = nullptr;
+    ctx->nw = ctx->nh = 0;
+    if (!nmap || w == 0 || h == 0) return VGB_OK;
+    vgb_status s = dalloc(ctx, &ctx->d_nmap, (size_t)w * h * 3 * sizeof(float));
+    if (s != VGB_OK) return s;
+    CK(cudaMemcpy(ctx->d_nmap, nmap, (size_t)w * h * 3 * sizeof(float), cudaMemcpyHostToDevice));
+    ctx->nw = w;
+    ctx->nh = h;
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
 VGB_API vgb_status vgb_scene_upload(vgb_context* ctx, const float* pos, uint32_t nverts, const uint32_t* idx,
                                     uint32_t ntris, uint32_t nbands, const float* valb, const float* vnrm,
                                     const float* vuv, const float* tex, uint32_t tw, uint32_t th) try {
@@ -1643,6 +1943,45 @@ VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable) try {
     return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
 }
 
+VGB_API vgb_status vgb_measure_l2_read(vgb_context* ctx, uint64_t bytes, uint32_t passes, uint32_t repeats,
+                                       double* gbps) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!gbps || bytes < (1u << 20) || bytes > (uint64_t(1) << 34) || bytes % 16 != 0 || passes == 0 || repeats == 0)
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "measure_l2_read: bytes in [1 MiB, 16 GiB], a multiple of 16; passes, repeats >= 1");
+    CK(cudaSetDevice(ctx->device));
+    void* buf = nullptr;
+    vgb_status s = dalloc(ctx, &buf, bytes + 256);
+    if (s != VGB_OK) return s;
+    struct Free { void* p; ~Free() { dfree(p); } } guard{buf};
+    uint32_t* sink = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(buf) + bytes);
+    CK(cudaMemsetAsync(buf, 0x5A, bytes, ctx->stream));
+    // warm-up: one pass brings the buffer into L2 (when it fits)
+    if (vgb::launch_l2_read(ctx->stream, buf, bytes, 1, sink, ctx->num_sms)) CK(cudaGetLastError());
+    double best = 0.0;
+    for (uint32_t r = 0; r < repeats; ++r) {
+        CK(cudaEventRecord(ctx->ev0, ctx->stream));
+        if (vgb::launch_l2_read(ctx->stream, buf, bytes, passes, sink, ctx->num_sms)) CK(cudaGetLastError());
+        CK(cudaEventRecord(ctx->ev1, ctx->stream));
+        CK(cudaEventSynchronize(ctx->ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        if (ms > 0.f) best = std::max(best, (double)bytes * passes / (ms * 1e-3) / 1e9);
+    }
+    *gbps = best;
+    ctx->stats.ms_last = (float)((double)bytes * passes / (best * 1e9) * 1e3);
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
+VGB_API vgb_status vgb_set_traversal_limit(vgb_context* ctx, uint32_t max_steps) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    ctx->iter_cap = max_steps ? max_steps : vgbd::kIterCap;
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
 VGB_API vgb_status vgb_dem_triangulate_gpu(vgb_context* ctx, const float* heights, uint32_t W, uint32_t H, double sx,
                                            double sy, float* pos, uint32_t* idx, uint32_t* nt_out, int on_device) try {
     if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
@@ -1830,7 +2169,8 @@ __device__ __forceinline__ bool raster_setup(const DevScene& s, const RasterPara
         if ((-c.z_dir * r.vc[k].z) >= 0) return false;   // Camera::behind (camera.ipp:1394-1397)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float hx = r.vc[k].x / r.vc[k].z, hy = r.vc[k].y / r.vc[k].z;
+        float hx = r.vc[k].x / r.vc[k].z, hy = r.vc[k].y / r.vc[k].z;
+        if (c.distortion) distort(c, hx, hy);   // Camera::projectCameraPoint (camera.ipp:1060-1080)
         float X = (rp.K[0] * hx + rp.K[1] * hy) + rp.K[2];
         const float Y = (rp.K[3] * hx + rp.K[4] * hy) + rp.K[5];
         if (c.z_dir < 0) X = (float)(c.width - 1) - X;   // Blender frame (camera.ipp:1062-1080)
@@ -1963,6 +2303,11 @@ __global__ void k_raster_resolve(DevScene s, RasterParams rp, const unsigned lon
 #pragma unroll
                 for (int k = 0; k < 3; ++k) vn[k] = ld3(__ldg(&s.vnrm[vi[k]]));
                 N = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
+            }
+            if (s.nmap) {   // the tangent frame and Material::getNormal (cpu_rasterizer.ipp:177-191)
+                F3 tg, bt;
+                tangent_frame(N, tg, bt);
+                N = mapped_normal(s, uvx, uvy, N, tg, bt);
             }
             if (rp.lighting) {
                 const F3 fc = (w[0] * r.vc[0] + w[1] * r.vc[1]) + w[2] * r.vc[2];
@@ -2344,14 +2689,14 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     if (opts->nbands != ctx->nbands) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: nbands differs from the scene");
     if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: at most 8 lights");
-    if (cam->width == 0 || cam->height == 0 || (uint64_t)cam->width * cam->height > (1ull << 31))
+    if (!frame_fits(cam->width, cam->height))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: bad resolution");
     if (film->received_power && !film->pixel_solid_angle)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render: received_power needs pixel_solid_angle");
     cudaSetDevice(ctx->device);
     const size_t P = (size_t)cam->width * cam->height;
     const uint32_t B = ctx->nbands;
-    vgb_status s = ensure_scratch(ctx, P, B, std::max<uint32_t>(1, nlights));
+    vgb_status s = ensure_scratch(ctx, P, tile_items(cam->width, cam->height), B, std::max<uint32_t>(1, nlights));
     if (s != VGB_OK) return s;
     FrameParams fp;
     std::memset(&fp, 0, sizeof(fp));
@@ -2365,21 +2710,23 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     // film planes: device pointers as given, or staging buffers for host films
     FilmOut f{};
     struct Plane { float** host_f; uint32_t** host_u; size_t n; };
-    float* hf[8] = {film->total_radiance, film->direct_radiance, film->indirect_radiance, film->received_power,
-                    film->albedo, film->normal_global, film->depth, film->alpha};
-    const size_t nplane[8] = {B * P, B * P, B * P, B * P, B * P, 3 * P, P, P};
-    float* df[8];
+    constexpr int NPL = 11;
+    float* hf[NPL] = {film->total_radiance, film->direct_radiance, film->indirect_radiance, film->received_power,
+                      film->albedo, film->normal_global, film->depth, film->alpha, film->velocity_global,
+                      film->velocity_camera, film->triangle_size};
+    const size_t nplane[NPL] = {B * P, B * P, B * P, B * P, B * P, 3 * P, P, P, 3 * P, 3 * P, P};
+    float* df[NPL];
     uint32_t* dtri = film->triangle_id;
     const float* domega = film->pixel_solid_angle;
     if (film->on_device) {
-        for (int k = 0; k < 8; ++k) df[k] = hf[k];
+        for (int k = 0; k < NPL; ++k) df[k] = hf[k];
     } else {
         size_t total = 0;
-        for (int k = 0; k < 8; ++k) if (hf[k]) total += nplane[k];
+        for (int k = 0; k < NPL; ++k) if (hf[k]) total += nplane[k];
         total += P + (film->pixel_solid_angle ? P : 0);
         if ((s = ensure_staging(ctx, total * sizeof(float))) != VGB_OK) return s;
         float* cur = (float*)ctx->staging_base;
-        for (int k = 0; k < 8; ++k) { df[k] = hf[k] ? cur : nullptr; if (hf[k]) cur += nplane[k]; }
+        for (int k = 0; k < NPL; ++k) { df[k] = hf[k] ? cur : nullptr; if (hf[k]) cur += nplane[k]; }
         dtri = film->triangle_id ? (uint32_t*)cur : nullptr;
         cur += P;
         if (film->pixel_solid_angle) {
@@ -2389,6 +2736,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     }
     f.total = df[0]; f.direct = df[1]; f.indirect = df[2]; f.power = df[3]; f.albedo = df[4];
     f.normal = df[5]; f.depth = df[6]; f.alpha = df[7]; f.tri = dtri; f.omega = domega;
+    f.vel_g = df[8]; f.vel_c = df[9]; f.tsz = df[10];
     FilmOut fr = f;  // the planes the render itself writes
     float* dn_scratch = nullptr;
     if (opts->denoise) {
@@ -2406,11 +2754,12 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
         if (!fr.depth) fr.depth = extra + (size_t)3 * B * P + 3 * P;
     }
     fp.aux = aux_for(fr) | (opts->adaptive_sampling ? AUX_DEP : 0u);  // the miss test reads the depth sum
+    fp.vel_g = fr.vel_g; fp.vel_c = fr.vel_c; fp.tsz = fr.tsz;
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
     uint32_t launches = 0;
     ctx->prof_used = 0;
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    dispatch_render<false>(ctx, fp, fr, launches);
+    dispatch_render<false>(ctx, fp, fr, ctx->st, true, launches);
     if (dn_scratch) {
         PowerScale ps{};
         for (uint32_t k = 0; k < B && k < VGB_MAX_BANDS; ++k) ps.v[k] = cam->power_scale[k];
@@ -2420,7 +2769,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!film->on_device) {
-        for (int k = 0; k < 8; ++k)
+        for (int k = 0; k < NPL; ++k)
             if (hf[k]) CK(cudaMemcpyAsync(hf[k], df[k], nplane[k] * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
         if (film->triangle_id) CK(cudaMemcpyAsync(film->triangle_id, dtri, P * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     }
@@ -2460,10 +2809,7 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
         none.power = nullptr;
         CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
         uint32_t l2 = 0;
-        const bool prof = ctx->profiling;
-        ctx->profiling = false;
-        dispatch_render<true>(ctx, fp, none, l2);
-        ctx->profiling = prof;
+        dispatch_render<true>(ctx, fp, none, ctx->st, false, l2);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(ctx->stream));
         CK(cudaMemcpy(hs, ctx->d_stats, sizeof(hs), cudaMemcpyDeviceToHost));
@@ -2548,60 +2894,31 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
 }  // extern "C"
 
 // ====================================================================== render without allocation
-// vgb_render_noalloc: the same wavefront kernels as vgb_render, but every byte of their scratch
-// (path state, live-path and shadow-ray queues, per-pixel accumulators, queue counters and the
-// device error word) lives in one fixed device array that is part of this library image.  It
-// exists for callers that must not allocate device memory once their scene is set up -- for
-// example a frame loop with a fixed memory budget, or a host application whose allocator owns
-// the device, where a cudaMalloc inside a render call would synchronize the device or could
-// fail.  The array is shared by every call on a device and keeps the previous call's contents.
-#include <mutex>
-
+// vgb_render_noalloc: the same launch sequence as vgb_render (launch_render), but every byte of
+// its scratch (path state, live-path and shadow-ray queues, per-pixel accumulators, hit records,
+// queue counters and the device error word) lives in one fixed device array that is part of this
+// library image.  It exists for callers that must not allocate device memory once their scene is
+// set up -- for example a frame loop with a fixed memory budget, or a host application whose own
+// allocator owns the device, where a cudaMalloc inside a render call would synchronize the device
+// or could fail.  The array is shared by every call on a device and keeps the previous call's
+// contents.
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB per device
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
 inline size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// Bytes of the fixed array a frame of P pixels, B bands and L lights needs.
-size_t noalloc_bytes(size_t P, size_t B, size_t L) {
+// Bytes of the fixed array a frame of P pixels (n_items bounce-0 queue items), B bands and L
+// lights needs.  With P and n_items at most 2^31 (frame_fits) and B, L at most 8, no term wraps.
+size_t noalloc_bytes(size_t P, size_t n_items, size_t B, size_t L) {
     const size_t f = 4;
     size_t n = 2 * 256;  // counters, statistics
-    const size_t planes[] = {3, 3, B, B, B, 1, B, B, B, 3, 1, 1, 1, 1, 1, 4};
+    const size_t planes[] = {3, 3, B, B, B, 1, B, B, B, 3, 1, 1, 1, 1, 1};
     for (size_t k : planes) n += up256(k * P * f);
+    n += up256(n_items * sizeof(float4));  // hit records
     n += L * (up256(3 * P * f) + up256(3 * P * f) + up256(P * f) + up256(P * f) + up256(B * P * f));
     return n;
-}
-
-template <int NB, int L>
-void launch_noalloc(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, uint32_t& launches) {
-    const DevScene s = dev_scene(ctx);
-    const uint32_t n0 = fp.tiles_x * fp.tiles_y * 32u;
-    const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
-    const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
-    const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
-    for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
-        uint32_t q = 0;
-        for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
-            cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
-            cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
-            k_trace<L, false><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
-            k_shade<NB><<<gs, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
-            launches += 2;
-            for (uint32_t l = 0; l < fp.nlights; ++l) {
-                k_shadow<NB, L, false><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
-                launches++;
-            }
-            q ^= 1u;
-        }
-        k_end_sample<NB, false><<<gp, 256, 0, ctx->stream>>>(st, fp, smp, smp + 1 == fp.opt.samples ? 1u : 0u, film);
-        launches++;
-    }
 }
 
 }  // namespace
@@ -2620,13 +2937,15 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: nbands differs from the scene");
     if (nlights > VGB_MAX_LIGHTS || (nlights && !lights))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: at most 8 lights");
-    if (cam->width == 0 || cam->height == 0)
+    if (!frame_fits(cam->width, cam->height))
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: bad resolution");
     if (film->received_power && !film->pixel_solid_angle)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: received_power needs pixel_solid_angle");
     const size_t P = (size_t)cam->width * cam->height;
+    const size_t n_items = tile_items(cam->width, cam->height);
     const uint32_t B = ctx->nbands;
-    const size_t need = noalloc_bytes(P, B, std::max<uint32_t>(1, nlights));
+    const uint32_t nq = std::max<uint32_t>(1, nlights);
+    const size_t need = noalloc_bytes(P, n_items, B, nq);
     if (need > kNoAllocScratchBytes) {
         char msg[256];
         std::snprintf(msg, sizeof(msg),
@@ -2635,26 +2954,21 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
                       need, kNoAllocScratchBytes, (size_t)cam->width, (size_t)cam->height, B, nlights);
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, msg);
     }
-    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
-        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_noalloc: device index beyond 63");
     CK(cudaSetDevice(ctx->device));
-    unsigned char* base = nullptr;
-    {
-        // Once per device, with that device current: the device address of the fixed array.
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_ptr[ctx->device]) {
-            void* p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p)
-                return fail(ctx, VGB_ERR_CUDA, std::string("render_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            g_noalloc_ptr[ctx->device] = static_cast<unsigned char*>(p);
-        }
-        base = g_noalloc_ptr[ctx->device];
+    if (!ctx->noalloc_base) {
+        // Once per context, with its device current: the device address of the fixed array (in
+        // host code the array's name stands for a host-side shadow, not for device memory).
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(ctx, VGB_ERR_CUDA, std::string("render_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        ctx->noalloc_base = static_cast<unsigned char*>(p);
     }
+    unsigned char* const base = ctx->noalloc_base;
     // Carve the frame's scratch out of the fixed array.
     DevState st{};
     size_t off = 0;
-    auto take = [&](size_t bytes) { unsigned char* p = base + off; off += up256(bytes); return p; };
+    auto take = [&](size_t bytes) { unsigned char* q = base + off; off += up256(bytes); return q; };
     const size_t f = sizeof(float);
     st.counters = reinterpret_cast<uint32_t*>(take(256));
     st.stats = reinterpret_cast<uint64_t*>(take(256));
@@ -2663,9 +2977,9 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     st.arad = (float*)take(B * P * f); st.adir = (float*)take(B * P * f); st.aalb = (float*)take(B * P * f);
     st.anrm = (float*)take(3 * P * f); st.adep = (float*)take(P * f); st.acnt = (uint32_t*)take(P * f);
     st.atri = (uint32_t*)take(P * f); st.pq[0] = (uint32_t*)take(P * f); st.pq[1] = (uint32_t*)take(P * f);
-    st.hit = (float4*)take(4 * P * f);
+    st.hit = (float4*)take(n_items * sizeof(float4));
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
-        if (l < std::max<uint32_t>(1, nlights)) {
+        if (l < nq) {
             st.sq_org[l] = (float*)take(3 * P * f); st.sq_dir[l] = (float*)take(3 * P * f);
             st.sq_tmax[l] = (float*)take(P * f); st.sq_slot[l] = (uint32_t*)take(P * f);
             st.sq_con[l] = (float*)take(B * P * f);
@@ -2673,6 +2987,7 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
             st.sq_org[l] = st.sq_dir[l] = st.sq_tmax[l] = st.sq_con[l] = nullptr; st.sq_slot[l] = nullptr;
         }
     }
+    if (off != need) return fail(ctx, VGB_ERR_INTERNAL, "render_noalloc: scratch layout differs from its size");
     st.P = P;
     FrameParams fp;
     std::memset(&fp, 0, sizeof(fp));
@@ -2687,31 +3002,37 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
     fo.total = film->total_radiance; fo.direct = film->direct_radiance; fo.indirect = film->indirect_radiance;
     fo.power = film->received_power; fo.albedo = film->albedo; fo.normal = film->normal_global;
     fo.depth = film->depth; fo.alpha = film->alpha; fo.tri = film->triangle_id; fo.omega = film->pixel_solid_angle;
+    fo.vel_g = film->velocity_global; fo.vel_c = film->velocity_camera; fo.tsz = film->triangle_size;
     fp.aux = aux_for(fo);
+    fp.vel_g = fo.vel_g; fp.vel_c = fo.vel_c; fp.tsz = fo.tsz;
     // The array keeps the last call's contents: the counters, statistics and error word must
     // start at zero; every other region is written before it is read.
     CK(cudaMemsetAsync(st.counters, 0, 256, ctx->stream));
     CK(cudaMemsetAsync(st.stats, 0, 256, ctx->stream));
     uint32_t launches = 0;
-    if (ctx->bvh_layout == 8) {
-        if (B <= 1) launch_noalloc<1, 8>(ctx, fp, fo, st, launches);
-        else if (B <= 4) launch_noalloc<4, 8>(ctx, fp, fo, st, launches);
-        else launch_noalloc<8, 8>(ctx, fp, fo, st, launches);
-    } else {
-        if (B <= 1) launch_noalloc<1, 2>(ctx, fp, fo, st, launches);
-        else if (B <= 4) launch_noalloc<4, 2>(ctx, fp, fo, st, launches);
-        else launch_noalloc<8, 2>(ctx, fp, fo, st, launches);
-    }
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    dispatch_render<false>(ctx, fp, fo, st, false, launches);
     CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
     uint32_t err_word = 0;
     uint64_t hs[8] = {0};
     CK(cudaMemcpyAsync(&err_word, &st.counters[C_ERR], sizeof(err_word), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(hs, st.stats, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    // the statistics this call measures; the counting pass and per-family profiling do not apply
+    // (their fields read 0); the BVH fields describe the scene and stay
+    const vgb_stats keep = ctx->stats;
+    ctx->stats = vgb_stats{};
+    ctx->stats.bvh_nodes = keep.bvh_nodes;
+    ctx->stats.bvh_node_bytes = keep.bvh_node_bytes;
+    ctx->stats.tri_record_bytes = keep.tri_record_bytes;
     ctx->stats.rays_closest = hs[2];
     ctx->stats.rays_shadow = hs[3];
     ctx->stats.hits_closest = hs[6];
     ctx->stats.kernel_launches = launches;
+    ctx->stats.ms_last = ms;
     ctx->stats.device_error = err_word;
     if (err_word)
         return fail(ctx, VGB_ERR_DEVICE_LIMIT,
@@ -2728,11 +3049,10 @@ extern "C" VGB_API vgb_status vgb_render_noalloc(vgb_context* ctx, const vgb_cam
 // those kernels' instruction footprint small (instruction fetch was their leading stall; the
 // batch kernel ran 12 % and the adjoint 28 % faster than with both loops inlined).
 template <int L>
-__device__ __noinline__ void trace_ool(const uint4* __restrict__ nodes, const float4* __restrict__ tris, WRay r,
-                                       float tmax, bool any, HitOut& h, uint32_t& err) {
+__device__ __noinline__ void trace_ool(const DevScene& s, WRay r, float tmax, bool any, HitOut& h, uint32_t& err) {
     Counters c{0, 0};
-    if (L == 8) traverse8_rt<false>(nodes, tris, r, tmax, any, h, err, c);
-    else traverse_rt<false>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, any, h, err, c);
+    if (L == 8) traverse8_rt<false>(s.nodes, s.tris, r, tmax, any, h, err, c, s.iter_cap);
+    else traverse_rt<false>(reinterpret_cast<const float4*>(s.nodes), s.tris, r, tmax, any, h, err, c, s.iter_cap);
 }
 
 // ====================================================================== batched trajectory
@@ -2836,21 +3156,8 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
             uint32_t stopped = 0;       // adaptive sampling: sample index at which the pixel stopped
             for (uint32_t sample = 0; sample < F.samples; ++sample) {
                 // camera ray (camera_ray with this frame's camera and key)
-                float X = (float)pi, Y = (float)pj;
-                if (sample != 0) {
-                    U4 jr = philox(U4{slot, sample, F.frame, kSlotJitter}, k0, k1);
-                    X = X + u01(jr.x);
-                    Y = Y + u01(jr.y);
-                }
-                const float* K = F.cam.kinv;
-                const float hx = (K[0] * X + K[2] * Y) + K[4] * 1.0f;
-                const float hy = (K[1] * X + K[3] * Y) + K[5] * 1.0f;
-                const F3 dc{hx, F.cam.z_dir * hy, F.cam.z_dir};
-                const float* R = F.cam.rotation;
-                const F3 dw{(R[0] * dc.x + R[3] * dc.y) + R[6] * dc.z, (R[1] * dc.x + R[4] * dc.y) + R[7] * dc.z,
-                            (R[2] * dc.x + R[5] * dc.y) + R[8] * dc.z};
-                F3 rd = normalize(dw);
-                F3 ro{F.cam.origin[0], F.cam.origin[1], F.cam.origin[2]};
+                F3 ro, rd;
+                pixel_ray(F.cam, pi, pj, slot, sample, F.frame, k0, k1, ro, rd);
                 float thr[NB], alb[NB];
 #define PRAD(k) acc[(3 * NB + 4 + (k)) * 32 + lane]
 #define BRAD(k) acc[(4 * NB + 4 + (k)) * 32 + lane]
@@ -2870,7 +3177,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     HitOut h;
                     h.U = h.V = h.W = 0.f; h.det = 1.f;
                     const WRay wr = make_wray(ro, rd);
-                    trace_ool<L>(s.nodes, s.tris, wr, 0.f, false, h, err);
+                    trace_ool<L>(s, wr, 0.f, false, h, err);
                     nclosest++;
                     if (h.id == VGB_NO_HIT) {
                         if (opt.simulate_lighting && opt.show_background) {
@@ -2887,10 +3194,15 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     }
                     const float rcp = 1.0f / h.det;
                     const float w0 = h.V * rcp, w1 = h.W * rcp;
-                    F3 Pp, N, fnrm, tg, bt;
-                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, alb);
+                    F3 Pp, N, fnrm, tg, bt, nf;
+                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, w0, w1, Pp, N, fnrm, tg, bt, nf, alb);
                     if (bounce == 0) {
-                        if (first_tri == VGB_NO_HIT) first_tri = h.id;
+                        if (first_tri == VGB_NO_HIT) {
+                            first_tri = h.id;
+                            if (F.film.tsz || F.film.vel_g || F.film.vel_c)
+                                first_hit_passes(s, F.cam, h.id, Pp, F.film.vel_g, F.film.vel_c, F.film.tsz,
+                                                 (size_t)W * H, slot);
+                        }
 #pragma unroll
                         for (int k = 0; k < NB; ++k) if (k < (int)nb) ACC(2 * NB + k) += alb[k];
                         ACC(3 * NB + 0) += N.x; ACC(3 * NB + 1) += N.y; ACC(3 * NB + 2) += N.z;
@@ -2917,7 +3229,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                         if (lpdf > 0) {
                             HitOut hs;
                             const WRay ws = make_wray(Pp, Ld);
-                            trace_ool<L>(s.nodes, s.tris, ws, dist, true, hs, err);
+                            trace_ool<L>(s, ws, dist, true, hs, err);
                             nshadow++;
                             if (hs.id == VGB_NO_HIT) {
                                 const float nl = dot(N, Ld);
@@ -2936,7 +3248,7 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
                     if (DIRECT || bounce >= opt.bounces) break;
                     bool new_ray = false;
                     F3 nd;
-                    const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, alb, thr, r0, slot,
+                    const bool cont = continue_path<NB>(F.lights, F.nlights, opt, nb, Pp, N, tg, bt, nf, alb, thr, r0, slot,
                                                         sample, F.frame, bounce, nd, new_ray);
                     if (!cont) break;
                     if (new_ray) { ro = Pp; rd = nd; }
@@ -2982,6 +3294,11 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
             if (f.depth) f.depth[slot] = (count == 0) ? __int_as_float(0x7f800000) : ACC(3 * NB + 3) / (float)count;
             if (f.alpha) f.alpha[slot] = (float)count / sf;
             if (f.tri) f.tri[slot] = first_tri;
+            if (first_tri == VGB_NO_HIT) {   // never hit: the passes' initial values
+                if (f.tsz) f.tsz[slot] = __int_as_float(0x7f800000);
+                if (f.vel_g) { f.vel_g[slot] = 0.f; f.vel_g[P + slot] = 0.f; f.vel_g[2 * P + slot] = 0.f; }
+                if (f.vel_c) { f.vel_c[slot] = 0.f; f.vel_c[P + slot] = 0.f; f.vel_c[2 * P + slot] = 0.f; }
+            }
         }
     }
 #undef ACC
@@ -3049,7 +3366,7 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
     std::vector<uint32_t> order(nframes);
     for (uint32_t f = 0; f < nframes; ++f) {
         const vgb_frame& fr = frames[f];
-        if (fr.samples == 0 || fr.camera.width == 0 || fr.camera.height == 0 || fr.nlights > VGB_MAX_LIGHTS ||
+        if (fr.samples == 0 || !frame_fits(fr.camera.width, fr.camera.height) || fr.nlights > VGB_MAX_LIGHTS ||
             !fr.film.on_device || (fr.film.received_power && !fr.film.pixel_solid_angle))
             return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: frame " + std::to_string(f) +
                                                            ": samples/resolution/lights/film invalid (film must be device memory)");
@@ -3090,6 +3407,7 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
         d.film.indirect = fr.film.indirect_radiance; d.film.power = fr.film.received_power;
         d.film.albedo = fr.film.albedo; d.film.normal = fr.film.normal_global; d.film.depth = fr.film.depth;
         d.film.alpha = fr.film.alpha; d.film.tri = fr.film.triangle_id; d.film.omega = fr.film.pixel_solid_angle;
+        d.film.vel_g = fr.film.velocity_global; d.film.vel_c = fr.film.velocity_camera; d.film.tsz = fr.film.triangle_size;
     }
     if (total_tiles >= (1ull << 31)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_batch: too many pixels");
     CK(cudaMemcpyAsync(ctx->d_frames, hf, sizeof(DevFrame) * nframes, cudaMemcpyHostToDevice, ctx->stream));
@@ -3249,7 +3567,7 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
         HitOut h;
         h.U = h.V = h.W = 0.f; h.det = 1.f;
         const WRay wr = make_wray(ro, rd);
-        trace_ool<L>(s.nodes, s.tris, wr, 0.f, false, h, err);
+        trace_ool<L>(s, wr, 0.f, false, h, err);
         nrays++;
         if (h.id == VGB_NO_HIT) {
             if (opt.simulate_lighting && opt.show_background) {
@@ -3274,9 +3592,9 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
         V.tri = h.id;
         V.w0 = h.V * rcp;
         V.w1 = h.W * rcp;
-        F3 Pp, N, fnrm, tg, bt;
+        F3 Pp, N, fnrm, tg, bt, nf;
         float uv[2];
-        surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, V.w0, V.w1, Pp, N, fnrm, tg, bt, V.alb, V.va, V.tex, uv);
+        surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, V.w0, V.w1, Pp, N, fnrm, tg, bt, nf, V.alb, V.va, V.tex, uv);
         V.uvx = uv[0]; V.uvy = uv[1];
         if (g) {
             // M^-1 e_a for the hit-point motion (caller order A=v0, B=v1, C=v2), by Cramer's rule:
@@ -3311,7 +3629,7 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
             if (!(lpdf > 0)) continue;
             HitOut hs;
             const WRay ws = make_wray(Pp, Ld);
-            trace_ool<L>(s.nodes, s.tris, ws, dist, true, hs, err);
+            trace_ool<L>(s, ws, dist, true, hs, err);
             nrays++;
             if (hs.id != VGB_NO_HIT) continue;
             const float nl = dot(N, Ld);
@@ -3339,7 +3657,7 @@ __device__ __forceinline__ int adj_replay(const DevScene& s, const vgb_camera& c
         if (bounce >= opt.bounces) break;
         bool new_ray = false;
         F3 nd;
-        const bool cont = continue_path<NB>(lights, nlights, opt, nb, Pp, N, tg, bt, V.alb, thr, r0, slot, sample,
+        const bool cont = continue_path<NB>(lights, nlights, opt, nb, Pp, N, tg, bt, nf, V.alb, thr, r0, slot, sample,
                                             frame, bounce, nd, new_ray);
         if (!cont) break;
         if (new_ray) { ro = Pp; rd = nd; }
@@ -3734,6 +4052,8 @@ vgb_status adjoint_common(vgb_context* ctx, const vgb_camera* cam, const vgb_lig
     if (opts->adaptive_sampling || opts->denoise)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": adaptive sampling and denoising are not differentiated");
     if (opts->bounces + 1 > (uint32_t)kAdjMaxVerts) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": at most 3 bounces");
+    if (!frame_fits(cam->width, cam->height)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": bad resolution");
+    if (ctx->d_nmap) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, w + ": normal maps are not differentiated");
     cudaSetDevice(ctx->device);
     FrameParams fp;
     std::memset(&fp, 0, sizeof(fp));
@@ -3813,12 +4133,13 @@ extern "C" VGB_API vgb_status vgb_render_adjoint_batch(vgb_context* ctx, const v
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: at most 3 bounces");
     if (opts->adaptive_sampling || opts->denoise)
         return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: adaptive sampling and denoising are not differentiated");
+    if (ctx->d_nmap) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: normal maps are not differentiated");
     cudaSetDevice(ctx->device);
     std::vector<DevView> hv(nviews);
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < nviews; ++i) {
         const vgb_view& v = views[i];
-        if (v.samples == 0 || v.nlights > VGB_MAX_LIGHTS || !v.target || v.camera.width == 0 || v.camera.height == 0)
+        if (v.samples == 0 || v.nlights > VGB_MAX_LIGHTS || !v.target || !frame_fits(v.camera.width, v.camera.height))
             return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "render_adjoint_batch: view " + std::to_string(i) + " invalid");
         DevView& d = hv[i];
         std::memset(&d, 0, sizeof(d));

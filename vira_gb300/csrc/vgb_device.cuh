@@ -20,7 +20,7 @@ constexpr uint32_t kSlotMain = 0u, kSlotRR = 0xFEu, kSlotJitter = 0xFFu;
 constexpr uint32_t kErrStack = 1u, kErrIter = 2u;
 
 constexpr int kStackSize = 64;
-constexpr uint32_t kIterCap = 1u << 22;  // traversal steps per ray before giving up
+constexpr uint32_t kIterCap = 1u << 22;  // default traversal steps per ray before giving up
 
 // ------------------------------------------------------------------ Philox-4x32-10
 // Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011.
@@ -189,7 +189,7 @@ __device__ __forceinline__ void slab(const SlabRay& q, float lox, float hix, flo
 template <bool COUNT>
 __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                             const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
-                                            Counters& cnt) {
+                                            Counters& cnt, uint32_t cap) {
     int stack[kStackSize];
     int sp = 0;
     int node = 0;
@@ -200,7 +200,7 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
     const SlabRay q = make_slab(r);
     while (true) {
         while (node >= 0) {
-            if (++iter > kIterCap) { err |= kErrIter; return; }
+            if (++iter > cap) { err |= kErrIter; return; }
             const float4 n0 = __ldg(&nodes[4 * node + 0]);
             const float4 n1 = __ldg(&nodes[4 * node + 1]);
             const float4 n2 = __ldg(&nodes[4 * node + 2]);
@@ -252,8 +252,9 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
 
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                         const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
-    traverse_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt);
+                                         const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
+                                         uint32_t cap) {
+    traverse_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt, cap);
 }
 
 // ------------------------------------------------------------------ compressed 8-wide traversal
@@ -277,7 +278,7 @@ __device__ __forceinline__ float q8(uint32_t w, int byte) { return (float)((w >>
 template <bool COUNT>
 __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                              const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
-                                             Counters& cnt) {
+                                             Counters& cnt, uint32_t cap) {
     const float widen = 1.0f + 0x1p-20f;
     const uint32_t oct = (r.d.x < 0.f ? 1u : 0u) | (r.d.y < 0.f ? 2u : 0u) | (r.d.z < 0.f ? 4u : 0u);
     uint2 stack[kStack8];
@@ -289,7 +290,7 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
     uint32_t iter = 0;
     const float ox = r.o.x, oy = r.o.y, oz = r.o.z, ix = r.ix, iy = r.iy, iz = r.iz;
     while (true) {
-        if (++iter > kIterCap) { err |= kErrIter; return; }
+        if (++iter > cap) { err |= kErrIter; return; }
         const uint4 w0 = __ldg(&nodes[5 * node + 0]);
         const uint4 w1 = __ldg(&nodes[5 * node + 1]);
         const uint4 w2 = __ldg(&nodes[5 * node + 2]);
@@ -359,16 +360,19 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
 
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse8(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
-    traverse8_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt);
+                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
+                                          uint32_t cap) {
+    traverse8_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt, cap);
 }
 
-// Dispatch on the node layout (2: binary, 8: compressed 8-wide).
+// Dispatch on the node layout (2: binary, 8: compressed 8-wide).  `cap`: traversal steps per
+// ray before the ray gives up and sets kErrIter.
 template <int LAYOUT, bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse_any_layout(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                    const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt) {
-    if (LAYOUT == 8) traverse8<ANY, COUNT>(nodes, tris, r, tmax, h, err, cnt);
-    else traverse<ANY, COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, h, err, cnt);
+                                                    const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
+                                                    uint32_t cap) {
+    if (LAYOUT == 8) traverse8<ANY, COUNT>(nodes, tris, r, tmax, h, err, cnt, cap);
+    else traverse<ANY, COUNT>(reinterpret_cast<const float4*>(nodes), tris, r, tmax, h, err, cnt, cap);
 }
 
 }  // namespace vgbd

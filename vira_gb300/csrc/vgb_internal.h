@@ -108,6 +108,10 @@ constexpr uint32_t kNoParent = 0xFFFFFFFFu;
 bool build_bvh(const float* positions, uint32_t nverts, const uint32_t* indices, uint32_t ntris,
                uint32_t max_leaf, uint32_t threads, uint32_t layout, BvhHost& out, const char** err);
 
+// L2 read-bandwidth probe (vgb_probe.cu): `passes` streaming reads (ld.global.cg) of `bytes` of
+// device memory at `buf` (16-byte aligned, a multiple of 16 bytes); sink: one device word.
+int launch_l2_read(void* stream, const void* buf, size_t bytes, uint32_t passes, uint32_t* sink, int num_sms);
+
 // Sensor chain and PSF kernels (vgb_sensor.cu); the C ABI in vgb_cuda.cu validates and stages
 // the planes and calls these on the context's stream.  All pointers are device memory.
 struct SensorParams {

@@ -44,6 +44,16 @@ class Camera:
         self.position = np.zeros(3, np.float64)          # FP64, scene (global) frame
         self.rotation = np.eye(3, dtype=np.float64)       # FP64, columns = camera axes
         self._kinv = None
+        # lens distortion: (capi distortion model, FP32 coefficients) or None; with interpolation
+        # (the reference's default) ray directions come from the table of integer-pixel directions
+        self.distortion = None
+        self.interpolate_distortion_directions = True
+        # depth of field (off by default, as in the reference); +inf focus keeps pinhole directions
+        self.depth_of_field = False
+        self.focus_distance = np.float32(np.inf)
+        # motion (global frame) for the velocity pass
+        self.velocity = np.zeros(3, np.float64)
+        self.angular_rate = np.zeros(3, np.float64)
         # the sensor chain after the film (exposure, photosite, noise model, PSF, filter mosaic)
         from .sensor import SensorModel
 
@@ -87,6 +97,39 @@ class Camera:
     def set_field_of_view(self, fov_deg: float):
         """Focal length giving the horizontal field of view for the current sensor width."""
         self.set_focal_length(float(self.sensor_size[0]) / 2.0 / math.tan(math.radians(fov_deg) / 2.0))
+
+    # --- lens distortion and depth of field (camera.ipp:183-206, 420-428, 795-840)
+    def set_brown_distortion_coefficients(self, k1=0.0, k2=0.0, k3=0.0, p1=0.0, p2=0.0):
+        self.distortion = (capi.DISTORTION_BROWN, np.array([k1, k2, k3, p1, p2], np.float32))
+
+    def set_opencv_distortion_coefficients(self, k1=0.0, k2=0.0, k3=0.0, k4=0.0, k5=0.0, k6=0.0, p1=0.0, p2=0.0,
+                                           s1=0.0, s2=0.0, s3=0.0, s4=0.0):
+        self.distortion = (capi.DISTORTION_OPENCV,
+                           np.array([k1, k2, k3, k4, k5, k6, p1, p2, s1, s2, s3, s4], np.float32))
+
+    def set_owen_distortion_coefficients(self, e1=0.0, e2=0.0, e3=0.0, e4=0.0, e5=0.0, e6=0.0):
+        self.distortion = (capi.DISTORTION_OWEN, np.array([e1, e2, e3, e4, e5, e6], np.float32))
+
+    def clear_distortion(self):
+        self.distortion = None
+
+    def has_distortion(self) -> bool:
+        return self.distortion is not None
+
+    def enable_distortion_interpolation(self, interpolation: bool = True):
+        self.interpolate_distortion_directions = bool(interpolation)
+
+    def enable_depth_of_field(self, depth_of_field: bool = True):
+        self.depth_of_field = bool(depth_of_field)
+
+    def set_focus_distance(self, focus_distance: float):
+        if math.isnan(focus_distance):
+            raise ValueError("Focus Distance must not be NaN")
+        self.focus_distance = np.float32(focus_distance)
+
+    def aperture_radius(self) -> np.float32:
+        """CircularAperture radius after Camera::initialize: (focal_length / f_stop) / 2 in FP32."""
+        return np.float32(np.float32(self.focal_length / self.f_stop) / np.float32(2.0))
 
     def set_optical_efficiency(self, eff):
         self.optical_efficiency = eff
@@ -167,7 +210,9 @@ class Camera:
         r = np.float32(d / np.float32(2.0))
         return np.float32(np.float32(PI_F * r) * r)
 
-    def to_c(self, scene_origin: np.ndarray, nbands: int) -> capi.Camera:
+    def to_c(self, scene_origin: np.ndarray, nbands: int, kinv=None) -> capi.Camera:
+        """The C-ABI camera: FP64 pose rebased on `scene_origin`, then FP32.  `kinv`: the six
+        FP32 entries of K^-1 when the caller has them (default: vgb_camera_intrinsics)."""
         c = capi.Camera()
         c.width, c.height = self.resolution
         o = (self.position - scene_origin).astype(np.float32)    # FP64 rebasing, then FP32
@@ -177,7 +222,7 @@ class Camera:
         for col in range(3):
             for row in range(3):
                 c.rotation[3 * col + row] = float(R[row, col])
-        kinv = self.kinv()
+        kinv = self.kinv() if kinv is None else np.asarray(kinv, np.float32)
         for k in range(6):
             c.kinv[k] = float(kinv[k])
         c.z_dir = float(self.z_dir)
@@ -185,6 +230,21 @@ class Camera:
         area = self.aperture_area()
         for k in range(nbands):
             c.power_scale[k] = float(np.float32(eff[k] * area))
+        if self.distortion is not None:
+            c.distortion = int(self.distortion[0])
+            for k, v in enumerate(self.distortion[1]):
+                c.distortion_coeffs[k] = float(v)
+        c.interpolate_directions = int(bool(self.interpolate_distortion_directions))
+        c.depth_of_field = int(bool(self.depth_of_field))
+        c.aperture_radius = float(self.aperture_radius())
+        c.focal_length = float(self.focal_length)
+        c.focus_distance = float(self.focus_distance)
+        c.sensor_size[0], c.sensor_size[1] = float(self.sensor_size[0]), float(self.sensor_size[1])
+        ro = (self.rotation @ np.asarray(scene_origin, np.float64)).astype(np.float32)
+        for k in range(3):
+            c.velocity[k] = float(np.float32(self.velocity[k]))
+            c.angular_rate[k] = float(np.float32(self.angular_rate[k]))
+            c.rot_origin[k] = float(ro[k])
         return c
 
 
@@ -199,6 +259,7 @@ class Mesh:
     uv: np.ndarray | None = None           # (n, 2) float32
     normals: np.ndarray | None = None      # (n, 3) float32; computed by Mesh::init when absent
     albedo_map: np.ndarray | None = None   # (h, w, B) float32 material albedo texture
+    normal_map: np.ndarray | None = None   # (h, w, 3) float32 tangent-space normals (Material::setNormalMap)
     smooth_shading: bool = False
     quipu: object = None                   # DEMQuipu the mesh's LoDs come from (Mesh::hasQuipu_)
     target_gsd: float = math.inf           # set by the level-of-detail manager
@@ -318,12 +379,20 @@ class Instance:
     rotation: np.ndarray = field(default_factory=lambda: np.eye(3))     # FP64
     scale: float = 1.0
     visible: bool = True
+    velocity: np.ndarray = field(default_factory=lambda: np.zeros(3))      # global frame, m/s
+    angular_rate: np.ndarray = field(default_factory=lambda: np.zeros(3))  # global frame, rad/s
 
     def set_local_position(self, x, y=None, z=None):
         self.position = np.array([x, y, z] if y is not None else x, np.float64).reshape(3)
 
     def set_local_rotation(self, matrix):
         self.rotation = np.array(matrix, np.float64).reshape(3, 3)
+
+    def set_velocity(self, v):
+        self.velocity = np.array(v, np.float64).reshape(3)
+
+    def set_angular_rate(self, w):
+        self.angular_rate = np.array(w, np.float64).reshape(3)
 
 
 @dataclass
@@ -398,6 +467,12 @@ class RenderPasses:
     mesh_id: object = None
     material_id: object = None
     normal_camera: object = None
+    # first-hit passes (passes.hpp:79-85), filled by the path tracer when requested
+    save_velocity: bool = False
+    velocity_global: object = None
+    velocity_camera: object = None
+    save_triangle_size: bool = False
+    triangle_size: object = None
 
 
 def _id_passes(rp: "RenderPasses", scene: "Scene", camera: "Camera", first: int, raster: bool):
@@ -496,9 +571,16 @@ class PathTracer:
             rp.received_power = torch.empty((B, H, W), dtype=torch.float32, device=dev)
         else:
             rp.total_radiance = rp.direct_radiance = rp.indirect_radiance = rp.received_power = None
+        if rp.save_velocity:
+            rp.velocity_global = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+            rp.velocity_camera = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+        else:
+            rp.velocity_global = rp.velocity_camera = None
+        rp.triangle_size = torch.empty((H, W), dtype=torch.float32, device=dev) if rp.save_triangle_size else None
         f = capi.Film()
         for name in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo",
-                     "normal_global", "depth", "alpha", "triangle_id"):
+                     "normal_global", "depth", "alpha", "triangle_id", "velocity_global", "velocity_camera",
+                     "triangle_size"):
             setattr(f, name, capi.ptr(getattr(rp, name)))
         f.pixel_solid_angle = capi.ptr(omega)
         f.on_device = 1
@@ -696,6 +778,8 @@ class Scene:
         B = self.bands.size
         pos, idx, alb, uv, nrm = [], [], [], [], []
         tex = None
+        nmap = None
+        moving = []
         base = 0
         tri_offsets = []
         for ii, inst in enumerate(self.instances):
@@ -718,7 +802,12 @@ class Scene:
                 if tex is not None and tex is not m.albedo_map:
                     raise ValueError("one albedo texture per scene is supported")
                 tex = m.albedo_map
+            if m.normal_map is not None:
+                if nmap is not None and nmap is not m.normal_map:
+                    raise ValueError("one normal map per scene is supported")
+                nmap = m.normal_map
             tri_offsets.append((ii, base, int(m.indices.shape[0])))
+            moving.append(bool(inst.velocity.any() or inst.angular_rate.any()))
             base += m.positions.shape[0]
         if not pos:
             raise ValueError("scene has no visible instances")
@@ -729,9 +818,27 @@ class Scene:
             uv=np.ascontiguousarray(np.concatenate(uv)),
             normals=np.ascontiguousarray(np.concatenate(nrm)),
             texture=None if tex is None else np.ascontiguousarray(tex, np.float32),
+            normal_map=None if nmap is None else np.ascontiguousarray(nmap, np.float32).reshape(nmap.shape[0], nmap.shape[1], 3),
             tri_offsets=tri_offsets,
+            motion=self._motion_table(tri_offsets) if any(moving) else None,
         )
         return self.flat
+
+    def _motion_table(self, tri_offsets):
+        """The instances' motion for the velocity pass: (first triangle in the flattened mesh,
+        velocity, angular rate, position rebased on the scene origin in FP64, then FP32)."""
+        arr = (capi.InstanceMotion * len(tri_offsets))()
+        first = 0
+        for k, (ii, _, ntri) in enumerate(tri_offsets):
+            inst = self.instances[ii]
+            arr[k].first_triangle = first
+            p = (inst.position - self.origin).astype(np.float32)
+            for a in range(3):
+                arr[k].velocity[a] = float(np.float32(inst.velocity[a]))
+                arr[k].angular_rate[a] = float(np.float32(inst.angular_rate[a]))
+                arr[k].position[a] = float(p[a])
+            first += ntri
+        return arr
 
     def build_tlas(self):
         """Scene::buildTLAS (scene.ipp:712-812): flatten, upload and build the BVH when dirty."""
@@ -746,6 +853,11 @@ class Scene:
                                         f["indices"].shape[0], self.bands.size, capi.ptr(f["albedo"]),
                                         capi.ptr(f["normals"]), capi.ptr(f["uv"]), capi.ptr(tex), tw, th),
                    ctx, "scene_upload")
+        if f["motion"] is not None:
+            capi.check(lib.vgb_scene_motion(ctx, C.cast(f["motion"], C.c_void_p), len(f["motion"])), ctx, "scene_motion")
+        nm = f["normal_map"]
+        if nm is not None:
+            capi.check(lib.vgb_scene_normal_map(ctx, capi.ptr(nm), nm.shape[1], nm.shape[0]), ctx, "scene_normal_map")
         capi.check(lib.vgb_bvh_build(ctx, C.byref(self.bvh_options)), ctx, "bvh_build")
         self._dirty = False
 
@@ -801,7 +913,8 @@ class Scene:
         """Camera::initializePixelSolidAngle (camera.ipp:1622-1666) on the device, FP64, cached."""
         import torch
 
-        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir))
+        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir), int(cam_c.distortion),
+               tuple(cam_c.distortion_coeffs))
         om = self._omega_cache.get(key)
         if om is None:
             W, H = camera.resolution
@@ -835,11 +948,11 @@ class Scene:
             keep.append(omega)
             out = {}
             for name in planes:
-                if name in ("depth", "alpha"):
+                if name in ("depth", "alpha", "triangle_size"):
                     out[name] = torch.empty((H, W), dtype=torch.float32, device=dev)
                 elif name == "triangle_id":
                     out[name] = torch.empty((H, W), dtype=torch.int32, device=dev)
-                elif name == "normal_global":
+                elif name in ("normal_global", "velocity_global", "velocity_camera"):
                     out[name] = torch.empty((3, H, W), dtype=torch.float32, device=dev)
                 else:
                     out[name] = torch.empty((B, H, W), dtype=torch.float32, device=dev)
@@ -873,7 +986,8 @@ class Scene:
     def _batch_omega(self, camera: Camera, cam_c):
         import torch
 
-        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir))
+        key = (camera.resolution, tuple(cam_c.kinv), float(cam_c.z_dir), int(cam_c.distortion),
+               tuple(cam_c.distortion_coeffs))
         cache = getattr(self, "_omega_batch", None)
         if cache is None:
             cache = self._omega_batch = {}

@@ -47,11 +47,14 @@ def _camera(scene: Scene, res: int, altitude: float, off_nadir_deg: float, fov_d
 
 
 def plain_direct(posts: int = 513, resolution: int = 1024, seed: int = 1, device: int = 0,
-                 deterministic: bool = True):
+                 deterministic: bool = True, mesher=None):
+    """`mesher(heights, posting, albedo, nbands) -> Mesh` triangulates the DEM (default
+    Mesh.from_dem); every other step is numpy."""
+    mesher = mesher or Mesh.from_dem
     posting = DEM_EXTENT_M / (posts - 1)
     h = synthetic.fbm_heights(posts, hurst=0.8, seed=seed, lo=-200.0, hi=200.0)
     scene = Scene(FOUR_BAND, device=device)
-    mesh = scene.add_mesh(Mesh.from_dem(h, posting, albedo=0.12, nbands=FOUR_BAND.size))
+    mesh = scene.add_mesh(mesher(h, posting, albedo=0.12, nbands=FOUR_BAND.size))
     scene.new_instance(mesh)
     sun = scene.new_sun(temperature=5778.0)
     scene.set_sun_direction(sun, azimuth_deg=0.0, elevation_deg=30.0)
@@ -66,14 +69,16 @@ def plain_direct(posts: int = 513, resolution: int = 1024, seed: int = 1, device
 
 
 def path_traced(posts: int = 4097, tex: int = 4096, resolution: int = 2048, spp: int = 64, bounces: int = 3,
-                rr_depth: int = 2, seed: int = 7, device: int = 0, altitude: float = 12000.0):
+                rr_depth: int = 2, seed: int = 7, device: int = 0, altitude: float = 12000.0, mesher=None):
+    """`mesher` as for plain_direct."""
+    mesher = mesher or Mesh.from_dem
     posting = PT_EXTENT_M / (posts - 1)
     h = synthetic.fbm_heights(posts, hurst=0.8, seed=seed, lo=-200.0, hi=200.0)
     h = synthetic.add_crater_field(h, posting, seed=seed + 1, dmin=20.0, dmax=2000.0, exponent=-2.5)
     alb = synthetic.lognormal_albedo(tex, 0.12, 0.3, seed=seed + 2)
     B = EIGHT_BAND.size
     scene = Scene(EIGHT_BAND, device=device)
-    mesh = Mesh.from_dem(h, posting, albedo=1.0, nbands=B)
+    mesh = mesher(h, posting, albedo=1.0, nbands=B)
     mesh.uv = synthetic.grid_uvs(posts, posts, tex)
     mesh.albedo_map = np.ascontiguousarray(np.repeat(alb[:, :, None], B, axis=2))
     mid = scene.add_mesh(mesh)
