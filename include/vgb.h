@@ -495,6 +495,13 @@ VGB_API vgb_status vgb_set_profiling(vgb_context* ctx, int enable);
  * larger one HBM.  The buffer is freed before return. */
 VGB_API vgb_status vgb_measure_l2_read(vgb_context* ctx, uint64_t bytes, uint32_t passes, uint32_t repeats,
                                        double* gbps);
+/* How vgb_render and vgb_render_noalloc traverse the binary BVH (no counterpart in the
+ * reference; results do not depend on it).  persistent = 0 (default): one thread per ray in
+ * grid-stride loops of many short blocks; persistent = 1: one resident wave of closest-hit and
+ * occlusion kernels whose warps hand queue rays to lanes as lanes finish, each ray advancing at
+ * most `budget` inner-node visits between hand-outs, a hand-out happening once `refill` lanes of
+ * a warp are free (0: the defaults, 32 and 8). */
+VGB_API vgb_status vgb_set_wavefront_tuning(vgb_context* ctx, uint32_t persistent, uint32_t budget, uint32_t refill);
 /* Traversal steps (node visits) one ray may take before it gives up; 0 restores the default
  * of 2^22.  A ray past the limit stops, the call returns VGB_ERR_DEVICE_LIMIT with a message
  * and the context stays usable.  The limit exists so that no kernel can run unbounded on a

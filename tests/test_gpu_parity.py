@@ -287,3 +287,37 @@ def test_adaptive_sampling_matches_oracle(gpu):
     assert (alpha == 0).any(), "no sky pixel"
     assert (alpha > 1.0).any(), "no pixel stopped early (alpha = hits / last index exceeds 1)"
     scene.close()
+
+
+@pytest.mark.parametrize("budget,refill", [(16, 8), (1, 1), (4, 32)])
+def test_persistent_traversal_equals_grid_stride(gpu, budget, refill):
+    """The persistent closest-hit and occlusion kernels (warps hand queue rays to free lanes,
+    rays advance a bounded number of node visits between hand-outs) give every plane bit for bit
+    as the one-thread-per-ray kernels, whatever the budget and refill threshold; the counting
+    pass sees the same node and triangle visits."""
+    scene, cam_id = workloads.path_traced(posts=129, tex=64, resolution=72, spp=3, bounces=3, rr_depth=2, seed=4)
+    s2 = scene.new_sphere_light(np.float32(4.0e5), 6.96e8)
+    scene.set_sun_direction(s2, azimuth_deg=210.0, elevation_deg=25.0)
+    scene.build_tlas()
+    lib = capi.load()
+    ctx = scene.context()
+    out = {}
+    for mode in ("grid", "persistent"):
+        if mode == "grid":
+            capi.check(lib.vgb_set_wavefront_tuning(ctx, 0, 0, 0), ctx)
+        else:
+            capi.check(lib.vgb_set_wavefront_tuning(ctx, 1, budget, refill), ctx)
+        lib.vgb_set_count_pass(ctx, 1)
+        out[mode] = gpu_render_host(scene, cam_id)
+        lib.vgb_set_count_pass(ctx, 0)
+        st = scene.pathtracer.last_stats
+        out[mode]["_counts"] = (st.rays_closest, st.rays_shadow, st.nodes_visited, st.tris_tested, st.nodes_closest)
+    capi.check(lib.vgb_set_wavefront_tuning(ctx, 0, 0, 0), ctx)
+    a, b = out["grid"], out["persistent"]
+    assert a["_counts"] == b["_counts"]
+    for k in a:
+        if k == "_counts":
+            continue
+        assert np.array_equal(a[k], b[k]) if k == "triangle_id" else same_bits(a[k], b[k]), k
+    assert a["indirect_radiance"].mean() > 0
+    scene.close()

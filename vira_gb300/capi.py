@@ -201,6 +201,7 @@ SIGNATURES = {
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
     "vgb_set_traversal_limit": (C.c_int, [_P, C.c_uint32]),
+    "vgb_set_wavefront_tuning": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "vgb_measure_l2_read": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]),
     "vgb_rasterize": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(RasterOptions), C.POINTER(Film)]),
     "vgb_quipu_open": (C.c_int, [C.c_char_p, C.POINTER(_P)]),

@@ -43,6 +43,11 @@ using namespace vgbd;
 #ifndef VGB_BATCH_DIRECT_MINB
 #define VGB_BATCH_DIRECT_MINB 2
 #endif
+// k_batch_direct: per-lane register sums, no shared memory; 4 blocks of 256 threads per SM cap it
+// at 64 registers.
+#ifndef VGB_BATCH_LEAN_MINB
+#define VGB_BATCH_LEAN_MINB 4
+#endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
 #endif
@@ -67,6 +72,23 @@ using namespace vgbd;
 // directions) at 60 blocks per SM against 0.418 / 2.01 ms at 8.
 #ifndef VGB_RAYS_GRID
 #define VGB_RAYS_GRID 60
+#endif
+// Persistent traversal kernels (off by default, vgb_set_wavefront_tuning): inner-node visits a
+// lane's ray advances between hand-outs of new rays, and how many free lanes of a warp trigger a
+// hand-out.  On the path-traced frame (GB300, 64 registers) they ran at 3096-3361 Mrays/s
+// (budget 8-64, refill 1-16; best budget 32, refill 8) against 3639 for the grid-stride kernels:
+// the closest-hit launches broke even at budget 32 and the occlusion launches lost 25 %.
+#ifndef VGB_TRACEP_MINB
+#define VGB_TRACEP_MINB 4
+#endif
+#ifndef VGB_SHADOWP_MINB
+#define VGB_SHADOWP_MINB 4
+#endif
+#ifndef VGB_TRAV_BUDGET
+#define VGB_TRAV_BUDGET 32
+#endif
+#ifndef VGB_TRAV_REFILL
+#define VGB_TRAV_REFILL 8
 #endif
 #ifndef VGB_ADJOINT_GRID
 #define VGB_ADJOINT_GRID 32
@@ -132,7 +154,15 @@ struct DevState {
     size_t P;            // plane stride
 };
 
-enum { C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_ERR = 2 + VGB_MAX_LIGHTS, C_BATCH = 3 + VGB_MAX_LIGHTS, C_COUNT = 4 + VGB_MAX_LIGHTS };
+// Device counters: live-path queue lengths, shadow queue lengths per light, the item counters of
+// the persistent closest-hit and occlusion launches (reset with the shadow queues each bounce),
+// the error word and the batch kernels' work counter.
+enum {
+    C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_FTRACE = 2 + VGB_MAX_LIGHTS, C_FSHADOW = 3 + VGB_MAX_LIGHTS,
+    C_ERR = 3 + 2 * VGB_MAX_LIGHTS, C_BATCH = 4 + 2 * VGB_MAX_LIGHTS, C_COUNT = 5 + 2 * VGB_MAX_LIGHTS
+};
+// counters cleared at the start of every bounce: the shadow queues and the persistent item counters
+constexpr int kBounceResetWords = 1 + 2 * VGB_MAX_LIGHTS;
 
 struct FrameParams {
     vgb_camera cam;
@@ -689,6 +719,180 @@ __global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s,
     }
 }
 
+// ------------------------------------------------------------------ persistent traversal (binary layout)
+// k_trace_p / k_shadow_p replace the grid-stride loops of k_trace / k_shadow for the binary BVH.
+// They launch one wave of resident blocks; each warp claims chunks of kWarpChunk consecutive queue
+// items from a launch-wide counter and hands them to its lanes as lanes become free, and every
+// lane advances its ray by at most `budget` inner-node visits between hand-outs (traverse_resume).
+// A lane whose ray finished thus starts the next ray while its neighbours are still traversing,
+// instead of idling until the warp's slowest ray is done, which is what left bounce-1 rays at
+// half-empty warps.  Rays, their order within a warp and every test are those of the grid-stride
+// kernels, so the hit records are identical.
+constexpr uint32_t kWarpChunk = 64;
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// The items a warp holds and has not handed out: [base, base + left), all below the launch's item
+// count; `done` once the launch-wide counter has passed it.  Warp-uniform.
+struct WarpItems {
+    uint32_t base, left;
+    bool done;
+};
+
+// Hands one item to every lane set in `idle` (the lanes' rank in `idle` orders them); returns this
+// lane's item, or n when there is none.  Claims a new chunk when the held items do not suffice.
+__device__ __forceinline__ uint32_t warp_take(WarpItems& wi, uint32_t* counter, uint32_t n, unsigned idle, int lane) {
+    const uint32_t k = __popc(idle);
+    const uint32_t r = __popc(idle & ((1u << lane) - 1u));
+    const bool mine = (idle >> lane) & 1u;
+    uint32_t item = n;
+    if (wi.left < k && !wi.done) {
+        uint32_t nb = 0;
+        if (lane == 0) nb = atomicAdd(counter, kWarpChunk);
+        nb = __shfl_sync(kFullMask, nb, 0);
+        const uint32_t fresh = nb < n ? min(kWarpChunk, n - nb) : 0u;
+        if (nb + kWarpChunk >= n) wi.done = true;
+        if (mine) {
+            if (r < wi.left) item = wi.base + r;
+            else if (r - wi.left < fresh) item = nb + (r - wi.left);
+        }
+        const uint32_t used = min(k - wi.left, fresh);
+        wi.base = nb + used;
+        wi.left = fresh - used;
+    } else {
+        const uint32_t take = min(k, wi.left);
+        if (mine && r < take) item = wi.base + r;
+        wi.base += take;
+        wi.left -= take;
+    }
+    return item;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(256, VGB_TRACEP_MINB) k_trace_p(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
+                                                 uint32_t bounce, uint32_t sample, uint32_t in_q,
+                                                 uint32_t n_items_bounce0, int budget, uint32_t refill) {
+    const size_t P = st.P;
+    const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
+    const uint32_t* in_queue = st.pq[in_q];
+    const float4* nodes = reinterpret_cast<const float4*>(s.nodes);
+    const int lane = threadIdx.x & 31;
+    uint32_t err = 0, nclosest = 0;
+    Counters cnt{0, 0};
+    WarpItems wi{0, 0, false};
+    bool live = false;
+    uint32_t item = 0;
+    WRay wr;
+    SlabRay q;
+    TravState ts;
+    HitOut h;
+    int stack[kStackSize];
+    while (true) {
+        const unsigned idle = __ballot_sync(kFullMask, !live);
+        if ((wi.left || !wi.done) && (__popc(idle) >= refill || idle == kFullMask)) {
+            const uint32_t it = warp_take(wi, &st.counters[C_FTRACE], n_items, idle, lane);
+            if (it < n_items) {
+                uint32_t slot = 0;
+                F3 ro, rd;
+                bool ok = true;
+                if (bounce == 0) {
+                    ok = camera_ray(fp, it, sample, slot, ro, rd);
+                    if (ok && fp.opt.adaptive_sampling && sample != 0 && st.anum[slot]) ok = false;  // stopped
+                } else {
+                    slot = in_queue[it];
+                    ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
+                    rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
+                }
+                if (ok) {
+                    item = it;
+                    wr = make_wray(ro, rd);
+                    q = make_slab(wr);
+                    ts = trav_start(0.f, false, h);
+                    live = true;
+                    nclosest++;
+                }
+            }
+        }
+        if (__ballot_sync(kFullMask, live) == 0) {
+            if (wi.done && wi.left == 0) break;
+            continue;
+        }
+        if (live && traverse_resume<COUNT>(nodes, s.tris, wr, q, 0.f, false, stack, ts, h, err, cnt, s.iter_cap, budget)) {
+            float w0 = 0.f, w1 = 0.f;
+            if (h.id != VGB_NO_HIT) {
+                const float rcp = 1.0f / h.det;
+                w0 = h.V * rcp;
+                w1 = h.W * rcp;
+            }
+            st.hit[item] = make_float4(h.t, __uint_as_float(h.id), w0, w1);
+            live = false;
+        }
+    }
+    if (err) atomicOr(&st.counters[C_ERR], err);
+    warp_reduce_add(&st.stats[2], nclosest);
+    if (COUNT) {
+        warp_reduce_add(&st.stats[0], cnt.nodes);
+        warp_reduce_add(&st.stats[1], cnt.tris);
+        warp_reduce_add(&st.stats[4], cnt.nodes);
+        warp_reduce_add(&st.stats[5], cnt.tris);
+    }
+}
+
+template <int NB, bool COUNT>
+__global__ void __launch_bounds__(256, VGB_SHADOWP_MINB) k_shadow_p(const DevScene s, DevState st, uint32_t light, uint32_t nb,
+                                                   int budget, uint32_t refill) {
+    const size_t P = st.P;
+    const uint32_t n = st.counters[C_SQ + light];
+    const float4* nodes = reinterpret_cast<const float4*>(s.nodes);
+    const int lane = threadIdx.x & 31;
+    uint32_t err = 0, nsh = 0;
+    Counters cnt{0, 0};
+    WarpItems wi{0, 0, false};
+    bool live = false;
+    uint32_t item = 0;
+    float tmax = 0.f;
+    WRay wr;
+    SlabRay q;
+    TravState ts;
+    HitOut h;
+    int stack[kStackSize];
+    while (true) {
+        const unsigned idle = __ballot_sync(kFullMask, !live);
+        if ((wi.left || !wi.done) && (__popc(idle) >= refill || idle == kFullMask)) {
+            const uint32_t it = warp_take(wi, &st.counters[C_FSHADOW + light], n, idle, lane);
+            if (it < n) {
+                item = it;
+                const F3 o{st.sq_org[light][it], st.sq_org[light][P + it], st.sq_org[light][2 * P + it]};
+                const F3 d{st.sq_dir[light][it], st.sq_dir[light][P + it], st.sq_dir[light][2 * P + it]};
+                tmax = st.sq_tmax[light][it];
+                wr = make_wray(o, d);
+                q = make_slab(wr);
+                ts = trav_start(tmax, true, h);
+                live = true;
+                nsh++;
+            }
+        }
+        if (__ballot_sync(kFullMask, live) == 0) {
+            if (wi.done && wi.left == 0) break;
+            continue;
+        }
+        if (live && traverse_resume<COUNT>(nodes, s.tris, wr, q, tmax, true, stack, ts, h, err, cnt, s.iter_cap, budget)) {
+            if (h.id == VGB_NO_HIT) {
+                const uint32_t slot = st.sq_slot[light][item];
+#pragma unroll
+                for (int k = 0; k < NB; ++k)
+                    if (k < (int)nb) st.brad[k * P + slot] += st.sq_con[light][k * P + item];
+            }
+            live = false;
+        }
+    }
+    if (err) atomicOr(&st.counters[C_ERR], err);
+    warp_reduce_add(&st.stats[3], nsh);
+    if (COUNT) {
+        warp_reduce_add(&st.stats[0], cnt.nodes);
+        warp_reduce_add(&st.stats[1], cnt.tris);
+    }
+}
+
 // ------------------------------------------------------------------ k_shade
 // processIntersection for every item of k_trace: AOVs, shading point, NEE shadow-ray enqueue,
 // BSDF-sampled continuation and live-path enqueue (warp-aggregated appends).
@@ -1181,6 +1385,9 @@ struct vgb_context {
     unsigned char* noalloc_base = nullptr;
     // traversal steps per ray before the ray gives up (vgb_set_traversal_limit)
     uint32_t iter_cap = vgbd::kIterCap;
+    // wavefront traversal (vgb_set_wavefront_tuning): persistent kernels, node visits per ray
+    // between hand-outs, free lanes that trigger a hand-out
+    uint32_t trav_persistent = 0, trav_budget = VGB_TRAV_BUDGET, trav_refill = VGB_TRAV_REFILL;
 };
 
 namespace {
@@ -1348,6 +1555,14 @@ inline bool frame_fits(uint32_t W, uint32_t H) {
 // The render's launch sequence (per sample: per bounce k_trace, k_shade, k_shadow per light;
 // then k_end_sample) over the scratch `st`.  vgb_render passes the context's scratch,
 // vgb_render_noalloc the fixed array; `prof` allows CUDA-event profiling of the launches.
+// Resident blocks of a 256-thread kernel on the whole GPU (one wave of a persistent launch).
+template <typename K>
+int resident_grid(const vgb_context* ctx, K kernel) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * ctx->num_sms;
+}
+
 template <int NB, int L, bool COUNT>
 void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film, const DevState& st, bool prof,
                    uint32_t& launches) {
@@ -1356,15 +1571,22 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
     const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
     const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
     const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
+    // persistent traversal (binary layout): one resident wave, lanes refilled from the queue
+    const bool persist = L == 2 && ctx->trav_persistent;
+    const int gtp = persist ? resident_grid(ctx, k_trace_p<COUNT>) : 0;
+    const int gop = persist ? resident_grid(ctx, k_shadow_p<NB, COUNT>) : 0;
+    const int budget = (int)ctx->trav_budget;
+    const uint32_t refill = ctx->trav_refill;
     for (uint32_t smp = 0; smp < fp.opt.samples; ++smp) {
         uint32_t q = 0;
         for (uint32_t b = 0; b <= fp.opt.bounces; ++b) {
-            // reset the output path queue and the shadow queues
+            // reset the output path queue, the shadow queues and the persistent item counters
             cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
-            cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * VGB_MAX_LIGHTS, ctx->stream);
+            cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * kBounceResetWords, ctx->stream);
             {
                 Prof p(ctx, 0, prof);
-                k_trace<L, COUNT><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                if (persist) k_trace_p<COUNT><<<gtp, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0, budget, refill);
+                else k_trace<L, COUNT><<<gt, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             {
                 Prof p(ctx, 3, prof);
@@ -1373,7 +1595,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
                 Prof p(ctx, 1, prof);
-                k_shadow<NB, L, COUNT><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
+                if (persist) k_shadow_p<NB, COUNT><<<gop, 256, 0, ctx->stream>>>(s, st, l, fp.nb, budget, refill);
+                else k_shadow<NB, L, COUNT><<<go, 256, 0, ctx->stream>>>(s, st, l, fp.nb);
                 launches++;
             }
             q ^= 1u;
@@ -1969,6 +2192,18 @@ VGB_API vgb_status vgb_measure_l2_read(vgb_context* ctx, uint64_t bytes, uint32_
     }
     *gbps = best;
     ctx->stats.ms_last = (float)((double)bytes * passes / (best * 1e9) * 1e3);
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
+VGB_API vgb_status vgb_set_wavefront_tuning(vgb_context* ctx, uint32_t persistent, uint32_t budget,
+                                            uint32_t refill) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (refill > 32) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "wavefront_tuning: refill is a lane count, 0..32");
+    ctx->trav_persistent = persistent ? 1u : 0u;
+    ctx->trav_budget = budget ? budget : VGB_TRAV_BUDGET;
+    ctx->trav_refill = refill ? refill : VGB_TRAV_REFILL;
     return VGB_OK;
 } catch (...) {
     return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
@@ -3068,6 +3303,7 @@ struct DevFrame {
 struct BatchParams {
     vgb_pt_options opt;
     uint32_t nframes, nb, total_tiles, grab, tile_stride;
+    uint32_t sums;   // some frame requests a direct, indirect, albedo or normal plane
 };
 
 __device__ __forceinline__ uint32_t find_frame(const DevFrame* __restrict__ frames, uint32_t n, uint32_t t) {
@@ -3307,6 +3543,176 @@ __global__ void __launch_bounds__(256, DIRECT ? VGB_BATCH_DIRECT_MINB : 1) k_bat
     warp_reduce_add(&stats[3], nshadow);
 }
 
+// k_batch for direct lighting without adaptive sampling, with the per-pixel sums in registers:
+// with no bounce the path throughput stays 1 and a sample's path radiance is its bounce-0
+// radiance (ambient + the unoccluded light contributions, or the background of a miss), so the
+// shared-memory planes of k_batch reduce to per-lane sums over the samples.  SUMS keeps the
+// direct, albedo and normal sums (films that request those planes or the indirect one).  The
+// arithmetic and its order are k_batch's (and the wavefront's): the planes are bit-identical.
+template <int NB, int L, bool SUMS>
+__global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const DevScene s, const DevFrame* __restrict__ frames,
+                                                              const __grid_constant__ BatchParams bp, uint32_t* counter,
+                                                              uint32_t* errw, uint64_t* stats) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nb = bp.nb;
+    const vgb_pt_options& opt = bp.opt;
+    const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
+    const uint32_t n_items = (bp.total_tiles + bp.tile_stride - 1) / bp.tile_stride;
+    uint32_t err = 0, nclosest = 0, nshadow = 0;
+    while (true) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, bp.grab);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_items) break;
+        const uint32_t end = min(base + bp.grab, n_items);
+        for (uint32_t it = base; it < end; ++it) {
+            const uint32_t t = it * bp.tile_stride;
+            const DevFrame& F = frames[find_frame(frames, bp.nframes, t)];
+            const uint32_t tile = t - F.tile_begin;
+            const uint32_t tx = tile % F.tiles_x, ty = tile / F.tiles_x;
+            const uint32_t pi = tx * 8u + (lane & 7u), pj = ty * 4u + (lane >> 3);
+            const uint32_t W = F.cam.width, H = F.cam.height;
+            if (pi >= W || pj >= H) continue;
+            const uint32_t slot = pj * W + pi;
+            float tot[NB], dir[SUMS ? NB : 1], albs[SUMS ? NB : 1];
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                tot[k] = 0.f;
+                if (SUMS) { dir[k] = 0.f; albs[k] = 0.f; }
+            }
+            F3 nsum{0.f, 0.f, 0.f};
+            float dsum = 0.f;
+            uint32_t count = 0, first_tri = VGB_NO_HIT;
+            for (uint32_t sample = 0; sample < F.samples; ++sample) {
+                F3 ro, rd;
+                pixel_ray(F.cam, pi, pj, slot, sample, F.frame, k0, k1, ro, rd);
+                HitOut h;
+                h.U = h.V = h.W = 0.f; h.det = 1.f;
+                {
+                    Counters c{0, 0};
+                    traverse_any_layout<L, false, false>(s.nodes, s.tris, make_wray(ro, rd), 0.f, h, err, c, s.iter_cap);
+                }
+                nclosest++;
+                if (h.id == VGB_NO_HIT) {
+                    if (opt.simulate_lighting && opt.show_background) {
+                        const float4 bw = background_weights(rd);
+#pragma unroll
+                        for (int k = 0; k < NB; ++k) {
+                            const float bgv = opt.background[k];
+                            const float bg = ((bw.x * bgv + bw.y * bgv) + bw.z * bgv) + bw.w * bgv;
+                            tot[k] = tot[k] + (0.f + 1.f * (bg * 1.f));
+                        }
+                    }
+                    continue;
+                }
+                const float rcp = 1.0f / h.det;
+                float alb[NB];
+                F3 Pp, N, fnrm, tg, bt, nf;
+                surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, h.V * rcp, h.W * rcp, Pp, N, fnrm, tg, bt, nf, alb);
+                if (first_tri == VGB_NO_HIT) {
+                    first_tri = h.id;
+                    if (F.film.tsz || F.film.vel_g || F.film.vel_c)
+                        first_hit_passes(s, F.cam, h.id, Pp, F.film.vel_g, F.film.vel_c, F.film.tsz, (size_t)W * H, slot);
+                }
+                if (SUMS) {
+#pragma unroll
+                    for (int k = 0; k < NB; ++k) if (k < (int)nb) albs[k] += alb[k];
+                    nsum = F3{nsum.x + N.x, nsum.y + N.y, nsum.z + N.z};
+                }
+                dsum += h.t;
+                count += 1u;
+                if (!opt.simulate_lighting) continue;
+                Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+                float br[NB];
+#pragma unroll
+                for (int k = 0; k < NB; ++k)
+                    br[k] = (opt.has_ambient && k < (int)nb) ? 0.f + 1.f * (opt.ambient[k] * alb[k]) : 0.f;
+                const U4 r0 = philox(U4{slot, sample, F.frame, kSlotMain}, k0, k1);
+                for (uint32_t l = 0; l < F.nlights; ++l) {
+                    float ru1, ru2;
+                    if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                    else {
+                        const U4 rl = philox(U4{slot, sample, F.frame, 1u + l}, k0, k1);
+                        ru1 = u01(rl.x); ru2 = u01(rl.y);
+                    }
+                    F3 Ld; float dist, lpdf = 0.f;
+                    light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
+                    if (lpdf > 0) {
+                        HitOut hs;
+                        Counters c{0, 0};
+                        traverse_any_layout<L, true, false>(s.nodes, s.tris, make_wray(Pp, Ld), dist, hs, err, c, s.iter_cap);
+                        nshadow++;
+                        if (hs.id == VGB_NO_HIT) {
+                            const float nl = dot(N, Ld);
+                            const float cos_t = smax(0.0f, dot(Ld, N));
+                            const float mpdf = (nl <= 0.f) ? 0.f : nl * kInvPi;
+                            const float wgt = power_heuristic(lpdf, mpdf);
+#pragma unroll
+                            for (int k = 0; k < NB; ++k) {
+                                const float bsdf = alb[k] * kInvPi * smax(nl, 0.f);
+                                br[k] += (k < (int)nb) ? 1.f * bsdf * F.lights[l].radiance[k] * cos_t * wgt / lpdf : 0.f;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < NB; ++k) {
+                    tot[k] = tot[k] + (0.f + br[k]);
+                    if (SUMS && k < (int)nb) dir[k] += br[k];
+                }
+            }
+            // RenderPasses::updateImages for this pixel
+            const size_t P = (size_t)W * H;
+            const float sf = (float)F.samples;
+            const FilmOut& f = F.film;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k < (int)nb) {
+                    const float total = tot[k] / sf;
+                    const float direct = SUMS ? dir[k] / sf : 0.f;
+                    if (f.total) f.total[k * P + slot] = total;
+                    if (SUMS && f.direct) f.direct[k * P + slot] = direct;
+                    if (SUMS && f.indirect) f.indirect[k * P + slot] = total - direct;
+                    if (SUMS && f.albedo) f.albedo[k * P + slot] = albs[k] / sf;
+                    if (f.power) f.power[k * P + slot] = (F.cam.power_scale[k] * f.omega[slot]) * total;
+                }
+            }
+            if (SUMS && f.normal) {
+                const F3 n = normalize(nsum);
+                f.normal[slot] = n.x; f.normal[P + slot] = n.y; f.normal[2 * P + slot] = n.z;
+            }
+            if (f.depth) f.depth[slot] = (count == 0) ? __int_as_float(0x7f800000) : dsum / (float)count;
+            if (f.alpha) f.alpha[slot] = (float)count / sf;
+            if (f.tri) f.tri[slot] = first_tri;
+            if (first_tri == VGB_NO_HIT) {
+                if (f.tsz) f.tsz[slot] = __int_as_float(0x7f800000);
+                if (f.vel_g) { f.vel_g[slot] = 0.f; f.vel_g[P + slot] = 0.f; f.vel_g[2 * P + slot] = 0.f; }
+                if (f.vel_c) { f.vel_c[slot] = 0.f; f.vel_c[P + slot] = 0.f; f.vel_c[2 * P + slot] = 0.f; }
+            }
+        }
+    }
+    if (err) atomicOr(errw, err);
+    warp_reduce_add(&stats[2], nclosest);
+    warp_reduce_add(&stats[3], nshadow);
+}
+
+// The lean direct-lighting kernel applies when there is no bounce and no adaptive sampling; SUMS
+// when a frame requests the direct, indirect, albedo or normal plane.
+inline bool batch_lean(const BatchParams& bp) { return bp.opt.bounces == 0 && !bp.opt.adaptive_sampling; }
+
+template <int NB, int L, bool SUMS>
+cudaError_t launch_batch_lean(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
+                              uint32_t bps) {
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, k_batch_direct<NB, L, SUMS>, (int)threads, 0);
+    const uint32_t b = std::max<uint32_t>(1, std::min<uint32_t>(bps, (uint32_t)std::max(1, maxb)));
+    cudaMemsetAsync(&ctx->d_counters[C_BATCH], 0, sizeof(uint32_t), ctx->stream);
+    k_batch_direct<NB, L, SUMS><<<b * ctx->num_sms, threads, 0, ctx->stream>>>(dev_scene(ctx), d_frames, bp,
+                                                                              &ctx->d_counters[C_BATCH],
+                                                                              &ctx->d_counters[C_ERR], ctx->d_stats);
+    return cudaGetLastError();
+}
+
 template <int NB, int L, bool DIRECT>
 cudaError_t launch_batch_t(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
                            uint32_t bps) {
@@ -3326,6 +3732,10 @@ cudaError_t launch_batch_t(vgb_context* ctx, const DevFrame* d_frames, const Bat
 template <int NB, int L>
 cudaError_t launch_batch(vgb_context* ctx, const DevFrame* d_frames, const BatchParams& bp, uint32_t threads,
                          uint32_t bps) {
+    if (batch_lean(bp)) {
+        if (bp.sums) return launch_batch_lean<NB, L, true>(ctx, d_frames, bp, threads, bps);
+        return launch_batch_lean<NB, L, false>(ctx, d_frames, bp, threads, bps);
+    }
     if (bp.opt.bounces == 0) return launch_batch_t<NB, L, true>(ctx, d_frames, bp, threads, bps);
     return launch_batch_t<NB, L, false>(ctx, d_frames, bp, threads, bps);
 }
@@ -3417,6 +3827,10 @@ extern "C" VGB_API vgb_status vgb_render_batch(vgb_context* ctx, const vgb_frame
     bp.nframes = nframes;
     bp.nb = ctx->nbands;
     bp.total_tiles = (uint32_t)total_tiles;
+    for (uint32_t f = 0; f < nframes; ++f) {
+        const vgb_film& fl = frames[f].film;
+        if (fl.direct_radiance || fl.indirect_radiance || fl.albedo || fl.normal_global) bp.sums = 1;
+    }
     const DevFrame* dfr = static_cast<const DevFrame*>(ctx->d_frames);
     uint32_t threads = bo && bo->block_threads ? bo->block_threads : (ctx->tuned_threads ? ctx->tuned_threads : 256);
     uint32_t bps = bo && bo->blocks_per_sm ? bo->blocks_per_sm : (ctx->tuned_bps ? ctx->tuned_bps : 4);

@@ -250,6 +250,89 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
     }
 }
 
+// Resumable form of traverse_rt for the persistent traversal kernels: the state of one ray's
+// traversal between calls (the stack itself lives in the caller's per-thread array).
+struct TravState {
+    int node;       // next node (>= 0 inner; < 0 a leaf to test)
+    int sp;         // stack depth
+    float best;     // closest-hit t so far (tmax for occlusion rays)
+    uint32_t iter;  // inner nodes visited
+};
+
+__device__ __forceinline__ TravState trav_start(float tmax, bool any, HitOut& h) {
+    h.t = __int_as_float(0x7f800000);
+    h.id = VGB_NO_HIT;
+    h.U = h.V = h.W = 0.f;
+    h.det = 1.f;
+    return TravState{0, 0, any ? tmax : __int_as_float(0x7f800000), 0u};
+}
+
+// Continues the traversal of ray r for at most `budget` inner-node visits.  Returns true when the
+// ray is finished (h holds its answer), false when it stopped early; the next call resumes where it
+// stopped.  Node order, box and triangle tests are traverse_rt's, so the answer is the same.
+template <bool COUNT>
+__device__ __forceinline__ bool traverse_resume(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                const WRay& r, const SlabRay& q, float tmax, const bool any,
+                                                int* stack, TravState& ts, HitOut& h, uint32_t& err, Counters& cnt,
+                                                uint32_t cap, int budget) {
+    int node = ts.node, sp = ts.sp;
+    float best = ts.best;
+    uint32_t iter = ts.iter;
+    while (true) {
+        while (node >= 0) {
+            if (budget-- <= 0) {
+                ts.node = node; ts.sp = sp; ts.best = best; ts.iter = iter;
+                return false;
+            }
+            if (++iter > cap) { err |= kErrIter; return true; }
+            const float4 n0 = __ldg(&nodes[4 * node + 0]);
+            const float4 n1 = __ldg(&nodes[4 * node + 1]);
+            const float4 n2 = __ldg(&nodes[4 * node + 2]);
+            const float4 n3 = __ldg(&nodes[4 * node + 3]);
+            if (COUNT) cnt.nodes++;
+            float tn0, tf0, tn1, tf1;
+            slab(q, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, best, tn0, tf0);
+            slab(q, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, best, tn1, tf1);
+            const bool h0 = tn0 <= tf0, h1 = tn1 <= tf1;
+            const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                int nearc = ch0, farc = ch1;
+                if (tn1 < tn0) { nearc = ch1; farc = ch0; }
+                if (sp >= kStackSize) { err |= kErrStack; return true; }
+                stack[sp++] = farc;
+                node = nearc;
+            } else if (h0) {
+                node = ch0;
+            } else if (h1) {
+                node = ch1;
+            } else {
+                if (sp == 0) return true;
+                node = stack[--sp];
+            }
+        }
+        const uint32_t x = ~(uint32_t)node;
+        const uint32_t start = x >> 3, cntl = (x & 7u) + 1u;
+        for (uint32_t k = 0; k < cntl; ++k) {
+            const float4 t0 = __ldg(&tris[3 * (start + k) + 0]);
+            const float4 t1 = __ldg(&tris[3 * (start + k) + 1]);
+            const float4 t2 = __ldg(&tris[3 * (start + k) + 2]);
+            if (COUNT) cnt.tris++;
+            float tt, U, V, W, det;
+            if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
+                const uint32_t id = __float_as_uint(t0.w);
+                if (any) {
+                    if (tt <= tmax) { h.t = tt; h.id = id; return true; }
+                } else if (tt < h.t || (tt == h.t && id < h.id)) {
+                    h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
+                    best = tt;
+                }
+            }
+        }
+        if (sp == 0) return true;
+        node = stack[--sp];
+    }
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
