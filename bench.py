@@ -82,6 +82,9 @@ def parse():
     ap.add_argument("--no-quipu", action="store_true", help="skip the DEM Quipu ingestion line item")
     ap.add_argument("--no-raster", action="store_true", help="skip the rasterizer line item")
     ap.add_argument("--no-bvh", action="store_true", help="skip the BVH build line item")
+    ap.add_argument("--profile-case", default=None,
+                    help="run one small case for a profiler capture instead of the benchmark "
+                         "(path | batch | adjoint | after_film | quipu | raster | lbvh)")
     return ap.parse_args()
 
 
@@ -1048,8 +1051,109 @@ def plain_direct_item(torch, dev, layout=2, cpu_seconds=0.0):
     return out
 
 
+def profile_case(kind: str, scale: float):
+    """Small cases of each kernel family for profiler captures (a few GB on the device at most):
+
+      path [--scale S]  k_trace / k_shade / k_shadow / k_end_sample: the path-traced workload shrunk
+                        by S (posts, texture, pixels; 4 spp), rendered twice
+      batch             k_batch / k_batch_direct: 24 trajectory frames of 256^2-1024^2 at 1-16 spp
+      adjoint [--scale] k_adjoint: 2 views of the inversion scene at 512^2 x S (crater DEM 1025^2 x S)
+      after_film        k_dn_*, k_psf, k_sensor on a 1024^2 frame
+      quipu             Quipu decode and DEM mesh kernels: a 2049^2 LoD read twice
+      raster            k_raster_*: 8.4M triangles at 1024^2, 8 bands, twice
+      lbvh              GPU BVH build of 8.4M triangles twice, then one refit
+    """
+    import torch
+
+    from vira_gb300 import workloads
+
+    if kind == "path":
+        posts = int(4096 * scale) + 1
+        scene, cam = workloads.path_traced(posts=posts, tex=int(4096 * scale), resolution=int(2048 * scale), spp=4)
+        for _ in range(2):
+            scene.pathtracer.render(scene[cam], scene)
+        torch.cuda.synchronize()
+        print("path", scene.pathtracer.last_stats.ms_last, "ms")
+    elif kind == "batch":
+        scene, frames = workloads.trajectory(nframes=24, resolutions=(256, 512, 1024), spps=(1, 4, 16))
+        for _ in range(2):
+            scene.render_batch(frames, autotune=False, use_graph=False)
+        torch.cuda.synchronize()
+        print("batch", scene.pathtracer.last_stats.ms_last, "ms")
+    elif kind == "adjoint":
+        from vira_gb300.autograd import adjoint_views, forward_views
+
+        posts = int(1024 * scale) + 1
+        scene, views = workloads.inversion(posts=posts, tex=max(2, posts - 1), resolution=max(8, int(512 * scale)),
+                                           nviews=2, spp=4)
+        dev = torch.device("cuda", 0)
+        imgs = forward_views(scene, views, dev)
+        gt, gz = adjoint_views(scene, views, [torch.ones_like(i) for i in imgs], dev)
+        torch.cuda.synchronize()
+        print("adjoint", float(gt.abs().sum()))
+    elif kind == "after_film":
+        from vira_gb300 import sensor
+
+        scene, cam = workloads.path_traced(posts=1025, tex=1024, resolution=1024, spp=2)
+        scene.pathtracer.options.denoise = True
+        rp = scene.pathtracer.render(scene[cam], scene)
+        sensor.psf_convolve(scene, rp.received_power, sensor.GaussianPSF(1.5).make_kernel(scene.bands, 81, 20))
+        sm = sensor.SensorModel(simulate_photon_noise=True, noise_model=sensor.NoiseModelConfig(dark_current=20.0))
+        img = sensor.simulate_sensor(scene, rp.received_power, sm)
+        torch.cuda.synchronize()
+        print("after_film", float(img.mean()))
+    elif kind == "quipu":
+        import tempfile
+        from pathlib import Path
+
+        import numpy as np
+
+        from vira_gb300 import quipu, synthetic
+
+        n = 2049
+        z = np.ascontiguousarray(synthetic.fbm_heights(n, 0.8, seed=21, lo=-200.0, hi=200.0), np.float32)
+        dem = quipu.DEM(z, quipu.DEMProjection(n, n, (1.0, 1.0)), synthetic.lognormal_albedo(n, 0.12, 0.3, seed=23),
+                        quipu.FLOAT_IMAGE_ALBEDO)
+        with tempfile.TemporaryDirectory() as tmp:
+            quipu.DEMQuipu.write(Path(tmp) / "dem", [dem], options=quipu.DEMQuipuWriterOptions(compress=True))
+            q = quipu.DEMQuipu(Path(tmp) / "dem.qld", nbands=8)
+            for _ in range(2):
+                out = q.read_lod_mesh(0, nbands=8, device_arrays=True)
+            torch.cuda.synchronize()
+            print("quipu", int(out[1].shape[0]), "triangles")
+            q.close()
+    elif kind in ("raster", "lbvh"):
+        import ctypes as C
+
+        from vira_gb300 import capi
+
+        scene, cam = workloads.path_traced(posts=2049, tex=2048, resolution=1024, spp=1)
+        scene.build_tlas()
+        if kind == "raster":
+            scene.rasterizer.render_passes.simulate_lighting = True
+            for _ in range(2):
+                scene.rasterizer.render(scene[cam], scene)
+            torch.cuda.synchronize()
+            print("raster", scene.rasterizer.last_stats.ms_last, "ms")
+        else:
+            lib = capi.load()
+            ctx = scene.context()
+            for _ in range(2):
+                capi.check(lib.vgb_bvh_build(ctx, C.byref(capi.BvhOptions(0, 1, 0, 2))), ctx, "bvh_build")
+            p = scene.meshes[0].positions.copy()
+            p[:, 2] += 1.0
+            scene.update_positions(0, p)
+            torch.cuda.synchronize()
+            print("lbvh + refit done")
+    else:
+        raise SystemExit(f"unknown profile case {kind!r}")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case, args.scale if args.scale != 1.0 else (1.0 if args.profile_case == "adjoint" else 0.25))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

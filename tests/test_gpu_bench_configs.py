@@ -38,7 +38,7 @@ def test_plain_direct_full_size(gpu):
     o, counts = oracle_render(scene, cam_id, omega=omega)
     assert np.array_equal(g["triangle_id"], o["triangle_id"])
     hit = o["triangle_id"] != capi.NO_HIT
-    assert hit.mean() > 0.9
+    assert hit.mean() > 0.5   # the far part of the view looks past the DEM's edge
     assert float(rel_err(g["depth"][hit], o["depth"][hit]).max()) <= 1e-5
     for k in ("total_radiance", "direct_radiance", "received_power", "albedo"):
         assert float(rel_err(g[k], o[k]).max()) <= 1e-4, k

@@ -44,9 +44,14 @@ using namespace vgbd;
 #define VGB_BATCH_DIRECT_MINB 2
 #endif
 // k_batch_direct: per-lane register sums, no shared memory; 4 blocks of 256 threads per SM cap it
-// at 64 registers.
+// at 64 registers.  On the 256-frame trajectory (per-lane traversal): 1.16 s at 64 registers,
+// 1.26 s at 80, 1.47 s at 128.
 #ifndef VGB_BATCH_LEAN_MINB
 #define VGB_BATCH_LEAN_MINB 4
+#endif
+// k_batch_direct traces a tile's camera rays and shadow rays as warp packets (binary layout).
+#ifndef VGB_BATCH_PACKET
+#define VGB_BATCH_PACKET 1
 #endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
@@ -3553,11 +3558,15 @@ template <int NB, int L, bool SUMS>
 __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const DevScene s, const DevFrame* __restrict__ frames,
                                                               const __grid_constant__ BatchParams bp, uint32_t* counter,
                                                               uint32_t* errw, uint64_t* stats) {
+    // The warp's lanes stay converged through every traversal (lanes outside the frame or whose
+    // ray missed carry flags), so the binary layout can trace the tile's rays as warp packets.
+    constexpr bool PACKET = L == 2 && VGB_BATCH_PACKET;
     const int lane = threadIdx.x & 31;
     const uint32_t nb = bp.nb;
     const vgb_pt_options& opt = bp.opt;
     const uint32_t k0 = (uint32_t)opt.seed, k1 = (uint32_t)(opt.seed >> 32);
     const uint32_t n_items = (bp.total_tiles + bp.tile_stride - 1) / bp.tile_stride;
+    const float4* nodes2 = reinterpret_cast<const float4*>(s.nodes);
     uint32_t err = 0, nclosest = 0, nshadow = 0;
     while (true) {
         uint32_t base = 0;
@@ -3572,8 +3581,8 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
             const uint32_t tx = tile % F.tiles_x, ty = tile / F.tiles_x;
             const uint32_t pi = tx * 8u + (lane & 7u), pj = ty * 4u + (lane >> 3);
             const uint32_t W = F.cam.width, H = F.cam.height;
-            if (pi >= W || pj >= H) continue;
-            const uint32_t slot = pj * W + pi;
+            const bool valid = pi < W && pj < H;
+            const uint32_t slot = valid ? pj * W + pi : 0u;
             float tot[NB], dir[SUMS ? NB : 1], albs[SUMS ? NB : 1];
 #pragma unroll
             for (int k = 0; k < NB; ++k) {
@@ -3584,63 +3593,81 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
             float dsum = 0.f;
             uint32_t count = 0, first_tri = VGB_NO_HIT;
             for (uint32_t sample = 0; sample < F.samples; ++sample) {
-                F3 ro, rd;
-                pixel_ray(F.cam, pi, pj, slot, sample, F.frame, k0, k1, ro, rd);
+                F3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 1.f};
+                if (valid) pixel_ray(F.cam, pi, pj, slot, sample, F.frame, k0, k1, ro, rd);
                 HitOut h;
                 h.U = h.V = h.W = 0.f; h.det = 1.f;
-                {
+                h.id = VGB_NO_HIT;
+                if (PACKET) {
+                    traverse_packet<false>(nodes2, s.tris, make_wray(ro, rd), 0.f, valid, h, err, s.iter_cap);
+                } else if (valid) {
                     Counters c{0, 0};
                     traverse_any_layout<L, false, false>(s.nodes, s.tris, make_wray(ro, rd), 0.f, h, err, c, s.iter_cap);
                 }
-                nclosest++;
-                if (h.id == VGB_NO_HIT) {
-                    if (opt.simulate_lighting && opt.show_background) {
-                        const float4 bw = background_weights(rd);
+                if (valid) nclosest++;
+                const bool hit = valid && h.id != VGB_NO_HIT;
+                if (valid && !hit && opt.simulate_lighting && opt.show_background) {
+                    const float4 bw = background_weights(rd);
 #pragma unroll
-                        for (int k = 0; k < NB; ++k) {
-                            const float bgv = opt.background[k];
-                            const float bg = ((bw.x * bgv + bw.y * bgv) + bw.z * bgv) + bw.w * bgv;
-                            tot[k] = tot[k] + (0.f + 1.f * (bg * 1.f));
-                        }
+                    for (int k = 0; k < NB; ++k) {
+                        const float bgv = opt.background[k];
+                        const float bg = ((bw.x * bgv + bw.y * bgv) + bw.z * bgv) + bw.w * bgv;
+                        tot[k] = tot[k] + (0.f + 1.f * (bg * 1.f));
                     }
-                    continue;
                 }
-                const float rcp = 1.0f / h.det;
-                float alb[NB];
-                F3 Pp, N, fnrm, tg, bt, nf;
-                surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, h.V * rcp, h.W * rcp, Pp, N, fnrm, tg, bt, nf, alb);
-                if (first_tri == VGB_NO_HIT) {
-                    first_tri = h.id;
-                    if (F.film.tsz || F.film.vel_g || F.film.vel_c)
-                        first_hit_passes(s, F.cam, h.id, Pp, F.film.vel_g, F.film.vel_c, F.film.tsz, (size_t)W * H, slot);
-                }
-                if (SUMS) {
+                float alb[NB], br[NB];
+                F3 Pp{0.f, 0.f, 0.f}, N{0.f, 0.f, 1.f};
 #pragma unroll
-                    for (int k = 0; k < NB; ++k) if (k < (int)nb) albs[k] += alb[k];
-                    nsum = F3{nsum.x + N.x, nsum.y + N.y, nsum.z + N.z};
-                }
-                dsum += h.t;
-                count += 1u;
-                if (!opt.simulate_lighting) continue;
-                Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
-                float br[NB];
+                for (int k = 0; k < NB; ++k) { alb[k] = 0.f; br[k] = 0.f; }
+                const bool lit = hit && opt.simulate_lighting;
+                if (hit) {
+                    const float rcp = 1.0f / h.det;
+                    F3 fnrm, tg, bt, nf;
+                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, h.V * rcp, h.W * rcp, Pp, N, fnrm, tg, bt, nf, alb);
+                    if (first_tri == VGB_NO_HIT) {
+                        first_tri = h.id;
+                        if (F.film.tsz || F.film.vel_g || F.film.vel_c)
+                            first_hit_passes(s, F.cam, h.id, Pp, F.film.vel_g, F.film.vel_c, F.film.tsz, (size_t)W * H, slot);
+                    }
+                    if (SUMS) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k)
-                    br[k] = (opt.has_ambient && k < (int)nb) ? 0.f + 1.f * (opt.ambient[k] * alb[k]) : 0.f;
-                const U4 r0 = philox(U4{slot, sample, F.frame, kSlotMain}, k0, k1);
+                        for (int k = 0; k < NB; ++k) if (k < (int)nb) albs[k] += alb[k];
+                        nsum = F3{nsum.x + N.x, nsum.y + N.y, nsum.z + N.z};
+                    }
+                    dsum += h.t;
+                    count += 1u;
+                    if (lit) {
+                        Pp = F3{offset1(Pp.x, fnrm.x), offset1(Pp.y, fnrm.y), offset1(Pp.z, fnrm.z)};
+#pragma unroll
+                        for (int k = 0; k < NB; ++k)
+                            br[k] = (opt.has_ambient && k < (int)nb) ? 0.f + 1.f * (opt.ambient[k] * alb[k]) : 0.f;
+                    }
+                }
+                U4 r0{0, 0, 0, 0};
+                if (lit) r0 = philox(U4{slot, sample, F.frame, kSlotMain}, k0, k1);
                 for (uint32_t l = 0; l < F.nlights; ++l) {
-                    float ru1, ru2;
-                    if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
-                    else {
-                        const U4 rl = philox(U4{slot, sample, F.frame, 1u + l}, k0, k1);
-                        ru1 = u01(rl.x); ru2 = u01(rl.y);
+                    F3 Ld{0.f, 0.f, 1.f};
+                    float dist = 0.f, lpdf = 0.f;
+                    if (lit) {
+                        float ru1, ru2;
+                        if (l == 0) { ru1 = u01(r0.x); ru2 = u01(r0.y); }
+                        else {
+                            const U4 rl = philox(U4{slot, sample, F.frame, 1u + l}, k0, k1);
+                            ru1 = u01(rl.x); ru2 = u01(rl.y);
+                        }
+                        light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
                     }
-                    F3 Ld; float dist, lpdf = 0.f;
-                    light_sample(F.lights[l], Pp, opt.deterministic_light != 0, ru1, ru2, Ld, dist, lpdf);
-                    if (lpdf > 0) {
-                        HitOut hs;
+                    const bool shadow = lit && lpdf > 0;
+                    HitOut hs;
+                    hs.id = VGB_NO_HIT;
+                    if (PACKET) {
+                        if (__any_sync(0xffffffffu, shadow))
+                            traverse_packet<true>(nodes2, s.tris, make_wray(Pp, Ld), dist, shadow, hs, err, s.iter_cap);
+                    } else if (shadow) {
                         Counters c{0, 0};
                         traverse_any_layout<L, true, false>(s.nodes, s.tris, make_wray(Pp, Ld), dist, hs, err, c, s.iter_cap);
+                    }
+                    if (shadow) {
                         nshadow++;
                         if (hs.id == VGB_NO_HIT) {
                             const float nl = dot(N, Ld);
@@ -3655,12 +3682,15 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
                         }
                     }
                 }
+                if (lit) {
 #pragma unroll
-                for (int k = 0; k < NB; ++k) {
-                    tot[k] = tot[k] + (0.f + br[k]);
-                    if (SUMS && k < (int)nb) dir[k] += br[k];
+                    for (int k = 0; k < NB; ++k) {
+                        tot[k] = tot[k] + (0.f + br[k]);
+                        if (SUMS && k < (int)nb) dir[k] += br[k];
+                    }
                 }
             }
+            if (!valid) continue;
             // RenderPasses::updateImages for this pixel
             const size_t P = (size_t)W * H;
             const float sf = (float)F.samples;

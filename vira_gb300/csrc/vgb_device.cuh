@@ -333,6 +333,95 @@ __device__ __forceinline__ bool traverse_resume(const float4* __restrict__ nodes
     }
 }
 
+// Warp-packet traversal of the binary BVH for coherent rays (a warp's 8x4 pixel tile of camera
+// rays, or their shadow rays towards one light).  Every lane of the warp calls it together; a
+// lane with active = false only takes part.  The warp walks one node sequence: each node is
+// fetched once for all lanes (the same address, one broadcast load), every active lane tests
+// both child boxes against its own ray and current best distance, and a child is entered when
+// any lane's ray overlaps it, the one more lanes reach first.  Leaves are tested by every active
+// lane.  A lane thus tests a superset of the triangles its own traversal would test, with the
+// same conservative box test and the same acceptance rule (closest t, ties to the smaller id;
+// any hit within tmax), so its answer is the same as traverse_rt's: the closest hit does not
+// depend on which boxes are opened, and an occlusion test only reports whether some triangle
+// lies within tmax.  The warp's node stack (kStackSize = 64 entries) is spread over the lanes'
+// registers: entry i is held by lane i % 32 in its register s0 (i < 32) or s1.
+template <bool ANY>
+__device__ __forceinline__ void traverse_packet(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                const WRay& r, float tmax, bool active, HitOut& h, uint32_t& err,
+                                                uint32_t cap) {
+    static_assert(kStackSize == 64, "two stack registers per lane");
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    h.t = __int_as_float(0x7f800000);
+    h.id = VGB_NO_HIT;
+    float best = ANY ? tmax : __int_as_float(0x7f800000);
+    bool live = active;
+    const SlabRay q = make_slab(r);
+    int sp = 0, node = 0, s0 = 0, s1 = 0;
+    uint32_t iter = 0;
+    if (!__any_sync(full, live)) return;
+    while (true) {
+        while (node >= 0) {
+            if (++iter > cap) { if (live) err |= kErrIter; return; }
+            const float4 n0 = __ldg(&nodes[4 * node + 0]);
+            const float4 n1 = __ldg(&nodes[4 * node + 1]);
+            const float4 n2 = __ldg(&nodes[4 * node + 2]);
+            const float4 n3 = __ldg(&nodes[4 * node + 3]);
+            bool h0 = false, h1 = false, near0 = false;
+            if (live) {
+                float tn0, tf0, tn1, tf1;
+                slab(q, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, best, tn0, tf0);
+                slab(q, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, best, tn1, tf1);
+                h0 = tn0 <= tf0;
+                h1 = tn1 <= tf1;
+                near0 = h0 && (!h1 || tn0 <= tn1);
+            }
+            const unsigned m0 = __ballot_sync(full, h0), m1 = __ballot_sync(full, h1);
+            const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
+            if (m0 && m1) {
+                const unsigned nm = __ballot_sync(full, near0);
+                const bool first0 = 2 * __popc(nm) >= __popc(m0 | m1);
+                if (sp >= kStackSize) { if (live) err |= kErrStack; return; }
+                if (lane == (sp & 31)) {
+                    if (sp < 32) s0 = first0 ? ch1 : ch0;
+                    else s1 = first0 ? ch1 : ch0;
+                }
+                ++sp;
+                node = first0 ? ch0 : ch1;
+            } else if (m0) {
+                node = ch0;
+            } else if (m1) {
+                node = ch1;
+            } else {
+                if (sp == 0) return;
+                --sp;
+                node = __shfl_sync(full, sp < 32 ? s0 : s1, sp & 31);
+            }
+        }
+        const uint32_t x = ~(uint32_t)node;
+        const uint32_t start = x >> 3, cntl = (x & 7u) + 1u;
+        for (uint32_t k = 0; k < cntl; ++k) {
+            const float4 t0 = __ldg(&tris[3 * (start + k) + 0]);
+            const float4 t1 = __ldg(&tris[3 * (start + k) + 1]);
+            const float4 t2 = __ldg(&tris[3 * (start + k) + 2]);
+            float tt, U, V, W, det;
+            if (live && wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
+                const uint32_t id = __float_as_uint(t0.w);
+                if (ANY) {
+                    if (tt <= tmax) { h.t = tt; h.id = id; live = false; }
+                } else if (tt < h.t || (tt == h.t && id < h.id)) {
+                    h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
+                    best = tt;
+                }
+            }
+        }
+        if (ANY && !__any_sync(full, live)) return;
+        if (sp == 0) return;
+        --sp;
+        node = __shfl_sync(full, sp < 32 ? s0 : s1, sp & 31);
+    }
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
