@@ -1051,7 +1051,7 @@ def plain_direct_item(torch, dev, layout=2, cpu_seconds=0.0):
     return out
 
 
-def profile_case(kind: str, scale: float):
+def profile_case(kind: str, scale: float, layout: int = 2):
     """Small cases of each kernel family for profiler captures (a few GB on the device at most):
 
       path [--scale S]  k_trace / k_shade / k_shadow / k_end_sample: the path-traced workload shrunk
@@ -1062,6 +1062,8 @@ def profile_case(kind: str, scale: float):
       quipu             Quipu decode and DEM mesh kernels: a 2049^2 LoD read twice
       raster            k_raster_*: 8.4M triangles at 1024^2, 8 bands, twice
       lbvh              GPU BVH build of 8.4M triangles twice, then one refit
+      l2                k_l2_read: the L2 read-bandwidth probe (64 MiB, 20 passes per launch)
+    `layout` selects the BVH node layout of the path case (2 binary, 8 compressed 8-wide).
     """
     import torch
 
@@ -1070,10 +1072,19 @@ def profile_case(kind: str, scale: float):
     if kind == "path":
         posts = int(4096 * scale) + 1
         scene, cam = workloads.path_traced(posts=posts, tex=int(4096 * scale), resolution=int(2048 * scale), spp=4)
+        scene.bvh_options.layout = layout
         for _ in range(2):
             scene.pathtracer.render(scene[cam], scene)
         torch.cuda.synchronize()
         print("path", scene.pathtracer.last_stats.ms_last, "ms")
+    elif kind == "l2":
+        from vira_gb300 import capi
+
+        lib = capi.load()
+        ctx = C.c_void_p()
+        capi.check(lib.vgb_context_create(C.byref(ctx), 0), None, "context_create")
+        print("l2 GB/s", l2_peak(lib, ctx))
+        lib.vgb_context_destroy(ctx)
     elif kind == "batch":
         scene, frames = workloads.trajectory(nframes=24, resolutions=(256, 512, 1024), spps=(1, 4, 16))
         for _ in range(2):
@@ -1152,7 +1163,8 @@ def profile_case(kind: str, scale: float):
 def main():
     args = parse()
     if args.profile_case:
-        profile_case(args.profile_case, args.scale if args.scale != 1.0 else (1.0 if args.profile_case == "adjoint" else 0.25))
+        profile_case(args.profile_case, args.scale if args.scale != 1.0 else (1.0 if args.profile_case == "adjoint" else 0.25),
+                     args.layout)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

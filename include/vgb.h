@@ -459,6 +459,30 @@ typedef struct vgb_sensor {
 VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_power, uint32_t width,
                                        uint32_t height, uint32_t nbands, const vgb_sensor* sensor,
                                        float* image, int on_device);
+/* Camera::simulateSensorRGB (cameras/camera.ipp:1253-1282) with getPhotonCountsRGB (:1337-1380)
+ * and Photosite::exposePixelRGB (photosites/photosite.ipp:145-154): each pixel's received power
+ * (times the filter mosaic when one is set) is converted to ColorRGB by spectralConvert
+ * (spectral_data.ipp:588-605: per RGB band the overlap-weighted sum of the spectral bands,
+ * SpectralData::integrateOver, divided by the RGB bandwidth), to photons per channel (exposure /
+ * ColorRGB photon energy), Poisson photon noise where the three channels hold one photon or more,
+ * one NoiseModel draw per channel, then qe_rgb * photons + noise, times the gain, over max ADU --
+ * with no clamp, as the reference's RGB photosite has none.  The sensor fields for the spectral
+ * bands (photon_energy, quantum_efficiency) are not read. */
+typedef struct vgb_rgb_conversion {
+    float band_min[8];                /* the spectral bands' edges in metres (FP32, as stored) */
+    float band_max[8];
+    float rgb_min[3];                 /* ColorRGB's bands: R 600-750, G 500-600, B 380-500 nm, in metres */
+    float rgb_max[3];
+    float rgb_bandwidth[3];           /* max - min in FP32 */
+    float rgb_photon_energy[3];       /* ColorRGB::photonEnergies */
+    float rgb_quantum_efficiency[3];  /* PhotositeConfig::quantum_efficiency_rgb */
+} vgb_rgb_conversion;
+
+/* received_power [B][H][W] -> image_rgb [3][H][W] (R, G, B planes).  Device memory if on_device
+ * else host. */
+VGB_API vgb_status vgb_sensor_simulate_rgb(vgb_context* ctx, const float* received_power, uint32_t width,
+                                           uint32_t height, uint32_t nbands, const vgb_sensor* sensor,
+                                           const vgb_rgb_conversion* rgb, float* image_rgb, int on_device);
 /* Image::convolveSpatial (images/image.ipp:1267-1340) of received_power ([B][H][W], in place)
  * with a per-band kernel ([B][kh][kw]): out(x, y) = sum over (kx, ky) of
  * in(x + kx - kw/2, y + ky - kh/2) * kernel(kx, ky), zero outside the image, rows of the kernel

@@ -57,6 +57,7 @@ def load():
         "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
         "oracle_sensor": (C.c_int, [P, P, U32, U32, U32, C.c_float, P, P, C.c_float, C.c_float, P]),
         "oracle_psf": (C.c_int, [P, U32, U32, U32, P, U32, U32, P]),
+        "oracle_sensor_rgb": (C.c_int, [P, P, U32, U32, U32, P, P, P, C.c_float, C.c_float, C.c_float, P]),
         "oracle_denoise": (C.c_int, [P, P, P, P, P, U32, U32, U32, U32, U32, C.c_float, C.c_float, C.c_float,
                                      C.c_float]),
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
@@ -167,6 +168,24 @@ def sensor(power, exposure_time, photon_energy, qe, gain, max_adu, mosaic=None):
                               e.ctypes.data, q.ctypes.data, gain, max_adu, out.ctypes.data)
     if rc != 0:
         raise ValueError("oracle_sensor rejected its arguments")
+    return out
+
+
+def sensor_rgb(power, band_min, band_max, rgb_min, rgb_max, rgb_bandwidth, rgb_photon_energy, rgb_qe, exposure_time,
+               gain, max_adu, mosaic=None):
+    """Noise-free RGB sensor restated: [B][H][W] received power -> [3][H][W] image."""
+    p = np.ascontiguousarray(power, np.float32)
+    B, H, W = p.shape
+    bmin = np.ascontiguousarray(np.asarray(band_min, np.float32)[:B])
+    bmax = np.ascontiguousarray(np.asarray(band_max, np.float32)[:B])
+    rgb = np.ascontiguousarray(np.concatenate([np.asarray(a, np.float32).reshape(3) for a in
+                                               (rgb_min, rgb_max, rgb_bandwidth, rgb_photon_energy, rgb_qe)]))
+    m = None if mosaic is None else np.ascontiguousarray(mosaic, np.float32)
+    out = np.empty((3, H, W), np.float32)
+    rc = load().oracle_sensor_rgb(p.ctypes.data, None if m is None else m.ctypes.data, W, H, B, bmin.ctypes.data,
+                                  bmax.ctypes.data, rgb.ctypes.data, exposure_time, gain, max_adu, out.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle_sensor_rgb rejected its arguments")
     return out
 
 

@@ -1731,6 +1731,46 @@ OAPI int oracle_sensor(const float* power, const float* mosaic, uint32_t width, 
     return 0;
 }
 
+// SpectralData::integrateOver (spectral_data.ipp:306-333) of n bands [bmin, bmax] with values v.
+static float integrate_over(const float* bmin_, const float* bmax_, const float* v, uint32_t n, float minLam,
+                            float maxLam) {
+    if (minLam > maxLam) std::swap(minLam, maxLam);
+    if (minLam == maxLam) return 0.f;
+    float integral = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        float bmin = bmin_[i], bmax = bmax_[i];
+        if (bmin > maxLam || bmax < minLam) continue;
+        float bound1 = std::max(bmin, minLam);
+        float bound2 = std::min(bmax, maxLam);
+        float dLam = bound2 - bound1;
+        integral += (dLam * v[i]);
+    }
+    return integral;
+}
+
+// Camera::simulateSensorRGB without noise (camera.ipp:1253-1282, 1337-1380; photosite.ipp:
+// 145-154): spectralConvert to ColorRGB, photons per channel, qe_rgb * photons + 0, gain, / ADU.
+// rgb = {rgb_min[3], rgb_max[3], rgb_bandwidth[3], rgb_photon_energy[3], rgb_qe[3]}.
+OAPI int oracle_sensor_rgb(const float* power, const float* mosaic, uint32_t width, uint32_t height, uint32_t nbands,
+                           const float* band_min, const float* band_max, const float* rgb, float exposure_time,
+                           float gain, float max_adu, float* out) {
+    if (!power || !band_min || !band_max || !rgb || !out || nbands == 0 || nbands > VGB_MAX_BANDS) return 1;
+    const size_t P = (size_t)width * height;
+    for (size_t p = 0; p < P; ++p) {
+        float v[VGB_MAX_BANDS];
+        for (uint32_t k = 0; k < nbands; ++k) v[k] = mosaic ? power[k * P + p] * mosaic[k * P + p] : power[k * P + p];
+        for (int c = 0; c < 3; ++c) {
+            float received = integrate_over(band_min, band_max, v, nbands, rgb[c], rgb[3 + c]) / rgb[6 + c];
+            float energy = exposure_time * received;
+            float photons = energy / rgb[9 + c];
+            float electrons = (rgb[12 + c] * photons) + 0.0f;
+            float amplified = gain * electrons;
+            out[c * P + p] = amplified / max_adu;
+        }
+    }
+    return 0;
+}
+
 // Image::convolveSpatial (images/image.ipp:1267-1340) for a planar spectral image: per band,
 // out(x, y) = sum over ky outer, kx inner of in(x + kx - kw/2, y + ky - kh/2) * kernel(kx, ky),
 // zero outside the image.  kernel is [B][kh][kw].

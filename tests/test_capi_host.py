@@ -46,7 +46,8 @@ def test_struct_layouts_match_the_header(tmp_path):
              "vgb_denoise_options": capi.DenoiseOptions, "vgb_quipu_header": capi.QuipuHeader,
              "vgb_quipu_projection": capi.QuipuProjection, "vgb_quipu_lod_info": capi.QuipuLodInfo,
              "vgb_quipu_read_options": capi.QuipuReadOptions, "vgb_quipu_lod_data": capi.QuipuLodData,
-             "vgb_raster_options": capi.RasterOptions, "vgb_instance_motion": capi.InstanceMotion}
+             "vgb_raster_options": capi.RasterOptions, "vgb_instance_motion": capi.InstanceMotion,
+             "vgb_rgb_conversion": capi.RgbConversion}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vgb.h"', "int main(void) {"]
     for cname, py in pairs.items():
         lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')

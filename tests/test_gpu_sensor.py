@@ -159,3 +159,82 @@ def test_pathtrace_render_returns_the_sensor_image(gpu):
     assert img.shape == (48, 48) and torch.equal(img, again)
     assert float(img.max()) > 0
     scene.close()
+
+
+def _rgb_sensor(bands, **kw):
+    sm = sensor.SensorModel(**kw)
+    return sm, sm.to_c(bands), sensor.rgb_conversion(bands, sm)
+
+
+@pytest.mark.parametrize("mosaic", [False, True])
+def test_rgb_sensor_noise_free_matches_oracle(gpu, mosaic):
+    """Camera::simulateSensorRGB without noise: bit-identical to the oracle's restatement."""
+    from oracle import oracle
+    from vira_gb300.spectral import EIGHT_BAND
+
+    lib, ctx = _ctx()
+    rng = np.random.default_rng(5)
+    B, H, W = 8, 37, 53
+    power = rng.lognormal(-26.0, 1.0, (B, H, W)).astype(np.float32)
+    sm, s, rgb = _rgb_sensor(EIGHT_BAND, exposure_time=0.02)
+    mos = rng.uniform(0.0, 1.0, (B, H, W)).astype(np.float32) if mosaic else None
+    if mos is not None:
+        s.filter_mosaic = capi.ptr(mos)
+    out = np.empty((3, H, W), np.float32)
+    capi.check(lib.vgb_sensor_simulate_rgb(ctx, capi.ptr(power), W, H, B, C.byref(s), C.byref(rgb), capi.ptr(out), 0),
+               ctx, "sensor_rgb")
+    ref = oracle.sensor_rgb(power, EIGHT_BAND.min_wavelength, EIGHT_BAND.max_wavelength, rgb.rgb_min, rgb.rgb_max,
+                            rgb.rgb_bandwidth, rgb.rgb_photon_energy, rgb.rgb_quantum_efficiency, s.exposure_time,
+                            s.gain, s.max_adu, mosaic=mos)
+    lib.vgb_context_destroy(ctx)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+    assert out.max() > 0 and (out > 1).any() == (ref > 1).any()   # no clamp in the RGB photosite
+
+
+def test_rgb_sensor_noise_moments(gpu):
+    """Per-channel noise-model draws and Poisson photon counts: means and variances over 2^20
+    pixels within 5 sigma of the models (dark current Poisson x exposure + Gaussian readout)."""
+    from vira_gb300.spectral import FOUR_BAND
+
+    lib, ctx = _ctx()
+    H = W = 1024
+    B = 4
+    sm, s, rgb = _rgb_sensor(FOUR_BAND, exposure_time=1.0,
+                             noise_model=sensor.NoiseModelConfig(dark_current=40.0, readout_noise_mean=2.0,
+                                                                 readout_noise_std=3.0))
+    s.gain = 1.0
+    s.max_adu = 1.0
+    for c in range(3):
+        rgb.rgb_quantum_efficiency[c] = 1.0
+    power = np.zeros((B, H, W), np.float32)
+    out = np.empty((3, H, W), np.float32)
+    capi.check(lib.vgb_sensor_simulate_rgb(ctx, capi.ptr(power), W, H, B, C.byref(s), C.byref(rgb), capi.ptr(out), 0),
+               ctx, "sensor_rgb")
+    lib.vgb_context_destroy(ctx)
+    n = H * W
+    mean, var = 40.0 + 2.0, 40.0 + 9.0
+    for c in range(3):
+        x = out[c].astype(np.float64)
+        assert abs(x.mean() - mean) < 5 * np.sqrt(var / n), c
+        assert abs(x.var() - var) < 5 * var * np.sqrt(2.0 / n) * 1.5, c
+    # the three channels draw independently
+    assert abs(np.corrcoef(out[0].ravel(), out[1].ravel())[0, 1]) < 0.01
+
+
+def test_pathtrace_render_rgb(gpu):
+    from oracle import oracle
+
+    scene, cam_id = workloads.plain_direct(posts=65, resolution=48)
+    cam = scene[cam_id]
+    cam.sensor.exposure_time = 0.5
+    rgb = scene.pathtrace_render_rgb(cam_id).cpu().numpy()
+    power = scene.pathtracer.render_passes.received_power.cpu().numpy()
+    c = sensor.rgb_conversion(scene.bands, cam.sensor)
+    s = cam.sensor.to_c(scene.bands)
+    ref = oracle.sensor_rgb(power, scene.bands.min_wavelength, scene.bands.max_wavelength, c.rgb_min, c.rgb_max,
+                            c.rgb_bandwidth, c.rgb_photon_energy, c.rgb_quantum_efficiency, s.exposure_time, s.gain,
+                            s.max_adu)
+    scene.close()
+    assert rgb.shape == (3, 48, 48)
+    assert np.array_equal(rgb.view(np.uint32), ref.view(np.uint32))
+    assert rgb.mean() > 0

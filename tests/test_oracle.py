@@ -530,3 +530,27 @@ def test_distortion_changes_the_pixel_solid_angle_consistently():
     o0, o1 = oracle.pixel_solid_angle(c0), oracle.pixel_solid_angle(c1)
     assert o1.sum() > o0.sum() * 1.01
     assert abs(float(o1[24, 32] / o0[24, 32]) - 1.0) < 1e-3
+
+
+def test_rgb_conversion_restatements_agree():
+    """spectralToRGB (integrateOver per ColorRGB band / bandwidth) in numpy FP32 against the
+    oracle's C restatement, through a noise-free RGB sensor with unit gain and photon energy."""
+    from oracle import oracle
+    from vira_gb300 import sensor
+    from vira_gb300.spectral import EIGHT_BAND, FOUR_BAND
+
+    rng = np.random.default_rng(2)
+    rb = sensor.rgb_bands()
+    for bands in (FOUR_BAND, EIGHT_BAND):
+        v = rng.uniform(0.0, 3.0, (bands.size, 2, 3)).astype(np.float32)
+        ones = np.ones(3, np.float32)
+        got = oracle.sensor_rgb(v, bands.min_wavelength, bands.max_wavelength, rb.min_wavelength, rb.max_wavelength,
+                                (rb.max_wavelength - rb.min_wavelength).astype(np.float32), ones, ones, 1.0, 1.0, 1.0)
+        for y in range(2):
+            for x in range(3):
+                assert np.array_equal(got[:, y, x], sensor.spectral_to_rgb(bands, v[:, y, x]))
+    # a flat spectrum over 400-1000 nm: R and G fully covered (value 1), B covered from 400 nm only
+    flat = sensor.spectral_to_rgb(EIGHT_BAND, np.ones(8, np.float32))
+    assert abs(flat[0] - 1) < 1e-6 and abs(flat[1] - 1) < 1e-6 and abs(flat[2] - 100.0 / 120.0) < 1e-6
+    qe = sensor.spectral_to_rgb(FOUR_BAND, sensor.default_qe(FOUR_BAND))
+    assert np.all(qe > 0) and qe[0] < qe[2]   # higher photon energy at the blue end

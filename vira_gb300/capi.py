@@ -101,6 +101,12 @@ class Sensor(C.Structure):
                 ("frame", C.c_uint32), ("seed", C.c_uint64), ("filter_mosaic", C.c_void_p)]
 
 
+class RgbConversion(C.Structure):
+    _fields_ = [("band_min", C.c_float * 8), ("band_max", C.c_float * 8), ("rgb_min", C.c_float * 3),
+                ("rgb_max", C.c_float * 3), ("rgb_bandwidth", C.c_float * 3), ("rgb_photon_energy", C.c_float * 3),
+                ("rgb_quantum_efficiency", C.c_float * 3)]
+
+
 class BatchOptions(C.Structure):
     _fields_ = [("autotune", C.c_uint32), ("use_graph", C.c_uint32), ("block_threads", C.c_uint32),
                 ("blocks_per_sm", C.c_uint32), ("tiles_per_grab", C.c_uint32)]
@@ -201,6 +207,7 @@ SIGNATURES = {
     "vgb_set_count_pass": (C.c_int, [_P, C.c_int]),
     "vgb_set_profiling": (C.c_int, [_P, C.c_int]),
     "vgb_set_traversal_limit": (C.c_int, [_P, C.c_uint32]),
+    "vgb_sensor_simulate_rgb": (C.c_int, [_P, _P, _U32, _U32, _U32, _P, _P, _P, C.c_int]),
     "vgb_set_wavefront_tuning": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32]),
     "vgb_measure_l2_read": (C.c_int, [_P, C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]),
     "vgb_rasterize": (C.c_int, [_P, C.POINTER(Camera), _P, _U32, C.POINTER(RasterOptions), C.POINTER(Film)]),

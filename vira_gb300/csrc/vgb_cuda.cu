@@ -44,14 +44,16 @@ using namespace vgbd;
 #define VGB_BATCH_DIRECT_MINB 2
 #endif
 // k_batch_direct: per-lane register sums, no shared memory; 4 blocks of 256 threads per SM cap it
-// at 64 registers.  On the 256-frame trajectory (per-lane traversal): 1.16 s at 64 registers,
-// 1.26 s at 80, 1.47 s at 128.
+// at 64 registers.  On the 256-frame trajectory: 1.16-1.17 s at 64 registers, 1.26 s at 80, 1.47 s
+// at 128.
 #ifndef VGB_BATCH_LEAN_MINB
 #define VGB_BATCH_LEAN_MINB 4
 #endif
-// k_batch_direct traces a tile's camera rays and shadow rays as warp packets (binary layout).
+// 1: k_batch_direct traces a tile's camera rays and shadow rays as warp packets (binary layout).
+// Off: on the 256-frame trajectory the packets took 1.45 s against 1.17 s for one traversal per
+// lane (same results; 64 registers each).
 #ifndef VGB_BATCH_PACKET
-#define VGB_BATCH_PACKET 1
+#define VGB_BATCH_PACKET 0
 #endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
@@ -2827,6 +2829,54 @@ VGB_API vgb_status vgb_sensor_simulate(vgb_context* ctx, const float* received_p
     }
     CK((cudaError_t)vgb::launch_sensor(ctx->stream, pw, width, height, nbands, sp, img, ctx->num_sms));
     if (!on_device) CK(cudaMemcpyAsync(image, img, P * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return VGB_OK;
+} catch (...) {
+    return vgb::status_of_exception(ctx ? &ctx->err : nullptr);
+}
+
+VGB_API vgb_status vgb_sensor_simulate_rgb(vgb_context* ctx, const float* received_power, uint32_t width,
+                                           uint32_t height, uint32_t nbands, const vgb_sensor* sensor,
+                                           const vgb_rgb_conversion* rgb, float* image_rgb, int on_device) try {
+    if (!ctx) return VGB_ERR_INVALID_ARGUMENT;
+    if (!received_power || !sensor || !rgb || !image_rgb || width == 0 || height == 0 || nbands == 0 ||
+        nbands > VGB_MAX_BANDS || (uint64_t)width * height > (1ull << 31))
+        return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate_rgb: null plane, sensor or conversion, bad size or bands outside 1..8");
+    if (!(sensor->max_adu > 0.f)) return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate_rgb: max_adu must be > 0");
+    for (int c = 0; c < 3; ++c)
+        if (!(rgb->rgb_photon_energy[c] > 0.f) || !(rgb->rgb_bandwidth[c] > 0.f))
+            return fail(ctx, VGB_ERR_INVALID_ARGUMENT, "sensor_simulate_rgb: RGB photon energies and bandwidths must be > 0");
+    cudaSetDevice(ctx->device);
+    const size_t P = (size_t)width * height, BP = (size_t)nbands * P;
+    vgb::SensorParams sp{};
+    sp.exposure_time = sensor->exposure_time;
+    sp.gain = sensor->gain; sp.max_adu = sensor->max_adu;
+    sp.photon_noise = sensor->simulate_photon_noise; sp.noise_model = sensor->noise_model;
+    sp.dark_current = sensor->dark_current; sp.readout_mean = sensor->readout_noise_mean; sp.readout_std = sensor->readout_noise_std;
+    sp.hscale = sensor->horizontal_scale; sp.vscale = sensor->vertical_scale;
+    sp.hperiod = sensor->horizontal_pattern_period; sp.vperiod = sensor->vertical_pattern_period;
+    sp.frame = sensor->frame; sp.seed = sensor->seed; sp.mosaic = sensor->filter_mosaic;
+    vgb::RgbParams rp{};
+    for (int k = 0; k < 8; ++k) { rp.band_min[k] = rgb->band_min[k]; rp.band_max[k] = rgb->band_max[k]; }
+    for (int c = 0; c < 3; ++c) {
+        rp.rgb_min[c] = rgb->rgb_min[c]; rp.rgb_max[c] = rgb->rgb_max[c]; rp.rgb_bw[c] = rgb->rgb_bandwidth[c];
+        rp.rgb_pe[c] = rgb->rgb_photon_energy[c]; rp.rgb_qe[c] = rgb->rgb_quantum_efficiency[c];
+    }
+    const float* pw = received_power;
+    float* img = image_rgb;
+    vgb_status s;
+    if (!on_device) {
+        if ((s = ensure_staging(ctx, (BP * (sensor->filter_mosaic ? 2 : 1) + 3 * P) * sizeof(float))) != VGB_OK) return s;
+        float* cur = (float*)ctx->staging_base;
+        CK(cudaMemcpyAsync(cur, received_power, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream)); pw = cur; cur += BP;
+        if (sensor->filter_mosaic) {
+            CK(cudaMemcpyAsync(cur, sensor->filter_mosaic, BP * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+            sp.mosaic = cur; cur += BP;
+        }
+        img = cur;
+    }
+    CK((cudaError_t)vgb::launch_sensor_rgb(ctx->stream, pw, width, height, nbands, sp, rp, img, ctx->num_sms));
+    if (!on_device) CK(cudaMemcpyAsync(image_rgb, img, 3 * P * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return VGB_OK;
 } catch (...) {

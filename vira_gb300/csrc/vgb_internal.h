@@ -124,6 +124,12 @@ struct SensorParams {
 };
 int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t height, uint32_t nbands,
                   const SensorParams& sp, float* image, int num_sms);
+// The RGB sensor (vgb_sensor_simulate_rgb): the conversion constants of vgb_rgb_conversion.
+struct RgbParams {
+    float band_min[8], band_max[8], rgb_min[3], rgb_max[3], rgb_bw[3], rgb_pe[3], rgb_qe[3];
+};
+int launch_sensor_rgb(void* stream, const float* power, uint32_t width, uint32_t height, uint32_t nbands,
+                      const SensorParams& sp, const RgbParams& rp, float* image_rgb, int num_sms);
 // out = correlation of in ([B][H][W]) with kernel ([B][kh][kw], zero padding); out != in.
 int launch_psf(void* stream, const float* in, float* out, uint32_t width, uint32_t height, uint32_t nbands,
                const float* kernel, uint32_t kw, uint32_t kh);

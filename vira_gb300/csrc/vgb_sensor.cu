@@ -133,6 +133,69 @@ __global__ void k_sensor(const float* __restrict__ power, uint32_t W, uint32_t H
     }
 }
 
+// NoiseModel::simulate (noise_models/noise_model.ipp:36-74) for one draw: dark-current Poisson
+// counts times the exposure plus Gaussian readout, scaled by the sinusoidal fixed pattern.
+// `purpose` separates the draws of one pixel (the RGB sensor draws once per channel).
+__device__ __forceinline__ float noise_draw(const vgb::SensorParams& sp, uint32_t p, uint32_t i, uint32_t j,
+                                            uint32_t purpose, uint32_t k0, uint32_t k1) {
+    const float dark = poisson(sp.dark_current, p, purpose, sp.frame, k0, k1) * sp.exposure_time;
+    const float readout = gaussian(sp.readout_mean, sp.readout_std, p, purpose + 1u, sp.frame, k0, k1);
+    float scale = 1.f;
+    if (sp.hperiod != 0)
+        scale *= (1.f - sp.hscale) + (sp.hscale * (1.f + sinf(2.f * kPi * (float)i / (2.f * (float)sp.hperiod))));
+    if (sp.vperiod != 0)
+        scale *= (1.f - sp.vscale) + (sp.vscale * (1.f + sinf(2.f * kPi * (float)j / (2.f * (float)sp.vperiod))));
+    return scale * (dark + readout);
+}
+
+// Camera::simulateSensorRGB per pixel (camera.ipp:1253-1282, 1337-1380; photosite.ipp:145-154),
+// FP32 in the reference's order; spectralConvert's integrateOver (spectral_data.ipp:306-333) per
+// RGB band.  Random draws: photon noise at purpose 0x200 + channel, the noise model's at
+// 0x110 + 0x10 * channel (and + 1).
+template <int NB>
+__global__ void k_sensor_rgb(const float* __restrict__ power, uint32_t W, uint32_t H, uint32_t nb,
+                             const vgb::SensorParams sp, const vgb::RgbParams rp, float* __restrict__ out) {
+    const size_t P = (size_t)W * H;
+    const uint32_t k0 = (uint32_t)sp.seed, k1 = (uint32_t)(sp.seed >> 32);
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)(p % W), j = (uint32_t)(p / W);
+        float v[NB];
+#pragma unroll
+        for (int k = 0; k < NB; ++k) {
+            v[k] = 0.f;
+            if (k < (int)nb) v[k] = sp.mosaic ? power[k * P + p] * sp.mosaic[k * P + p] : power[k * P + p];
+        }
+        float ph[3];
+        float total = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float lo = rp.rgb_min[c], hi = rp.rgb_max[c];
+            float integral = 0.f;
+#pragma unroll
+            for (int k = 0; k < NB; ++k) {
+                if (k >= (int)nb) break;
+                const float bmin = rp.band_min[k], bmax = rp.band_max[k];
+                if (bmin > hi || bmax < lo) continue;
+                const float b1 = smax(bmin, lo), b2 = smin(bmax, hi);
+                integral += (b2 - b1) * v[k];
+            }
+            const float rgb = integral / rp.rgb_bw[c];
+            ph[c] = (sp.exposure_time * rgb) / rp.rgb_pe[c];
+            total += ph[c];
+        }
+        if (sp.photon_noise && total >= 1.f) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ph[c] = poisson(ph[c], (uint32_t)p, 0x200u + c, sp.frame, k0, k1);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float noise = sp.noise_model ? noise_draw(sp, (uint32_t)p, i, j, 0x110u + 0x10u * c, k0, k1) : 0.f;
+            const float electrons = (rp.rgb_qe[c] * ph[c]) + noise;
+            out[c * P + p] = (sp.gain * electrons) / sp.max_adu;
+        }
+    }
+}
+
 constexpr int kTileW = 128, kTileH = 8;  // outputs per block: 32 threads x 4 columns, 8 rows
 constexpr int kMaxKernel = 127;
 
@@ -209,6 +272,17 @@ int launch_sensor(void* stream, const float* power, uint32_t width, uint32_t hei
     if (nbands <= 1) k_sensor<1><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
     else if (nbands <= 4) k_sensor<4><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
     else k_sensor<8><<<g, 256, 0, s>>>(power, width, height, nbands, sp, image);
+    return (int)cudaGetLastError();
+}
+
+int launch_sensor_rgb(void* stream, const float* power, uint32_t width, uint32_t height, uint32_t nbands,
+                      const SensorParams& sp, const RgbParams& rp, float* image_rgb, int num_sms) {
+    const size_t P = (size_t)width * height;
+    const int g = (int)std::max<size_t>(1, std::min<size_t>((P + 255) / 256, (size_t)num_sms * 8));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nbands <= 1) k_sensor_rgb<1><<<g, 256, 0, s>>>(power, width, height, nbands, sp, rp, image_rgb);
+    else if (nbands <= 4) k_sensor_rgb<4><<<g, 256, 0, s>>>(power, width, height, nbands, sp, rp, image_rgb);
+    else k_sensor_rgb<8><<<g, 256, 0, s>>>(power, width, height, nbands, sp, rp, image_rgb);
     return (int)cudaGetLastError();
 }
 

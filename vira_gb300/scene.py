@@ -1040,6 +1040,27 @@ class Scene:
             raise ValueError("pathtrace_render needs render_passes.simulate_lighting")
         return simulate_sensor(self, rp.received_power, cam.sensor, frame=self.pathtracer.options.frame)
 
+    def pathtrace_render_rgb(self, camera_id):
+        """Scene::pathtraceRenderRGB (scene.ipp:847-853): renders, then Camera::simulateSensorRGB
+        on the received power; returns [3][H][W] (R, G, B; torch CUDA tensor)."""
+        from .sensor import simulate_sensor_rgb
+
+        cam = self[camera_id]
+        rp = self.pathtracer.render(cam, self)
+        if rp.received_power is None:
+            raise ValueError("pathtrace_render_rgb needs render_passes.simulate_lighting")
+        return simulate_sensor_rgb(self, rp.received_power, cam.sensor, frame=self.pathtracer.options.frame)
+
+    def rasterize_render_rgb(self, camera_id):
+        """Scene::rasterizeRenderRGB (scene.ipp:864-870)."""
+        from .sensor import simulate_sensor_rgb
+
+        cam = self[camera_id]
+        rp = self.rasterizer.render(cam, self)
+        if rp.received_power is None:
+            raise ValueError("rasterize_render_rgb needs rasterizer.render_passes.simulate_lighting")
+        return simulate_sensor_rgb(self, rp.received_power, cam.sensor)
+
     def intersect(self, origins: np.ndarray, directions: np.ndarray, any_hit: bool = False, tmax=None):
         """Scene::intersect / TLAS::intersect (scene.hpp:230) for a batch of rays (host arrays)."""
         self.build_tlas()

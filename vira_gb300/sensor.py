@@ -38,6 +38,44 @@ def default_qe(bands) -> np.ndarray:
     return np.array([np.float32(np.float32(0.5) * v / total) for v in e], np.float32)
 
 
+# ColorRGB (spectral_data.hpp:205): SpectralData<3, BOUNDS, 600, 750, 500, 600, 380, 500>
+RGB_BANDS_NM = ((600.0, 750.0), (500.0, 600.0), (380.0, 500.0))
+
+
+def rgb_bands():
+    from .spectral import SpectralBands
+
+    return SpectralBands.bounds(RGB_BANDS_NM)
+
+
+def integrate_over(bands, values, min_lam, max_lam) -> np.float32:
+    """SpectralData::integrateOver (spectral_data.ipp:306-333) in FP32."""
+    f = np.float32
+    lo, hi = f(min_lam), f(max_lam)
+    if lo > hi:
+        lo, hi = hi, lo
+    if lo == hi:
+        return f(0.0)
+    integral = f(0.0)
+    for bmin, bmax, v in zip(bands.min_wavelength, bands.max_wavelength, values):
+        if bmin > hi or bmax < lo:
+            continue
+        b1 = max(f(bmin), lo)
+        b2 = min(f(bmax), hi)
+        integral = f(integral + f(f(b2 - b1) * f(v)))
+    return integral
+
+
+def spectral_to_rgb(bands, values) -> np.ndarray:
+    """spectralToRGB_val (spectral_data.ipp:588-605): per ColorRGB band, integrateOver / bandwidth."""
+    rb = rgb_bands()
+    out = []
+    for k in range(3):
+        lo, hi = rb.min_wavelength[k], rb.max_wavelength[k]
+        out.append(np.float32(integrate_over(bands, values, lo, hi) / np.float32(hi - lo)))
+    return np.array(out, np.float32)
+
+
 @dataclass
 class PhotositeConfig:
     bit_depth: int = 8
@@ -46,6 +84,10 @@ class PhotositeConfig:
     unity_gain_db: float = 0.0
     quantum_efficiency: np.ndarray | None = None   # default_qe(bands) when None
     linear_scale_factor: float = 1.0
+    # RGB quantum efficiency (PhotositeConfig::quantum_efficiency_rgb); None: the constructor's
+    # default, spectralToRGB of the default spectral QE (photosite.ipp:84-94) -- a spectral QE set
+    # later does not change it, as in the reference
+    quantum_efficiency_rgb: np.ndarray | None = None
 
     def set_gain_db(self, gain_db: float, new_unity_gain_db: float = 0.0):
         """PhotositeConfig::setGainDB (photosite.ipp:34-38)."""
@@ -192,6 +234,47 @@ def simulate_sensor(scene, received_power, sensor: SensorModel, frame: int = 0):
     p = received_power.contiguous()
     torch.cuda.current_stream(received_power.device).synchronize()
     capi.check(lib.vgb_sensor_simulate(ctx, p.data_ptr(), W, H, B, C.byref(s), img.data_ptr(), 1), ctx, "sensor_simulate")
+    return img
+
+
+def rgb_conversion(bands, sensor: SensorModel) -> capi.RgbConversion:
+    """The constants of vgb_sensor_simulate_rgb for the scene's bands and this sensor."""
+    c = capi.RgbConversion()
+    for k in range(bands.size):
+        c.band_min[k] = float(bands.min_wavelength[k])
+        c.band_max[k] = float(bands.max_wavelength[k])
+    rb = rgb_bands()
+    pe = photon_energies(rb)
+    qe = sensor.photosite.quantum_efficiency_rgb
+    qe = spectral_to_rgb(bands, default_qe(bands)) if qe is None else np.asarray(qe, np.float32).reshape(3)
+    for k in range(3):
+        c.rgb_min[k] = float(rb.min_wavelength[k])
+        c.rgb_max[k] = float(rb.max_wavelength[k])
+        c.rgb_bandwidth[k] = float(np.float32(rb.max_wavelength[k] - rb.min_wavelength[k]))
+        c.rgb_photon_energy[k] = float(pe[k])
+        c.rgb_quantum_efficiency[k] = float(qe[k])
+    return c
+
+
+def simulate_sensor_rgb(scene, received_power, sensor: SensorModel, frame: int = 0):
+    """Camera::simulateSensorRGB on a torch CUDA [B][H][W] received-power plane: returns [3][H][W]
+    (R, G, B), not clamped (the reference's RGB photosite does not clamp)."""
+    import torch
+
+    lib = capi.load()
+    ctx = scene.context()
+    B, H, W = received_power.shape
+    img = torch.empty((3, H, W), dtype=torch.float32, device=received_power.device)
+    s = sensor.to_c(scene.bands, frame)
+    rgb = rgb_conversion(scene.bands, sensor)
+    mos = None
+    if sensor.filter_mosaic is not None:
+        mos = torch.as_tensor(sensor.filter_mosaic, dtype=torch.float32, device=received_power.device).contiguous()
+        s.filter_mosaic = mos.data_ptr()
+    p = received_power.contiguous()
+    torch.cuda.current_stream(received_power.device).synchronize()
+    capi.check(lib.vgb_sensor_simulate_rgb(ctx, p.data_ptr(), W, H, B, C.byref(s), C.byref(rgb), img.data_ptr(), 1),
+               ctx, "sensor_simulate_rgb")
     return img
 
 
