@@ -1216,13 +1216,19 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
     const size_t plane = (size_t)W * H;
     int nt = std::max(1, nthreads);
     const CameraRays cr(*cam, nt);
-    std::atomic<uint32_t> next_row{row_begin};
+    // threads take chunks of 32 pixels of the rows [row_begin, row_end) in row-major order, so a
+    // band of one row keeps every thread busy too
+    constexpr uint64_t kChunk = 32;
+    const uint64_t first = (uint64_t)row_begin * W, last = (uint64_t)std::max(row_end, row_begin) * W;
+    std::atomic<uint64_t> next_px{first};
     std::vector<RenderCounters> rcs(nt);
     auto work = [&](int tid) {
         while (true) {
-            uint32_t j = next_row.fetch_add(1);
-            if (j >= row_end) break;
-            for (uint32_t i = 0; i < W; ++i) {
+            const uint64_t p0 = next_px.fetch_add(kChunk);
+            if (p0 >= last) break;
+            const uint64_t p1 = std::min(last, p0 + kChunk);
+            for (uint64_t pp = p0; pp < p1; ++pp) {
+                const uint32_t i = (uint32_t)(pp % W), j = (uint32_t)(pp / W);
                 PixelOut po;
                 render_pixel(s, cr, lights, nlights, *opts, i, j, po, rcs[tid]);
                 size_t p = (size_t)j * W + i;

@@ -20,6 +20,10 @@ constexpr uint32_t kSlotMain = 0u, kSlotRR = 0xFEu, kSlotJitter = 0xFFu;
 constexpr uint32_t kErrStack = 1u, kErrIter = 2u;
 
 constexpr int kStackSize = 64;
+// 1: the wavefront traversal kernels postpone leaves speculatively (traverse_spec_rt).
+#ifndef VGB_TRAV_SPECULATIVE
+#define VGB_TRAV_SPECULATIVE 0
+#endif
 constexpr uint32_t kIterCap = 1u << 22;  // default traversal steps per ray before giving up
 
 // ------------------------------------------------------------------ Philox-4x32-10
@@ -422,11 +426,90 @@ __device__ __forceinline__ void traverse_packet(const float4* __restrict__ nodes
     }
 }
 
+// traverse_rt with speculative leaf postponing (Aila and Laine, HPG 2009, "speculative
+// while-while"): a lane that reaches a leaf while others are still among inner nodes keeps the
+// leaf aside and goes on to the next inner node; the warp tests leaves once every converged lane
+// holds one.  The set of leaves tested and the acceptance rule are traverse_rt's, only their
+// order changes, so the answer is the same (the closest hit does not depend on the order).
+template <bool COUNT>
+__device__ __forceinline__ void traverse_spec_rt(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                 const WRay& r, float tmax, const bool any, HitOut& h,
+                                                 uint32_t& err, Counters& cnt, uint32_t cap) {
+    constexpr int kDone = 0x7fffffff;   // beyond every node index: traversal finished
+    int stack[kStackSize];
+    int sp = 0;
+    int node = 0, leaf = kDone;          // leaf < 0: a postponed leaf
+    float best = any ? tmax : __int_as_float(0x7f800000);
+    h.t = __int_as_float(0x7f800000);
+    h.id = VGB_NO_HIT;
+    uint32_t iter = 0;
+    const SlabRay q = make_slab(r);
+    while (node != kDone || leaf < 0) {
+        while (node >= 0 && node != kDone) {
+            if (++iter > cap) { err |= kErrIter; return; }
+            const float4 n0 = __ldg(&nodes[4 * node + 0]);
+            const float4 n1 = __ldg(&nodes[4 * node + 1]);
+            const float4 n2 = __ldg(&nodes[4 * node + 2]);
+            const float4 n3 = __ldg(&nodes[4 * node + 3]);
+            if (COUNT) cnt.nodes++;
+            float tn0, tf0, tn1, tf1;
+            slab(q, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, best, tn0, tf0);
+            slab(q, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, best, tn1, tf1);
+            const bool h0 = tn0 <= tf0, h1 = tn1 <= tf1;
+            const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
+            if (h0 && h1) {
+                int nearc = ch0, farc = ch1;
+                if (tn1 < tn0) { nearc = ch1; farc = ch0; }
+                if (sp >= kStackSize) { err |= kErrStack; return; }
+                stack[sp++] = farc;
+                node = nearc;
+            } else if (h0) {
+                node = ch0;
+            } else if (h1) {
+                node = ch1;
+            } else {
+                node = sp ? stack[--sp] : kDone;
+            }
+            if (node < 0 && leaf >= 0) {   // postpone the first leaf, keep descending
+                leaf = node;
+                node = sp ? stack[--sp] : kDone;
+            }
+            if (!__any_sync(__activemask(), leaf >= 0)) break;
+        }
+        while (leaf < 0) {
+            const uint32_t x = ~(uint32_t)leaf;
+            const uint32_t start = x >> 3, cntl = (x & 7u) + 1u;
+            for (uint32_t k = 0; k < cntl; ++k) {
+                const float4 t0 = __ldg(&tris[3 * (start + k) + 0]);
+                const float4 t1 = __ldg(&tris[3 * (start + k) + 1]);
+                const float4 t2 = __ldg(&tris[3 * (start + k) + 2]);
+                if (COUNT) cnt.tris++;
+                float tt, U, V, W, det;
+                if (wt_test(r, ld3(t0), ld3(t1), ld3(t2), tt, U, V, W, det)) {
+                    const uint32_t id = __float_as_uint(t0.w);
+                    if (any) {
+                        if (tt <= tmax) { h.t = tt; h.id = id; return; }
+                    } else if (tt < h.t || (tt == h.t && id < h.id)) {
+                        h.t = tt; h.id = id; h.U = U; h.V = V; h.W = W; h.det = det;
+                        best = tt;
+                    }
+                }
+            }
+            leaf = node;                   // the current node may be a leaf too
+            if (node < 0) node = sp ? stack[--sp] : kDone;
+        }
+    }
+}
+
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ void traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                          const WRay& r, float tmax, HitOut& h, uint32_t& err, Counters& cnt,
                                          uint32_t cap) {
+#if VGB_TRAV_SPECULATIVE
+    traverse_spec_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt, cap);
+#else
     traverse_rt<COUNT>(nodes, tris, r, tmax, ANY, h, err, cnt, cap);
+#endif
 }
 
 // ------------------------------------------------------------------ compressed 8-wide traversal
