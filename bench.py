@@ -203,16 +203,15 @@ STEP_PLANES = ("total_radiance", "received_power", "triangle_id", "depth")
 
 
 def cpu_step(cam, lights, nl, opts, osc, threads: int, omega):
-    """One pass of the oracle over the sampled rows, writing the planes the GPU arm writes;
-    returns (rays, pixel samples, seconds)."""
-    rays = 0
+    """One pass of the oracle over the sampled rows (one call, the threads sharing all of them),
+    writing the planes the GPU arm writes; returns (rays, pixel samples, seconds)."""
+    rows = sample_rows(cam.height)
+    step = rows[1] - rows[0] if len(rows) > 1 else 1
     t = time.perf_counter()
-    for row in sample_rows(cam.height):
-        _, counts = osc.render(cam, lights, nl, opts, omega=omega, rows=(row, row + 1), threads=threads,
-                               outputs=STEP_PLANES, fill=False)
-        rays += counts[0] + counts[1]
+    _, counts = osc.render(cam, lights, nl, opts, omega=omega, rows=(rows[0], rows[-1] + 1, step), threads=threads,
+                           outputs=STEP_PLANES, fill=False)
     dt = time.perf_counter() - t
-    return rays, len(sample_rows(cam.height)) * cam.width * opts.samples, dt
+    return counts[0] + counts[1], len(rows) * cam.width * opts.samples, dt
 
 
 def cpu_sample(cam, lights, nl, opts, osc, seconds: float, threads: int, omega):
@@ -1080,9 +1079,11 @@ def profile_case(kind: str, scale: float, layout: int = 2):
     elif kind == "l2":
         from vira_gb300 import capi
 
+        import ctypes
+
         lib = capi.load()
-        ctx = C.c_void_p()
-        capi.check(lib.vgb_context_create(C.byref(ctx), 0), None, "context_create")
+        ctx = ctypes.c_void_p()
+        capi.check(lib.vgb_context_create(ctypes.byref(ctx), 0), None, "context_create")
         print("l2 GB/s", l2_peak(lib, ctx))
         lib.vgb_context_destroy(ctx)
     elif kind == "batch":

@@ -53,7 +53,7 @@ def load():
         "oracle_scene_bvh_nodes": (U32, [P]),
         "oracle_trace": (C.c_int, [P, P, P, P, U32, C.c_int, C.c_int, P, P, P, C.c_int, P, P]),
         "oracle_render": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions),
-                                    C.POINTER(capi.Film), U32, U32, C.c_int, P]),
+                                    C.POINTER(capi.Film), U32, U32, U32, C.c_int, P]),
         "oracle_adjoint": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P, C.c_int]),
         "oracle_sensor": (C.c_int, [P, P, U32, U32, U32, C.c_float, P, P, C.c_float, C.c_float, P]),
         "oracle_psf": (C.c_int, [P, U32, U32, U32, P, U32, U32, P]),
@@ -331,7 +331,8 @@ class OracleScene:
 
     def render(self, cam: capi.Camera, lights, nlights: int, opts: capi.PtOptions, omega=None, rows=None,
                threads=None, outputs=None, fill=True):
-        """Renders rows [r0, r1) (all rows by default) into host planes; returns (planes, ray_counts).
+        """Renders rows [r0, r1) (all rows by default; `rows=(r0, r1, step)` takes every step-th
+        row from r0) into host planes; returns (planes, ray_counts).
         `outputs`: the planes to write (default all; received_power too when omega is given);
         `fill=False` leaves the rows not rendered uninitialised (cheap for a band of rows)."""
         W, H, B = cam.width, cam.height, self.nbands
@@ -355,10 +356,10 @@ class OracleScene:
             f.received_power = planes["received_power"].ctypes.data
             f.pixel_solid_angle = om.ctypes.data
         f.on_device = 0
-        r0, r1 = rows if rows is not None else (0, H)
+        r0, r1, step = (tuple(rows) + (1,))[:3] if rows is not None else (0, H, 1)
         counts = (C.c_uint64 * 2)()
         rc = load().oracle_render(self.h, C.byref(cam), C.cast(lights, C.c_void_p) if nlights else None, nlights,
-                                  C.byref(opts), C.byref(f), r0, r1, threads or nthreads(), counts)
+                                  C.byref(opts), C.byref(f), r0, r1, step, threads or nthreads(), counts)
         if rc != 0:
             raise ValueError("oracle_render rejected its arguments")
         return planes, (int(counts[0]), int(counts[1]))

@@ -1201,12 +1201,12 @@ OAPI int oracle_trace(void* h, const float* orig, const float* dirs, const float
     return 0;
 }
 
-// Renders rows [row_begin, row_end) into host film planes of the full image size.
-// ray_counts_out[0] = closest-hit queries, [1] = shadow queries.
+// Renders rows row_begin, row_begin + row_step, ... (below row_end) into host film planes of the
+// full image size.  ray_counts_out[0] = closest-hit queries, [1] = shadow queries.
 OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, uint32_t nlights,
                        const vgb_pt_options* opts, vgb_film* film, uint32_t row_begin,
-                       uint32_t row_end, int nthreads, uint64_t* ray_counts_out) {
-    if (!h || !cam || !opts || !film) return 1;
+                       uint32_t row_end, uint32_t row_step, int nthreads, uint64_t* ray_counts_out) {
+    if (!h || !cam || !opts || !film || row_step == 0) return 1;
     if (opts->samples == 0 || (nlights && !lights)) return 1;
     if (opts->adaptive_sampling && (opts->samples_per_batch == 0 || opts->samples_to_detect_miss == 0)) return 1;
     const Scene& s = *static_cast<Scene*>(h);
@@ -1216,11 +1216,12 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
     const size_t plane = (size_t)W * H;
     int nt = std::max(1, nthreads);
     const CameraRays cr(*cam, nt);
-    // threads take chunks of 32 pixels of the rows [row_begin, row_end) in row-major order, so a
-    // band of one row keeps every thread busy too
+    // threads take chunks of 32 pixels of the selected rows in row-major order, so a band of one
+    // row keeps every thread busy too
     constexpr uint64_t kChunk = 32;
-    const uint64_t first = (uint64_t)row_begin * W, last = (uint64_t)std::max(row_end, row_begin) * W;
-    std::atomic<uint64_t> next_px{first};
+    const uint64_t nrows = row_end > row_begin ? (row_end - row_begin + row_step - 1) / row_step : 0;
+    const uint64_t last = nrows * W;
+    std::atomic<uint64_t> next_px{0};
     std::vector<RenderCounters> rcs(nt);
     auto work = [&](int tid) {
         while (true) {
@@ -1228,7 +1229,7 @@ OAPI int oracle_render(void* h, const vgb_camera* cam, const vgb_light* lights, 
             if (p0 >= last) break;
             const uint64_t p1 = std::min(last, p0 + kChunk);
             for (uint64_t pp = p0; pp < p1; ++pp) {
-                const uint32_t i = (uint32_t)(pp % W), j = (uint32_t)(pp / W);
+                const uint32_t i = (uint32_t)(pp % W), j = row_begin + (uint32_t)(pp / W) * row_step;
                 PixelOut po;
                 render_pixel(s, cr, lights, nlights, *opts, i, j, po, rcs[tid]);
                 size_t p = (size_t)j * W + i;

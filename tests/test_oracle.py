@@ -223,10 +223,18 @@ def test_render_is_deterministic_and_thread_count_invariant():
     osc = oracle.OracleScene.from_flat(f, 8)
     a, ca = osc.render(cam, lights, nl, opts, threads=1)
     b, cb = osc.render(cam, lights, nl, opts, threads=5)
+    # a row sample (every 5th row from 3, as the CPU baseline takes them) renders those rows
+    # exactly as the whole frame does and leaves the others untouched
+    c, cc = osc.render(cam, lights, nl, opts, rows=(3, 24, 5), threads=3)
     osc.close()
     assert ca == cb
     for k in a:
         assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+        sel = [3, 8, 13, 18, 23]
+        other = [j for j in range(24) if j not in sel]
+        assert np.array_equal(a[k][..., sel, :].view(np.uint32), c[k][..., sel, :].view(np.uint32)), k
+        assert np.all(c[k][..., other, :].view(np.uint32) == (0xFFFFFFFF if k == "triangle_id" else 0x7FC00000)), k
+    assert 0 < cc[0] < ca[0]
     assert np.all(a["indirect_radiance"] >= -1e-6)
     assert a["indirect_radiance"].mean() > 0
 
