@@ -44,10 +44,16 @@ using namespace vgbd;
 #define VGB_BATCH_DIRECT_MINB 2
 #endif
 // k_batch_direct: per-lane register sums, no shared memory; 4 blocks of 256 threads per SM cap it
-// at 64 registers.  On the 256-frame trajectory: 1.16-1.17 s at 64 registers, 1.26 s at 80, 1.47 s
-// at 128.
+// at 64 registers.  On the 256-frame trajectory: 1.16-1.17 s at 64 registers, 1.21 s at 5 blocks
+// (48 registers), 1.36 s at 6, 1.26 s at 80 registers, 1.47 s at 128.
 #ifndef VGB_BATCH_LEAN_MINB
 #define VGB_BATCH_LEAN_MINB 4
+#endif
+// 1: k_batch_direct calls the out-of-line traversal (trace_ool) for camera and shadow rays
+// instead of inlining a closest-hit and an occlusion copy of the loop.  On the 256-frame
+// trajectory: 1.07 s against 1.17 s inlined (64 registers both; 1.11 s at 48, 1.14 s at 85).
+#ifndef VGB_BATCH_LEAN_OOL
+#define VGB_BATCH_LEAN_OOL 1
 #endif
 // 1: k_batch_direct traces a tile's camera rays and shadow rays as warp packets (binary layout).
 // Off: on the 256-frame trajectory the packets took 1.45 s against 1.17 s for one traversal per
@@ -57,6 +63,13 @@ using namespace vgbd;
 #endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
+#endif
+// the same two knobs for the compressed 8-wide layout (k_trace<8>, k_shadow<NB, 8>)
+#ifndef VGB_TRACE8_MINB
+#define VGB_TRACE8_MINB 5
+#endif
+#ifndef VGB_SHADOW8_MINB
+#define VGB_SHADOW8_MINB 5
 #endif
 // Grids of the wavefront kernels (grid-stride loops over the bounce's items), in blocks per SM;
 // 0 launches one 256-thread block per 256 items.  Many waves of short blocks let the block
@@ -685,7 +698,7 @@ __device__ __noinline__ void first_hit_passes(const DevScene& s, const vgb_camer
 // after.  Writes one 16-byte hit record per queue item; kept lean so that enough warps are
 // resident to hide the latency of the node and triangle fetches.
 template <int L, bool COUNT>
-__global__ void __launch_bounds__(256, VGB_TRACE_MINB) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
+__global__ void __launch_bounds__(256, L == 8 ? VGB_TRACE8_MINB : VGB_TRACE_MINB) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
                                                uint32_t bounce, uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const size_t P = st.P;
     const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
@@ -1116,7 +1129,7 @@ __global__ void __launch_bounds__(256, VGB_SHADE_MINB) k_shade(const DevScene s,
 
 // ------------------------------------------------------------------ k_shadow
 template <int NB, int L, bool COUNT>
-__global__ void __launch_bounds__(256, VGB_SHADOW_MINB) k_shadow(const DevScene s, DevState st, uint32_t light, uint32_t nb) {
+__global__ void __launch_bounds__(256, L == 8 ? VGB_SHADOW8_MINB : VGB_SHADOW_MINB) k_shadow(const DevScene s, DevState st, uint32_t light, uint32_t nb) {
     const size_t P = st.P;
     const uint32_t n = st.counters[C_SQ + light];
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -3651,8 +3664,13 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
                 if (PACKET) {
                     traverse_packet<false>(nodes2, s.tris, make_wray(ro, rd), 0.f, valid, h, err, s.iter_cap);
                 } else if (valid) {
-                    Counters c{0, 0};
-                    traverse_any_layout<L, false, false>(s.nodes, s.tris, make_wray(ro, rd), 0.f, h, err, c, s.iter_cap);
+                    if (VGB_BATCH_LEAN_OOL) {
+                        trace_ool<L>(s, make_wray(ro, rd), 0.f, false, h, err);
+                    } else {
+                        Counters c{0, 0};
+                        traverse_any_layout<L, false, false>(s.nodes, s.tris, make_wray(ro, rd), 0.f, h, err, c,
+                                                             s.iter_cap);
+                    }
                 }
                 if (valid) nclosest++;
                 const bool hit = valid && h.id != VGB_NO_HIT;
@@ -3714,8 +3732,13 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
                         if (__any_sync(0xffffffffu, shadow))
                             traverse_packet<true>(nodes2, s.tris, make_wray(Pp, Ld), dist, shadow, hs, err, s.iter_cap);
                     } else if (shadow) {
-                        Counters c{0, 0};
-                        traverse_any_layout<L, true, false>(s.nodes, s.tris, make_wray(Pp, Ld), dist, hs, err, c, s.iter_cap);
+                        if (VGB_BATCH_LEAN_OOL) {
+                            trace_ool<L>(s, make_wray(Pp, Ld), dist, true, hs, err);
+                        } else {
+                            Counters c{0, 0};
+                            traverse_any_layout<L, true, false>(s.nodes, s.tris, make_wray(Pp, Ld), dist, hs, err, c,
+                                                                s.iter_cap);
+                        }
                     }
                     if (shadow) {
                         nshadow++;

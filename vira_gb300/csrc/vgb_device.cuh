@@ -528,7 +528,32 @@ __device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t o) {
     return m;
 }
 
-__device__ __forceinline__ float q8(uint32_t w, int byte) { return (float)((w >> (8 * byte)) & 0xFFu); }
+// Quantised coordinate `byte` of w as a float, exactly: the byte goes into the mantissa of
+// 2^23 (byte permute) and 2^23 is subtracted, so no integer-to-float conversion is issued.
+__device__ __forceinline__ float q8(uint32_t w, int byte) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)byte)) - 8388608.0f;
+}
+
+// Nonzero bytes of w as a 4-bit mask (bit k: byte k != 0).
+__device__ __forceinline__ uint32_t nonzero_bytes(uint32_t w) {
+    const uint32_t m = ((w & 0x7F7F7F7Fu) + 0x7F7F7F7Fu | w) & 0x80808080u;
+    return ((m >> 7) & 1u) | ((m >> 14) & 2u) | ((m >> 21) & 4u) | ((m >> 28) & 8u);
+}
+
+// Plane distances of one node axis for the ray: t(q) = fma(q, a, b -+ e) with a = 2^e_axis / d
+// (exact) and b = (p - o) / d.  Against (p + 2^e q - o) / d in exact arithmetic the error is a
+// relative part below 2^-23 (the final fma and the relative part of b), an absolute part below
+// 2^-23 |b| (b's two roundings) and, because the builder bounds the FP32-rounded dequantised
+// plane, not the exact one, an absolute part below 2^-24 |p + 2^e q| / |d|.  The margin
+// e = 2^-20 (|b| + |1/d| (|p| + 255 * 2^e)) covers the absolute parts 8x; the relative part is
+// covered by widening the exit distance by 2^-20, as in the binary test.
+struct AxisPlanes { float a, bn, bf; };
+__device__ __forceinline__ AxisPlanes axis_planes(float p, float s, float o, float inv) {
+    const float a = s * inv;
+    const float b = (p - o) * inv;
+    const float e = 0x1p-20f * fmaf(fabsf(inv), fmaf(255.0f, s, fabsf(p)), fabsf(b));
+    return AxisPlanes{a, b - e, b + e};
+}
 
 template <bool COUNT>
 __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
@@ -536,6 +561,8 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
                                              Counters& cnt, uint32_t cap) {
     const float widen = 1.0f + 0x1p-20f;
     const uint32_t oct = (r.d.x < 0.f ? 1u : 0u) | (r.d.y < 0.f ? 2u : 0u) | (r.d.z < 0.f ? 4u : 0u);
+    // the near plane of an axis is the box's low side for a positive reciprocal, else the high side
+    const bool nx = r.ix < 0.f, ny = r.iy < 0.f, nz = r.iz < 0.f;
     uint2 stack[kStack8];
     int sp = 0;
     uint32_t node = 0;
@@ -543,7 +570,6 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
     h.t = __int_as_float(0x7f800000);
     h.id = VGB_NO_HIT;
     uint32_t iter = 0;
-    const float ox = r.o.x, oy = r.o.y, oz = r.o.z, ix = r.ix, iy = r.iy, iz = r.iz;
     while (true) {
         if (++iter > cap) { err |= kErrIter; return; }
         const uint4 w0 = __ldg(&nodes[5 * node + 0]);
@@ -552,30 +578,36 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
         const uint4 w3 = __ldg(&nodes[5 * node + 3]);
         const uint4 w4 = __ldg(&nodes[5 * node + 4]);
         if (COUNT) cnt.nodes++;
-        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
-        const float sx = __uint_as_float((w0.w & 0xFFu) << 23);
-        const float sy = __uint_as_float(((w0.w >> 8) & 0xFFu) << 23);
-        const float sz = __uint_as_float(((w0.w >> 16) & 0xFFu) << 23);
+        const AxisPlanes X = axis_planes(__uint_as_float(w0.x), __uint_as_float((w0.w & 0xFFu) << 23), r.o.x, r.ix);
+        const AxisPlanes Y = axis_planes(__uint_as_float(w0.y), __uint_as_float(((w0.w >> 8) & 0xFFu) << 23), r.o.y, r.iy);
+        const AxisPlanes Z = axis_planes(__uint_as_float(w0.z), __uint_as_float(((w0.w >> 16) & 0xFFu) << 23), r.o.z, r.iz);
         const uint32_t imask = w0.w >> 24;
         const uint32_t child_base = w1.x, tri_base = w1.y;
-        uint32_t ihits = 0, tbits = 0;
+        const uint32_t valid = nonzero_bytes(w1.z) | (nonzero_bytes(w1.w) << 4);
+        // quantised near / far planes per axis, slots 0-3 and 4-7
+        const uint32_t nx0 = nx ? w3.z : w2.x, nx1 = nx ? w3.w : w2.y, fx0 = nx ? w2.x : w3.z, fx1 = nx ? w2.y : w3.w;
+        const uint32_t ny0 = ny ? w4.x : w2.z, ny1 = ny ? w4.y : w2.w, fy0 = ny ? w2.z : w4.x, fy1 = ny ? w2.w : w4.y;
+        const uint32_t nz0 = nz ? w4.z : w3.x, nz1 = nz ? w4.w : w3.y, fz0 = nz ? w3.x : w4.z, fz1 = nz ? w3.y : w4.w;
+        uint32_t hits = 0;
 #pragma unroll
         for (int sl = 0; sl < 8; ++sl) {
-            const uint32_t meta = ((sl < 4 ? w1.z : w1.w) >> (8 * (sl & 3))) & 0xFFu;
             const int b = sl & 3;
-            const uint32_t lx = sl < 4 ? w2.x : w2.y, ly = sl < 4 ? w2.z : w2.w, lz = sl < 4 ? w3.x : w3.y;
-            const uint32_t hx = sl < 4 ? w3.z : w3.w, hy = sl < 4 ? w4.x : w4.y, hz = sl < 4 ? w4.z : w4.w;
-            const float a0 = (fmaf(sx, q8(lx, b), px) - ox) * ix, a1 = (fmaf(sx, q8(hx, b), px) - ox) * ix;
-            const float b0 = (fmaf(sy, q8(ly, b), py) - oy) * iy, b1 = (fmaf(sy, q8(hy, b), py) - oy) * iy;
-            const float c0 = (fmaf(sz, q8(lz, b), pz) - oz) * iz, c1 = (fmaf(sz, q8(hz, b), pz) - oz) * iz;
-            const float tn = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
-            const float tf = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), best)) * widen;
-            if (meta != 0u && tn <= tf) {
-                if (imask & (1u << sl)) ihits |= 1u << sl;
-                else tbits |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-            }
+            const float tnx = fmaf(q8(sl < 4 ? nx0 : nx1, b), X.a, X.bn), tfx = fmaf(q8(sl < 4 ? fx0 : fx1, b), X.a, X.bf);
+            const float tny = fmaf(q8(sl < 4 ? ny0 : ny1, b), Y.a, Y.bn), tfy = fmaf(q8(sl < 4 ? fy0 : fy1, b), Y.a, Y.bf);
+            const float tnz = fmaf(q8(sl < 4 ? nz0 : nz1, b), Z.a, Z.bn), tfz = fmaf(q8(sl < 4 ? fz0 : fz1, b), Z.a, Z.bf);
+            const float tn = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
+            const float tf = fmin3(tfx, tfy, fminf(tfz, best)) * widen;
+            hits |= (tn <= tf ? 1u : 0u) << sl;
         }
+        hits &= valid;
         // triangles of the hit leaves of this node
+        uint32_t leaves = hits & ~imask, tbits = 0;
+        while (leaves) {
+            const uint32_t sl = __ffs(leaves) - 1;
+            leaves &= leaves - 1;
+            const uint32_t meta = ((sl < 4 ? w1.z : w1.w) >> (8 * (sl & 3))) & 0xFFu;
+            tbits |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+        }
         while (tbits) {
             const uint32_t k = __ffs(tbits) - 1;
             tbits &= tbits - 1;
@@ -596,7 +628,7 @@ __device__ __forceinline__ void traverse8_rt(const uint4* __restrict__ nodes, co
             }
         }
         // next node: the nearest remaining hit child of this node, else of the stacked groups
-        uint32_t pending = octant_order(ihits, oct), base = child_base, im = imask;
+        uint32_t pending = octant_order(hits & imask, oct), base = child_base, im = imask;
         if (!pending) {
             if (sp == 0) return;
             const uint2 g = stack[--sp];
