@@ -61,6 +61,12 @@ using namespace vgbd;
 #ifndef VGB_BATCH_PACKET
 #define VGB_BATCH_PACKET 0
 #endif
+// > 0: before each continuation bounce, k_bin_rays sorts the live-path queue into this many
+// bins by the rays' vertical direction component, and k_trace takes its items bin by bin (the
+// hit records keep the queue order, so k_shade reads them unchanged).  Up to 8.
+#ifndef VGB_TRACE_BINS
+#define VGB_TRACE_BINS 0
+#endif
 #ifndef VGB_SHADOW_MINB
 #define VGB_SHADOW_MINB 5
 #endif
@@ -164,6 +170,7 @@ struct DevState {
     uint32_t* sq_slot[VGB_MAX_LIGHTS];
     float* sq_con[VGB_MAX_LIGHTS];   // [B][P]
     float4* hit;         // [P] closest-hit record per queue item: (t, id bits, w(v1), w(v2))
+    uint32_t* binq;      // [VGB_TRACE_BINS][P] queue items binned by ray direction (null: off)
     // adaptive sampling: per pixel the sums of the path-radiance magnitude and of its square,
     // and the sample index at which the pixel stopped (0 while it samples on)
     float* as1;
@@ -179,7 +186,8 @@ struct DevState {
 // the error word and the batch kernels' work counter.
 enum {
     C_PQ0 = 0, C_PQ1 = 1, C_SQ = 2, C_FTRACE = 2 + VGB_MAX_LIGHTS, C_FSHADOW = 3 + VGB_MAX_LIGHTS,
-    C_ERR = 3 + 2 * VGB_MAX_LIGHTS, C_BATCH = 4 + 2 * VGB_MAX_LIGHTS, C_COUNT = 5 + 2 * VGB_MAX_LIGHTS
+    C_ERR = 3 + 2 * VGB_MAX_LIGHTS, C_BATCH = 4 + 2 * VGB_MAX_LIGHTS, C_BIN = 5 + 2 * VGB_MAX_LIGHTS,
+    C_COUNT = C_BIN + 8
 };
 // counters cleared at the start of every bounce: the shadow queues and the persistent item counters
 constexpr int kBounceResetWords = 1 + 2 * VGB_MAX_LIGHTS;
@@ -711,8 +719,21 @@ __global__ void __launch_bounds__(256, L == 8 ? VGB_TRACE8_MINB : VGB_TRACE_MINB
         if (bounce == 0) {
             if (!camera_ray(fp, item, sample, slot, ro, rd)) continue;
             if (fp.opt.adaptive_sampling && sample != 0 && st.anum[slot]) continue;  // pixel has stopped
-        } else {
-            slot = in_queue[item];
+        }
+        uint32_t qi = item;  // the queue position this ray's hit record goes to
+        if (bounce != 0) {
+#if VGB_TRACE_BINS > 0
+            if (st.binq) {
+                uint32_t first = 0;
+#pragma unroll
+                for (int b = 0; b < VGB_TRACE_BINS; ++b) {
+                    const uint32_t c = st.counters[C_BIN + b];
+                    if (item >= first && item - first < c) qi = st.binq[b * P + (item - first)];
+                    first += c;
+                }
+            }
+#endif
+            slot = in_queue[qi];
             ro = F3{st.org[slot], st.org[P + slot], st.org[2 * P + slot]};
             rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
         }
@@ -727,7 +748,7 @@ __global__ void __launch_bounds__(256, L == 8 ? VGB_TRACE8_MINB : VGB_TRACE_MINB
             w0 = h.V * rcp;
             w1 = h.W * rcp;
         }
-        st.hit[item] = make_float4(h.t, __uint_as_float(h.id), w0, w1);
+        st.hit[qi] = make_float4(h.t, __uint_as_float(h.id), w0, w1);
     }
     if (err) atomicOr(&st.counters[C_ERR], err);
     warp_reduce_add(&st.stats[2], nclosest);
@@ -738,6 +759,35 @@ __global__ void __launch_bounds__(256, L == 8 ? VGB_TRACE8_MINB : VGB_TRACE_MINB
         warp_reduce_add(&st.stats[5], cnt.tris);
     }
 }
+
+#if VGB_TRACE_BINS > 0
+// The live-path queue `in_q` binned by the vertical component of each ray's direction (bins of
+// equal width over [-1, 1]), so that a warp of k_trace takes rays of similar traversal length:
+// on terrain the near-horizontal rays cross far more of the tree than the steep ones.  Each bin
+// lists queue positions; the appends are warp-aggregated per bin.  Sum of the bins = the queue.
+__global__ void __launch_bounds__(256) k_bin_rays(DevState st, uint32_t in_q) {
+    const size_t P = st.P;
+    const uint32_t n = st.counters[in_q];
+    const uint32_t* in_queue = st.pq[in_q];
+    const int lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t item = base + lane;
+        const bool valid = item < n;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (!valid) continue;
+        const float dz = st.dir[2 * P + in_queue[item]];
+        const float x = fminf(fmaxf((dz + 1.0f) * (0.5f * VGB_TRACE_BINS), 0.0f), (float)(VGB_TRACE_BINS - 1));
+        const uint32_t b = (uint32_t)x;
+        const unsigned grp = __match_any_sync(vmask, b);
+        const int leader = __ffs(grp) - 1;
+        uint32_t pos = 0;
+        if (lane == leader) pos = atomicAdd(&st.counters[C_BIN + b], (uint32_t)__popc(grp));
+        pos = __shfl_sync(grp, pos, leader) + (uint32_t)__popc(grp & ((1u << lane) - 1u));
+        st.binq[b * P + pos] = item;
+    }
+}
+#endif
 
 // ------------------------------------------------------------------ persistent traversal (binary layout)
 // k_trace_p / k_shadow_p replace the grid-stride loops of k_trace / k_shadow for the binary BVH.
@@ -1500,6 +1550,8 @@ vgb_status ensure_scratch(vgb_context* ctx, size_t P, size_t n_items, uint32_t B
     AL(st.pq[0], P * u); AL(st.pq[1], P * u);
     AL(st.hit, n_items * sizeof(float4));
     AL(st.as1, P * f); AL(st.as2, P * f); AL(st.anum, P * u);
+    st.binq = nullptr;
+    if (VGB_TRACE_BINS > 0) AL(st.binq, VGB_TRACE_BINS * P * u);
     for (uint32_t l = 0; l < VGB_MAX_LIGHTS; ++l) {
         if (l < L) {
             AL(st.sq_org[l], 3 * P * f); AL(st.sq_dir[l], 3 * P * f); AL(st.sq_tmax[l], P * f);
@@ -1603,6 +1655,13 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             // reset the output path queue, the shadow queues and the persistent item counters
             cudaMemsetAsync(&st.counters[(q ^ 1u)], 0, sizeof(uint32_t), ctx->stream);
             cudaMemsetAsync(&st.counters[C_SQ], 0, sizeof(uint32_t) * kBounceResetWords, ctx->stream);
+#if VGB_TRACE_BINS > 0
+            if (b != 0 && st.binq && !persist) {
+                cudaMemsetAsync(&st.counters[C_BIN], 0, sizeof(uint32_t) * VGB_TRACE_BINS, ctx->stream);
+                k_bin_rays<<<gs, 256, 0, ctx->stream>>>(st, q);
+                launches++;
+            }
+#endif
             {
                 Prof p(ctx, 0, prof);
                 if (persist) k_trace_p<COUNT><<<gtp, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0, budget, refill);
