@@ -44,9 +44,10 @@ MEASURED_TRAFFIC = {
 # bounce 0 (camera rays) and bounce 1 (diffuse continuation rays).
 MEASURED_TRACE_COUNTERS = {
     "case": "path_traced scale 0.25 (1025^2 DEM + craters, 512^2, 4 spp, 3 bounces)",
-    "issue_active_pct": {"bounce0": 57.7, "bounce1": 48.65},
-    "l1_throughput_pct": {"bounce0": 49.27, "bounce1": 31.2},
-    "threads_per_warp_inst": {"bounce0": 26.0, "bounce1": 16.02},
+    "issue_active_pct": {"bounce0": 56.58, "bounce1": 48.14},
+    "l1_throughput_pct": {"bounce0": 48.74, "bounce1": 31.13},
+    "threads_per_warp_inst": {"bounce0": 26.05, "bounce1": 16.06},
+    "long_scoreboard_stalls_per_issue": {"bounce0": 5.96, "bounce1": 5.62},
 }
 L2_PROBE_BYTES = 64 << 20
 sys.path.insert(0, str(ROOT))

@@ -112,3 +112,38 @@ def test_adjoint_rejects_a_normal_map(gpu):
     assert lib.vgb_adjoint(ctx, C.byref(cam), lights, 1, C.byref(opts), capi.ptr(dl), capi.ptr(gt), None, 0) == 1
     assert b"normal map" in lib.vgb_last_error(ctx)
     scene.close()
+
+
+@pytest.mark.parametrize("bounces", [0, 2], ids=["direct", "path"])
+def test_batch_with_normal_map_equals_per_frame(gpu, bounces):
+    """The batched trajectory kernels shade through the same normal map: the lean direct kernel
+    (which builds the tangent frame only for the map) and the general one with bounces."""
+    import torch
+
+    scene, frames = workloads.trajectory(nframes=3, posts=129, resolutions=(40, 56), spps=(1, 3), seed=7,
+                                         alt_top=5000.0, alt_bottom=2500.0)
+    m = scene.meshes[0]
+    if m.uv is None:
+        m.uv = synthetic.grid_uvs(129, 129, 8)
+    m.normal_map = bumpy_normal_map()
+    scene.mark_dirty()
+    scene.pathtracer.options.bounces = bounces
+    scene.pathtracer.options.rr_depth = 0
+    planes = ("total_radiance", "normal_global", "triangle_id", "depth")
+    batch = scene.render_batch(frames, autotune=False, use_graph=False, planes=planes)
+    torch.cuda.synchronize()
+    pt = scene.pathtracer
+    for fr, b in zip(frames, batch):
+        for k, L in enumerate(scene.lights):
+            L.position = np.asarray(fr.light_positions[k], np.float64)
+        pt.options.samples = fr.samples
+        pt.options.frame = fr.frame
+        rp = pt.render(fr.camera, scene)
+        torch.cuda.synchronize()
+        for k in planes:
+            got, want = b[k].cpu().numpy(), getattr(rp, k).cpu().numpy()
+            if k == "triangle_id":
+                assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+            else:
+                assert same_bits_or_nan(got, want), k
+    scene.close()

@@ -63,7 +63,9 @@ using namespace vgbd;
 #endif
 // > 0: before each continuation bounce, k_bin_rays sorts the live-path queue into this many
 // bins by the rays' vertical direction component, and k_trace takes its items bin by bin (the
-// hit records keep the queue order, so k_shade reads them unchanged).  Up to 8.
+// hit records keep the queue order, so k_shade reads them unchanged).  Up to 8.  Off: on the
+// path-traced frame 4 bins cut the closest-hit time by under 2 % and the binning pass cost more
+// (3469 and 3485 Mrays/s with 4 and 8 bins against 3639).
 #ifndef VGB_TRACE_BINS
 #define VGB_TRACE_BINS 0
 #endif
@@ -373,11 +375,16 @@ __device__ __forceinline__ F3 sample_normal_map(const DevScene& s, float u, floa
 
 // Material::getNormal (materials/material.ipp:129-143): the tangent-space normal map sample taken
 // to the scene frame by [tangent | bitangent | N] and normalised; N itself without a map.
-__device__ __forceinline__ F3 mapped_normal(const DevScene& s, float u, float v, F3 N, F3 tg, F3 bt) {
-    if (!s.nmap) return N;
+// Out of line: a scene without a normal map never runs it, and the kernels that shade keep a
+// smaller instruction footprint.
+__device__ __noinline__ F3 normal_from_map(const DevScene& s, float u, float v, F3 N, F3 tg, F3 bt) {
     const F3 t = sample_normal_map(s, u, v);
     return normalize(F3{(tg.x * t.x + bt.x * t.y) + N.x * t.z, (tg.y * t.x + bt.y * t.y) + N.y * t.z,
                         (tg.z * t.x + bt.z * t.y) + N.z * t.z});
+}
+__device__ __forceinline__ F3 mapped_normal(const DevScene& s, float u, float v, F3 N, F3 tg, F3 bt) {
+    if (!s.nmap) return N;
+    return normal_from_map(s, u, v, N, tg, bt);
 }
 
 // The tangent frame of the shading normal (cpu_path_tracer.ipp:318-321).
@@ -391,8 +398,10 @@ __device__ __forceinline__ void tangent_frame(F3 N, F3& tg, F3& bt) {
 // shading normals, tangent frame, the normal map, albedo (vertex albedo x texture), interpolated
 // position and computeShadingPoint (:494-511).  The normal matrix is the identity in the
 // flattened frame.  N: the shading normal after the normal map (NEE, MIS and the film's normal);
-// (tg, bt, nf): the tangent frame built before the map, which the continuation samples in.
-template <int NB>
+// (tg, bt, nf): the tangent frame built before the map, which the continuation samples in;
+// FRAME = false for callers that sample no continuation (tg and bt are then left unset unless
+// the scene has a normal map, which needs them).
+template <int NB, bool FRAME = true>
 __device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool smooth, uint32_t t, float w0f,
                                            float w1f, F3& Pp, F3& N, F3& fnrm, F3& tg, F3& bt, F3& nf, float* alb,
                                            float* va_out = nullptr, float* tex_out = nullptr, float* uv_out = nullptr) {
@@ -414,8 +423,11 @@ __device__ __forceinline__ void surface_at(const DevScene& s, uint32_t nb, bool 
     F3 Nl = fnrm;
     if (smooth) Nl = normalize((w[0] * vn[0] + w[1] * vn[1]) + w[2] * vn[2]);
     nf = Nl;
-    tangent_frame(Nl, tg, bt);
-    N = mapped_normal(s, uvx, uvy, Nl, tg, bt);
+    N = Nl;
+    if (FRAME || s.nmap) {
+        tangent_frame(Nl, tg, bt);
+        N = mapped_normal(s, uvx, uvy, Nl, tg, bt);
+    }
     float texv[NB];
     sample_uvs<NB>(s, nb, uvx, uvy, texv);
 #pragma unroll
@@ -3750,7 +3762,8 @@ __global__ void __launch_bounds__(256, VGB_BATCH_LEAN_MINB) k_batch_direct(const
                 if (hit) {
                     const float rcp = 1.0f / h.det;
                     F3 fnrm, tg, bt, nf;
-                    surface_at<NB>(s, nb, opt.smooth_shading != 0, h.id, h.V * rcp, h.W * rcp, Pp, N, fnrm, tg, bt, nf, alb);
+                    surface_at<NB, false>(s, nb, opt.smooth_shading != 0, h.id, h.V * rcp, h.W * rcp, Pp, N, fnrm, tg, bt,
+                                          nf, alb);
                     if (first_tri == VGB_NO_HIT) {
                         first_tri = h.id;
                         if (F.film.tsz || F.film.vel_g || F.film.vel_c)
