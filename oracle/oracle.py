@@ -63,7 +63,8 @@ def load():
         "oracle_adjoint_positions": (C.c_int, [P, C.POINTER(capi.Camera), P, U32, C.POINTER(capi.PtOptions), P, P, P,
                                                C.c_int]),
         "oracle_lz4_decompress": (C.c_int64, [P, C.c_uint64, P, C.c_uint64]),
-        "oracle_rasterize": (C.c_int, [P, C.POINTER(capi.Camera), P, P, U32, C.c_int, C.c_int, P, P, P, P, P, P, P, P]),
+        "oracle_rasterize": (C.c_int, [P, C.POINTER(capi.Camera), P, P, U32, C.c_int, C.c_int, P, P, P, P, P, P, P, P,
+                                       P, P, P]),
         "oracle_normal_cone": (C.c_int, [P, C.c_uint64, P]),
     }
     for name, (res, args) in sig.items():
@@ -265,14 +266,20 @@ class OracleScene:
         except Exception:
             pass
 
-    def rasterize(self, cam: capi.Camera, K, lights, nlights: int, lighting: bool, smooth: bool, omega=None):
+    def rasterize(self, cam: capi.Camera, K, lights, nlights: int, lighting: bool, smooth: bool, omega=None,
+                  passes=False):
         """The CPURasterizer restatement: planes depth, alpha, albedo, normal_global, triangle_id
-        (index + 1), total_radiance and received_power (with lighting)."""
+        (index + 1), total_radiance and received_power (with lighting); with `passes` also
+        triangle_size, velocity_global and velocity_camera."""
         W, H, B = cam.width, cam.height, self.nbands
         k = np.ascontiguousarray(K, np.float32)
         out = dict(depth=np.empty((H, W), np.float32), alpha=np.empty((H, W), np.float32),
                    albedo=np.empty((B, H, W), np.float32), normal_global=np.empty((3, H, W), np.float32),
                    triangle_id=np.empty((H, W), np.uint32))
+        if passes:
+            out["triangle_size"] = np.empty((H, W), np.float32)
+            out["velocity_global"] = np.empty((3, H, W), np.float32)
+            out["velocity_camera"] = np.empty((3, H, W), np.float32)
         if lighting:
             out["total_radiance"] = np.empty((B, H, W), np.float32)
             out["received_power"] = np.empty((B, H, W), np.float32)
@@ -281,7 +288,8 @@ class OracleScene:
         assert load().oracle_rasterize(self.h, C.byref(cam), k.ctypes.data, lights, nlights, int(lighting), int(smooth),
                                        p(out["depth"]), p(out["alpha"]), p(out["albedo"]), p(out["normal_global"]),
                                        p(out["triangle_id"]), p(out.get("total_radiance")), p(out.get("received_power")),
-                                       p(om)) == 0
+                                       p(om), p(out.get("triangle_size")), p(out.get("velocity_global")),
+                                       p(out.get("velocity_camera"))) == 0
         return out
 
     def trace(self, origins, dirs, any_hit=False, tmax=None, mode=0, threads=None):

@@ -632,6 +632,8 @@ struct PixelOut {
 // (reference_frame.ipp:367-373); the camera's point velocity at rotation * p_global (the
 // reference passes intersection_global to the camera's localPointToGlobalVelocity), the
 // difference taken to the camera frame by the transposed rotation.
+static void point_velocities(const Scene& s, const vgb_camera& cam, uint32_t t, V3 P, V3& vel_g, V3& vel_c);
+
 static void first_hit_passes(const Scene& s, const vgb_camera& cam, uint32_t t, V3 P, PixelOut& out) {
     const V3 a = s.pos[s.idx[3 * t + 1]], b = s.pos[s.idx[3 * t + 2]], c = s.pos[s.idx[3 * t]];
     float e01 = length(b - a), e02 = length(c - a), e12 = length(c - b);
@@ -640,6 +642,13 @@ static void first_hit_passes(const Scene& s, const vgb_camera& cam, uint32_t t, 
     float gx = distance * cam.sensor_size[0] / (cam.focal_length * (float)cam.width);
     float gy = distance * cam.sensor_size[1] / (cam.focal_length * (float)cam.height);
     out.tsz = edge / std::min(gx, gy);
+    point_velocities(s, cam, t, P, out.vel_g, out.vel_c);
+}
+
+// The instance's point velocity at P and the velocity relative to the camera in the camera frame
+// (the path tracer's first hit, cpu_path_tracer.ipp:365-371, and the rasterizer's fragment,
+// cpu_rasterizer.ipp:213-218, compute the same).
+static void point_velocities(const Scene& s, const vgb_camera& cam, uint32_t t, V3 P, V3& vel_g, V3& vel_c) {
     V3 v{0, 0, 0}, w{0, 0, 0}, o{0, 0, 0};
     for (const vgb_instance_motion& m : s.motion)
         if (m.first_triangle <= t) {
@@ -647,14 +656,14 @@ static void first_hit_passes(const Scene& s, const vgb_camera& cam, uint32_t t, 
             w = V3{m.angular_rate[0], m.angular_rate[1], m.angular_rate[2]};
             o = V3{m.position[0], m.position[1], m.position[2]};
         }
-    out.vel_g = v + cross(w, P - o);
+    vel_g = v + cross(w, P - o);
     V3 rp = mat3_mul(cam.rotation, P) + V3{cam.rot_origin[0], cam.rot_origin[1], cam.rot_origin[2]};
     V3 cv = V3{cam.velocity[0], cam.velocity[1], cam.velocity[2]} +
             cross(V3{cam.angular_rate[0], cam.angular_rate[1], cam.angular_rate[2]}, rp);
-    V3 rv = out.vel_g - cv;
+    V3 rv = vel_g - cv;
     const float* R = cam.rotation;
-    out.vel_c = V3{(R[0] * rv.x + R[1] * rv.y) + R[2] * rv.z, (R[3] * rv.x + R[4] * rv.y) + R[5] * rv.z,
-                   (R[6] * rv.x + R[7] * rv.y) + R[8] * rv.z};
+    vel_c = V3{(R[0] * rv.x + R[1] * rv.y) + R[2] * rv.z, (R[3] * rv.x + R[4] * rv.y) + R[5] * rv.z,
+               (R[6] * rv.x + R[7] * rv.y) + R[8] * rv.z};
 }
 
 struct RenderCounters { uint64_t closest = 0, shadow = 0; };
@@ -1880,9 +1889,12 @@ static inline float edge_fn(float ax, float ay, float bx, float by, float cx, fl
     return (cx - ax) * (by - ay) - (cy - ay) * (bx - ax);
 }
 
+// tsz_o, velg_o, velc_o (optional): the triangle-size pass (the longest projected edge in pixels,
+// cpu_rasterizer.ipp:123-129) and the velocity passes (:211-218) of the fragment that stays.
 OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const vgb_light* lights, uint32_t nlights,
                           int lighting, int smooth, float* depth_o, float* alpha_o, float* albedo_o, float* normal_o,
-                          uint32_t* tri_o, float* total_o, float* power_o, const float* omega) {
+                          uint32_t* tri_o, float* total_o, float* power_o, const float* omega, float* tsz_o,
+                          float* velg_o, float* velc_o) {
     const Scene& s = *static_cast<Scene*>(h);
     const uint32_t W = cam->width, H = cam->height, B = s.nbands;
     const size_t P = (size_t)W * H;
@@ -1890,6 +1902,11 @@ OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const 
         depth_o[v] = INFINITY; alpha_o[v] = 0.f; tri_o[v] = 0xFFFFFFFFu;
         for (int k = 0; k < 3; ++k) normal_o[k * P + v] = 0.f;
         for (uint32_t b = 0; b < B; ++b) { albedo_o[b * P + v] = 0.f; if (total_o) total_o[b * P + v] = 0.f; }
+        if (tsz_o) tsz_o[v] = INFINITY;   // DataPayload defaults
+        for (int k = 0; k < 3; ++k) {
+            if (velg_o) velg_o[k * P + v] = 0.f;
+            if (velc_o) velc_o[k * P + v] = 0.f;
+        }
     }
     const V3 O{cam->origin[0], cam->origin[1], cam->origin[2]};
     const V3 ax{cam->rotation[0], cam->rotation[1], cam->rotation[2]};
@@ -1925,6 +1942,11 @@ OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const 
         const int x1 = std::clamp(ex, 0, (int)W), y1 = std::clamp(ey, 0, (int)H);
         const float d0 = length(vc[0]), d1 = length(vc[1]), d2 = length(vc[2]);
         const float area = edge_fn(px[0], py[0], px[1], py[1], px[2], py[2]);
+        // size of the triangle: glm's length of the projected edges
+        const float e01 = std::sqrt((px[1] - px[0]) * (px[1] - px[0]) + (py[1] - py[0]) * (py[1] - py[0]));
+        const float e02 = std::sqrt((px[2] - px[0]) * (px[2] - px[0]) + (py[2] - py[0]) * (py[2] - py[0]));
+        const float e12 = std::sqrt((px[2] - px[1]) * (px[2] - px[1]) + (py[2] - py[1]) * (py[2] - py[1]));
+        const float tri_size = std::max(e01, std::max(e02, e12));
         for (int X = x0; X < x1; ++X) {
             for (int Y = y0; Y < y1; ++Y) {
                 const float fx = (float)X, fy = (float)Y;
@@ -1955,12 +1977,19 @@ OAPI int oracle_rasterize(void* h, const vgb_camera* cam, const float* K, const 
                     N = get_normal(s, uvx, uvy, N, tangent, bitangent);
                 }
                 float rad[VGB_MAX_BANDS] = {0};
+                const V3 fc = (w0 * vc[0] + w1 * vc[1]) + w2 * vc[2];
+                const float* R = cam->rotation;
+                const V3 fg{((R[0] * fc.x + R[3] * fc.y) + R[6] * fc.z) + cam->origin[0],
+                            ((R[1] * fc.x + R[4] * fc.y) + R[7] * fc.z) + cam->origin[1],
+                            ((R[2] * fc.x + R[5] * fc.y) + R[8] * fc.z) + cam->origin[2]};
+                if (tsz_o) tsz_o[v] = tri_size;
+                if (velg_o || velc_o) {
+                    V3 vg, vcam;
+                    point_velocities(s, *cam, t, fg, vg, vcam);
+                    if (velg_o) { velg_o[v] = vg.x; velg_o[P + v] = vg.y; velg_o[2 * P + v] = vg.z; }
+                    if (velc_o) { velc_o[v] = vcam.x; velc_o[P + v] = vcam.y; velc_o[2 * P + v] = vcam.z; }
+                }
                 if (lighting) {
-                    const V3 fc = (w0 * vc[0] + w1 * vc[1]) + w2 * vc[2];
-                    const float* R = cam->rotation;
-                    const V3 fg{((R[0] * fc.x + R[3] * fc.y) + R[6] * fc.z) + cam->origin[0],
-                                ((R[1] * fc.x + R[4] * fc.y) + R[7] * fc.z) + cam->origin[1],
-                                ((R[2] * fc.x + R[5] * fc.y) + R[8] * fc.z) + cam->origin[2]};
                     for (uint32_t l = 0; l < nlights; ++l) {
                         V3 L; float dist, pdf;
                         light_sample(lights[l], fg, true, 0.f, 0.f, L, dist, pdf);

@@ -121,3 +121,61 @@ def test_first_hit_passes_host_film_noalloc_and_batch(gpu):
     for k in PASSES:
         assert same_bits(out[0][k].cpu().numpy(), ref[k]), k
     s.close()
+
+
+def test_rasterizer_passes_match_oracle(gpu):
+    """The rasterizer's passes (cpu_rasterizer.ipp:123-129, 211-218): the triangle size is the
+    longest projected edge in pixels, the velocities those of the path tracer's first hit at the
+    fragment's scene position; bit-identical to the oracle's sequential rasterizer, the same from
+    a host film with every plane requested (all staged on the device)."""
+    import torch
+
+    from oracle import oracle
+
+    s, cid = _scene()
+    rr = s.rasterizer.render_passes
+    rr.simulate_lighting = True
+    rr.save_velocity = True
+    rr.save_triangle_size = True
+    rp = s.rasterizer.render(s[cid], s)
+    torch.cuda.synchronize()
+    got = {k: getattr(rp, k).cpu().numpy() for k in PASSES}
+    B = s.bands.size
+    cam = s[cid].to_c(s.origin, B)
+    lights, nl = s.c_lights()
+    omega = s.pixel_solid_angle(s[cid], cam).cpu().numpy()
+    osc = oracle.OracleScene.from_flat(s.flat, B)
+    ref = osc.rasterize(cam, s[cid].intrinsic_matrix(), lights, nl, True, s.smooth_shading(), omega, passes=True)
+    osc.close()
+    drawn = ref["triangle_id"] != 0xFFFFFFFF
+    assert 0.3 < drawn.mean() < 1.0
+    for k in PASSES:
+        assert same_bits_or_nan(got[k], ref[k]), k
+    assert np.all(np.isinf(got["triangle_size"][~drawn])) and np.all(got["velocity_camera"][:, ~drawn] == 0)
+    assert np.all(got["triangle_size"][drawn] > 0)
+    assert np.unique(np.round(got["velocity_global"][0][drawn])).size > 2
+    # host film with every plane the rasterizer writes
+    lib = capi.load()
+    ctx = s.context()
+    o = capi.RasterOptions()
+    o.intrinsic[:] = [float(x) for x in s[cid].intrinsic_matrix()]
+    o.simulate_lighting = 1
+    o.nbands = B
+    H, W = cam.height, cam.width
+    host = {"depth": (H, W), "alpha": (H, W), "albedo": (B, H, W), "normal_global": (3, H, W),
+            "total_radiance": (B, H, W), "direct_radiance": (B, H, W), "indirect_radiance": (B, H, W),
+            "received_power": (B, H, W), "velocity_global": (3, H, W), "velocity_camera": (3, H, W),
+            "triangle_size": (H, W)}
+    host = {k: np.full(v, -5.0, np.float32) for k, v in host.items()}
+    host["triangle_id"] = np.zeros((H, W), np.uint32)
+    om = np.ascontiguousarray(omega, np.float32)
+    f = capi.Film()
+    for k, a in host.items():
+        setattr(f, k, a.ctypes.data)
+    f.pixel_solid_angle = om.ctypes.data
+    f.on_device = 0
+    capi.check(lib.vgb_rasterize(ctx, C.byref(cam), lights, nl, C.byref(o), C.byref(f)), ctx, "rasterize")
+    for k in PASSES + ("depth", "total_radiance", "received_power", "albedo"):
+        assert same_bits_or_nan(host[k], getattr(rp, k).cpu().numpy()), k
+    assert np.all(host["direct_radiance"] == 0) and np.all(host["indirect_radiance"] == 0)
+    s.close()

@@ -82,3 +82,24 @@ def test_intrinsic_matrix_is_the_inverse_of_kinv():
         M = np.array([[K[0], K[1], K[2]], [K[3], K[4], K[5]], [0, 0, 1]])
         Mi = np.array([[Ki[0], Ki[2], Ki[4]], [Ki[1], Ki[3], Ki[5]], [0, 0, 1]])
         assert np.allclose(M @ Mi, np.eye(3), atol=1e-4)   # FP32 entries, principal point ~300 px
+
+
+def test_square_triangle_size_and_velocity_passes():
+    """The square's triangles project to right triangles with legs of 20 pixels: the triangle-size
+    pass is the hypotenuse sqrt(800) (the longest projected edge, cpu_rasterizer.ipp:123-129);
+    a static scene under a camera moving at v reads 0 global velocity and -v in the camera frame
+    (identity rotation)."""
+    pos = np.array([[-1, -1, 10], [1, -1, 10], [1, 1, 10], [-1, 1, 10]], np.float32)
+    idx = np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+    osc = oracle.OracleScene(pos, idx, 4)
+    cam, K = _square_camera()
+    cam.velocity[:] = [1.0, 2.0, 3.0]
+    out = osc.rasterize(cam, K, None, 0, False, False, passes=True)
+    osc.close()
+    cov = np.isfinite(out["depth"])
+    assert cov.sum() == 400
+    assert np.all(out["triangle_size"][cov] == np.float32(math.sqrt(800.0)))
+    assert np.all(np.isinf(out["triangle_size"][~cov]))
+    assert np.all(out["velocity_global"] == 0.0)
+    for k, v in enumerate((-1.0, -2.0, -3.0)):
+        assert np.all(out["velocity_camera"][k][cov] == v) and np.all(out["velocity_camera"][k][~cov] == 0.0)

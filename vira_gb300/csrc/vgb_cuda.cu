@@ -2578,6 +2578,7 @@ struct RasterOut {
     float *depth, *alpha, *albedo, *normal, *total, *direct, *indirect, *power;
     uint32_t* tri;
     const float* omega;
+    float *tsz, *vel_g, *vel_c;   // first-fragment passes (null when not requested)
 };
 
 // The winner's passes (cpu_rasterizer.ipp:148-250, passes.ipp:80-128): the fragment is
@@ -2635,12 +2636,24 @@ __global__ void k_raster_resolve(DevScene s, RasterParams rp, const unsigned lon
                 tangent_frame(N, tg, bt);
                 N = mapped_normal(s, uvx, uvy, N, tg, bt);
             }
+            // the fragment's scene position: camera-frame corners interpolated with the screen-space
+            // weights, then R p + origin (camera.localToGlobal)
+            const F3 fc = (w[0] * r.vc[0] + w[1] * r.vc[1]) + w[2] * r.vc[2];
+            const vgb_camera& c = rp.cam;
+            const F3 fg{((c.rotation[0] * fc.x + c.rotation[3] * fc.y) + c.rotation[6] * fc.z) + c.origin[0],
+                        ((c.rotation[1] * fc.x + c.rotation[4] * fc.y) + c.rotation[7] * fc.z) + c.origin[1],
+                        ((c.rotation[2] * fc.x + c.rotation[5] * fc.y) + c.rotation[8] * fc.z) + c.origin[2]};
+            if (o.tsz) {
+                // the longest projected edge in pixels (cpu_rasterizer.ipp:123-129)
+                const float e01 = sqrtf((r.px[1] - r.px[0]) * (r.px[1] - r.px[0]) + (r.py[1] - r.py[0]) * (r.py[1] - r.py[0]));
+                const float e02 = sqrtf((r.px[2] - r.px[0]) * (r.px[2] - r.px[0]) + (r.py[2] - r.py[0]) * (r.py[2] - r.py[0]));
+                const float e12 = sqrtf((r.px[2] - r.px[1]) * (r.px[2] - r.px[1]) + (r.py[2] - r.py[1]) * (r.py[2] - r.py[1]));
+                o.tsz[v] = smax(e01, smax(e02, e12));
+            }
+            // the instance's and the camera's point velocities at the fragment (:211-218), as the
+            // path tracer's first hit computes them
+            if (o.vel_g || o.vel_c) first_hit_passes(s, c, t, fg, o.vel_g, o.vel_c, nullptr, P, (uint32_t)v);
             if (rp.lighting) {
-                const F3 fc = (w[0] * r.vc[0] + w[1] * r.vc[1]) + w[2] * r.vc[2];
-                const vgb_camera& c = rp.cam;
-                const F3 fg{((c.rotation[0] * fc.x + c.rotation[3] * fc.y) + c.rotation[6] * fc.z) + c.origin[0],
-                            ((c.rotation[1] * fc.x + c.rotation[4] * fc.y) + c.rotation[7] * fc.z) + c.origin[1],
-                            ((c.rotation[2] * fc.x + c.rotation[5] * fc.y) + c.rotation[8] * fc.z) + c.origin[2]};
                 for (uint32_t l = 0; l < rp.nlights; ++l) {
                     F3 L;
                     float dist, pdf;
@@ -2658,6 +2671,10 @@ __global__ void k_raster_resolve(DevScene s, RasterParams rp, const unsigned lon
             tri = t + 1u;
         } else {
             depth = __int_as_float(0x7f800000);
+            // DataPayload's defaults where no fragment was drawn
+            if (o.tsz) o.tsz[v] = __int_as_float(0x7f800000);
+            if (o.vel_g) { o.vel_g[v] = 0.f; o.vel_g[P + v] = 0.f; o.vel_g[2 * P + v] = 0.f; }
+            if (o.vel_c) { o.vel_c[v] = 0.f; o.vel_c[P + v] = 0.f; o.vel_c[2 * P + v] = 0.f; }
         }
         if (o.depth) o.depth[v] = depth;
         if (o.alpha) o.alpha[v] = alpha;
@@ -2700,7 +2717,10 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
     rp.lighting = opts->simulate_lighting ? 1u : 0u;
     // scratch: keys (P x 8 B), big-triangle queue and its count
     const size_t key_floats = 2 * P, q_floats = (size_t)ctx->ntris + 4;
-    const size_t host_planes = film->on_device ? 0 : (size_t)(5 * B + 6) * P + 4 * 8;
+    // host film: every plane staged on the device (albedo and the four radiance planes of B bands;
+    // depth, alpha, triangle id, triangle size, the pixel solid angle and three 3-vector planes),
+    // each rounded up to 4 floats
+    const size_t host_planes = film->on_device ? 0 : (size_t)(5 * B + 14) * P + 4 * 13;
     vgb_status s;
     if ((s = ensure_dn_scratch(ctx, key_floats + q_floats + host_planes)) != VGB_OK) return s;
     unsigned long long* keys = reinterpret_cast<unsigned long long*>(ctx->d_dn);
@@ -2708,7 +2728,7 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
     uint32_t* nbig = bigq + ctx->ntris;
     RasterOut o{film->depth, film->alpha, film->albedo, film->normal_global, film->total_radiance,
                 film->direct_radiance, film->indirect_radiance, film->received_power, film->triangle_id,
-                film->pixel_solid_angle};
+                film->pixel_solid_angle, film->triangle_size, film->velocity_global, film->velocity_camera};
     if (!rp.lighting) o.total = o.direct = o.indirect = o.power = nullptr;
     float* stage = ctx->d_dn + key_floats + q_floats;
     if (!film->on_device) {
@@ -2717,6 +2737,9 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
         o.depth = take(film->depth, P); o.alpha = take(film->alpha, P); o.albedo = take(film->albedo, B * P);
         o.normal = take(film->normal_global, 3 * P);
         o.tri = reinterpret_cast<uint32_t*>(take(reinterpret_cast<float*>(film->triangle_id), P));
+        o.tsz = take(film->triangle_size, P);
+        o.vel_g = take(film->velocity_global, 3 * P);
+        o.vel_c = take(film->velocity_camera, 3 * P);
         if (rp.lighting) {
             o.total = take(film->total_radiance, B * P); o.direct = take(film->direct_radiance, B * P);
             o.indirect = take(film->indirect_radiance, B * P); o.power = take(film->received_power, B * P);
@@ -2743,6 +2766,9 @@ VGB_API vgb_status vgb_rasterize(vgb_context* ctx, const vgb_camera* cam, const 
         CK(back(film->depth, o.depth, P * 4)); CK(back(film->alpha, o.alpha, P * 4));
         CK(back(film->albedo, o.albedo, B * P * 4)); CK(back(film->normal_global, o.normal, 3 * P * 4));
         CK(back(film->triangle_id, o.tri, P * 4));
+        CK(back(film->triangle_size, o.tsz, P * 4));
+        CK(back(film->velocity_global, o.vel_g, 3 * P * 4));
+        CK(back(film->velocity_camera, o.vel_c, 3 * P * 4));
         if (rp.lighting) {
             CK(back(film->total_radiance, o.total, B * P * 4)); CK(back(film->direct_radiance, o.direct, B * P * 4));
             CK(back(film->indirect_radiance, o.indirect, B * P * 4)); CK(back(film->received_power, o.power, B * P * 4));

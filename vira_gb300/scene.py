@@ -631,6 +631,13 @@ class Rasterizer:
         rp.albedo = torch.empty((B, H, W), dtype=torch.float32, device=dev)
         rp.normal_global = torch.empty((3, H, W), dtype=torch.float32, device=dev)
         rp.triangle_id = torch.empty((H, W), dtype=torch.int32, device=dev)
+        # the fragment's velocities and projected size (cpu_rasterizer.ipp:123-129, 211-218)
+        if rp.save_velocity:
+            rp.velocity_global = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+            rp.velocity_camera = torch.empty((3, H, W), dtype=torch.float32, device=dev)
+        else:
+            rp.velocity_global = rp.velocity_camera = None
+        rp.triangle_size = torch.empty((H, W), dtype=torch.float32, device=dev) if rp.save_triangle_size else None
         omega = None
         if rp.simulate_lighting:
             omega = scene.pixel_solid_angle(camera, cam)
@@ -640,7 +647,8 @@ class Rasterizer:
             rp.total_radiance = rp.direct_radiance = rp.indirect_radiance = rp.received_power = None
         f = capi.Film()
         for name in ("total_radiance", "direct_radiance", "indirect_radiance", "received_power", "albedo",
-                     "normal_global", "depth", "alpha", "triangle_id"):
+                     "normal_global", "depth", "alpha", "triangle_id", "velocity_global", "velocity_camera",
+                     "triangle_size"):
             setattr(f, name, capi.ptr(getattr(rp, name)))
         f.pixel_solid_angle = capi.ptr(omega)
         f.on_device = 1
