@@ -173,7 +173,10 @@ typedef struct vgb_film {
     float* alpha;              /* [H][W] */
     uint32_t* triangle_id;     /* [H][W]; VGB_NO_HIT where nothing was hit */
     const float* pixel_solid_angle; /* [H][W] input, from vgb_pixel_solid_angle */
-    int32_t on_device;         /* 1: every pointer is device memory; 0: host memory */
+    int32_t on_device;         /* 1: every pointer is device memory; 0: host memory (vgb_render:
+                                  pinned planes, cudaHostAlloc or cudaHostRegister, are written by
+                                  the kernels through their mapped address; pageable ones are
+                                  staged in device memory and copied back) */
     /* renderPasses.save_velocity / save_triangle_size (passes.hpp:79-85), set at a pixel's first
      * hit (cpu_path_tracer.ipp:356-372); pixels that never hit keep 0 / +inf */
     float* velocity_global;    /* [3][H][W] the hit point's velocity (instance motion) */

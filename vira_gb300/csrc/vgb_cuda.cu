@@ -1533,6 +1533,18 @@ void free_staging(vgb_context* ctx) {
     ctx->staging_bytes = 0;
 }
 
+// The device address of a pinned, mapped host allocation (cudaHostAlloc, cudaHostRegister) on the
+// current device, or null for device memory, pageable memory and null pointers.
+void* mapped_host(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost && a.devicePointer) ? a.devicePointer : nullptr;
+}
+
 vgb_status ensure_staging(vgb_context* ctx, size_t bytes) {
     if (bytes <= ctx->staging_bytes) return VGB_OK;
     free_staging(ctx);
@@ -3133,18 +3145,40 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     float* df[NPL];
     uint32_t* dtri = film->triangle_id;
     const float* domega = film->pixel_solid_angle;
+    bool staged[NPL] = {false};
+    bool tri_staged = false;
     if (film->on_device) {
         for (int k = 0; k < NPL; ++k) df[k] = hf[k];
     } else {
+        // Host planes that the CUDA runtime reports as pinned and mapped (cudaHostAlloc or
+        // cudaHostRegister memory) are written by the kernels through their device alias, across
+        // the host link, with no device staging and no copy after the render; other host planes
+        // are staged in device memory and copied back.
+        float* mapped[NPL];
         size_t total = 0;
-        for (int k = 0; k < NPL; ++k) if (hf[k]) total += nplane[k];
-        total += P + (film->pixel_solid_angle ? P : 0);
-        if ((s = ensure_staging(ctx, total * sizeof(float))) != VGB_OK) return s;
-        float* cur = (float*)ctx->staging_base;
-        for (int k = 0; k < NPL; ++k) { df[k] = hf[k] ? cur : nullptr; if (hf[k]) cur += nplane[k]; }
-        dtri = film->triangle_id ? (uint32_t*)cur : nullptr;
-        cur += P;
-        if (film->pixel_solid_angle) {
+        for (int k = 0; k < NPL; ++k) {
+            mapped[k] = static_cast<float*>(mapped_host(hf[k]));
+            staged[k] = hf[k] && !mapped[k];
+            if (staged[k]) total += nplane[k];
+        }
+        uint32_t* tri_mapped = static_cast<uint32_t*>(mapped_host(film->triangle_id));
+        tri_staged = film->triangle_id && !tri_mapped;
+        const float* omega_mapped = static_cast<const float*>(mapped_host(film->pixel_solid_angle));
+        const bool omega_staged = film->pixel_solid_angle && !omega_mapped;
+        total += (tri_staged ? P : 0) + (omega_staged ? P : 0);
+        float* cur = nullptr;
+        if (total) {
+            if ((s = ensure_staging(ctx, total * sizeof(float))) != VGB_OK) return s;
+            cur = (float*)ctx->staging_base;
+        }
+        for (int k = 0; k < NPL; ++k) {
+            df[k] = staged[k] ? cur : mapped[k];
+            if (staged[k]) cur += nplane[k];
+        }
+        dtri = tri_staged ? (uint32_t*)cur : tri_mapped;
+        if (tri_staged) cur += P;
+        domega = omega_mapped;
+        if (omega_staged) {
             CK(cudaMemcpyAsync(cur, film->pixel_solid_angle, P * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
             domega = cur;
         }
@@ -3185,8 +3219,8 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!film->on_device) {
         for (int k = 0; k < NPL; ++k)
-            if (hf[k]) CK(cudaMemcpyAsync(hf[k], df[k], nplane[k] * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
-        if (film->triangle_id) CK(cudaMemcpyAsync(film->triangle_id, dtri, P * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+            if (staged[k]) CK(cudaMemcpyAsync(hf[k], df[k], nplane[k] * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        if (tri_staged) CK(cudaMemcpyAsync(film->triangle_id, dtri, P * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
     float ms = 0.f;
