@@ -95,6 +95,9 @@ using namespace vgbd;
 #ifndef VGB_SHADE_GRID
 #define VGB_SHADE_GRID 48
 #endif
+#ifndef VGB_END_GRID
+#define VGB_END_GRID 8
+#endif
 #ifndef VGB_SHADOW_GRID
 #define VGB_SHADOW_GRID 60
 #endif
@@ -1672,7 +1675,7 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
     const uint32_t n0 = (uint32_t)tile_items(fp.cam.width, fp.cam.height);
     const int gt = grid_for(ctx, n0, VGB_TRACE_GRID), gs = grid_for(ctx, n0, VGB_SHADE_GRID);
     const int go = grid_for(ctx, n0, VGB_SHADOW_GRID);
-    const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height);
+    const int gp = grid_for(ctx, (size_t)fp.cam.width * fp.cam.height, VGB_END_GRID);
     // persistent traversal (binary layout): one resident wave, lanes refilled from the queue
     const bool persist = L == 2 && ctx->trav_persistent;
     const int gtp = persist ? resident_grid(ctx, k_trace_p<COUNT>) : 0;
