@@ -68,3 +68,40 @@ def test_host_film_pinned_and_pageable_equal_device(gpu, mix):
             assert same_bits_or_nan(got, ref[k]), k
     assert (ref["triangle_id"] != -1).mean() > 0.3
     scene.close()
+
+
+@pytest.mark.parametrize("any_hit", [False, True], ids=["closest", "any"])
+def test_trace_rays_pinned_and_pageable_buffers(gpu, any_hit):
+    """vgb_trace_rays (the TLAS::intersect seam) reads pinned ray buffers and writes pinned result
+    buffers through their mapped addresses, pageable ones through staging: same answers."""
+    import torch
+
+    scene, cam_id = workloads.plain_direct(posts=129, resolution=64)
+    scene.build_tlas()
+    lib = capi.load()
+    ctx = scene.context()
+    rng = np.random.default_rng(8)
+    n = 5000
+    o = np.zeros((n, 3), np.float32)
+    o[:, :2] = rng.uniform(-400.0, 400.0, (n, 2))
+    o[:, 2] = 3000.0
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d[:, 2] = -np.abs(d[:, 2]) - 0.5
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    tm = np.full(n, 5000.0, np.float32)
+    results = []
+    for pinned in (False, True):
+        buf = {"o": torch.from_numpy(o.copy()), "d": torch.from_numpy(d.copy()), "tm": torch.from_numpy(tm.copy()),
+               "tri": torch.zeros(n, dtype=torch.int32), "t": torch.zeros(n), "w": torch.zeros((n, 3))}
+        if pinned:
+            buf = {k: v.pin_memory() for k, v in buf.items()}
+        capi.check(lib.vgb_trace_rays(ctx, buf["o"].data_ptr(), buf["d"].data_ptr(), buf["tm"].data_ptr(), n,
+                                      int(any_hit), buf["tri"].data_ptr(), buf["t"].data_ptr(), buf["w"].data_ptr(), 0),
+                   ctx, "trace_rays")
+        results.append({k: buf[k].numpy().copy() for k in ("tri", "t", "w")})
+    a, b = results
+    assert np.array_equal(a["tri"], b["tri"])
+    assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+    assert np.array_equal(a["w"].view(np.uint32), b["w"].view(np.uint32))
+    assert (a["tri"] != -1).mean() > 0.3
+    scene.close()

@@ -3287,20 +3287,32 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
     uint32_t* dtri = tri;
     float *dt = tout, *db = bary;
     vgb_status s;
+    // host buffers: pinned, mapped ones (cudaHostAlloc, cudaHostRegister) are read and written by
+    // the kernel through their device address; the others are staged in device memory
+    void* mp[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (!on_device) {
-        size_t need = (size_t)n * (3 + 3 + (tmax ? 1 : 0) + 1 + (tout ? 1 : 0) + (bary ? 3 : 0));
-        if ((s = ensure_staging(ctx, need * 4)) != VGB_OK) return s;
-        float* cur = (float*)ctx->staging_base;
-        float* o2 = cur; cur += 3 * (size_t)n;
-        float* d2 = cur; cur += 3 * (size_t)n;
-        float* m2 = nullptr; if (tmax) { m2 = cur; cur += n; }
-        uint32_t* r2 = (uint32_t*)cur; cur += n;
-        float* t2 = nullptr; if (tout) { t2 = cur; cur += n; }
-        float* b2 = nullptr; if (bary) { b2 = cur; cur += 3 * (size_t)n; }
-        CK(cudaMemcpyAsync(o2, org, 12 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
-        CK(cudaMemcpyAsync(d2, dir, 12 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
-        if (tmax) CK(cudaMemcpyAsync(m2, tmax, 4 * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
-        dorg = o2; ddir = d2; dtmax = m2; dtri = r2; dt = t2; db = b2;
+        const void* hb[6] = {org, dir, tmax, tri, tout, bary};
+        const size_t words[6] = {3, 3, 1, 1, 1, 3};
+        size_t need = 0;
+        for (int k = 0; k < 6; ++k) {
+            mp[k] = mapped_host(hb[k]);
+            if (hb[k] && !mp[k]) need += words[k] * (size_t)n;
+        }
+        float* cur = nullptr;
+        if (need) {
+            if ((s = ensure_staging(ctx, need * 4)) != VGB_OK) return s;
+            cur = (float*)ctx->staging_base;
+        }
+        void* dv[6];
+        for (int k = 0; k < 6; ++k) {
+            dv[k] = hb[k] ? (mp[k] ? mp[k] : (void*)cur) : nullptr;
+            if (hb[k] && !mp[k]) cur += words[k] * (size_t)n;
+        }
+        for (int k = 0; k < 3; ++k)
+            if (hb[k] && !mp[k])
+                CK(cudaMemcpyAsync(dv[k], hb[k], 4 * words[k] * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+        dorg = (const float*)dv[0]; ddir = (const float*)dv[1]; dtmax = (const float*)dv[2];
+        dtri = (uint32_t*)dv[3]; dt = (float*)dv[4]; db = (float*)dv[5];
     }
     const DevScene sc = dev_scene(ctx);
     CK(cudaMemsetAsync(ctx->d_stats, 0, sizeof(uint64_t) * 8, ctx->stream));
@@ -3321,9 +3333,9 @@ VGB_API vgb_status vgb_trace_rays(vgb_context* ctx, const float* org, const floa
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     if (!on_device) {
-        CK(cudaMemcpyAsync(tri, dtri, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
-        if (tout) CK(cudaMemcpyAsync(tout, dt, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
-        if (bary) CK(cudaMemcpyAsync(bary, db, 12 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (!mp[3]) CK(cudaMemcpyAsync(tri, dtri, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (tout && !mp[4]) CK(cudaMemcpyAsync(tout, dt, 4 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+        if (bary && !mp[5]) CK(cudaMemcpyAsync(bary, db, 12 * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
     float ms = 0.f;
