@@ -44,10 +44,10 @@ MEASURED_TRAFFIC = {
 # bounce 0 (camera rays) and bounce 1 (diffuse continuation rays).
 MEASURED_TRACE_COUNTERS = {
     "case": "path_traced scale 0.25 (1025^2 DEM + craters, 512^2, 4 spp, 3 bounces)",
-    "issue_active_pct": {"bounce0": 56.58, "bounce1": 48.14},
-    "l1_throughput_pct": {"bounce0": 48.74, "bounce1": 31.13},
+    "issue_active_pct": {"bounce0": 56.4, "bounce1": 48.61},
+    "l1_throughput_pct": {"bounce0": 47.76, "bounce1": 31.07},
     "threads_per_warp_inst": {"bounce0": 26.05, "bounce1": 16.06},
-    "long_scoreboard_stalls_per_issue": {"bounce0": 5.96, "bounce1": 5.62},
+    "long_scoreboard_stalls_per_issue": {"bounce0": 5.63, "bounce1": 5.59},
 }
 L2_PROBE_BYTES = 64 << 20
 sys.path.insert(0, str(ROOT))
