@@ -24,6 +24,13 @@ constexpr int kStackSize = 64;
 #ifndef VGB_TRAV_SPECULATIVE
 #define VGB_TRAV_SPECULATIVE 0
 #endif
+// 1: traverse_rt keeps each pushed child's entry distance on the stack and, for closest-hit
+// rays, drops a popped entry whose box starts beyond the current closest hit without fetching it
+// (the box test re-evaluated with the new bound; results unchanged).  Off: on the path-traced
+// frame the closest-hit launches took 82.2 against 81.5 ms per frame with it.
+#ifndef VGB_TRAV_CULL
+#define VGB_TRAV_CULL 0
+#endif
 constexpr uint32_t kIterCap = 1u << 22;  // default traversal steps per ray before giving up
 
 // ------------------------------------------------------------------ Philox-4x32-10
@@ -195,6 +202,9 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
                                             const WRay& r, float tmax, const bool any, HitOut& h, uint32_t& err,
                                             Counters& cnt, uint32_t cap) {
     int stack[kStackSize];
+#if VGB_TRAV_CULL
+    float stack_tn[kStackSize];   // entry distance of each stacked child's box
+#endif
     int sp = 0;
     int node = 0;
     float best = any ? tmax : __int_as_float(0x7f800000);
@@ -202,6 +212,25 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
     h.id = VGB_NO_HIT;
     uint32_t iter = 0;
     const SlabRay q = make_slab(r);
+    // The next stacked node, or false when the stack is empty.  With culling, a closest-hit
+    // ray skips entries whose box test, re-run against the current closest hit, would fail: the
+    // test passes iff tn <= min(tf, best) * widen, and tn <= tf * widen held when it was pushed.
+    auto pop = [&](int& nd) -> bool {
+#if VGB_TRAV_CULL
+        const float bound = best * (1.0f + 0x1p-20f);
+        while (sp > 0) {
+            --sp;
+            if (!any && stack_tn[sp] > bound) continue;
+            nd = stack[sp];
+            return true;
+        }
+        return false;
+#else
+        if (sp == 0) return false;
+        nd = stack[--sp];
+        return true;
+#endif
+    };
     while (true) {
         while (node >= 0) {
             if (++iter > cap) { err |= kErrIter; return; }
@@ -217,8 +246,14 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
             const int ch0 = __float_as_int(n3.x), ch1 = __float_as_int(n3.y);
             if (h0 && h1) {
                 int nearc = ch0, farc = ch1;
-                if (tn1 < tn0) { nearc = ch1; farc = ch0; }
+                float tfar = tn1;
+                if (tn1 < tn0) { nearc = ch1; farc = ch0; tfar = tn0; }
                 if (sp >= kStackSize) { err |= kErrStack; return; }
+#if VGB_TRAV_CULL
+                stack_tn[sp] = tfar;
+#else
+                (void)tfar;
+#endif
                 stack[sp++] = farc;
                 node = nearc;
             } else if (h0) {
@@ -226,8 +261,7 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
             } else if (h1) {
                 node = ch1;
             } else {
-                if (sp == 0) return;
-                node = stack[--sp];
+                if (!pop(node)) return;
             }
         }
         // leaf
@@ -249,8 +283,7 @@ __device__ __forceinline__ void traverse_rt(const float4* __restrict__ nodes, co
                 }
             }
         }
-        if (sp == 0) return;
-        node = stack[--sp];
+        if (!pop(node)) return;
     }
 }
 
