@@ -1024,14 +1024,16 @@ __device__ __noinline__ float4 background_weights(F3 rd) {
     return make_float4((1.f - ddx) * (1.f - ddy), ddx * (1.f - ddy), (1.f - ddx) * ddy, ddx * ddy);
 }
 
-template <int NB>
+// B0: the launch shades bounce 0 (camera hits); the bounce-0-only and later-bounce-only code
+// paths are compiled into separate instantiations.
+template <int NB, bool B0>
 __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SHADE_BLOCK) k_shade(const DevScene s, DevState st, const __grid_constant__ FrameParams fp, uint32_t bounce,
                                                uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const uint32_t nb = fp.nb;
     const size_t P = st.P;
     const int lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
+    const uint32_t n_items = (B0) ? n_items_bounce0 : st.counters[in_q];
     uint32_t* out_count = &st.counters[(in_q ^ 1u)];
     uint32_t* out_q = st.pq[in_q ^ 1u];
     const uint32_t* in_queue = st.pq[in_q];
@@ -1047,7 +1049,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
         const uint32_t aux = fp.aux;
         uint32_t pendv = 0u;  // this item's fold state, written once below
         if (active) {
-            if (bounce == 0) {
+            if (B0) {
                 active = camera_ray(fp, item, sample, slot, ro, rd);
                 if (active && fp.opt.adaptive_sampling) {
                     if (sample == 0) { st.as1[slot] = 0.f; st.as2[slot] = 0.f; st.anum[slot] = 0u; }
@@ -1111,7 +1113,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
         const uint32_t k0 = (uint32_t)fp.opt.seed, k1 = (uint32_t)(fp.opt.seed >> 32);
         if (active && !hit) {
             if (fp.opt.simulate_lighting && fp.opt.show_background) {
-                if (bounce != 0) rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
+                if (!B0) rd = F3{st.dir[slot], st.dir[P + slot], st.dir[2 * P + slot]};
                 const float4 bw = background_weights(rd);
                 const float a = bw.x, b = bw.y, c = bw.z, e = bw.w;
 #pragma unroll
@@ -1119,7 +1121,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
                     if (k < (int)nb) {
                         const float bgv = fp.opt.background[k];
                         float bg = ((a * bgv + b * bgv) + c * bgv) + e * bgv;
-                        const float tk = (bounce == 0) ? 1.f : st.thr[k * P + slot];
+                        const float tk = (B0) ? 1.f : st.thr[k * P + slot];
                         const float pr = (pendv & kPradEmpty) ? 0.f : st.prad[k * P + slot];
                         st.prad[k * P + slot] = pr + tk * (bg * 1.f);
                     }
@@ -1133,7 +1135,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
             const uint32_t t = hid;
             F3 fnrm;
             surface_at<NB>(s, nb, fp.opt.smooth_shading != 0, t, hr.z, hr.w, Pp, N, fnrm, tg, bt, nf, alb);
-            if (bounce == 0) {
+            if (B0) {
                 if ((aux & AUX_TRI) && st.atri[slot] == VGB_NO_HIT) {
                     st.atri[slot] = t;
                     if (fp.tsz || fp.vel_g || fp.vel_c)
@@ -1150,7 +1152,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
             }
             if (fp.opt.simulate_lighting) {
                 lit = true;
-                if (bounce != 0) {
+                if (!B0) {
 #pragma unroll
                     for (int k = 0; k < NB; ++k)
                         if (k < (int)nb) thr[k] = st.thr[k * P + slot];
@@ -1159,9 +1161,9 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
 #pragma unroll
                 for (int k = 0; k < NB; ++k) {
                     if (k < (int)nb)
-                        st.brad[k * P + slot] = (bounce == 0 && fp.opt.has_ambient) ? 0.f + thr[k] * (fp.opt.ambient[k] * alb[k]) : 0.f;
+                        st.brad[k * P + slot] = (B0 && fp.opt.has_ambient) ? 0.f + thr[k] * (fp.opt.ambient[k] * alb[k]) : 0.f;
                 }
-                pendv = (pendv & kPradEmpty) | ((bounce == 0) ? 1u : 2u);
+                pendv = (pendv & kPradEmpty) | ((B0) ? 1u : 2u);
                 r0 = philox(U4{slot, sample, fp.opt.frame, (bounce << 8) | kSlotMain}, k0, k1);
             }
         }
@@ -1211,7 +1213,7 @@ __global__ void __launch_bounds__(VGB_SHADE_BLOCK, VGB_SHADE_MINB * 256 / VGB_SH
             }
             // a path that keeps its incoming ray (sampled pdf 0) already has it in the state,
             // except a camera ray
-            if (cont && (new_ray || bounce == 0)) {
+            if (cont && (new_ray || B0)) {
                 st.org[slot] = ro.x; st.org[P + slot] = ro.y; st.org[2 * P + slot] = ro.z;
                 st.dir[slot] = rd.x; st.dir[P + slot] = rd.y; st.dir[2 * P + slot] = rd.z;
             }
@@ -1712,7 +1714,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
     if (!carved) {
         cudaFuncSetAttribute(k_trace<L, COUNT>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
         cudaFuncSetAttribute(k_shadow<NB, L, COUNT>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
-        cudaFuncSetAttribute(k_shade<NB>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
+        cudaFuncSetAttribute(k_shade<NB, true>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
+        cudaFuncSetAttribute(k_shade<NB, false>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
         carved = true;
     }
 #endif
@@ -1736,7 +1739,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             }
             {
                 Prof p(ctx, 3, prof);
-                k_shade<NB><<<gs, VGB_SHADE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                if (b == 0) k_shade<NB, true><<<gs, VGB_SHADE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                else k_shade<NB, false><<<gs, VGB_SHADE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             launches += 2;
             for (uint32_t l = 0; l < fp.nlights; ++l) {
