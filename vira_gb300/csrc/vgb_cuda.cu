@@ -750,23 +750,24 @@ __device__ __noinline__ void first_hit_passes(const DevScene& s, const vgb_camer
 // Scene::intersect for every live path: camera rays at bounce 0, queued continuation rays
 // after.  Writes one 16-byte hit record per queue item; kept lean so that enough warps are
 // resident to hide the latency of the node and triangle fetches.
-template <int L, bool COUNT>
+// B0: the launch traces bounce 0 (camera rays generated in place); later bounces read the queue.
+template <int L, bool COUNT, bool B0>
 __global__ void __launch_bounds__(VGB_TRACE_BLOCK, (L == 8 ? VGB_TRACE8_MINB : VGB_TRACE_MINB) * 256 / VGB_TRACE_BLOCK) k_trace(const DevScene s, DevState st, const __grid_constant__ FrameParams fp,
                                                uint32_t bounce, uint32_t sample, uint32_t in_q, uint32_t n_items_bounce0) {
     const size_t P = st.P;
-    const uint32_t n_items = (bounce == 0) ? n_items_bounce0 : st.counters[in_q];
+    const uint32_t n_items = (B0) ? n_items_bounce0 : st.counters[in_q];
     const uint32_t* in_queue = st.pq[in_q];
     uint32_t err = 0, nclosest = 0;
     Counters cnt{0, 0};
     for (uint32_t item = blockIdx.x * blockDim.x + threadIdx.x; item < n_items; item += gridDim.x * blockDim.x) {
         uint32_t slot = 0;
         F3 ro, rd;
-        if (bounce == 0) {
+        if (B0) {
             if (!camera_ray(fp, item, sample, slot, ro, rd)) continue;
             if (fp.opt.adaptive_sampling && sample != 0 && st.anum[slot]) continue;  // pixel has stopped
         }
         uint32_t qi = item;  // the queue position this ray's hit record goes to
-        if (bounce != 0) {
+        if (!B0) {
 #if VGB_TRACE_BINS > 0
             if (st.binq) {
                 uint32_t first = 0;
@@ -1712,7 +1713,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
 #if VGB_L1_CARVEOUT >= 0
     static bool carved = false;   // once per instantiation (the attribute is the function's)
     if (!carved) {
-        cudaFuncSetAttribute(k_trace<L, COUNT>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
+        cudaFuncSetAttribute(k_trace<L, COUNT, true>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
+        cudaFuncSetAttribute(k_trace<L, COUNT, false>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
         cudaFuncSetAttribute(k_shadow<NB, L, COUNT>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
         cudaFuncSetAttribute(k_shade<NB, true>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
         cudaFuncSetAttribute(k_shade<NB, false>, cudaFuncAttributePreferredSharedMemoryCarveout, VGB_L1_CARVEOUT);
@@ -1735,7 +1737,8 @@ void launch_render(vgb_context* ctx, const FrameParams& fp, const FilmOut& film,
             {
                 Prof p(ctx, 0, prof);
                 if (persist) k_trace_p<COUNT><<<gtp, 256, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0, budget, refill);
-                else k_trace<L, COUNT><<<gt, VGB_TRACE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                else if (b == 0) k_trace<L, COUNT, true><<<gt, VGB_TRACE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
+                else k_trace<L, COUNT, false><<<gt, VGB_TRACE_BLOCK, 0, ctx->stream>>>(s, st, fp, b, smp, q, n0);
             }
             {
                 Prof p(ctx, 3, prof);
