@@ -319,7 +319,9 @@ VGB_API vgb_status vgb_render(vgb_context* ctx, const vgb_camera* cam, const vgb
  * and BVH layout may load those kernels' code onto the device under CUDA's lazy module loading
  * (CUDA_MODULE_LOADING=EAGER loads them all at start-up).  Each call waits for ctx's stream
  * and copies the device error word and ray counts to the host before it returns, as vgb_render
- * does; vgb_get_stats then reports the rays, launches and device time of this call and zeros
+ * does, so no call may be made while ctx's stream is being captured into a CUDA graph.  The
+ * context keeps the array's address; like every other device object of the context it does not
+ * survive a cudaDeviceReset (destroy the context first).  vgb_get_stats then reports the rays, launches and device time of this call and zeros
  * for the counting-pass and profiling fields, which this entry point does not fill.  All calls
  * on a device share the array and it keeps the last call's contents (each call clears its
  * counters itself): calls that overlap on the GPU -- two contexts or two streams rendering at
