@@ -129,6 +129,8 @@ public:
     bool interpolate_distortion_directions = true;
     bool depth_of_field = false;
     float focus_distance = INFINITY;
+    // the camera's own motion (global frame) for the velocity passes
+    Vec3 velocity{0, 0, 0}, angular_rate{0, 0, 0};
 
     void setBrownDistortionCoefficients(float k1, float k2, float k3, float p1, float p2) {
         setDistortion(VGB_DISTORTION_BROWN, {k1, k2, k3, p1, p2});
@@ -196,6 +198,15 @@ public:
         c.aperture_radius = d / 2.f;
         c.focal_length = focal_length;
         c.focus_distance = focus_distance;
+        c.sensor_size[0] = sensor_x;
+        c.sensor_size[1] = sensor_y;
+        for (int r = 0; r < 3; ++r) {
+            c.velocity[r] = (float)velocity[r];
+            c.angular_rate[r] = (float)angular_rate[r];
+            // rotation * origin in FP64 (the velocity passes evaluate the camera's point velocity
+            // at rotation * p_global, as the reference does)
+            c.rot_origin[r] = (float)(rotation[r] * origin[0] + rotation[3 + r] * origin[1] + rotation[6 + r] * origin[2]);
+        }
         return c;
     }
 
@@ -255,10 +266,13 @@ struct CPUPathTracerOptions {  // cpu_path_tracer.hpp:30-43, plus the RNG key an
 
 struct RenderPasses {  // passes.hpp:51-95, planar [B][H][W]
     bool simulate_lighting = false;
+    bool save_velocity = false, save_triangle_size = false;
     uint32_t width = 0, height = 0, bands = 0;
     std::vector<float> total_radiance, direct_radiance, indirect_radiance, received_power, albedo, normal_global,
         depth, alpha;
     std::vector<uint32_t> triangle_id;
+    // first-hit passes (passes.hpp:79-85): [3][H][W] velocities, [H][W] triangle size in pixels
+    std::vector<float> velocity_global, velocity_camera, triangle_size;
 };
 
 class Scene;
@@ -412,6 +426,18 @@ inline void GpuPathTracer::render(Camera& camera, Scene& scene) {
     vgb_film f{};
     f.depth = rp.depth.data(); f.alpha = rp.alpha.data(); f.albedo = rp.albedo.data();
     f.normal_global = rp.normal_global.data(); f.triangle_id = rp.triangle_id.data();
+    if (rp.save_velocity) {
+        rp.velocity_global.assign(3 * P, 0.f); rp.velocity_camera.assign(3 * P, 0.f);
+        f.velocity_global = rp.velocity_global.data(); f.velocity_camera = rp.velocity_camera.data();
+    } else {
+        rp.velocity_global.clear(); rp.velocity_camera.clear();
+    }
+    if (rp.save_triangle_size) {
+        rp.triangle_size.assign(P, INFINITY);
+        f.triangle_size = rp.triangle_size.data();
+    } else {
+        rp.triangle_size.clear();
+    }
     if (rp.simulate_lighting) {
         rp.total_radiance.assign(B * P, 0.f); rp.direct_radiance.assign(B * P, 0.f);
         rp.indirect_radiance.assign(B * P, 0.f); rp.received_power.assign(B * P, 0.f);

@@ -1,7 +1,9 @@
 // Renders the plain direct-lighting terrain scene through the C++ host API (include/vgb.hpp), the
 // way a Vira program drives CPUPathTracer: scene.pathtracer.options / renderPasses, then render.
 // Usage: drop_in_render heights.bin posts resolution out.bin
-// heights.bin: posts*posts float32, row-major; out.bin: total radiance [4][R][R] then triangle ids.
+// heights.bin: posts*posts float32, row-major; out.bin: total radiance [4][R][R], triangle ids,
+// then the first-hit passes velocity_camera [3][R][R] and triangle_size [R][R] (camera moving at
+// (30, -4, 2) m/s, turning at (0, 0.01, 0) rad/s).
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -33,11 +35,17 @@ int main(int argc, char** argv) {
         scene.pathtracer.options.deterministic_light = true;
         scene.pathtracer.options.seed = 1;
         scene.pathtracer.renderPasses.simulate_lighting = true;
+        scene.pathtracer.renderPasses.save_velocity = true;
+        scene.pathtracer.renderPasses.save_triangle_size = true;
+        cam.velocity = {30.0, -4.0, 2.0};
+        cam.angular_rate = {0.0, 0.01, 0.0};
         scene.pathtracer.render(cam, scene);
         const auto& rp = scene.pathtracer.renderPasses;
         std::ofstream out(argv[4], std::ios::binary);
         out.write(reinterpret_cast<const char*>(rp.total_radiance.data()), (std::streamsize)(rp.total_radiance.size() * 4));
         out.write(reinterpret_cast<const char*>(rp.triangle_id.data()), (std::streamsize)(rp.triangle_id.size() * 4));
+        out.write(reinterpret_cast<const char*>(rp.velocity_camera.data()), (std::streamsize)(rp.velocity_camera.size() * 4));
+        out.write(reinterpret_cast<const char*>(rp.triangle_size.data()), (std::streamsize)(rp.triangle_size.size() * 4));
         std::printf("rendered %ux%u, %zu triangles\n", res, res, scene.meshes[0].indices.size() / 3);
     } catch (const vgb::Error& e) {
         std::fprintf(stderr, "vgb error %d: %s\n", (int)e.status, e.what());

@@ -29,14 +29,29 @@ def test_cpp_drop_in_matches_python_host(gpu, tmp_path):
     r = subprocess.run([str(exe), str(hf), str(posts), str(res), str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(out, np.float32)
-    rad_c = raw[: 4 * res * res].reshape(4, res, res)
-    tri_c = raw[4 * res * res:].view(np.uint32).reshape(res, res)
+    P = res * res
+    rad_c = raw[: 4 * P].reshape(4, res, res)
+    tri_c = raw[4 * P: 5 * P].view(np.uint32).reshape(res, res)
+    velc_c = raw[5 * P: 8 * P].reshape(3, res, res)
+    tsz_c = raw[8 * P: 9 * P].reshape(res, res)
     scene, cam_id = workloads.plain_direct(posts=posts, resolution=res)
-    rp = scene.pathtracer.render(scene[cam_id], scene)
+    cam = scene[cam_id]
+    cam.velocity = np.array([30.0, -4.0, 2.0])
+    cam.angular_rate = np.array([0.0, 0.01, 0.0])
+    scene.pathtracer.render_passes.save_velocity = True
+    scene.pathtracer.render_passes.save_triangle_size = True
+    rp = scene.pathtracer.render(cam, scene)
     torch.cuda.synchronize()
     rad_p = rp.total_radiance.cpu().numpy()
     tri_p = rp.triangle_id.cpu().numpy().view(np.uint32)
+    velc_p = rp.velocity_camera.cpu().numpy()
+    tsz_p = rp.triangle_size.cpu().numpy()
     scene.close()
+    hit = (tri_c == tri_p) & (tri_p != capi.NO_HIT)
+    assert hit.mean() > 0.5
+    # the C++ layer passes the camera's motion, sensor size and rotation-origin term as the Python host
+    assert float(np.abs(velc_c[:, hit] - velc_p[:, hit]).max()) <= 1e-3 * float(np.abs(velc_p[:, hit]).max())
+    assert float((np.abs(tsz_c[hit] - tsz_p[hit]) / tsz_p[hit]).max()) <= 1e-4
     assert np.mean(tri_c == tri_p) >= 0.999
     same = tri_c == tri_p
     rel = np.abs(rad_c - rad_p)[:, same] / np.maximum(np.abs(rad_p[:, same]), 1e-30)
